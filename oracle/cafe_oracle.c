@@ -1,0 +1,469 @@
+/* CPU oracle for the CAFE5 likelihood hot path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Plain-C FP64 restatement of the reference algorithm. Each function cites
+ * the reference lines it follows (paths relative to the CAFE5 project).
+ * Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg use
+ * this file, and only as the checker / the timed CPU baseline.
+ */
+#include "cafe_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* src/probability.cpp:82-91. The reference serves n, r < 100 from a cache
+ * and n < 1024 from an lgamma table (probability.cpp:55-80); both hold the
+ * same libm lgamma values used here directly. */
+double oracle_chooseln(double n, double r) {
+    if (r == 0 || (n == 0 && r == 0)) return 0;
+    if (n <= 0 || r <= 0) return log(0.0);
+    return lgamma(n + 1) - lgamma(r + 1) - lgamma(n - r + 1);
+}
+
+/* src/probability.cpp:104-148: Eqn (1) of Hahn et al. 2005, one exp and
+ * one pow per binomial term, summed in j order, clamped to [0, 1]. */
+double oracle_bd_rate(int s, int c, double log_alpha, double coeff) {
+    int m = c < s ? c : s;
+    int s_add_c = s + c;
+    double result = 0.0;
+    for (int j = 0; j <= m; j++) {
+        double t = oracle_chooseln(s, j) + oracle_chooseln(s_add_c - 1 - j, s - 1) +
+                   (s_add_c - 2 * j) * log_alpha;
+        result += exp(t) * pow(coeff, j);
+    }
+    if (result > 1.0) result = 1.0;
+    if (result < 0.0) result = 0.0;
+    return result;
+}
+
+/* src/probability.cpp:150-167 and src/matrix_cache.cpp:78-85 (parent size
+ * 0 stays 0). */
+double oracle_transition(double lambda, double t, int s, int c) {
+    if (s == 0) return c == 0 ? 1.0 : 0.0;
+    double alpha = lambda * t / (1 + lambda * t);
+    double coeff = 1 - 2 * alpha;
+    if (coeff > 0 && coeff != 1) return oracle_bd_rate(s, c, log(alpha), coeff);
+    return 0.0;
+}
+
+/* src/matrix_cache.h:49-62: matrices are computed at lambda truncated to
+ * 1e-9 and t truncated to 1e-3. */
+void oracle_quantize(double lambda, double t, double* lambda_q, double* t_q) {
+    long lq = (long)(lambda * 1000000000);
+    long tq = (long)(t * 1000);
+    *lambda_q = (double)lq / 1000000000.0;
+    *t_q = (double)tq / 1000.0;
+}
+
+/* src/matrix_cache.cpp:107-111 */
+int oracle_is_saturated(double t, double lambda) {
+    double alpha = lambda * t / (1 + lambda * t);
+    return (1 - 2 * alpha) < 0;
+}
+
+/* src/matrix_cache.cpp:113-163 for one key (lambda, t already quantized):
+ * row 0 is delta(c, 0); rows s >= 1 are filled unless saturated. */
+void oracle_fill_matrix(double lambda, double t, int size, double* out) {
+    memset(out, 0, sizeof(double) * (size_t)size * (size_t)size);
+    out[0] = 1.0;
+    if (oracle_is_saturated(t, lambda)) return;
+    for (int s = 1; s < size; s++)
+        for (int c = 0; c < size; c++)
+            out[(size_t)s * size + c] = oracle_transition(lambda, t, s, c);
+}
+
+/* src/matrix_cache.cpp:32-58 (the scalar branch; the BLAS branch is not
+ * compiled in the reference build). */
+void oracle_multiply(const double* m, int size, const double* v, int s_min, int s_max,
+                     int c_min, int c_max, double* result) {
+    for (int s = s_min; s <= s_max; s++) {
+        double acc = 0;
+        const double* row = m + (size_t)s * size;
+        for (int c = c_min; c <= c_max; c++) acc += row[c] * v[c - c_min];
+        result[s - s_min] = acc;
+    }
+}
+
+/* Reverse-level order (src/clade.cpp:69-100): breadth-first from the root,
+ * children in descendant order, then reversed. */
+static int* reverse_level_order(const oracle_tree* tree, int** child_start_out, int** children_out) {
+    int n = tree->n_nodes;
+    int* nchild = calloc((size_t)n + 1, sizeof(int));
+    int* start = calloc((size_t)n + 1, sizeof(int));
+    int* children = malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int* fill = calloc((size_t)n + 1, sizeof(int));
+    int root = -1;
+    for (int i = 0; i < n; i++) {
+        if (tree->parent[i] < 0) root = i;
+        else nchild[tree->parent[i]]++;
+    }
+    for (int i = 0; i < n; i++) start[i + 1] = start[i] + nchild[i];
+    for (int i = 0; i < n; i++)
+        if (tree->parent[i] >= 0) {
+            int p = tree->parent[i];
+            children[start[p] + fill[p]++] = i;
+        }
+    int* queue = malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int head = 0, tail = 0;
+    if (root >= 0) queue[tail++] = root;
+    while (head < tail) {
+        int v = queue[head++];
+        for (int k = start[v]; k < start[v + 1]; k++) queue[tail++] = children[k];
+    }
+    int* order = malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    for (int i = 0; i < tail; i++) order[i] = queue[tail - 1 - i];
+    free(queue);
+    free(nchild);
+    free(fill);
+    *child_start_out = start;
+    *children_out = children;
+    return order;
+}
+
+static void rescale(double* v, int len, long* expo) {
+    double mx = 0;
+    for (int i = 0; i < len; i++)
+        if (v[i] > mx) mx = v[i];
+    if (mx > 0 && isfinite(mx)) {
+        int e;
+        frexp(mx, &e);
+        for (int i = 0; i < len; i++) v[i] = ldexp(v[i], -e);
+        *expo += e;
+    }
+}
+
+typedef struct {
+    const oracle_tree* tree;
+    const int* order;
+    const int* cstart;
+    const int* children;
+    int root;
+} tree_view;
+
+/* inference_prune (src/core.cpp:134-145) over compute_node_probability
+ * (src/probability.cpp:175-234). vec is n_nodes * stride scratch, res is
+ * stride scratch, expo is n_nodes scratch. */
+static int prune_one(const tree_view* tv, const int32_t* counts_row, const double* const* node_matrix,
+                     int size, const double* err_rows, int err_nrows, int err_ndev, int S, int R,
+                     int scaled, double* vec, int stride, double* res, long* expo, double* root_out,
+                     double* log_scale) {
+    const oracle_tree* tree = tv->tree;
+    int n = tree->n_nodes;
+    for (int oi = 0; oi < n; oi++) {
+        int v = tv->order[oi];
+        double* L = vec + (size_t)v * stride;
+        expo[v] = 0;
+        if (tv->cstart[v] == tv->cstart[v + 1]) {
+            /* leaf: src/probability.cpp:184-203 */
+            int cnt = counts_row[tree->leaf_col[v]];
+            for (int i = 0; i <= S; i++) L[i] = 0;
+            if (cnt < 0 || cnt > S) return -1;
+            if (err_rows) {
+                const double* p = err_rows + (size_t)(cnt < err_nrows ? cnt : err_nrows - 1) * err_ndev;
+                int offset = cnt - (err_ndev - 1) / 2;
+                for (int i = 0; i < err_ndev; i++) {
+                    if (offset + i < 0 || offset + i > S) continue;
+                    L[offset + i] = p[i];
+                }
+            } else {
+                L[cnt] = 1.0;
+            }
+        } else {
+            int is_root = (v == tv->root);
+            int len = is_root ? R : S + 1;
+            for (int i = 0; i < len; i++) L[i] = 1;
+            for (int k = tv->cstart[v]; k < tv->cstart[v + 1]; k++) {
+                int ch = tv->children[k];
+                const double* m = node_matrix[ch];
+                if (!m) return -2;
+                if (is_root) oracle_multiply(m, size, vec + (size_t)ch * stride, 1, R, 0, S, res);
+                else oracle_multiply(m, size, vec + (size_t)ch * stride, 0, S, 0, S, res);
+                for (int i = 0; i < len; i++) L[i] *= res[i];
+                expo[v] += expo[ch];
+            }
+            if (scaled) rescale(L, len, &expo[v]);
+        }
+    }
+    memcpy(root_out, vec + (size_t)tv->root * stride, sizeof(double) * (size_t)R);
+    *log_scale = (double)expo[tv->root] * log(2.0);
+    return 0;
+}
+
+int oracle_prune(const oracle_tree* tree, const int32_t* counts_row, const double* const* node_matrix,
+                 int size, const double* err_rows, int err_nrows, int err_ndev, int S, int R,
+                 int scaled, double* root_out, double* log_scale) {
+    tree_view tv;
+    int *cstart, *children;
+    tv.tree = tree;
+    tv.order = reverse_level_order(tree, &cstart, &children);
+    tv.cstart = cstart;
+    tv.children = children;
+    tv.root = tv.order[tree->n_nodes - 1];
+    int stride = (S + 1 > R ? S + 1 : R) + 4;
+    double* vec = calloc((size_t)tree->n_nodes * stride, sizeof(double));
+    double* res = calloc((size_t)stride + 1024, sizeof(double));
+    long* expo = calloc((size_t)tree->n_nodes, sizeof(long));
+    int rc = prune_one(&tv, counts_row, node_matrix, size, err_rows, err_nrows, err_ndev, S, R, scaled,
+                       vec, stride, res, expo, root_out, log_scale);
+    free(vec);
+    free(res);
+    free(expo);
+    free((void*)tv.order);
+    free(cstart);
+    free(children);
+    return rc;
+}
+
+/* ---- matrix cache: keys (long(lambda*1e9), long(t*1e3)) ---- */
+typedef struct {
+    long lq, tq;
+    double* m;
+} cache_entry;
+
+static int find_key(const cache_entry* e, int n, long lq, long tq) {
+    for (int i = 0; i < n; i++)
+        if (e[i].lq == lq && e[i].tq == tq) return i;
+    return -1;
+}
+
+int oracle_score(const oracle_tree* tree, const int32_t* counts, int64_t F, int n_leaves,
+                 const double* lambdas, int n_lambdas, int lambda_kind, int K, const double* multipliers,
+                 const double* cat_probs, const double* prior, int n_prior, const double* err_rows,
+                 int err_nrows, int err_ndev, int S, int R, const int* fam_S, const int* fam_R, int model,
+                 int dedupe, int scaled, int n_threads, double* fam_lnl, double* cat_lh, double* total) {
+    int n = tree->n_nodes;
+    if (n <= 0 || F < 0 || n_lambdas <= 0) return -1;
+    double one = 1.0;
+    if (model == 0) {
+        K = 1;
+        multipliers = &one;
+    }
+    if (K <= 0) return -1;
+
+    /* lambda::is_valid (src/lambda.h:58-60, src/lambda.cpp:172-175) */
+    int valid = 1;
+    double largest = lambdas[0];
+    for (int i = 0; i < n_lambdas; i++) {
+        if (lambda_kind == 0 ? !(lambdas[i] > 0) : (lambdas[i] < 0)) valid = 0;
+        if (lambdas[i] > largest) largest = lambdas[i];
+    }
+    /* distinct positive branch lengths, root branch included
+     * (src/clade.cpp:236-245) */
+    double* bl = malloc(sizeof(double) * (size_t)n);
+    int nbl = 0;
+    double longest = 0;
+    for (int i = 0; i < n; i++) {
+        double t = tree->branch_length[i];
+        if (!(t > 0)) continue;
+        int dup = 0;
+        for (int j = 0; j < nbl; j++)
+            if (bl[j] == t) dup = 1;
+        if (!dup) bl[nbl++] = t;
+        if (t > longest) longest = t;
+    }
+    /* base_model.cpp:56-60; gamma_core.cpp:123-141, 174-178 */
+    if (!valid || (model == 1 && nbl > 0 && oracle_is_saturated(longest, largest))) {
+        free(bl);
+        *total = INFINITY;
+        for (int64_t f = 0; f < F; f++) fam_lnl[f] = NAN;
+        return 0;
+    }
+
+    int Smax = S, Rmax = R;
+    if (fam_S) {
+        Smax = 0;
+        Rmax = 0;
+        for (int64_t f = 0; f < F; f++) {
+            if (fam_S[f] > Smax) Smax = fam_S[f];
+            if (fam_R[f] > Rmax) Rmax = fam_R[f];
+        }
+    }
+    int size = (Rmax > Smax ? Rmax : Smax) + 1; /* base_model.cpp:65 */
+
+    /* precalculate_matrices for every (lambda_i * m_k, t) */
+    int cap = K * n_lambdas * (nbl > 0 ? nbl : 1);
+    cache_entry* cache = calloc((size_t)cap, sizeof(cache_entry));
+    int ncache = 0;
+    for (int k = 0; k < K; k++)
+        for (int i = 0; i < n_lambdas; i++)
+            for (int b = 0; b < nbl; b++) {
+                double lam = lambdas[i] * multipliers[k];
+                long lq = (long)(lam * 1000000000), tq = (long)(bl[b] * 1000);
+                if (find_key(cache, ncache, lq, tq) >= 0) continue;
+                cache[ncache].lq = lq;
+                cache[ncache].tq = tq;
+                cache[ncache].m = malloc(sizeof(double) * (size_t)size * size);
+                ncache++;
+            }
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < ncache; i++) {
+        double lq, tq;
+        lq = (double)cache[i].lq / 1000000000.0;
+        tq = (double)cache[i].tq / 1000.0;
+        oracle_fill_matrix(lq, tq, size, cache[i].m);
+    }
+    /* node -> matrix per category */
+    const double** nm = calloc((size_t)K * n, sizeof(double*));
+    for (int k = 0; k < K; k++)
+        for (int v = 0; v < n; v++) {
+            if (tree->parent[v] < 0) continue;
+            double lam = lambdas[tree->lambda_index[v]] * multipliers[k];
+            int idx = find_key(cache, ncache, (long)(lam * 1000000000), (long)(tree->branch_length[v] * 1000));
+            nm[(size_t)k * n + v] = idx >= 0 ? cache[idx].m : NULL;
+        }
+
+    tree_view tv;
+    int *cstart, *children;
+    tv.tree = tree;
+    tv.order = reverse_level_order(tree, &cstart, &children);
+    tv.cstart = cstart;
+    tv.children = children;
+    tv.root = tv.order[n - 1];
+
+    /* base_model.cpp:27-51: identical families are pruned once */
+    int64_t* ref = malloc(sizeof(int64_t) * (size_t)(F > 0 ? F : 1));
+    for (int64_t f = 0; f < F; f++) ref[f] = f;
+    if (dedupe && model == 0 && !fam_S) {
+        /* hash rows, then confirm equality */
+        int64_t nb = 1;
+        while (nb < 2 * F) nb <<= 1;
+        int64_t* head = malloc(sizeof(int64_t) * (size_t)nb);
+        for (int64_t i = 0; i < nb; i++) head[i] = -1;
+        for (int64_t f = 0; f < F; f++) {
+            const int32_t* row = counts + (size_t)f * n_leaves;
+            uint64_t h = 1469598103934665603ull;
+            for (int c = 0; c < n_leaves; c++) h = (h ^ (uint32_t)row[c]) * 1099511628211ull;
+            int64_t slot = (int64_t)(h & (uint64_t)(nb - 1));
+            for (;;) {
+                int64_t g = head[slot];
+                if (g < 0) {
+                    head[slot] = f;
+                    break;
+                }
+                if (memcmp(counts + (size_t)g * n_leaves, row, sizeof(int32_t) * (size_t)n_leaves) == 0) {
+                    ref[f] = g;
+                    break;
+                }
+                slot = (slot + 1) & (nb - 1);
+            }
+        }
+        free(head);
+    }
+
+    int fail = 0;
+    int stride = (Smax + 1 > Rmax ? Smax + 1 : Rmax) + 4;
+#pragma omp parallel
+    {
+        double* vec = malloc(sizeof(double) * (size_t)n * stride);
+        double* res = malloc(sizeof(double) * (size_t)stride);
+        double* root = malloc(sizeof(double) * (size_t)stride);
+        long* expo = malloc(sizeof(long) * (size_t)n);
+#pragma omp for schedule(dynamic, 8)
+        for (int64_t f = 0; f < F; f++) {
+            if (ref[f] != f) continue;
+            int Sf = fam_S ? fam_S[f] : S, Rf = fam_S ? fam_R[f] : R;
+            const int32_t* row = counts + (size_t)f * n_leaves;
+            if (model == 0) {
+                double ls;
+                int rc = prune_one(&tv, row, nm, size, err_rows, err_nrows, err_ndev, Sf, Rf, scaled, vec,
+                                   stride, res, expo, root, &ls);
+                if (rc) {
+#pragma omp atomic write
+                    fail = rc;
+                    continue;
+                }
+                /* base_model.cpp:80-90: max_j log L[j] + log prior(j) */
+                double best = -INFINITY;
+                for (int j = 0; j < Rf; j++) {
+                    double eq = j < n_prior ? prior[j] : 0.0;
+                    double v = log(root[j]) + log(eq);
+                    if (j == 0 || v > best) best = v;
+                }
+                fam_lnl[f] = best + ls;
+            } else {
+                /* gamma_core.cpp:143-165, 196-207 */
+                double fam_lh = 0.0;
+                double cmax = -INFINITY;
+                double* clog = cat_lh ? cat_lh + (size_t)f * K : NULL;
+                double lcat[64];
+                int bad = 0;
+                for (int k = 0; k < K && !bad; k++) {
+                    double ls;
+                    int rc = prune_one(&tv, row, nm + (size_t)k * n, size, err_rows, err_nrows, err_ndev, Sf, Rf,
+                                       scaled, vec, stride, res, expo, root, &ls);
+                    if (rc) {
+#pragma omp atomic write
+                        fail = rc;
+                        bad = 1;
+                        break;
+                    }
+                    double sum = 0.0;
+                    for (int j = 0; j < Rf; j++) sum += root[j];
+                    if (sum == 0.0) {
+                        bad = 1;
+                        break;
+                    }
+                    double mx = 0;
+                    for (int j = 0; j < Rf; j++) {
+                        double eq = j < n_prior ? prior[j] : 0.0;
+                        double v = root[j] * eq;
+                        if (j == 0 || v > mx) mx = v;
+                    }
+                    double cat = mx * cat_probs[k];
+                    if (scaled) {
+                        lcat[k < 64 ? k : 63] = log(cat) + ls;
+                        if (log(cat) + ls > cmax) cmax = log(cat) + ls;
+                    } else {
+                        fam_lh += cat;
+                    }
+                    if (clog) clog[k] = log(cat) + ls;
+                }
+                if (bad) {
+                    fam_lnl[f] = NAN;
+#pragma omp atomic write
+                    fail = fail ? fail : 1;
+                    continue;
+                }
+                if (scaled) {
+                    double acc = 0;
+                    for (int k = 0; k < K; k++) acc += exp(lcat[k] - cmax);
+                    fam_lnl[f] = cmax + log(acc);
+                } else {
+                    fam_lnl[f] = log(fam_lh);
+                }
+            }
+        }
+        free(vec);
+        free(res);
+        free(root);
+        free(expo);
+    }
+    for (int64_t f = 0; f < F; f++)
+        if (ref[f] != f) fam_lnl[f] = fam_lnl[ref[f]];
+
+    if (fail < 0) {
+        *total = NAN;
+    } else if (fail > 0) {
+        *total = INFINITY; /* gamma_core.cpp:216-225 */
+    } else {
+        double acc = 0.0;
+        for (int64_t f = 0; f < F; f++) acc += fam_lnl[f];
+        *total = -acc; /* base_model.cpp:95, gamma_core.cpp:233 */
+    }
+
+    free(ref);
+    free((void*)tv.order);
+    free(cstart);
+    free(children);
+    free(nm);
+    for (int i = 0; i < ncache; i++) free(cache[i].m);
+    free(cache);
+    free(bl);
+    return fail < 0 ? -1 : 0;
+}

@@ -1,0 +1,79 @@
+/* CPU oracle for the CAFE5 likelihood hot path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C, FP64 restatement of the reference algorithm, used by tests/,
+ * by __graft_entry__.smoke() and by bench.py's cpu_baseline leg as the
+ * checker. The product (cafe5_gb300/, include/) never links or calls it.
+ *
+ * Parity is pinned two ways (see tests/test_oracle_cpu.py):
+ *   - against the known-answer values in the reference's own test.cpp
+ *     (committed in tests/golden/reference_kats.json), and
+ *   - against hex-float outputs of the reference itself, compiled from its
+ *     own sources by oracle/Makefile (committed in tests/golden/ref_*.json,
+ *     generated by tests/golden/make_golden.py).
+ */
+#ifndef CAFE_ORACLE_H
+#define CAFE_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* A rooted tree as flat arrays. Node i has parent parent[i] (-1 for the
+ * root). The children of a node are taken in increasing node index, which
+ * is the reference's descendant order when nodes are numbered in Newick
+ * order. leaf_col[i] is the counts column of leaf i (-1 for internal
+ * nodes); lambda_index[i] selects the rate of the branch above node i. */
+typedef struct {
+    int n_nodes;
+    const int* parent;
+    const double* branch_length;
+    const int* lambda_index;
+    const int* leaf_col;
+} oracle_tree;
+
+double oracle_chooseln(double n, double r);
+double oracle_bd_rate(int s, int c, double log_alpha, double coeff);
+double oracle_transition(double lambda, double t, int s, int c);
+void oracle_quantize(double lambda, double t, double* lambda_q, double* t_q);
+int oracle_is_saturated(double t, double lambda);
+void oracle_fill_matrix(double lambda, double t, int size, double* out);
+void oracle_multiply(const double* m, int size, const double* v, int s_min, int s_max,
+                     int c_min, int c_max, double* result);
+
+/* Prunes one family with matrices given per node (node_matrix[i] is the
+ * size x size matrix of the branch above node i; unused for the root).
+ * Writes the root vector (R values, index j <-> root size j+1). With
+ * scaled != 0, every node vector is renormalised by a power of two and the
+ * accumulated natural-log scale is written to *log_scale. */
+int oracle_prune(const oracle_tree* tree, const int32_t* counts_row,
+                 const double* const* node_matrix, int size,
+                 const double* err_rows, int err_nrows, int err_ndev,
+                 int S, int R, int scaled, double* root_out, double* log_scale);
+
+/* One infer_family_likelihoods call.
+ *   model        0 = base model, 1 = gamma model
+ *   lambda_kind  0 = single_lambda (valid iff > 0), 1 = multiple_lambda
+ *                (valid iff none < 0)
+ *   S, R         global max_family_size / max_root_family_size
+ *   fam_S, fam_R optional per-family bounds (binned mode); NULL = global
+ *   prior        prior[j] for root index j (already float-rounded), 0 past n_prior
+ *   dedupe       prune identical count rows once (base model)
+ *   scaled       0 = reference arithmetic, 1 = per-node power-of-two rescale
+ * Outputs fam_lnl[F], cat_lh[F*K] (natural log of each category term for
+ * the gamma model; NULL allowed) and *total (= -sum lnL, +inf on the
+ * reference's rejection paths). Returns 0, or -1 on invalid input. */
+int oracle_score(const oracle_tree* tree, const int32_t* counts, int64_t F, int n_leaves,
+                 const double* lambdas, int n_lambdas, int lambda_kind,
+                 int K, const double* multipliers, const double* cat_probs,
+                 const double* prior, int n_prior,
+                 const double* err_rows, int err_nrows, int err_ndev,
+                 int S, int R, const int* fam_S, const int* fam_R,
+                 int model, int dedupe, int scaled, int n_threads,
+                 double* fam_lnl, double* cat_lh, double* total);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

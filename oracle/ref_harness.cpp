@@ -1,0 +1,261 @@
+// Test infrastructure only: a command-line probe that links the CAFE5
+// reference objects (compiled from the reference's own sources by
+// oracle/Makefile into oracle/_ref/) and calls the reference's likelihood
+// hot path exactly as its users do:
+//
+//   base_model::infer_family_likelihoods   (src/base_model.cpp:53-100)
+//   gamma_model::infer_family_likelihoods  (src/gamma_core.cpp:168-237)
+//   matrix_cache::precalculate_matrices    (src/matrix_cache.cpp:113-163)
+//   inference_prune                        (src/core.cpp:134-145)
+//
+// It reads the reference's own file formats (Newick tree, CAFE family
+// table, error-model file) through the reference's own readers
+// (src/clade.cpp:293-419, src/io.cpp:134-217, src/io.cpp:228-274), and
+// prints the total -lnL plus every per-family result as C99 hex floats so
+// that the parity tests compare bit patterns, not printed decimals.
+//
+// Nothing in the product links or runs this file.
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <random>
+#include <set>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "easylogging++.h"
+#include "base_model.h"
+#include "clade.h"
+#include "core.h"
+#include "error_model.h"
+#include "gamma.h"
+#include "gamma_core.h"
+#include "gene_family.h"
+#include "io.h"
+#include "lambda.h"
+#include "matrix_cache.h"
+#include "probability.h"
+#include "root_equilibrium_distribution.h"
+
+INITIALIZE_EASYLOGGINGPP
+
+std::mt19937 randomizer_engine(10);
+
+void init_lgamma_cache();
+
+namespace {
+
+// Subclasses only to read the protected per-family results vector.
+struct probe_base : public base_model {
+    using base_model::base_model;
+    const std::vector<family_info_stash>& stash() const { return results; }
+};
+
+struct probe_gamma : public gamma_model {
+    using gamma_model::gamma_model;
+    const std::vector<family_info_stash>& stash() const { return results; }
+};
+
+std::string slurp(const std::string& path) {
+    std::ifstream f(path);
+    if (!f) throw std::runtime_error("cannot open " + path);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    return ss.str();
+}
+
+std::vector<double> parse_list(const std::string& s) {
+    std::vector<double> v;
+    std::stringstream ss(s);
+    std::string tok;
+    while (std::getline(ss, tok, ',')) v.push_back(std::stod(tok));
+    return v;
+}
+
+void usage() {
+    std::fprintf(stderr,
+        "cafe_ref_harness --tree T.nwk --families F.tab --lambdas l1[,l2..]\n"
+        "   [--lambda-tree L.nwk] [--error E.txt]\n"
+        "   [--gamma-alpha A --gamma-k K] [--gamma-mult m1,.. --gamma-prob p1,..]\n"
+        "   [--max-family S --max-root R] [--prior uniform|uniform:N|poisson:X|rootdist:s=n,..]\n"
+        "   [--repeat N] [--quiet]\n");
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    el::Configurations conf;
+    conf.setToDefault();
+    conf.set(el::Level::Global, el::ConfigurationType::Enabled, "false");
+    conf.set(el::Level::Global, el::ConfigurationType::ToFile, "false");
+    el::Loggers::reconfigureAllLoggers(conf);
+
+    // "matrix <lambda> <t> <size>": dump one cached transition matrix
+    // (matrix_cache::precalculate_matrices + get_matrix) as hex floats.
+    if (argc == 5 && std::string(argv[1]) == "matrix") {
+        init_lgamma_cache();
+        double l = std::stod(argv[2]), t = std::stod(argv[3]);
+        int size = std::stoi(argv[4]);
+        matrix_cache calc(size);
+        calc.precalculate_matrices({l}, std::set<double>{t});
+        const matrix* mm = calc.get_matrix(t, l);
+        for (int s = 0; s < size; ++s) {
+            for (int c = 0; c < size; ++c) std::printf("%a ", mm->get(s, c));
+            std::printf("\n");
+        }
+        return 0;
+    }
+    // "rate <s> <c> <log_alpha> <coeff>": birthdeath_rate_with_log_alpha.
+    if (argc == 6 && std::string(argv[1]) == "rate") {
+        init_lgamma_cache();
+        double v = birthdeath_rate_with_log_alpha(std::stoi(argv[2]), std::stoi(argv[3]),
+                                                  std::stod(argv[4]), std::stod(argv[5]));
+        std::printf("%a\n", v);
+        return 0;
+    }
+
+    // "gamma <K> <alpha>": category probabilities and lambda multipliers
+    // from get_gamma (src/gamma.cpp:225-241).
+    if (argc == 4 && std::string(argv[1]) == "gamma") {
+        int k = std::stoi(argv[2]);
+        std::vector<double> freq(k), rate(k);
+        get_gamma(freq, rate, std::stod(argv[3]));
+        for (int i = 0; i < k; ++i) std::printf("%a %a\n", freq[i], rate[i]);
+        return 0;
+    }
+
+    std::string tree_path, fam_path, lambda_tree_path, err_path, prior_spec = "uniform";
+    std::vector<double> lambdas, gmult, gprob;
+    double alpha = -1;
+    int gk = 0, S = -1, R = -1, repeat = 1;
+    bool quiet = false;
+    for (int i = 1; i < argc; ++i) {
+        std::string a = argv[i];
+        auto next = [&]() -> std::string {
+            if (i + 1 >= argc) { usage(); std::exit(2); }
+            return argv[++i];
+        };
+        if (a == "--tree") tree_path = next();
+        else if (a == "--families") fam_path = next();
+        else if (a == "--lambda-tree") lambda_tree_path = next();
+        else if (a == "--lambdas") lambdas = parse_list(next());
+        else if (a == "--error") err_path = next();
+        else if (a == "--gamma-alpha") alpha = std::stod(next());
+        else if (a == "--gamma-k") gk = std::stoi(next());
+        else if (a == "--gamma-mult") gmult = parse_list(next());
+        else if (a == "--gamma-prob") gprob = parse_list(next());
+        else if (a == "--max-family") S = std::stoi(next());
+        else if (a == "--max-root") R = std::stoi(next());
+        else if (a == "--prior") prior_spec = next();
+        else if (a == "--repeat") repeat = std::stoi(next());
+        else if (a == "--quiet") quiet = true;
+        else { usage(); return 2; }
+    }
+    if (tree_path.empty() || fam_path.empty() || lambdas.empty()) { usage(); return 2; }
+
+    try {
+        init_lgamma_cache();
+        std::string nwk = slurp(tree_path);
+        std::unique_ptr<clade> tree(parse_newick(nwk, false));
+        std::vector<gene_family> families;
+        {
+            std::ifstream f(fam_path);
+            read_gene_families(f, tree.get(), families);
+        }
+        // Global bounds exactly as user_data::read_gene_family_data computes
+        // them (src/user_data.cpp:39-48) unless overridden.
+        int mx = 0;
+        for (auto& gf : families) mx = std::max(mx, gf.get_max_size());
+        int max_root = std::max(30, static_cast<int>(std::rint(mx * 1.25)));
+        int max_fam = mx + std::max(50, mx / 5);
+        if (S >= 0) max_fam = S;
+        if (R >= 0) max_root = R;
+
+        std::unique_ptr<clade> ltree;
+        std::unique_ptr<lambda> lam;
+        if (!lambda_tree_path.empty()) {
+            ltree.reset(parse_newick(slurp(lambda_tree_path), true));
+            lam.reset(new multiple_lambda(ltree->get_lambda_index_map(), lambdas));
+        } else {
+            lam.reset(new single_lambda(lambdas[0]));
+        }
+
+        std::unique_ptr<error_model> em;
+        if (!err_path.empty()) {
+            em.reset(new error_model());
+            std::ifstream f(err_path);
+            read_error_model_file(f, em.get());
+        }
+
+        std::unique_ptr<root_equilibrium_distribution> prior;
+        if (prior_spec == "uniform") prior.reset(new root_equilibrium_distribution(size_t(max_root)));
+        else if (prior_spec.rfind("uniform:", 0) == 0)
+            prior.reset(new root_equilibrium_distribution(size_t(std::stoul(prior_spec.substr(8)))));
+        else if (prior_spec.rfind("rootdist:", 0) == 0) {
+            // rootdist:size=count,size=count,...
+            std::map<int, int> rd;
+            std::stringstream ss(prior_spec.substr(9));
+            std::string tok;
+            while (std::getline(ss, tok, ',')) {
+                auto eq = tok.find('=');
+                rd[std::stoi(tok.substr(0, eq))] = std::stoi(tok.substr(eq + 1));
+            }
+            prior.reset(new root_equilibrium_distribution(rd));
+        }
+        else if (prior_spec.rfind("poisson:", 0) == 0)
+            prior.reset(new root_equilibrium_distribution(std::stod(prior_spec.substr(8)), size_t(max_root)));
+        else throw std::runtime_error("bad prior " + prior_spec);
+
+        bool is_gamma = (alpha > 0 && gk > 1) || !gmult.empty();
+        std::unique_ptr<model> m;
+        probe_base* pb = nullptr;
+        probe_gamma* pg = nullptr;
+        if (is_gamma) {
+            if (!gmult.empty()) {
+                pg = new probe_gamma(lam.get(), tree.get(), &families, max_fam, max_root, gprob, gmult, em.get());
+            } else {
+                pg = new probe_gamma(lam.get(), tree.get(), &families, max_fam, max_root, gk, alpha, em.get());
+            }
+            m.reset(pg);
+        } else {
+            pb = new probe_base(lam.get(), tree.get(), &families, max_fam, max_root, em.get());
+            m.reset(pb);
+        }
+
+        double total = 0;
+        double best_ms = 1e300, sum_ms = 0;
+        for (int r = 0; r < repeat; ++r) {
+            auto t0 = std::chrono::steady_clock::now();
+            total = m->infer_family_likelihoods(*prior, lam.get());
+            auto t1 = std::chrono::steady_clock::now();
+            double ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+            best_ms = std::min(best_ms, ms);
+            sum_ms += ms;
+        }
+        std::printf("bounds %d %d\n", max_fam, max_root);
+        std::printf("families %zu\n", families.size());
+        std::printf("total %.17g %a\n", total, total);
+        std::printf("time_ms best %.6f mean %.6f repeat %d\n", best_ms, sum_ms / repeat, repeat);
+        if (!quiet) {
+            if (pb) {
+                for (auto& s : pb->stash())
+                    std::printf("fam %s %a\n", s.family_id.c_str(), s.posterior_probability);
+            } else if (pg) {
+                for (auto& s : pg->stash())
+                    std::printf("cat %s %a %a %a\n", s.family_id.c_str(), s.lambda_multiplier,
+                                s.category_likelihood, s.family_likelihood);
+            }
+        }
+    } catch (std::exception& e) {
+        std::fprintf(stderr, "error: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}

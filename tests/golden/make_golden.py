@@ -1,0 +1,171 @@
+"""Regenerate the reference golden fixtures in this folder.
+
+Runs the CAFE5 reference itself -- compiled from its own sources by
+oracle/Makefile into oracle/_ref/cafe_ref_harness -- on small seeded
+synthetic cases and on the inputs of the reference's own known-answer
+tests, and stores inputs plus hex-float outputs:
+
+  ref_cases.json     end-to-end infer_family_likelihoods cases
+  ref_matrices.json  transition matrices from matrix_cache
+
+Only this script reads the reference (it needs /root/reference and the
+built harness); the tests read the committed JSON. Usage:
+    make -C oracle ref && python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from cafe5_gb300.families import FamilySet, global_bounds, write_families  # noqa: E402
+from cafe5_gb300.inputs import ErrorModel, RootPrior, discrete_gamma  # noqa: E402
+from cafe5_gb300.synth import simulate_families, workload, yule_tree  # noqa: E402
+from cafe5_gb300.tree import lambda_index_of_nodes, parse_newick  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "cafe_ref_harness")
+
+
+def run(args):
+    out = subprocess.run([HARNESS] + args, check=True, capture_output=True, text=True).stdout
+    return out
+
+
+def parse_output(out: str):
+    res = {"fam": {}, "cat": {}}
+    for ln in out.splitlines():
+        tok = ln.split()
+        if tok[0] == "total":
+            res["total_hex"] = tok[2]
+        elif tok[0] == "bounds":
+            res["S"], res["R"] = int(tok[1]), int(tok[2])
+        elif tok[0] == "fam":
+            res["fam"][tok[1]] = tok[2]
+        elif tok[0] == "cat":
+            res["cat"].setdefault(tok[1], []).append({"mult": tok[2], "cat_lh": tok[3], "fam_lh": tok[4]})
+    return res
+
+
+def lambda_tree_newick(tree, lam_idx):
+    def rec(v):
+        lab = tree.name[v] if tree.is_leaf(v) else "(" + ",".join(rec(c) for c in tree.children[v]) + ")"
+        if tree.parent[v] >= 0:
+            lab += f":{lam_idx[v] + 1}"
+        return lab
+    return rec(tree.root) + ";"
+
+
+def make_case(name, tree, fams, lambdas, *, lam_idx=None, model="base", mult=None, probs=None,
+              err=None, S=None, R=None, prior="uniform", note=""):
+    with tempfile.TemporaryDirectory() as d:
+        tp, fp = os.path.join(d, "t.nwk"), os.path.join(d, "f.tab")
+        nwk = tree.to_newick()
+        open(tp, "w").write(nwk)
+        write_families(fp, fams, tree)
+        args = ["--tree", tp, "--families", fp, "--lambdas", ",".join(repr(x) for x in lambdas),
+                "--prior", prior]
+        lnwk = None
+        if lam_idx is not None:
+            lp = os.path.join(d, "l.nwk")
+            lnwk = lambda_tree_newick(tree, lam_idx)
+            open(lp, "w").write(lnwk)
+            args += ["--lambda-tree", lp]
+        err_text = None
+        if err is not None:
+            ep = os.path.join(d, "e.txt")
+            err_text = err
+            open(ep, "w").write(err)
+            args += ["--error", ep]
+        if model == "gamma":
+            args += ["--gamma-mult", ",".join(repr(x) for x in mult), "--gamma-prob", ",".join(repr(x) for x in probs)]
+        if S is not None:
+            args += ["--max-family", str(S), "--max-root", str(R)]
+        out = parse_output(run(args))
+    case = {
+        "name": name, "note": note, "newick": nwk, "lambda_newick": lnwk, "taxa": tree.leaf_names,
+        "ids": fams.ids, "counts": fams.counts.tolist(), "lambdas": [float(x).hex() for x in lambdas],
+        "model": model, "multipliers": None if mult is None else [float(x).hex() for x in mult],
+        "cat_probs": None if probs is None else [float(x).hex() for x in probs],
+        "error_model": err_text, "prior": prior, "S": out["S"], "R": out["R"],
+        "expected": {"total_hex": out["total_hex"], "fam_lnl_hex": [out["fam"].get(i) for i in fams.ids],
+                     "cat": [out["cat"].get(i) for i in fams.ids] if model == "gamma" else None},
+    }
+    return case
+
+
+def main():
+    if not os.path.exists(HARNESS):
+        raise SystemExit("build the harness first: make -C oracle ref")
+    cases = []
+    # -- the reference's own known-answer inputs (test.cpp) --------------
+    t = parse_newick("(A:1,B:1);")
+    fams = FamilySet(["f1", "f2", "f3", "f4"], np.array([[1, 2], [2, 1], [3, 6], [6, 3]], np.int32))
+    cases.append(make_case("kat_infer_processes", t, fams, [0.01], S=56, R=8, prior="uniform:100",
+                           note="test.cpp:461-488, expected -lnL 46.56632"))
+    t = parse_newick("(A:1,B:3):7;")
+    fams = FamilySet(["f1"], np.array([[3, 6]], np.int32))
+    cases.append(make_case("kat_gamma_prune", t, fams, [0.005], model="gamma", mult=[0.1, 0.5], probs=[0.01, 0.05],
+                           S=10, R=8, prior="rootdist:1=2,2=2,3=2,4=2,5=1",
+                           note="test.cpp:1269-1294, log category likelihoods -23.04433, -16.68005"))
+    t = parse_newick("(A:1,B:3):7;")
+    cases.append(make_case("kat_gamma_saturated", t, fams, [0.9], model="gamma", mult=[0.1, 0.5], probs=[1.0, 1.0],
+                           S=10, R=8, prior="uniform:100", note="test.cpp:1296-1311: saturated -> +inf"))
+    # -- seeded synthetic cases ---------------------------------------------
+    w0 = workload(0, n_families=150, seed=3)
+    cases.append(make_case("syn_base_12taxa", w0.tree, w0.families, [0.0025],
+                           note="config-0 shape, global S/R, uniform prior"))
+    cases.append(make_case("syn_base_12taxa_poisson", w0.tree, w0.families, [0.004], prior="poisson:5.5",
+                           note="Poisson root prior (float-rounded)"))
+    zero = FamilySet(w0.families.ids[:20] + ["zero"], np.vstack([w0.families.counts[:20],
+                                                                  np.zeros((1, 12), np.int32)]))
+    cases.append(make_case("syn_base_zero_family", w0.tree, zero, [0.003], note="an all-zero family row"))
+    cases.append(make_case("syn_base_invalid_lambda", w0.tree, zero, [0.0], note="lambda <= 0 -> +inf"))
+    w1 = workload(1, n_families=120, seed=4)
+    cases.append(make_case("syn_gamma_24taxa_k4", w1.tree, w1.families, [0.002], model="gamma",
+                           mult=w1.multipliers, probs=w1.cat_probs, note="config-1 shape, K=4 alpha=0.5"))
+    probs8, mult8 = discrete_gamma(0.5, 8)
+    cases.append(make_case("syn_gamma_24taxa_k8_small_cat", w1.tree, FamilySet(w1.families.ids[:40],
+                                                                              w1.families.counts[:40]),
+                           [0.003], model="gamma", mult=mult8, probs=probs8, note="K=8"))
+    w2 = workload(2, n_families=400, seed=5)
+    keep = w2.families.max_counts() <= 30
+    f2 = FamilySet([i for i, k in zip(w2.families.ids, keep) if k][:80], w2.families.counts[keep][:80])
+    err = "maxcnt: 200\ncntdiff: -1 0 1\n0 0 0.95 0.05\n1 0.05 0.9 0.05\n"
+    cases.append(make_case("syn_multilambda_error_32taxa", w2.tree, f2, [0.0015, 0.006], lam_idx=w2.lambda_of_node,
+                           err=err, note="config-2 shape (counts<=30), two lambdas + error model"))
+    # a family whose likelihood underflows FP64 (alternating 0 / 50 counts)
+    uf = FamilySet(["alt", "flat"], np.array([[0 if i % 2 else 50 for i in range(24)], [1] * 24], np.int32))
+    cases.append(make_case("syn_base_underflow", w1.tree, uf, [0.001], S=110, R=75,
+                           note="first family underflows to L = 0 in FP64 -> -lnL = +inf"))
+    # non-binary tree (a polytomy)
+    tp = parse_newick("((A:2,B:2,C:2):3,(D:4,E:4):1);")
+    rng = np.random.default_rng(7)
+    cnt = simulate_families(tp, 30, np.full(30, 0.01), rng.integers(1, 6, 30), seed=8)
+    cases.append(make_case("syn_polytomy", tp, FamilySet([f"p{i}" for i in range(30)], cnt), [0.01],
+                           note="three children at one node"))
+    json.dump({"generator": "tests/golden/make_golden.py", "cases": cases},
+              open(os.path.join(HERE, "ref_cases.json"), "w"), indent=1)
+
+    mats = []
+    for lam, tt, size in [(0.05, 5.0, 5), (0.006335, 68.7105, 12), (0.002, 13.4, 40), (0.0125, 3.333, 30),
+                          (0.05, 25.0, 6), (0.0005, 150.0, 64)]:
+        out = run(["matrix", repr(lam), repr(tt), str(size)])
+        mats.append({"lambda": lam, "t": tt, "size": size, "hex": [ln.split() for ln in out.splitlines()]})
+    gam = []
+    for k, a in [(4, 0.5), (8, 0.5), (4, 1.7), (6, 0.37)]:
+        rows = [ln.split() for ln in run(["gamma", str(k), repr(a)]).splitlines()]
+        gam.append({"K": k, "alpha": a, "probs": [r[0] for r in rows], "multipliers": [r[1] for r in rows]})
+    json.dump({"generator": "tests/golden/make_golden.py", "matrices": mats, "gamma": gam},
+              open(os.path.join(HERE, "ref_matrices.json"), "w"))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,92 @@
+"""Loads the committed golden fixtures into ready-to-score inputs (test helper)."""
+from __future__ import annotations
+
+import json
+import os
+from dataclasses import dataclass
+from typing import List, Optional
+
+import numpy as np
+
+from cafe5_gb300.inputs import ErrorModel, RootPrior
+from cafe5_gb300.tree import Tree, lambda_index_of_nodes, parse_newick
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+
+
+def load_json(name):
+    with open(os.path.join(GOLDEN, name)) as f:
+        return json.load(f)
+
+
+def hexf(x):
+    return float.fromhex(x) if x not in (None, "inf", "-inf", "nan") else float(x) if x else None
+
+
+@dataclass
+class Case:
+    name: str
+    tree: Tree
+    lambda_of_node: List[int]
+    lambda_kind: int
+    counts: np.ndarray
+    lambdas: List[float]
+    model: int
+    multipliers: List[float]
+    cat_probs: List[float]
+    prior: np.ndarray
+    err_rows: Optional[np.ndarray]
+    S: int
+    R: int
+    total: float
+    fam_lnl: List[Optional[float]]
+    cat: Optional[list]
+
+
+def prior_from_spec(spec: str, R: int) -> RootPrior:
+    if spec == "uniform":
+        return RootPrior.uniform(R)
+    if spec.startswith("uniform:"):
+        return RootPrior.uniform(int(spec[8:]))
+    if spec.startswith("poisson:"):
+        return RootPrior.poisson(float(spec[8:]), R)
+    if spec.startswith("rootdist:"):
+        rd = {}
+        for tok in spec[9:].split(","):
+            a, b = tok.split("=")
+            rd[int(a)] = int(b)
+        return RootPrior.from_rootdist(rd)
+    raise ValueError(spec)
+
+
+def load_cases() -> List[Case]:
+    out = []
+    for c in load_json("ref_cases.json")["cases"]:
+        tree = parse_newick(c["newick"])
+        assert tree.leaf_names == c["taxa"]
+        lam_idx = [0] * tree.n_nodes
+        kind = 0
+        if c["lambda_newick"]:
+            lam_idx = lambda_index_of_nodes(tree, parse_newick(c["lambda_newick"], lambda_tree=True))
+            kind = 1
+        err = None
+        if c["error_model"]:
+            err = ErrorModel.parse(c["error_model"]).table()
+        prior = prior_from_spec(c["prior"], c["R"]).vector()
+        model = 1 if c["model"] == "gamma" else 0
+        cat = None
+        if c["expected"]["cat"] is not None:
+            cat = c["expected"]["cat"]
+        out.append(Case(
+            name=c["name"], tree=tree, lambda_of_node=lam_idx, lambda_kind=kind,
+            counts=np.asarray(c["counts"], dtype=np.int32).reshape(len(c["ids"]), len(c["taxa"])),
+            lambdas=[hexf(x) for x in c["lambdas"]], model=model,
+            multipliers=[hexf(x) for x in c["multipliers"]] if c["multipliers"] else [1.0],
+            cat_probs=[hexf(x) for x in c["cat_probs"]] if c["cat_probs"] else [1.0],
+            prior=prior, err_rows=err, S=c["S"], R=c["R"],
+            total=float.fromhex(c["expected"]["total_hex"]) if "x" in c["expected"]["total_hex"]
+            else float(c["expected"]["total_hex"]),
+            fam_lnl=[hexf(x) if x is not None else None for x in c["expected"]["fam_lnl_hex"]],
+            cat=cat))
+    return out

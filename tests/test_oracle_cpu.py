@@ -1,0 +1,216 @@
+"""Pins the CPU oracle (oracle/cafe_oracle.c) before anything is checked
+against it:
+
+* the known-answer values of the reference's own unit tests (test.cpp),
+* bit patterns produced by the reference itself, compiled from its own
+  sources (tests/golden/ref_*.json, made by tests/golden/make_golden.py).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from cafe5_gb300.inputs import ErrorModel, RootPrior, discrete_gamma
+from cafe5_gb300.tree import parse_newick
+from golden_cases import load_cases, load_json
+
+KAT = load_json("reference_kats.json")
+CASES = load_cases()
+
+
+def approx5(a, b, rel=1.1920929e-5):
+    """doctest::Approx's default rule (epsilon = 100 * FLT_EPSILON, scale 1):
+    |a - b| < eps * (1 + max(|a|, |b|)). The test.cpp values are printed to
+    5-6 digits, so these checks pin about 5 significant digits; bit-exact
+    parity comes from the reference-generated fixtures below."""
+    return abs(a - b) < rel * (1.0 + max(abs(a), abs(b)))
+
+
+def test_transition_kats():
+    # the test prints 5-6 significant digits (truncated): one unit in the
+    # last printed place
+    for k in KAT["transition"]:
+        assert abs(oracle.transition(k["lambda"], k["t"], k["s"], k["c"]) - k["value"]) <= 1e-5, k
+
+
+def test_cached_matrix_entry_uses_quantized_keys():
+    for k in KAT["cached_matrix_entry"]:
+        m = oracle.fill_matrix(k["lambda"], k["t"], 8)       # quantized lambda / t
+        assert approx5(m[k["s"], k["c"]], k["value"], k["rel"]), k
+    # 68.7105 is computed as 68.710 (matrix_cache.h:49-62)
+    assert oracle.quantize(0.006335, 68.7105) == (0.006335, 68.71)
+
+
+def test_matrix_5x5():
+    k = KAT["matrix_5x5"]
+    m = oracle.fill_matrix(k["lambda"], k["t"], 5)
+    assert np.max(np.abs(m - np.asarray(k["values"]))) < k["abs"]
+
+
+def test_bd_rate_kats():
+    for k in KAT["bd_rate_log"]:
+        assert approx5(math.log(oracle.bd_rate(k["s"], k["c"], k["log_alpha"], k["coeff"])), k["log_value"]), k
+    for k in KAT["bd_rate"]:
+        assert approx5(oracle.bd_rate(k["s"], k["c"], k["log_alpha"], k["coeff"]), k["value"]), k
+
+
+def test_multiply_subrange():
+    k = KAT["multiply"]
+    m = np.asarray(k["matrix"], dtype=np.float64)
+    v = np.asarray(k["v"], dtype=np.float64)
+    out = np.zeros(3)
+    lib = oracle.lib()
+    lib.oracle_multiply(m.ctypes.data, 3, v.ctypes.data, 0, 2, 0, 2, out.ctypes.data)
+    assert out.tolist() == k["result"]
+    big = np.zeros((8, 8))
+    big[3:6, 3:6] = m
+    lib.oracle_multiply(big.ctypes.data, 8, v.ctypes.data, 3, 5, 3, 5, out.ctypes.data)
+    assert out.tolist() == k["result"]
+
+
+def test_saturation():
+    for k in KAT["saturation"]:
+        assert bool(oracle.lib().oracle_is_saturated(k["t"], k["lambda"])) == k["saturated"]
+
+
+def test_cache_key_quantization():
+    k = KAT["cache_key_quantization"]
+    keys = set()
+    lam = 0.0
+    for _ in range(k["n_accumulated"]):
+        lam += k["step"]
+        keys.add((int(lam * 1000000000), int(k["t"] * 1000)))
+    assert len(keys) == k["distinct"]
+    assert (int(k["probe_lambda"] * 1000000000), int(k["t"] * 1000)) in keys
+
+
+def _tree_mats(newick, lam, size):
+    t = parse_newick(newick)
+    ta = oracle.TreeArrays.from_tree(t)
+    mats = [None if t.parent[v] < 0 else oracle.fill_matrix(lam, t.branch_length[v], size) for v in range(t.n_nodes)]
+    return t, ta, mats
+
+
+def test_prune_root_vector_kat():
+    k = KAT["prune_root_log"]
+    t, ta, mats = _tree_mats(k["newick"], k["lambda"] * k["multiplier"], k["matrix_size"])
+    counts = [k["counts"][n] for n in t.leaf_names]
+    root, _ = oracle.prune(ta, counts, mats, k["matrix_size"], k["S"], k["R"])
+    for a, b in zip(np.log(root), k["log_expected"]):
+        assert approx5(a, b), (a, b)
+    k = KAT["root_vector_log"]
+    t, ta, mats = _tree_mats(k["newick"], k["lambda"], k["matrix_size"])
+    root, _ = oracle.prune(ta, [k["counts"][n] for n in t.leaf_names], mats, k["matrix_size"], k["S"], k["R"])
+    for a, b in zip(np.log(root), k["log_expected"]):
+        assert approx5(a, b), (a, b)
+
+
+def test_leaf_vectors_through_identity_branch():
+    """A root with one leaf child on an identity matrix exposes the leaf
+    vector as root[j] = leaf[j + 1] (test.cpp:1685-1727, 1765-1804)."""
+    t = parse_newick("(A:1);")
+    ta = oracle.TreeArrays.from_tree(t)
+    eye = np.eye(22)
+    mats = [None if t.parent[v] < 0 else eye for v in range(t.n_nodes)]
+    k = KAT["leaf_error_model"]
+    em = ErrorModel()
+    for i, r in enumerate(k["rows"]):
+        em.set_probabilities(i, r)
+    root, _ = oracle.prune(ta, [k["count"]], mats, 22, k["S"], k["S"], err_rows=em.table())
+    assert root.tolist() == k["expected"][1:k["S"] + 1]
+    kk = KAT["leaf_one_hot"]
+    root, _ = oracle.prune(ta, [kk["B"]], mats, 22, kk["S"], kk["S"])
+    assert root.tolist() == [1.0 if j + 1 == kk["B"] else 0.0 for j in range(kk["S"])]
+
+
+def test_base_total_kat():
+    k = KAT["base_total"]
+    t = parse_newick(k["newick"])
+    ta = oracle.TreeArrays.from_tree(t)
+    prior = RootPrior.uniform(k["prior_uniform"]).vector()
+    tot, fam, _ = oracle.score(ta, np.asarray(k["counts"]), [k["lambda"]], prior=prior, S=k["S"], R=k["R"])
+    assert approx5(tot, k["neg_lnl"])
+
+
+def test_gamma_kats():
+    k = KAT["gamma_prune"]
+    t = parse_newick(k["newick"])
+    ta = oracle.TreeArrays.from_tree(t)
+    prior = RootPrior.from_rootdist({int(a): b for a, b in k["rootdist"].items()}).vector()
+    tot, fam, cat = oracle.score(ta, np.asarray(k["counts"]), [k["lambda"]], model=1,
+                                 multipliers=k["multipliers"], cat_probs=k["cat_probs"], prior=prior, S=k["S"],
+                                 R=k["R"])
+    assert approx5(cat[0, 0], k["log_cat"][0]) and approx5(cat[0, 1], k["log_cat"][1])
+    k = KAT["gamma_saturated"]
+    tot, _, _ = oracle.score(ta, np.asarray(k["counts"]), [k["lambda"]], model=1, multipliers=k["multipliers"],
+                             cat_probs=k["cat_probs"], prior=RootPrior.uniform(100).vector(), S=k["S"], R=k["R"])
+    assert tot == math.inf
+
+
+def test_reference_matrices_bit_exact():
+    d = load_json("ref_matrices.json")
+    for m in d["matrices"]:
+        ours = oracle.fill_matrix(m["lambda"], m["t"], m["size"])
+        ref = np.array([[float.fromhex(x) for x in row] for row in m["hex"]])
+        assert np.array_equal(ours, ref), (m["lambda"], m["t"])
+
+
+def test_discrete_gamma_matches_reference():
+    d = load_json("ref_matrices.json")
+    for g in d["gamma"]:
+        probs, mult = discrete_gamma(g["alpha"], g["K"])
+        ref = [float.fromhex(x) for x in g["multipliers"]]
+        assert np.allclose(mult, ref, rtol=2e-6, atol=0), (g["K"], g["alpha"])
+        assert probs == [float.fromhex(x) for x in g["probs"]]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c.name for c in CASES])
+def test_oracle_matches_reference_end_to_end(case):
+    ta = oracle.TreeArrays.from_tree(case.tree, case.lambda_of_node)
+    tot, fam, cat = oracle.score(ta, case.counts, case.lambdas, lambda_kind=case.lambda_kind, model=case.model,
+                                 multipliers=case.multipliers, cat_probs=case.cat_probs, prior=case.prior,
+                                 err_rows=case.err_rows, S=case.S, R=case.R)
+    if math.isinf(case.total):
+        assert tot == case.total
+        return
+    assert tot == case.total, (tot, case.total)          # bit-exact
+    if case.model == 0:
+        for a, b in zip(fam, case.fam_lnl):
+            assert a == b
+    else:
+        for f, cats in enumerate(case.cat):
+            lh = sum(float.fromhex(c["cat_lh"]) for c in cats)
+            assert math.log(float.fromhex(cats[0]["fam_lh"])) == fam[f]
+            for k, c in enumerate(cats):
+                assert cat[f, k] == math.log(float.fromhex(c["cat_lh"]))
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if not math.isinf(c.total)][:6], ids=lambda c: c.name)
+def test_scaled_oracle_agrees_where_reference_is_finite(case):
+    ta = oracle.TreeArrays.from_tree(case.tree, case.lambda_of_node)
+    tot, fam, _ = oracle.score(ta, case.counts, case.lambdas, lambda_kind=case.lambda_kind, model=case.model,
+                               multipliers=case.multipliers, cat_probs=case.cat_probs, prior=case.prior,
+                               err_rows=case.err_rows, S=case.S, R=case.R, scaled=True)
+    assert abs(tot - case.total) <= 1e-12 * abs(case.total)
+
+
+def test_scaled_oracle_is_finite_where_reference_underflows():
+    case = [c for c in CASES if c.name == "syn_base_underflow"][0]
+    assert math.isinf(case.total) and math.isinf(case.fam_lnl[0]) and math.isfinite(case.fam_lnl[1])
+    ta = oracle.TreeArrays.from_tree(case.tree, case.lambda_of_node)
+    tot, fam, _ = oracle.score(ta, case.counts, case.lambdas, prior=case.prior, S=case.S, R=case.R, scaled=True)
+    assert math.isfinite(tot) and np.all(np.isfinite(fam))
+    assert fam[1] == case.fam_lnl[1]
+
+
+def test_saturated_category_is_rejected_by_both():
+    """K=8 at lambda 0.003: the largest category saturates on the longest
+    branch, so the reference returns +inf (gamma_core.cpp:151-152, 216-225)
+    and so does the rescaled oracle."""
+    case = [c for c in CASES if c.name == "syn_gamma_24taxa_k8_small_cat"][0]
+    assert math.isinf(case.total)
+    ta = oracle.TreeArrays.from_tree(case.tree, case.lambda_of_node)
+    tot, _, _ = oracle.score(ta, case.counts, case.lambdas, model=1, multipliers=case.multipliers,
+                             cat_probs=case.cat_probs, prior=case.prior, S=case.S, R=case.R, scaled=True)
+    assert tot == math.inf
