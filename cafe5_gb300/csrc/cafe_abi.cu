@@ -1,0 +1,1063 @@
+// C ABI and host runtime of the GB300 CAFE5 likelihood path.
+//
+// Mirrors what the reference does around its hot path, in one process on
+// one GPU:
+//   matrix_cache::precalculate_matrices / get_matrix / is_saturated
+//     (src/matrix_cache.cpp:88-163)    -> device-resident matrix cache + K1
+//   base_model / gamma_model ::infer_family_likelihoods
+//     (src/base_model.cpp:53-100, src/gamma_core.cpp:168-237)
+//                                        -> cafe_score: K1 + K3/K4 + finish
+// and adds the batch-level boundary, S-binning and a serving loop.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <numeric>
+
+#include "runtime.h"
+
+using namespace cafe;
+
+namespace cafe {
+
+const int kDefaultBins[] = {32, 64, 96, 128, 192, 256, 384, 512, 768, 1024};
+const int kNumDefaultBins = sizeof(kDefaultBins) / sizeof(int);
+
+DevBuf::~DevBuf() {
+    if (p) cudaFree(p);
+}
+cudaError_t DevBuf::reserve(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    size_t want = std::max<size_t>(n, 256);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        cudaGetLastError();
+        return e;
+    }
+    bytes = want;
+    return cudaSuccess;
+}
+PinnedBuf::~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+}
+cudaError_t PinnedBuf::reserve(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    size_t want = std::max<size_t>(n * 2, 4096);
+    cudaError_t e = cudaMallocHost(&p, want);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        cudaGetLastError();
+        return e;
+    }
+    bytes = want;
+    return cudaSuccess;
+}
+Workspace::~Workspace() {
+    if (stream) cudaStreamDestroy(stream);
+    if (ev_start) cudaEventDestroy(ev_start);
+    if (ev_stop) cudaEventDestroy(ev_stop);
+}
+int Workspace::init(int device) {
+    (void)device;
+    if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return CAFE_ERR_CUDA;
+    if (cudaEventCreate(&ev_start) != cudaSuccess) return CAFE_ERR_CUDA;
+    if (cudaEventCreate(&ev_stop) != cudaSuccess) return CAFE_ERR_CUDA;
+    return CAFE_OK;
+}
+
+cudaError_t launch_fill(double* p, int64_t n, double v, cudaStream_t s);
+cudaError_t launch_fill_i32(int32_t* p, int64_t n, int32_t v, cudaStream_t s);
+
+}  // namespace cafe
+
+namespace {
+
+int fail(cafe_ctx* C, int code, const char* fmt, ...) {
+    if (C) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        C->last_error = buf;
+    }
+    return code;
+}
+
+int cuda_fail(cafe_ctx* C, cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation) return fail(C, CAFE_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+    return fail(C, CAFE_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                                        \
+    do {                                                      \
+        cudaError_t _e = (expr);                              \
+        if (_e != cudaSuccess) return cuda_fail(C, _e, what); \
+    } while (0)
+
+// Post-order of internal nodes, children with the larger slot need first
+// (Sethi-Ullman), and greedy slot reuse.
+void build_plan(TreeHost& T) {
+    const int n = T.n_nodes;
+    std::vector<int> need(n, 0);
+    std::function<int(int)> rec_need = [&](int v) -> int {
+        if (T.children[v].empty()) return need[v] = 0;
+        std::vector<int> cn;
+        for (int c : T.children[v]) cn.push_back(rec_need(c));
+        std::sort(cn.begin(), cn.end(), std::greater<int>());
+        int m = 0;
+        for (size_t i = 0; i < cn.size(); ++i) m = std::max(m, cn[i] + (int)i);
+        int held = 0;
+        for (int c : T.children[v]) held += T.children[c].empty() ? 0 : 1;
+        return need[v] = std::max(m, held + 1);
+    };
+    rec_need(T.root);
+    std::vector<int> order;
+    std::function<void(int)> visit = [&](int v) {
+        if (T.children[v].empty()) return;
+        std::vector<int> cs = T.children[v];
+        std::stable_sort(cs.begin(), cs.end(), [&](int a, int b) { return need[a] > need[b]; });
+        for (int c : cs) visit(c);
+        order.push_back(v);
+    };
+    visit(T.root);
+    T.internal.assign(order.begin(), order.end());
+    T.cstart.assign(1, 0);
+    T.child.clear();
+    T.slot.assign(n, -1);
+    T.max_children = 0;
+    std::vector<int> free_slots;
+    int n_slots = 0;
+    for (int v : order) {
+        for (int c : T.children[v]) T.child.push_back(c);   // product order: descendant order
+        T.cstart.push_back((int)T.child.size());
+        T.max_children = std::max<int>(T.max_children, (int)T.children[v].size());
+        int s;
+        if (!free_slots.empty()) {
+            auto it = std::min_element(free_slots.begin(), free_slots.end());
+            s = *it;
+            free_slots.erase(it);
+        } else {
+            s = n_slots++;
+        }
+        T.slot[v] = s;
+        for (int c : T.children[v])
+            if (!T.children[c].empty()) free_slots.push_back(T.slot[c]);
+    }
+    T.n_slots = n_slots;
+}
+
+int upload_plan(cafe_ctx* C, TreeHost& T) {
+    const int ni = (int)T.internal.size();
+    std::vector<int32_t> blob;
+    auto put = [&](const std::vector<int32_t>& v) {
+        size_t off = blob.size();
+        blob.insert(blob.end(), v.begin(), v.end());
+        return off;
+    };
+    size_t o_int = put(T.internal), o_cs = put(T.cstart), o_ch = put(T.child), o_lc = put(T.leaf_col),
+           o_sl = put(T.slot);
+    CK(T.d_plan.reserve(blob.size() * sizeof(int32_t)), "tree plan");
+    CK(cudaMemcpy(T.d_plan.p, blob.data(), blob.size() * sizeof(int32_t), cudaMemcpyHostToDevice), "tree plan");
+    const int32_t* b = T.d_plan.as<int32_t>();
+    T.plan.n_nodes = T.n_nodes;
+    T.plan.n_internal = ni;
+    T.plan.n_leaves = T.n_leaves;
+    T.plan.root = T.root;
+    T.plan.n_slots = T.n_slots;
+    T.plan.max_children = T.max_children;
+    T.plan.internal = b + o_int;
+    T.plan.cstart = b + o_cs;
+    T.plan.child = b + o_ch;
+    T.plan.leaf_col = b + o_lc;
+    T.plan.slot = b + o_sl;
+    return CAFE_OK;
+}
+
+int compute_bins(cafe_ctx* C, FamSet& S) {
+    BinPlan& B = S.bins;
+    const int64_t F = S.F;
+    std::vector<int> wf(F), rf(F);
+    for (int64_t f = 0; f < F; ++f) {
+        const int mx = S.max_count[f];
+        const int need = (int)std::ceil(1.2 * mx) + 20 + 1;
+        int w = kDefaultBins[kNumDefaultBins - 1];
+        for (int i = 0; i < kNumDefaultBins; ++i)
+            if (kDefaultBins[i] >= need) {
+                w = kDefaultBins[i];
+                break;
+            }
+        wf[f] = w;
+        const int Sf = w - 1;
+        rf[f] = std::min(Sf, std::max(30, (int)std::rint(mx * 1.25)));
+    }
+    std::vector<int64_t> perm(F);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::stable_sort(perm.begin(), perm.end(), [&](int64_t a, int64_t b) { return wf[a] < wf[b]; });
+    B.widths.clear();
+    B.bin_first.clear();
+    B.bin_count.clear();
+    B.W_max = 0;
+    for (int64_t i = 0; i < F; ++i) {
+        const int w = wf[perm[i]];
+        if (B.widths.empty() || B.widths.back() != w) {
+            B.widths.push_back(w);
+            B.bin_first.push_back(i);
+            B.bin_count.push_back(0);
+        }
+        B.bin_count.back()++;
+        B.W_max = std::max(B.W_max, w);
+    }
+    std::vector<int32_t> rf32(rf.begin(), rf.end());
+    CK(B.d_perm.reserve(std::max<int64_t>(F, 1) * sizeof(int64_t)), "bins");
+    CK(B.d_famR.reserve(std::max<int64_t>(F, 1) * sizeof(int32_t)), "bins");
+    if (F) {
+        CK(cudaMemcpy(B.d_perm.p, perm.data(), F * sizeof(int64_t), cudaMemcpyHostToDevice), "bins");
+        CK(cudaMemcpy(B.d_famR.p, rf32.data(), F * sizeof(int32_t), cudaMemcpyHostToDevice), "bins");
+    }
+    return CAFE_OK;
+}
+
+int prepare_set(cafe_ctx* C, FamSet& S) {
+    const int64_t F = S.F;
+    const int nl = S.n_leaves;
+    S.max_count.assign(F, 0);
+    for (int64_t f = 0; f < F; ++f) {
+        int m = 0;
+        for (int c = 0; c < nl; ++c) m = std::max(m, S.h_counts[f * nl + c]);
+        S.max_count[f] = m;
+    }
+    // dedupe (build_reference_list, src/base_model.cpp:27-51), hashed
+    std::vector<int64_t> ref(F);
+    std::unordered_map<uint64_t, std::vector<int64_t>> buckets;
+    S.unique.clear();
+    for (int64_t f = 0; f < F; ++f) {
+        const int32_t* row = &S.h_counts[f * nl];
+        uint64_t h = 1469598103934665603ull;
+        for (int c = 0; c < nl; ++c) h = (h ^ (uint32_t)row[c]) * 1099511628211ull;
+        auto& b = buckets[h];
+        int64_t found = -1;
+        for (int64_t g : b)
+            if (std::memcmp(&S.h_counts[g * nl], row, sizeof(int32_t) * nl) == 0) {
+                found = g;
+                break;
+            }
+        if (found < 0) {
+            b.push_back(f);
+            S.unique.push_back(f);
+            ref[f] = f;
+        } else {
+            ref[f] = found;
+        }
+    }
+    std::vector<int64_t> ident(F);
+    std::iota(ident.begin(), ident.end(), 0);
+    const size_t nb = std::max<int64_t>(F, 1) * sizeof(int64_t);
+    CK(S.d_ref.reserve(nb), "families");
+    CK(S.d_identity.reserve(nb), "families");
+    CK(S.d_unique.reserve(nb), "families");
+    if (F) {
+        CK(cudaMemcpy(S.d_ref.p, ref.data(), F * sizeof(int64_t), cudaMemcpyHostToDevice), "families");
+        CK(cudaMemcpy(S.d_identity.p, ident.data(), F * sizeof(int64_t), cudaMemcpyHostToDevice), "families");
+        CK(cudaMemcpy(S.d_unique.p, S.unique.data(), S.unique.size() * sizeof(int64_t), cudaMemcpyHostToDevice),
+           "families");
+    }
+    return compute_bins(C, S);
+}
+
+// Matrix cache: look up or schedule (size, lambda, t). Caller holds C->mu.
+struct PendingJobs {
+    std::vector<MatKey> keys;
+    std::vector<double> lam, t;
+};
+
+double* cache_lookup(cafe_ctx* C, const MatKey& k) {
+    auto it = C->cache.find(k);
+    return it == C->cache.end() ? nullptr : it->second.d;
+}
+
+// Allocate and enqueue K1 for the pending keys on `ws`.
+int cache_build(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
+    const size_t n = P.keys.size();
+    if (!n) return CAFE_OK;
+    size_t total = 0;
+    int max_size = 0;
+    for (auto& k : P.keys) {
+        total += (size_t)k.size * k.size * sizeof(double);
+        max_size = std::max(max_size, k.size);
+    }
+    bool idle;
+    {
+        std::lock_guard<std::mutex> lk(C->qmu);
+        idle = C->in_flight == 0 && C->queue.empty();
+    }
+    if (C->cache_cap && C->cache_bytes + total > C->cache_cap && idle) {
+        // over the cap: start a fresh cache (the reference's cache lives for
+        // one evaluation; keeping matrices across calls is only a speed-up)
+        cudaDeviceSynchronize();
+        for (void* p : C->chunks) cudaFree(p);
+        C->chunks.clear();
+        C->cache.clear();
+        C->cache_bytes = 0;
+    }
+    void* chunk = nullptr;
+    CK(cudaMalloc(&chunk, total), "matrix cache");
+    C->chunks.push_back(chunk);
+    C->cache_bytes += total;
+    CK(ws.h_jobs.reserve(n * sizeof(MatrixJob)), "jobs");
+    CK(ws.jobs.reserve(n * sizeof(MatrixJob)), "jobs");
+    MatrixJob* J = ws.h_jobs.as<MatrixJob>();
+    char* cur = static_cast<char*>(chunk);
+    for (size_t i = 0; i < n; ++i) {
+        const MatKey& k = P.keys[i];
+        MatrixJob j{};
+        j.lambda = (double)k.lq / 1000000000.0;
+        j.t = (double)k.tq / 1000.0;
+        j.dst = reinterpret_cast<double*>(cur);
+        j.size = k.size;
+        J[i] = j;
+        MatEntry e;
+        e.d = j.dst;
+        e.chunk = (int)C->chunks.size() - 1;
+        C->cache[k] = e;
+        cur += (size_t)k.size * k.size * sizeof(double);
+    }
+    CK(cudaMemcpyAsync(ws.jobs.p, J, n * sizeof(MatrixJob), cudaMemcpyHostToDevice, ws.stream), "jobs");
+    CK(launch_matrix_build(ws.jobs.as<MatrixJob>(), (int)n, max_size, ws.stream), "matrix build");
+    // the pinned job buffer is reused by the next request on this stream
+    CK(cudaStreamSynchronize(ws.stream), "matrix build");
+    P.keys.clear();
+    return CAFE_OK;
+}
+
+MatKey make_key(int size, double lambda, double t) {
+    MatKey k;
+    k.size = size;
+    k.lq = (long)(lambda * 1000000000);
+    k.tq = (long)(t * 1000);
+    return k;
+}
+
+void schedule(cafe_ctx* C, PendingJobs& P, const MatKey& k) {
+    if (cache_lookup(C, k)) return;
+    for (auto& q : P.keys)
+        if (q == k) return;
+    P.keys.push_back(k);
+}
+
+struct ScoreInfo {
+    int64_t F = 0;
+    int K = 1;
+    bool rejected = false;
+    int reject_status = CAFE_OK;
+    bool scaled = false;
+    size_t footprint = 0;
+};
+
+// Enqueue one evaluation on ws.stream. Caller holds C->mu.
+int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_fam, double* d_total,
+                  ScoreInfo* info) {
+    if (!R) return fail(C, CAFE_ERR_INVALID, "null request");
+    auto ti = C->trees.find(R->tree_id);
+    if (ti == C->trees.end()) return fail(C, CAFE_ERR_NOT_FOUND, "unknown tree id %d", R->tree_id);
+    auto si = C->sets.find(R->set_id);
+    if (si == C->sets.end()) return fail(C, CAFE_ERR_NOT_FOUND, "unknown family set id %d", R->set_id);
+    TreeHost& T = *ti->second;
+    FamSet& S = *si->second;
+    if (S.tree_id != R->tree_id) return fail(C, CAFE_ERR_INVALID, "family set %d belongs to tree %d", R->set_id, S.tree_id);
+    if (R->n_lambdas < 1 || !R->lambdas) return fail(C, CAFE_ERR_INVALID, "no lambdas");
+    for (int v = 0; v < T.n_nodes; ++v)
+        if (T.parent[v] >= 0 && (T.lambda_index[v] < 0 || T.lambda_index[v] >= R->n_lambdas))
+            return fail(C, CAFE_ERR_INVALID, "lambda index %d out of range at node %d", T.lambda_index[v], v);
+    const bool gamma = R->model == CAFE_MODEL_GAMMA;
+    if (R->model != CAFE_MODEL_BASE && !gamma) return fail(C, CAFE_ERR_INVALID, "bad model %d", R->model);
+    const int K = gamma ? R->n_categories : 1;
+    if (gamma && (K < 1 || !R->multipliers || !R->cat_probs)) return fail(C, CAFE_ERR_INVALID, "gamma needs K >= 1");
+    if (C->prior.empty()) return fail(C, CAFE_ERR_INVALID, "no prior set (cafe_prior_set)");
+    if (R->use_error_model && C->err_rows == 0) return fail(C, CAFE_ERR_INVALID, "no error model set");
+    if (R->precision == CAFE_PREC_MIXED_BF16X3) return fail(C, CAFE_ERR_INVALID, "mixed precision path not built");
+    if (R->precision != CAFE_PREC_FP64_REF && R->precision != CAFE_PREC_FP64_BINNED)
+        return fail(C, CAFE_ERR_INVALID, "bad precision %d", R->precision);
+    const int64_t F = S.F;
+    info->F = F;
+    info->K = K;
+
+    // lambda::is_valid (src/lambda.h:58-60, src/lambda.cpp:172-175)
+    bool valid = true;
+    double largest = R->lambdas[0];
+    for (int i = 0; i < R->n_lambdas; ++i) {
+        const double l = R->lambdas[i];
+        if (R->lambda_kind == CAFE_LAMBDA_SINGLE ? !(l > 0) : (l < 0)) valid = false;
+        largest = std::max(largest, l);
+    }
+    bool reject = !valid;
+    // gamma_model::can_infer (src/gamma_core.cpp:123-141)
+    if (!reject && gamma && T.longest_branch > 0) {
+        const double a = largest * T.longest_branch / (1 + largest * T.longest_branch);
+        if ((1 - 2 * a) < 0) reject = true;
+    }
+    if (reject) {
+        info->rejected = true;
+        info->reject_status = valid ? CAFE_ERR_SATURATED : CAFE_OK;
+        if (d_total) CK(launch_fill(d_total, 1, INFINITY, ws.stream), "fill");
+        if (d_fam && F) CK(launch_fill(d_fam, F, NAN, ws.stream), "fill");
+        return CAFE_OK;
+    }
+
+    const bool ref_mode = R->precision == CAFE_PREC_FP64_REF;
+    const bool scaled = !ref_mode;
+    info->scaled = scaled;
+    int Sg = 0, Rg = 0, msize, W;
+    int maxc = 0;
+    for (int64_t f = 0; f < F; ++f) maxc = std::max(maxc, S.max_count[f]);
+    if (ref_mode) {
+        Sg = R->max_family_size;
+        Rg = R->max_root_family_size;
+        if (Sg < 1 || Rg < 1) return fail(C, CAFE_ERR_INVALID, "FP64_REF needs max_family_size and max_root_family_size");
+        if (maxc > Sg) return fail(C, CAFE_ERR_INVALID, "a count (%d) exceeds max_family_size (%d)", maxc, Sg);
+        msize = std::max(Rg, Sg) + 1;   // base_model.cpp:65
+        W = std::max(Sg + 1, Rg);
+    } else {
+        msize = S.bins.W_max;
+        W = S.bins.W_max;
+    }
+
+    // matrices for every (category, non-root node)
+    PendingJobs P;
+    std::vector<MatKey> node_key((size_t)K * T.n_nodes);
+    for (int k = 0; k < K; ++k) {
+        const double m = gamma ? R->multipliers[k] : 1.0;
+        for (int v = 0; v < T.n_nodes; ++v) {
+            if (T.parent[v] < 0) continue;
+            const double lam = R->lambdas[T.lambda_index[v]] * m;
+            const MatKey key = make_key(msize, lam, T.branch_length[v]);
+            node_key[(size_t)k * T.n_nodes + v] = key;
+            schedule(C, P, key);
+        }
+    }
+    int rc = cache_build(C, ws, P);
+    if (rc) return rc;
+    CK(ws.h_mats.reserve((size_t)K * T.n_nodes * sizeof(double*)), "mats");
+    CK(ws.mats.reserve((size_t)K * T.n_nodes * sizeof(double*)), "mats");
+    double** hm = ws.h_mats.as<double*>();
+    for (int k = 0; k < K; ++k)
+        for (int v = 0; v < T.n_nodes; ++v)
+            hm[(size_t)k * T.n_nodes + v] = T.parent[v] < 0 ? nullptr : cache_lookup(C, node_key[(size_t)k * T.n_nodes + v]);
+
+    // tiles
+    std::vector<PruneTile>& tiles = ws.tile_vec;
+    tiles.clear();
+    const int TFm = 32;
+    const int64_t* d_perm;
+    const int32_t* d_famR = nullptr;
+    const bool dedupe = R->dedupe && !gamma && ref_mode;
+    if (ref_mode) {
+        const int64_t nf = dedupe ? (int64_t)S.unique.size() : F;
+        d_perm = dedupe ? S.d_unique.as<int64_t>() : S.d_identity.as<int64_t>();
+        for (int k = 0; k < K; ++k)
+            for (int64_t i = 0; i < nf; i += TFm) {
+                PruneTile t{};
+                t.first = (int)i;
+                t.count = (int)std::min<int64_t>(TFm, nf - i);
+                t.k = k;
+                t.S = Sg;
+                t.R = Rg;
+                tiles.push_back(t);
+            }
+    } else {
+        d_perm = S.bins.d_perm.as<int64_t>();
+        d_famR = S.bins.d_famR.as<int32_t>();
+        for (int k = 0; k < K; ++k)
+            for (size_t b = 0; b < S.bins.widths.size(); ++b)
+                for (int64_t i = 0; i < S.bins.bin_count[b]; i += TFm) {
+                    PruneTile t{};
+                    t.first = (int)(S.bins.bin_first[b] + i);
+                    t.count = (int)std::min<int64_t>(TFm, S.bins.bin_count[b] - i);
+                    t.k = k;
+                    t.S = S.bins.widths[b] - 1;
+                    t.R = S.bins.widths[b] - 1;
+                    tiles.push_back(t);
+                }
+    }
+    const int n_tiles = (int)tiles.size();
+    CK(ws.h_tiles.reserve(std::max(n_tiles, 1) * sizeof(PruneTile)), "tiles");
+    CK(ws.tiles.reserve(std::max(n_tiles, 1) * sizeof(PruneTile)), "tiles");
+    std::memcpy(ws.h_tiles.p, tiles.data(), n_tiles * sizeof(PruneTile));
+
+    const int n_ctas = std::max(1, std::min(n_tiles, C->n_ctas));
+    const int64_t per_cta = (int64_t)T.n_slots * W * TFm;
+    CK(ws.scratch.reserve((size_t)n_ctas * per_cta * sizeof(double)), "scratch");
+    CK(ws.cat.reserve((size_t)std::max<int64_t>(F, 1) * K * sizeof(double)), "category buffer");
+    CK(ws.nfail.reserve(sizeof(int32_t)), "fail counter");
+    info->footprint = (size_t)n_ctas * per_cta * sizeof(double) + (size_t)F * K * sizeof(double);
+
+    CK(cudaMemcpyAsync(ws.tiles.p, ws.h_tiles.p, n_tiles * sizeof(PruneTile), cudaMemcpyHostToDevice, ws.stream),
+       "tiles");
+    CK(cudaMemcpyAsync(ws.mats.p, hm, (size_t)K * T.n_nodes * sizeof(double*), cudaMemcpyHostToDevice, ws.stream),
+       "mats");
+    if (gamma && !scaled) CK(launch_fill(ws.cat.as<double>(), F * K, 0.0, ws.stream), "fill");
+
+    Prune64Args a{};
+    a.plan = T.plan;
+    a.tiles = ws.tiles.as<PruneTile>();
+    a.n_tiles = n_tiles;
+    a.counts = S.d_counts.as<int32_t>();
+    a.perm = d_perm;
+    a.mats = ws.mats.as<const double*>();
+    a.ld_mat = msize;
+    a.prior = C->d_prior.as<double>();
+    a.n_prior = (int)C->prior.size();
+    a.err = R->use_error_model ? C->d_err.as<double>() : nullptr;
+    a.err_rows = C->err_rows;
+    a.err_ndev = C->err_ndev;
+    a.fam_R = d_famR;
+    a.scratch = ws.scratch.as<double>();
+    a.scratch_per_cta = per_cta;
+    a.scaled = scaled ? 1 : 0;
+    a.model = gamma ? 1 : 0;
+    a.out = ws.cat.as<double>();
+    a.K = K;
+    a.cat_probs = nullptr;
+    if (gamma) {
+        CK(ws.h_catp.reserve((size_t)K * sizeof(double)), "cat probs");
+        CK(ws.catp.reserve((size_t)K * sizeof(double)), "cat probs");
+        std::memcpy(ws.h_catp.p, R->cat_probs, K * sizeof(double));
+        CK(cudaMemcpyAsync(ws.catp.p, ws.h_catp.p, K * sizeof(double), cudaMemcpyHostToDevice, ws.stream), "cat probs");
+        a.cat_probs = ws.catp.as<double>();
+    }
+    a.tile_families = TFm;
+    a.W = W;
+    CK(launch_prune64(a, n_ctas, ws.stream), "prune");
+
+    FinishArgs fa{};
+    fa.F = F;
+    fa.K = K;
+    fa.model = gamma ? 1 : 0;
+    fa.scaled = scaled ? 1 : 0;
+    fa.cat = ws.cat.as<double>();
+    fa.ref = dedupe ? S.d_ref.as<int64_t>() : nullptr;
+    fa.family_lnl = d_fam;
+    fa.total = d_total;
+    fa.n_failed = ws.nfail.as<int32_t>();
+    CK(launch_finish(fa, ws.stream), "finish");
+    return CAFE_OK;
+}
+
+// Phase 1 of a host-visible score: enqueue the evaluation and the copies
+// back into pinned staging (caller holds C->mu).
+int score_enqueue(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_result* res, ScoreInfo* info) {
+    auto si = C->sets.find(R ? R->set_id : -1);
+    if (si == C->sets.end()) return fail(C, CAFE_ERR_NOT_FOUND, "unknown family set");
+    const int64_t F = si->second->F;
+    CK(ws.fam_lnl.reserve(std::max<int64_t>(F, 1) * sizeof(double)), "family buffer");
+    CK(ws.total.reserve(sizeof(double)), "total");
+    CK(cudaEventRecord(ws.ev_start, ws.stream), "event");
+    int rc = enqueue_score(C, ws, R, ws.fam_lnl.as<double>(), ws.total.as<double>(), info);
+    if (rc) return rc;
+    CK(cudaEventRecord(ws.ev_stop, ws.stream), "event");
+    const int K = info->K;
+    const size_t out_bytes = sizeof(double) + sizeof(int32_t) + (size_t)F * sizeof(double) +
+                             (res && res->category_lnl ? (size_t)F * K * sizeof(double) : 0);
+    CK(ws.h_out.reserve(out_bytes + 64), "host staging");
+    char* h = static_cast<char*>(ws.h_out.p);
+    double* h_total = reinterpret_cast<double*>(h);
+    int32_t* h_fail = reinterpret_cast<int32_t*>(h + 8);
+    double* h_fam = reinterpret_cast<double*>(h + 16);
+    double* h_cat = h_fam + F;
+    CK(cudaMemcpyAsync(h_total, ws.total.p, sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");
+    if (!info->rejected) CK(cudaMemcpyAsync(h_fail, ws.nfail.p, sizeof(int32_t), cudaMemcpyDeviceToHost, ws.stream), "d2h");
+    else *h_fail = 0;
+    if (F) CK(cudaMemcpyAsync(h_fam, ws.fam_lnl.p, F * sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");
+    const bool want_cat = res && res->category_lnl && !info->rejected;
+    if (want_cat && F)
+        CK(cudaMemcpyAsync(h_cat, ws.cat.p, (size_t)F * K * sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");
+    return CAFE_OK;
+}
+
+// Phase 2: wait for the stream and fill the result (no context lock needed:
+// the workspace belongs to the caller).
+int score_complete(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_result* res, const ScoreInfo& info) {
+    CK(cudaStreamSynchronize(ws.stream), "score");
+    if (!res) return CAFE_OK;
+    const int64_t F = info.F;
+    const int K = info.K;
+    char* h = static_cast<char*>(ws.h_out.p);
+    double* h_total = reinterpret_cast<double*>(h);
+    int32_t* h_fail = reinterpret_cast<int32_t*>(h + 8);
+    double* h_fam = reinterpret_cast<double*>(h + 16);
+    double* h_cat = h_fam + F;
+    const bool want_cat = res->category_lnl && !info.rejected;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ws.ev_start, ws.ev_stop);
+    res->device_ms = ms;
+    res->total_neg_lnl = *h_total;
+    res->n_failed = info.rejected ? 0 : *h_fail;
+    res->n_fallback = 0;
+    if (res->family_lnl && F) std::memcpy(res->family_lnl, h_fam, F * sizeof(double));
+    if (res->category_lnl && F) {
+        const bool gamma = R->model == CAFE_MODEL_GAMMA;
+        for (int64_t f = 0; f < F; ++f)
+            for (int k = 0; k < K; ++k) {
+                double v = NAN;
+                if (want_cat && gamma) {
+                    const double c = h_cat[f * K + k];
+                    v = info.scaled ? c : (c < 0 ? NAN : std::log(c));
+                } else if (want_cat) {
+                    v = h_fam[f];
+                }
+                res->category_lnl[f * K + k] = v;
+            }
+    }
+    if (info.rejected) res->status = info.reject_status;
+    else if (res->n_failed) res->status = CAFE_ERR_SATURATED;
+    else if (std::isinf(res->total_neg_lnl)) res->status = CAFE_ERR_UNDERFLOW;
+    else res->status = CAFE_OK;
+    return CAFE_OK;
+}
+
+int score_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_result* res) {
+    ScoreInfo info;
+    int rc = score_enqueue(C, ws, R, res, &info);
+    if (rc) return rc;
+    return score_complete(C, ws, R, res, info);
+}
+
+}  // namespace
+
+// ===================================================================== ABI
+
+extern "C" {
+
+int cafe_version(void) { return 1; }
+
+const char* cafe_status_string(int s) {
+    switch (s) {
+        case CAFE_OK: return "ok";
+        case CAFE_ERR_OOM: return "out of device memory";
+        case CAFE_ERR_MISSING_MATRIX: return "missing matrix";
+        case CAFE_ERR_SATURATED: return "saturated";
+        case CAFE_ERR_UNDERFLOW: return "underflow";
+        case CAFE_ERR_TIMEOUT: return "timeout";
+        case CAFE_ERR_INVALID: return "invalid argument";
+        case CAFE_ERR_CUDA: return "CUDA error";
+        case CAFE_ERR_BUSY: return "busy";
+        case CAFE_ERR_NOT_FOUND: return "not found";
+        default: return "unknown status";
+    }
+}
+
+const char* cafe_last_error(const cafe_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+int cafe_is_saturated(double branch_length, double lambda) {
+    const double alpha = lambda * branch_length / (1 + lambda * branch_length);
+    return (1 - 2 * alpha) < 0;
+}
+
+int cafe_ctx_create(const cafe_config* cfg, cafe_ctx** out) {
+    if (!out) return CAFE_ERR_INVALID;
+    *out = nullptr;
+    int dev = cfg ? cfg->device : 0;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return CAFE_ERR_CUDA;
+    }
+    if (dev < 0 || dev >= n) return CAFE_ERR_INVALID;
+    if (cudaSetDevice(dev) != cudaSuccess) return CAFE_ERR_CUDA;
+    auto* C = new cafe_ctx();
+    C->device = dev;
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, dev);
+    C->sm_count = prop.multiProcessorCount;
+    C->n_ctas = prop.multiProcessorCount * 4;
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    C->cache_cap = (cfg && cfg->matrix_cache_bytes) ? cfg->matrix_cache_bytes : fr / 4;
+    const int n_streams = (cfg && cfg->n_streams > 0) ? cfg->n_streams : 4;
+    for (int i = 0; i <= n_streams; ++i) {
+        auto w = std::make_unique<Workspace>();
+        if (w->init(dev) != CAFE_OK) {
+            delete C;
+            return CAFE_ERR_CUDA;
+        }
+        C->ws.push_back(std::move(w));
+    }
+    *out = C;
+    return CAFE_OK;
+}
+
+void cafe_serving_stop(cafe_ctx* C);
+
+int cafe_ctx_destroy(cafe_ctx* C) {
+    if (!C) return CAFE_ERR_INVALID;
+    cudaSetDevice(C->device);
+    cafe_serving_stop(C);
+    cudaDeviceSynchronize();
+    for (void* p : C->chunks) cudaFree(p);
+    C->chunks.clear();
+    delete C;
+    return CAFE_OK;
+}
+
+int cafe_tree_upload(cafe_ctx* C, int n_nodes, const int32_t* parent, const double* branch_length,
+                     const int32_t* lambda_index, int* tree_id) {
+    if (!C || !parent || !branch_length || !tree_id || n_nodes < 2 || n_nodes > kMaxNodes)
+        return fail(C, CAFE_ERR_INVALID, "bad tree arguments (n_nodes %d)", n_nodes);
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    auto T = std::make_unique<TreeHost>();
+    T->n_nodes = n_nodes;
+    T->parent.assign(parent, parent + n_nodes);
+    T->branch_length.assign(branch_length, branch_length + n_nodes);
+    T->lambda_index.assign(n_nodes, 0);
+    if (lambda_index) T->lambda_index.assign(lambda_index, lambda_index + n_nodes);
+    T->children.assign(n_nodes, {});
+    int roots = 0;
+    for (int i = 0; i < n_nodes; ++i) {
+        const int p = parent[i];
+        if (p < 0) {
+            roots++;
+            T->root = i;
+        } else if (p >= n_nodes || p == i) {
+            return fail(C, CAFE_ERR_INVALID, "bad parent %d of node %d", p, i);
+        } else {
+            T->children[p].push_back(i);
+        }
+    }
+    if (roots != 1) return fail(C, CAFE_ERR_INVALID, "tree needs exactly one root (got %d)", roots);
+    // reject cycles: every node must reach the root
+    for (int i = 0; i < n_nodes; ++i) {
+        int v = i, steps = 0;
+        while (parent[v] >= 0 && steps <= n_nodes) {
+            v = parent[v];
+            steps++;
+        }
+        if (steps > n_nodes) return fail(C, CAFE_ERR_INVALID, "cycle through node %d", i);
+    }
+    T->leaf_col.assign(n_nodes, -1);
+    for (int i = 0; i < n_nodes; ++i)
+        if (T->children[i].empty()) T->leaf_col[i] = T->n_leaves++;
+    for (int i = 0; i < n_nodes; ++i) {
+        if (i != T->root && !(branch_length[i] > 0))
+            return fail(C, CAFE_ERR_INVALID, "branch length of node %d must be > 0", i);
+        if (branch_length[i] > 0) {
+            T->longest_branch = std::max(T->longest_branch, branch_length[i]);
+            T->distinct_lengths.push_back(branch_length[i]);
+        }
+    }
+    std::sort(T->distinct_lengths.begin(), T->distinct_lengths.end());
+    T->distinct_lengths.erase(std::unique(T->distinct_lengths.begin(), T->distinct_lengths.end()),
+                              T->distinct_lengths.end());
+    if (T->n_leaves == n_nodes || T->root < 0) return fail(C, CAFE_ERR_INVALID, "tree has no internal node");
+    build_plan(*T);
+    int rc = upload_plan(C, *T);
+    if (rc) return rc;
+    *tree_id = C->next_tree++;
+    C->trees[*tree_id] = std::move(T);
+    return CAFE_OK;
+}
+
+int cafe_families_upload(cafe_ctx* C, int tree_id, const int32_t* counts, int64_t n_families, int n_leaves,
+                         int* set_id) {
+    if (!C || !set_id || n_families < 0 || (n_families > 0 && !counts)) return fail(C, CAFE_ERR_INVALID, "bad family arguments");
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    auto ti = C->trees.find(tree_id);
+    if (ti == C->trees.end()) return fail(C, CAFE_ERR_NOT_FOUND, "unknown tree id %d", tree_id);
+    if (n_leaves != ti->second->n_leaves)
+        return fail(C, CAFE_ERR_INVALID, "tree has %d leaves, counts have %d columns", ti->second->n_leaves, n_leaves);
+    for (int64_t i = 0; i < n_families * n_leaves; ++i)
+        if (counts[i] < 0) return fail(C, CAFE_ERR_INVALID, "negative count at %lld", (long long)i);
+    auto S = std::make_unique<FamSet>();
+    S->tree_id = tree_id;
+    S->F = n_families;
+    S->n_leaves = n_leaves;
+    S->h_counts.assign(counts, counts + n_families * n_leaves);
+    const size_t bytes = std::max<size_t>((size_t)n_families * n_leaves * sizeof(int32_t), 4);
+    CK(S->d_counts.reserve(bytes), "counts");
+    if (n_families) CK(cudaMemcpy(S->d_counts.p, counts, (size_t)n_families * n_leaves * sizeof(int32_t), cudaMemcpyHostToDevice), "counts");
+    int rc = prepare_set(C, *S);
+    if (rc) return rc;
+    *set_id = C->next_set++;
+    C->sets[*set_id] = std::move(S);
+    return CAFE_OK;
+}
+
+int cafe_families_update(cafe_ctx* C, int set_id, const int32_t* counts) {
+    if (!C) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    auto si = C->sets.find(set_id);
+    if (si == C->sets.end()) return fail(C, CAFE_ERR_NOT_FOUND, "unknown family set id %d", set_id);
+    FamSet& S = *si->second;
+    const size_t n = (size_t)S.F * S.n_leaves;
+    for (size_t i = 0; i < n; ++i)
+        if (counts[i] < 0) return fail(C, CAFE_ERR_INVALID, "negative count");
+    S.h_counts.assign(counts, counts + n);
+    Workspace& ws = *C->ws[0];
+    CK(cudaMemcpyAsync(S.d_counts.p, counts, n * sizeof(int32_t), cudaMemcpyHostToDevice, ws.stream), "counts");
+    CK(cudaStreamSynchronize(ws.stream), "counts");
+    return prepare_set(C, S);
+}
+
+int cafe_families_free(cafe_ctx* C, int set_id) {
+    if (!C) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    cudaDeviceSynchronize();
+    if (!C->sets.erase(set_id)) return fail(C, CAFE_ERR_NOT_FOUND, "unknown family set id %d", set_id);
+    return CAFE_OK;
+}
+
+int cafe_prior_set(cafe_ctx* C, const double* prior, int n) {
+    if (!C || n < 1 || !prior) return fail(C, CAFE_ERR_INVALID, "bad prior");
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    cudaDeviceSynchronize();
+    C->prior.assign(prior, prior + n);
+    CK(C->d_prior.reserve(n * sizeof(double)), "prior");
+    CK(cudaMemcpy(C->d_prior.p, prior, n * sizeof(double), cudaMemcpyHostToDevice), "prior");
+    return CAFE_OK;
+}
+
+int cafe_error_model_set(cafe_ctx* C, const double* rows, int n_rows, int n_dev) {
+    if (!C || n_rows < 0 || (n_rows > 0 && (!rows || n_dev < 1 || n_dev % 2 == 0)))
+        return fail(C, CAFE_ERR_INVALID, "bad error model (n_dev must be odd)");
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    cudaDeviceSynchronize();
+    C->err.assign(rows, rows + (size_t)n_rows * n_dev);
+    C->err_rows = n_rows;
+    C->err_ndev = n_rows ? n_dev : 0;
+    if (n_rows) {
+        CK(C->d_err.reserve((size_t)n_rows * n_dev * sizeof(double)), "error model");
+        CK(cudaMemcpy(C->d_err.p, rows, (size_t)n_rows * n_dev * sizeof(double), cudaMemcpyHostToDevice), "error model");
+    }
+    return CAFE_OK;
+}
+
+int cafe_matrices_build(cafe_ctx* C, const double* lambdas, int n_lambdas, const double* branch_lengths,
+                        int n_t, int matrix_size) {
+    if (!C || n_lambdas < 0 || n_t < 0 || matrix_size < 1 || (n_lambdas && !lambdas) || (n_t && !branch_lengths))
+        return fail(C, CAFE_ERR_INVALID, "bad matrix build arguments");
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    PendingJobs P;
+    for (int i = 0; i < n_lambdas; ++i)
+        for (int j = 0; j < n_t; ++j) schedule(C, P, make_key(matrix_size, lambdas[i], branch_lengths[j]));
+    Workspace& ws = *C->ws[0];
+    int rc = cache_build(C, ws, P);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ws.stream), "matrix build");
+    return CAFE_OK;
+}
+
+int cafe_matrix_get(cafe_ctx* C, double lambda, double branch_length, int matrix_size, double* out) {
+    if (!C || !out || matrix_size < 1) return fail(C, CAFE_ERR_INVALID, "bad matrix_get arguments");
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    double* d = cache_lookup(C, make_key(matrix_size, lambda, branch_length));
+    if (!d)
+        return fail(C, CAFE_ERR_MISSING_MATRIX, "Failed to find matrix for %d,%g,%g", matrix_size, branch_length, lambda);
+    CK(cudaMemcpy(out, d, (size_t)matrix_size * matrix_size * sizeof(double), cudaMemcpyDeviceToHost), "matrix_get");
+    return CAFE_OK;
+}
+
+int cafe_matrix_cache_size(cafe_ctx* C, int64_t* n) {
+    if (!C || !n) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->mu);
+    *n = (int64_t)C->cache.size();
+    return CAFE_OK;
+}
+
+int cafe_matrix_cache_clear(cafe_ctx* C) {
+    if (!C) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    cudaDeviceSynchronize();
+    for (void* p : C->chunks) cudaFree(p);
+    C->chunks.clear();
+    C->cache.clear();
+    C->cache_bytes = 0;
+    return CAFE_OK;
+}
+
+int cafe_score(cafe_ctx* C, const cafe_request* req, cafe_result* res) {
+    if (!C) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    return score_sync(C, *C->ws[0], req, res);
+}
+
+int cafe_score_device(cafe_ctx* C, const cafe_request* req, double* d_family_lnl, double* d_total, void* stream) {
+    if (!C) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    Workspace& ws = *C->ws[0];
+    cudaStream_t user = static_cast<cudaStream_t>(stream);
+    ScoreInfo info;
+    auto si = C->sets.find(req ? req->set_id : -1);
+    if (si == C->sets.end()) return fail(C, CAFE_ERR_NOT_FOUND, "unknown family set");
+    const int64_t F = si->second->F;
+    CK(ws.fam_lnl.reserve(std::max<int64_t>(F, 1) * sizeof(double)), "family buffer");
+    CK(ws.total.reserve(sizeof(double)), "total");
+    if (user) {
+        // order the workspace stream after the caller's stream, and back
+        CK(cudaEventRecord(ws.ev_start, user), "event");
+        CK(cudaStreamWaitEvent(ws.stream, ws.ev_start, 0), "event");
+    }
+    int rc = enqueue_score(C, ws, req, d_family_lnl ? d_family_lnl : ws.fam_lnl.as<double>(),
+                           d_total ? d_total : ws.total.as<double>(), &info);
+    if (rc) return rc;
+    if (user) {
+        CK(cudaEventRecord(ws.ev_stop, ws.stream), "event");
+        CK(cudaStreamWaitEvent(user, ws.ev_stop, 0), "event");
+    }
+    return CAFE_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------- serving loop
+
+namespace cafe {
+struct Request {
+    cafe_request req{};
+    std::vector<double> lambdas, mult, probs;
+    cafe_result* res = nullptr;
+    int rc = CAFE_OK;
+    bool done = false;
+    std::chrono::steady_clock::time_point t_submit;
+    std::mutex m;
+    std::condition_variable cv;
+};
+}  // namespace cafe
+
+namespace {
+
+void server_loop(cafe_ctx* C, int wi) {
+    cudaSetDevice(C->device);
+    Workspace& ws = *C->ws[wi];
+    for (;;) {
+        std::shared_ptr<Request> r;
+        {
+            std::unique_lock<std::mutex> lk(C->qmu);
+            C->qcv.wait(lk, [&] { return C->stop || !C->queue.empty(); });
+            if (C->stop && C->queue.empty()) return;
+            r = C->queue.front();
+            C->queue.pop_front();
+            C->in_flight++;
+        }
+        int rc;
+        ScoreInfo info;
+        {
+            // enqueue under the context lock; the GPU work of this request
+            // then overlaps with requests running on the other streams
+            std::unique_lock<std::mutex> lk(C->mu);
+            rc = score_enqueue(C, ws, &r->req, r->res, &info);
+        }
+        if (rc == CAFE_OK) rc = score_complete(C, ws, &r->req, r->res, info);
+        const double ms =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - r->t_submit).count();
+        {
+            std::lock_guard<std::mutex> lk(C->qmu);
+            C->in_flight--;
+            C->completed++;
+            C->latencies_ms.push_back(ms);
+        }
+        {
+            std::lock_guard<std::mutex> lk(r->m);
+            r->rc = rc;
+            r->done = true;
+        }
+        r->cv.notify_all();
+    }
+}
+
+}  // namespace
+
+void cafe_serving_stop(cafe_ctx* C) {
+    {
+        std::lock_guard<std::mutex> lk(C->qmu);
+        C->stop = true;
+    }
+    C->qcv.notify_all();
+    for (auto& t : C->servers)
+        if (t.joinable()) t.join();
+    C->servers.clear();
+}
+
+extern "C" {
+
+int cafe_submit(cafe_ctx* C, const cafe_request* req, cafe_result* res, uint64_t* ticket) {
+    if (!C || !req || !ticket) return CAFE_ERR_INVALID;
+    auto r = std::make_shared<Request>();
+    r->req = *req;
+    r->lambdas.assign(req->lambdas, req->lambdas + std::max(req->n_lambdas, 0));
+    r->req.lambdas = r->lambdas.data();
+    if (req->model == CAFE_MODEL_GAMMA && req->n_categories > 0) {
+        r->mult.assign(req->multipliers, req->multipliers + req->n_categories);
+        r->probs.assign(req->cat_probs, req->cat_probs + req->n_categories);
+        r->req.multipliers = r->mult.data();
+        r->req.cat_probs = r->probs.data();
+    }
+    r->res = res;
+    r->t_submit = std::chrono::steady_clock::now();
+    std::lock_guard<std::mutex> lk(C->qmu);
+    if (C->servers.empty()) {
+        C->stop = false;
+        for (size_t i = 1; i < C->ws.size(); ++i) C->servers.emplace_back(server_loop, C, (int)i);
+    }
+    *ticket = C->next_ticket++;
+    C->tickets[*ticket] = r;
+    C->queue.push_back(r);
+    C->qcv.notify_one();
+    return CAFE_OK;
+}
+
+int cafe_poll(cafe_ctx* C, uint64_t ticket, int wait_ms) {
+    if (!C) return CAFE_ERR_INVALID;
+    std::shared_ptr<Request> r;
+    {
+        std::lock_guard<std::mutex> lk(C->qmu);
+        auto it = C->tickets.find(ticket);
+        if (it == C->tickets.end()) return CAFE_ERR_NOT_FOUND;
+        r = it->second;
+    }
+    std::unique_lock<std::mutex> lk(r->m);
+    if (!r->done) {
+        if (wait_ms < 0) r->cv.wait(lk, [&] { return r->done; });
+        else if (wait_ms > 0) r->cv.wait_for(lk, std::chrono::milliseconds(wait_ms), [&] { return r->done; });
+    }
+    if (!r->done) return CAFE_ERR_BUSY;
+    const int rc = r->rc;
+    lk.unlock();
+    std::lock_guard<std::mutex> lk2(C->qmu);
+    C->tickets.erase(ticket);
+    return rc;
+}
+
+int cafe_serving_stats(cafe_ctx* C, int64_t* completed, double* p50, double* p99, int* in_flight) {
+    if (!C) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->qmu);
+    std::vector<double> v = C->latencies_ms;
+    std::sort(v.begin(), v.end());
+    auto pct = [&](double q) { return v.empty() ? 0.0 : v[std::min(v.size() - 1, (size_t)(q * (v.size() - 1) + 0.5))]; };
+    if (completed) *completed = C->completed;
+    if (p50) *p50 = pct(0.50);
+    if (p99) *p99 = pct(0.99);
+    if (in_flight) *in_flight = C->in_flight + (int)C->queue.size();
+    return CAFE_OK;
+}
+
+}  // extern "C"

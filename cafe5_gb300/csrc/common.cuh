@@ -1,0 +1,105 @@
+// Shared definitions of the GB300 CAFE5 likelihood kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cafe {
+
+// Transition-matrix build job: one (lambda, t) matrix of side `size`,
+// computed at the quantized values (matrix_cache_key, src/matrix_cache.h:49-62).
+struct MatrixJob {
+    double lambda;    // quantized lambda
+    double t;         // quantized branch length
+    double* dst;      // FP64 row-major size x size, M[parent s][child c]
+    float* colT;      // optional: FP32 transposed, column-normalised (size x size), or null
+    int32_t* colE;    // optional: per-column power-of-two exponent (size), or null
+    uint16_t* hi;     // optional: BF16 hi part, row-major (size x ld_bf16), or null
+    uint16_t* lo;     // optional: BF16 lo part
+    int size;
+    int ld_bf16;      // leading dimension of hi/lo in elements (multiple of 8)
+};
+
+// Work tile of the pruning kernels: `count` families (indices into the
+// request's family permutation starting at `first`) scored in category `k`
+// with state bound S (vectors of S + 1 states) and root rows 1..R.
+struct PruneTile {
+    int first;
+    int count;
+    int k;
+    int S;
+    int R;
+    int pad[3];
+};
+
+// Flattened tree for the kernels, in one device allocation.
+//   internal[i]                internal nodes in post-order (root last)
+//   cstart[i]..cstart[i+1]     children of internal[i] (indices into child[])
+//   child[j]                   child node id
+//   leaf_col[node]             counts column of a leaf, -1 for internal
+//   slot[node]                 scratch slot of an internal node
+struct TreePlan {
+    int n_nodes;
+    int n_internal;
+    int n_leaves;
+    int root;
+    int n_slots;
+    int max_children;
+    const int32_t* internal;
+    const int32_t* cstart;
+    const int32_t* child;
+    const int32_t* leaf_col;
+    const int32_t* slot;
+};
+
+constexpr int kMaxNodes = 512;
+
+}  // namespace cafe
+
+// Launch wrappers implemented in the .cu files (host side).
+namespace cafe {
+
+cudaError_t launch_matrix_build(const MatrixJob* d_jobs, int n_jobs, int max_size, cudaStream_t s);
+
+struct Prune64Args {
+    TreePlan plan;
+    const PruneTile* tiles;
+    int n_tiles;
+    const int32_t* counts;       // [F][n_leaves]
+    const int64_t* perm;         // family index of each tile slot
+    const double* const* mats;   // [K][n_nodes] FP64 matrix per (category, node)
+    int ld_mat;                  // row stride of every FP64 matrix (= matrix size)
+    const double* prior;         // [n_prior]
+    int n_prior;
+    const double* err;           // [err_rows][err_ndev] or null
+    int err_rows;
+    int err_ndev;
+    const int32_t* fam_R;        // per-family root bound, or null (tile R)
+    double* scratch;             // n_ctas * per_cta doubles
+    int64_t scratch_per_cta;
+    int scaled;                  // per-node power-of-two rescale
+    int model;                   // 0 base, 1 gamma
+    double* out;                 // base: [F] lnl; gamma: [F][K] category value
+    int K;
+    const double* cat_probs;     // [K]
+    int tile_families;           // families per tile (<= 32)
+    int W;                       // max vector length over tiles (S + 1 or R)
+};
+
+cudaError_t launch_prune64(const Prune64Args& a, int n_ctas, cudaStream_t s);
+
+struct FinishArgs {
+    int64_t F;
+    int K;
+    int model;
+    int scaled;
+    const double* cat;           // gamma: [F][K] (linear if !scaled, log if scaled); base: [F] lnl
+    const int64_t* ref;          // dedupe reference per family, or null
+    double* family_lnl;          // [F] out
+    double* total;               // [1] out
+    int32_t* n_failed;           // [1] out
+};
+
+cudaError_t launch_finish(const FinishArgs& a, cudaStream_t s);
+
+}  // namespace cafe

@@ -1,0 +1,340 @@
+// K3/K4 (FP64): Felsenstein pruning of family tiles up the species tree,
+// with the root weighting fused into the last node.
+//
+// Replaces inference_prune (src/core.cpp:134-145) ->
+// compute_node_probability (src/probability.cpp:175-234) ->
+// lambda::calculate_child_factor (src/lambda.cpp:13-40) ->
+// matrix::multiply (src/matrix_cache.cpp:32-58), and the per-family root
+// reductions of base_model::infer_family_likelihoods
+// (src/base_model.cpp:77-95) and gamma_model::prune
+// (src/gamma_core.cpp:143-165).
+//
+// One CTA walks one tile of up to 32 families of one gamma category through
+// the tree in post-order. Node vectors live in a per-CTA scratch area
+// (L2-resident), state-major: V[state][family]. For every internal node the
+// product over children is formed in descendant order starting from the
+// first child's factor (= 1 * factor, as the reference does):
+//   leaf child      factor[s] = M[s][n]              (a column gather; the
+//                   reference's dense product with a one-hot vector adds only
+//                   exact zeros), or the error-model row sum over n-1, n, n+1
+//   internal child  factor[s] = sum_j M[s][j] L[j]   (an FP64 GEMM tile,
+//                   64 states x 32 families, K staged through shared memory)
+// Internal nodes use states 0..S; the root uses rows 1..R (root index j is
+// root size j + 1, src/probability.cpp:206-219). With `scaled`, each node
+// vector is renormalised per family by a power of two and the exponents are
+// carried as integers, which keeps families finite where unscaled FP64
+// underflows.
+#include "common.cuh"
+
+#include <math.h>
+
+#include <algorithm>
+
+namespace cafe {
+namespace {
+
+constexpr int TF = 32;      // families per tile
+constexpr int RT = 64;      // GEMM rows per pass
+constexpr int KT = 32;      // GEMM K chunk
+constexpr int NT = 256;     // threads
+
+__device__ __forceinline__ double* slot_ptr(double* base, int slot, int W) {
+    return base + (size_t)slot * W * TF;
+}
+
+__global__ void __launch_bounds__(NT) k_prune64(Prune64Args a) {
+    __shared__ double Ms[RT][KT + 1];
+    __shared__ double Ls[KT][TF + 1];
+    __shared__ int64_t fam[TF];
+    __shared__ double red[NT / 32][TF];
+    __shared__ int redi[NT / 32][TF];
+    extern __shared__ int s_exp[];   // [n_slots][TF] power-of-two exponents
+
+    const TreePlan& P = a.plan;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    double* base = a.scratch + (size_t)blockIdx.x * a.scratch_per_cta;
+    const int W = a.W;
+
+    for (int t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
+        const PruneTile tile = a.tiles[t];
+        const int cnt = tile.count, S = tile.S, R = tile.R, k = tile.k;
+        if (tid < TF) fam[tid] = tid < cnt ? a.perm[tile.first + tid] : -1;
+        __syncthreads();
+        const double* const* mats = a.mats + (size_t)k * P.n_nodes;
+
+        for (int ii = 0; ii < P.n_internal; ++ii) {
+            const int v = P.internal[ii];
+            const bool is_root = (v == P.root);
+            const int rows = is_root ? R : S + 1;
+            const int row0 = is_root ? 1 : 0;
+            const int vs = P.slot[v];
+            double* dst = slot_ptr(base, vs, W);
+            if (tid < TF) s_exp[vs * TF + tid] = 0;
+            __syncthreads();
+            for (int ci = P.cstart[ii]; ci < P.cstart[ii + 1]; ++ci) {
+                const int ch = P.child[ci];
+                const bool first = (ci == P.cstart[ii]);
+                const double* __restrict__ M = mats[ch];
+                const int ld = a.ld_mat;
+                const int lc = P.leaf_col[ch];
+                if (lc >= 0) {
+                    // leaf: column gather (or the 3-term error-model sum)
+                    for (int idx = tid; idx < rows * TF; idx += NT) {
+                        const int r = idx / TF, i = idx % TF;
+                        if (i >= cnt) continue;
+                        const int s = row0 + r;
+                        const int n = a.counts[(size_t)fam[i] * P.n_leaves + lc];
+                        double val = 0.0;
+                        const double* Mr = M + (size_t)s * ld;
+                        if (a.err) {
+                            const double* pr = a.err + (size_t)(n < a.err_rows ? n : a.err_rows - 1) * a.err_ndev;
+                            const int off = n - (a.err_ndev - 1) / 2;
+                            for (int d = 0; d < a.err_ndev; ++d) {
+                                const int c = off + d;
+                                if (c < 0 || c > S) continue;
+                                val = fma(Mr[c], pr[d], val);
+                            }
+                        } else if (n >= 0 && n <= S) {
+                            val = Mr[n];
+                        }
+                        double* o = dst + (size_t)r * TF + i;
+                        *o = first ? val : *o * val;
+                    }
+                } else {
+                    // internal child: dst[r][i] (*)= sum_j M[row0 + r][j] * L[j][i]
+                    const double* L = slot_ptr(base, P.slot[ch], W);
+                    const int ty = tid >> 4, tx = tid & 15;   // 16 x 16 threads: 4 rows x 2 families each
+                    for (int r0 = 0; r0 < rows; r0 += RT) {
+                        double acc[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+                        for (int j0 = 0; j0 <= S; j0 += KT) {
+                            for (int e = tid; e < RT * KT; e += NT) {
+                                const int rr = e / KT, jj = e % KT;
+                                const int r = r0 + rr, j = j0 + jj;
+                                Ms[rr][jj] = (r < rows && j <= S) ? M[(size_t)(row0 + r) * ld + j] : 0.0;
+                            }
+                            for (int e = tid; e < KT * TF; e += NT) {
+                                const int jj = e / TF, i = e % TF;
+                                const int j = j0 + jj;
+                                Ls[jj][i] = (j <= S && i < cnt) ? L[(size_t)j * TF + i] : 0.0;
+                            }
+                            __syncthreads();
+#pragma unroll 8
+                            for (int jj = 0; jj < KT; ++jj) {
+                                const double b0 = Ls[jj][tx * 2], b1 = Ls[jj][tx * 2 + 1];
+#pragma unroll
+                                for (int q = 0; q < 4; ++q) {
+                                    const double av = Ms[ty * 4 + q][jj];
+                                    acc[q][0] = fma(av, b0, acc[q][0]);
+                                    acc[q][1] = fma(av, b1, acc[q][1]);
+                                }
+                            }
+                            __syncthreads();
+                        }
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const int r = r0 + ty * 4 + q;
+                            if (r >= rows) continue;
+#pragma unroll
+                            for (int p = 0; p < 2; ++p) {
+                                const int i = tx * 2 + p;
+                                if (i >= cnt) continue;
+                                double* o = dst + (size_t)r * TF + i;
+                                *o = first ? acc[q][p] : *o * acc[q][p];
+                            }
+                        }
+                    }
+                    if (tid < TF) s_exp[vs * TF + tid] += s_exp[P.slot[ch] * TF + tid];
+                }
+                __syncthreads();
+            }
+            if (a.scaled) {
+                // per-family max over states -> power-of-two renormalisation
+                double mx = 0.0;
+                for (int r = warp; r < rows; r += NT / 32) {
+                    const double x = dst[(size_t)r * TF + lane];
+                    mx = x > mx ? x : mx;
+                }
+                red[warp][lane] = mx;
+                __syncthreads();
+                if (warp == 0) {
+                    double m = 0.0;
+                    for (int w = 0; w < NT / 32; ++w) m = red[w][lane] > m ? red[w][lane] : m;
+                    int e = 0;
+                    if (m > 0.0 && isfinite(m)) frexp(m, &e);
+                    redi[0][lane] = e;
+                    s_exp[vs * TF + lane] += e;
+                }
+                __syncthreads();
+                const int e = redi[0][lane];
+                if (e != 0)
+                    for (int r = warp; r < rows; r += NT / 32) {
+                        double* o = dst + (size_t)r * TF + lane;
+                        *o = scalbn(*o, -e);
+                    }
+                __syncthreads();
+            }
+        }
+
+        // ---- root weighting (K4) ----
+        const int rs = P.slot[P.root];
+        const double* root = slot_ptr(base, rs, W);
+        const int i = lane;
+        const int64_t f = i < cnt ? fam[i] : -1;
+        const int Rf = (f >= 0 && a.fam_R) ? a.fam_R[f] : R;
+        if (a.model == 0) {
+            double best = -INFINITY;
+            bool any = false;
+            for (int j = warp; j < Rf; j += NT / 32) {
+                const double eq = j < a.n_prior ? a.prior[j] : 0.0;
+                const double vv = log(root[(size_t)j * TF + i]) + log(eq);
+                if (!any || vv > best) best = vv;
+                any = true;
+            }
+            red[warp][lane] = any ? best : NAN;
+            __syncthreads();
+            if (warp == 0 && f >= 0) {
+                double b = -INFINITY;
+                bool got = false;
+                for (int w = 0; w < NT / 32; ++w) {
+                    const double x = red[w][lane];
+                    if (isnan(x)) continue;
+                    if (!got || x > b) b = x;
+                    got = true;
+                }
+                a.out[f] = b + (double)s_exp[rs * TF + i] * 0.69314718055994530942;
+            }
+        } else {
+            double mx = 0.0;
+            int nz = 0;
+            for (int j = warp; j < Rf; j += NT / 32) {
+                const double x = root[(size_t)j * TF + i];
+                const double eq = j < a.n_prior ? a.prior[j] : 0.0;
+                const double vv = x * eq;
+                mx = vv > mx ? vv : mx;
+                nz |= (x != 0.0);
+            }
+            red[warp][lane] = mx;
+            redi[warp][lane] = nz;
+            __syncthreads();
+            if (warp == 0 && f >= 0) {
+                double m = 0.0;
+                int z = 0;
+                for (int w = 0; w < NT / 32; ++w) {
+                    m = red[w][lane] > m ? red[w][lane] : m;
+                    z |= redi[w][lane];
+                }
+                const double cat = m * a.cat_probs[k];
+                double o;
+                if (!z) o = a.scaled ? NAN : -1.0;   // all-zero root vector: family fails
+                else if (a.scaled) o = log(cat) + (double)s_exp[rs * TF + i] * 0.69314718055994530942;
+                else o = cat;
+                a.out[(size_t)f * a.K + k] = o;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Per-family lnL from category values, and -sum lnL with a deterministic
+// compensated reduction (one block).
+__global__ void __launch_bounds__(1024) k_finish(FinishArgs a) {
+    __shared__ double ssum[1024], scomp[1024];
+    __shared__ int sfail[1024];
+    double sum = 0.0, comp = 0.0;
+    int fail = 0;
+    for (int64_t f = threadIdx.x; f < a.F; f += blockDim.x) {
+        const int64_t r = a.ref ? a.ref[f] : f;
+        double lnl;
+        if (a.model == 0) {
+            lnl = a.cat[r];
+        } else if (!a.scaled) {
+            // gamma_core.cpp:196-207: family likelihood = sum_k category terms
+            double lh = 0.0;
+            bool bad = false;
+            for (int k = 0; k < a.K; ++k) {
+                const double c = a.cat[(size_t)r * a.K + k];
+                if (c < 0) bad = true;
+                lh += c;
+            }
+            lnl = bad ? NAN : log(lh);
+            fail += bad;
+        } else {
+            double mx = -INFINITY;
+            bool bad = false;
+            for (int k = 0; k < a.K; ++k) {
+                const double c = a.cat[(size_t)r * a.K + k];
+                if (isnan(c)) bad = true;
+                else mx = c > mx ? c : mx;
+            }
+            double acc = 0.0;
+            if (!bad && mx > -INFINITY)
+                for (int k = 0; k < a.K; ++k) acc += exp(a.cat[(size_t)r * a.K + k] - mx);
+            lnl = bad ? NAN : (mx > -INFINITY ? mx + log(acc) : -INFINITY);
+            fail += bad;
+        }
+        a.family_lnl[f] = lnl;
+        if (!isnan(lnl)) {
+            // Neumaier summation
+            const double tt = sum + lnl;
+            if (fabs(sum) >= fabs(lnl)) comp += (sum - tt) + lnl;
+            else comp += (lnl - tt) + sum;
+            sum = tt;
+        }
+    }
+    ssum[threadIdx.x] = sum;
+    scomp[threadIdx.x] = comp;
+    sfail[threadIdx.x] = fail;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0, c = 0.0;
+        int fl = 0;
+        for (int i = 0; i < (int)blockDim.x; ++i) {
+            const double x = ssum[i];
+            const double tt = s + x;
+            if (fabs(s) >= fabs(x)) c += (s - tt) + x;
+            else c += (x - tt) + s;
+            s = tt;
+            c += scomp[i];
+            fl += sfail[i];
+        }
+        *a.n_failed = fl;
+        *a.total = fl ? INFINITY : -(s + c);
+    }
+}
+
+__global__ void k_fill(double* p, int64_t n, double v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+__global__ void k_fill_i32(int32_t* p, int64_t n, int32_t v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+}  // namespace
+
+cudaError_t launch_fill(double* p, int64_t n, double v, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
+    k_fill<<<blocks, 256, 0, s>>>(p, n, v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_i32(int32_t* p, int64_t n, int32_t v, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
+    k_fill_i32<<<blocks, 256, 0, s>>>(p, n, v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prune64(const Prune64Args& a, int n_ctas, cudaStream_t s) {
+    if (a.n_tiles <= 0) return cudaSuccess;
+    size_t smem = sizeof(int) * (size_t)a.plan.n_slots * TF;
+    k_prune64<<<n_ctas, NT, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finish(const FinishArgs& a, cudaStream_t s) {
+    k_finish<<<1, 1024, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace cafe

@@ -1,0 +1,138 @@
+// Host runtime of the GB300 CAFE5 likelihood path (internal).
+#pragma once
+
+#include <condition_variable>
+#include <cstdint>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <tuple>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/cafe_gb300.h"
+#include "common.cuh"
+
+namespace cafe {
+
+// Default S-bin widths (vector length = states 0..W-1).
+extern const int kDefaultBins[];
+extern const int kNumDefaultBins;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf();
+    cudaError_t reserve(size_t n);
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct PinnedBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~PinnedBuf();
+    cudaError_t reserve(size_t n);
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct TreeHost {
+    int n_nodes = 0, n_leaves = 0, root = -1;
+    std::vector<int32_t> parent, lambda_index, leaf_col;
+    std::vector<double> branch_length;
+    std::vector<std::vector<int>> children;
+    // plan (internal nodes in post-order) and its device copy
+    std::vector<int32_t> internal, cstart, child, slot;
+    int n_slots = 0, max_children = 0;
+    DevBuf d_plan;
+    TreePlan plan{};
+    double longest_branch = 0.0;
+    std::vector<double> distinct_lengths;   // positive, sorted (root branch included)
+};
+
+struct BinPlan {
+    // families grouped by bin; perm holds family indices bin by bin
+    std::vector<int> widths;                 // bin widths used
+    std::vector<int64_t> bin_first, bin_count;
+    DevBuf d_perm, d_famR;
+    int W_max = 0;
+};
+
+struct FamSet {
+    int tree_id = 0;
+    int64_t F = 0;
+    int n_leaves = 0;
+    DevBuf d_counts;
+    std::vector<int32_t> h_counts;
+    std::vector<int32_t> max_count;
+    // dedupe: unique families and reference per family
+    std::vector<int64_t> unique;
+    DevBuf d_unique, d_ref, d_identity;
+    BinPlan bins;
+};
+
+struct MatKey {
+    int size;
+    long lq, tq;
+    bool operator==(const MatKey& o) const { return size == o.size && lq == o.lq && tq == o.tq; }
+};
+struct MatKeyHash {
+    size_t operator()(const MatKey& k) const {
+        return std::hash<long>()(k.lq * 1000003L ^ k.tq) ^ std::hash<int>()(k.size);
+    }
+};
+
+struct MatEntry {
+    double* d = nullptr;       // FP64 row-major size x size
+    int chunk = -1;
+};
+
+// Per-request device workspace (one per stream).
+struct Workspace {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    DevBuf scratch, tiles, mats, cat, fam_lnl, total, nfail, jobs, catp;
+    PinnedBuf h_tiles, h_mats, h_jobs, h_out, h_catp;
+    std::vector<PruneTile> tile_vec;
+    ~Workspace();
+    int init(int device);
+};
+
+struct Request;   // serving-loop request record
+
+}  // namespace cafe
+
+struct cafe_ctx {
+    int device = 0;
+    std::string last_error;
+    std::mutex mu;
+    std::map<int, std::unique_ptr<cafe::TreeHost>> trees;
+    std::map<int, std::unique_ptr<cafe::FamSet>> sets;
+    int next_tree = 1, next_set = 1;
+    std::vector<double> prior;
+    cafe::DevBuf d_prior;
+    std::vector<double> err;
+    int err_rows = 0, err_ndev = 0;
+    cafe::DevBuf d_err;
+    // matrix cache
+    std::unordered_map<cafe::MatKey, cafe::MatEntry, cafe::MatKeyHash> cache;
+    std::vector<void*> chunks;
+    size_t cache_bytes = 0, cache_cap = 0;
+    // workspaces: [0] for synchronous calls, [1..] for the serving loop
+    std::vector<std::unique_ptr<cafe::Workspace>> ws;
+    int n_ctas = 0;
+    int sm_count = 0;
+    // serving loop
+    std::mutex qmu;
+    std::condition_variable qcv;
+    std::deque<std::shared_ptr<cafe::Request>> queue;
+    std::map<uint64_t, std::shared_ptr<cafe::Request>> tickets;
+    std::vector<std::thread> servers;
+    bool stop = false;
+    uint64_t next_ticket = 1;
+    int in_flight = 0;
+    std::vector<double> latencies_ms;
+    int64_t completed = 0;
+};

@@ -1,0 +1,410 @@
+"""Python mirror of the reference's likelihood API over the C ABI.
+
+Same names and argument meaning as the CAFE5 classes on the hot path:
+
+* `MatrixCache`      matrix_cache (src/matrix_cache.h:70-96)
+* `SingleLambda`, `MultipleLambda`  lambda (src/lambda.h:21-100)
+* `BaseModel`        base_model::infer_family_likelihoods (src/base_model.cpp:53-100)
+* `GammaModel`       gamma_model (src/gamma_core.h, src/gamma_core.cpp:168-237)
+* `LambdaOptimizerScorer`, `GammaLambdaOptimizerScorer`, `LambdaEpsilonOptimizerScorer`
+                     inference_optimizer_scorer and subclasses
+                     (src/optimizer_scorer.cpp:22-180): NaN scores become +inf.
+
+All arithmetic runs in libcafe_gb300.so on the GPU; this module only moves
+arguments and results.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from .families import FamilySet, global_bounds
+from .inputs import ErrorModel, RootPrior, discrete_gamma
+from .tree import Tree, lambda_index_of_nodes
+
+PREC = {"fp64_ref": _lib.PREC_FP64_REF, "fp64_binned": _lib.PREC_FP64_BINNED,
+        "mixed_bf16x3": _lib.PREC_MIXED_BF16X3}
+
+
+def _p(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data
+
+
+@dataclass
+class ScoreResult:
+    total: float
+    family_lnl: np.ndarray
+    category_lnl: Optional[np.ndarray]
+    status: int
+    n_failed: int
+    n_fallback: int
+    device_ms: float
+
+
+class Context:
+    """One device context: trees, family sets, prior, error model and the
+    device-resident matrix cache."""
+
+    def __init__(self, device: int = 0, n_streams: int = 4, matrix_cache_bytes: int = 0):
+        self.lib = _lib.load()
+        cfg = _lib.Config(device, matrix_cache_bytes, n_streams, 0)
+        h = C.c_void_p()
+        rc = self.lib.cafe_ctx_create(C.byref(cfg), C.byref(h))
+        if rc:
+            raise _lib.CafeError(rc, "cafe_ctx_create failed (is a CUDA GPU visible?)")
+        self.h = h
+        self._tree_leaves = {}
+        self._set_shape = {}
+
+    def close(self):
+        if self.h:
+            self.lib.cafe_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise _lib.CafeError(rc, self.lib.cafe_last_error(self.h).decode())
+
+    # ---- inputs -----------------------------------------------------------
+    def upload_tree(self, tree: Tree, lambda_of_node: Optional[Sequence[int]] = None) -> int:
+        a = tree.arrays(list(lambda_of_node) if lambda_of_node is not None else None)
+        tid = C.c_int()
+        self._check(self.lib.cafe_tree_upload(self.h, tree.n_nodes, _p(a["parent"]), _p(a["branch_length"]),
+                                              _p(a["lambda_index"]), C.byref(tid)))
+        self._tree_leaves[tid.value] = len(tree.leaves)
+        return tid.value
+
+    def upload_families(self, tree_id: int, counts: np.ndarray) -> int:
+        counts = np.ascontiguousarray(counts, dtype=np.int32)
+        sid = C.c_int()
+        self._check(self.lib.cafe_families_upload(self.h, tree_id, _p(counts), counts.shape[0], counts.shape[1],
+                                                  C.byref(sid)))
+        self._set_shape[sid.value] = counts.shape
+        return sid.value
+
+    def update_families(self, set_id: int, counts: np.ndarray):
+        counts = np.ascontiguousarray(counts, dtype=np.int32)
+        assert counts.shape == self._set_shape[set_id]
+        self._check(self.lib.cafe_families_update(self.h, set_id, _p(counts)))
+
+    def free_families(self, set_id: int):
+        self._check(self.lib.cafe_families_free(self.h, set_id))
+        self._set_shape.pop(set_id, None)
+
+    def set_prior(self, prior: np.ndarray):
+        prior = np.ascontiguousarray(prior, dtype=np.float64)
+        self._check(self.lib.cafe_prior_set(self.h, _p(prior), len(prior)))
+
+    def set_error_model(self, table: Optional[np.ndarray]):
+        if table is None:
+            self._check(self.lib.cafe_error_model_set(self.h, None, 0, 0))
+            return
+        t = np.ascontiguousarray(table, dtype=np.float64)
+        self._check(self.lib.cafe_error_model_set(self.h, _p(t), t.shape[0], t.shape[1]))
+
+    # ---- matrix cache -------------------------------------------------------
+    def matrices_build(self, lambdas, branch_lengths, size: int):
+        l = np.ascontiguousarray(lambdas, dtype=np.float64)
+        t = np.ascontiguousarray(branch_lengths, dtype=np.float64)
+        self._check(self.lib.cafe_matrices_build(self.h, _p(l), len(l), _p(t), len(t), size))
+
+    def matrix_get(self, lam: float, t: float, size: int) -> np.ndarray:
+        out = np.zeros((size, size))
+        self._check(self.lib.cafe_matrix_get(self.h, lam, t, size, _p(out)))
+        return out
+
+    def cache_size(self) -> int:
+        n = C.c_int64()
+        self._check(self.lib.cafe_matrix_cache_size(self.h, C.byref(n)))
+        return n.value
+
+    def cache_clear(self):
+        self._check(self.lib.cafe_matrix_cache_clear(self.h))
+
+    # ---- scoring ------------------------------------------------------------
+    def make_request(self, tree_id, set_id, lambdas, *, model=0, lambda_kind=0, multipliers=(1.0,),
+                     cat_probs=(1.0,), use_error_model=False, S=0, R=0, precision="fp64_ref", dedupe=False):
+        keep = {"lam": np.ascontiguousarray(lambdas, dtype=np.float64),
+                "mult": np.ascontiguousarray(multipliers, dtype=np.float64),
+                "prob": np.ascontiguousarray(cat_probs, dtype=np.float64)}
+        req = _lib.Request(tree_id, set_id, model, lambda_kind, len(keep["lam"]), _p(keep["lam"]),
+                           len(keep["mult"]) if model == _lib.MODEL_GAMMA else 1, _p(keep["mult"]), _p(keep["prob"]),
+                           1 if use_error_model else 0, int(S), int(R),
+                           PREC[precision] if isinstance(precision, str) else int(precision), 1 if dedupe else 0)
+        return req, keep
+
+    def score(self, tree_id, set_id, lambdas, *, want_categories=False, **kw) -> ScoreResult:
+        req, keep = self.make_request(tree_id, set_id, lambdas, **kw)
+        F = self._set_shape[set_id][0]
+        K = req.n_categories
+        fam = np.zeros(F)
+        cat = np.zeros((F, K)) if want_categories else None
+        res = _lib.Result(_p(fam), _p(cat), 0.0, 0, 0, 0, 0.0)
+        self._check(self.lib.cafe_score(self.h, C.byref(req), C.byref(res)))
+        return ScoreResult(res.total_neg_lnl, fam, cat, res.status, res.n_failed, res.n_fallback, res.device_ms)
+
+    def score_device(self, tree_id, set_id, lambdas, d_family_lnl=0, d_total=0, stream=0, **kw):
+        req, keep = self.make_request(tree_id, set_id, lambdas, **kw)
+        self._check(self.lib.cafe_score_device(self.h, C.byref(req), d_family_lnl or None, d_total or None,
+                                               stream or None))
+
+    def submit(self, tree_id, set_id, lambdas, **kw):
+        """Queue a request for the serving loop; returns a handle for poll()."""
+        want_cat = kw.pop("want_categories", False)
+        req, keep = self.make_request(tree_id, set_id, lambdas, **kw)
+        F = self._set_shape[set_id][0]
+        fam = np.zeros(F)
+        cat = np.zeros((F, req.n_categories)) if want_cat else None
+        res = _lib.Result(_p(fam), _p(cat), 0.0, 0, 0, 0, 0.0)
+        t = C.c_uint64()
+        self._check(self.lib.cafe_submit(self.h, C.byref(req), C.byref(res), C.byref(t)))
+        return {"ticket": t.value, "res": res, "fam": fam, "cat": cat, "keep": keep}
+
+    def poll(self, handle, wait_ms: int = -1) -> Optional[ScoreResult]:
+        rc = self.lib.cafe_poll(self.h, handle["ticket"], wait_ms)
+        if rc == 8:
+            return None
+        self._check(rc)
+        r = handle["res"]
+        return ScoreResult(r.total_neg_lnl, handle["fam"], handle["cat"], r.status, r.n_failed, r.n_fallback,
+                           r.device_ms)
+
+    def serving_stats(self):
+        n = C.c_int64()
+        p50 = C.c_double()
+        p99 = C.c_double()
+        inf = C.c_int()
+        self._check(self.lib.cafe_serving_stats(self.h, C.byref(n), C.byref(p50), C.byref(p99), C.byref(inf)))
+        return {"completed": n.value, "p50_ms": p50.value, "p99_ms": p99.value, "in_flight": inf.value}
+
+
+_default_ctx: Optional[Context] = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context()
+    return _default_ctx
+
+
+# ---------------------------------------------------------------- reference mirror
+
+class MatrixCache:
+    """matrix_cache: precalculate_matrices / get_matrix / get_cache_size /
+    is_saturated, backed by the device-resident cache."""
+
+    def __init__(self, matrix_size: int, ctx: Optional[Context] = None):
+        self.ctx = ctx or default_context()
+        self.size = matrix_size
+        self._keys = set()
+
+    def precalculate_matrices(self, lambdas: Sequence[float], branch_lengths: Sequence[float]):
+        self.ctx.matrices_build(list(lambdas), list(branch_lengths), self.size)
+        for l in lambdas:
+            for t in branch_lengths:
+                self._keys.add((int(l * 1000000000), int(t * 1000)))
+
+    def get_matrix(self, branch_length: float, lam: float) -> np.ndarray:
+        return self.ctx.matrix_get(lam, branch_length, self.size)
+
+    def get_cache_size(self) -> int:
+        return len(self._keys)
+
+    def get_matrix_size(self) -> int:
+        return self.size
+
+    @staticmethod
+    def is_saturated(branch_length: float, lam: float) -> bool:
+        return bool(_lib.load().cafe_is_saturated(branch_length, lam))
+
+
+class SingleLambda:
+    def __init__(self, lam: float):
+        self.values = [float(lam)]
+        self.kind = _lib.LAMBDA_SINGLE
+
+    def multiply(self, factor):
+        return SingleLambda(self.values[0] * factor)
+
+    def update(self, values):
+        self.values = [float(values[0])]
+
+    def count(self):
+        return 1
+
+    def is_valid(self):
+        return self.values[0] > 0
+
+
+class MultipleLambda:
+    def __init__(self, lambda_tree: Tree, lambdas: Sequence[float]):
+        self.lambda_tree = lambda_tree
+        self.values = [float(x) for x in lambdas]
+        self.kind = _lib.LAMBDA_MULTIPLE
+
+    def multiply(self, factor):
+        return MultipleLambda(self.lambda_tree, [v * factor for v in self.values])
+
+    def update(self, values):
+        self.values = [float(v) for v in values[:len(self.values)]]
+
+    def count(self):
+        return len(self.values)
+
+    def is_valid(self):
+        return all(v >= 0 for v in self.values)
+
+
+class BaseModel:
+    """base_model over the GPU path. `precision` selects fp64_ref (the
+    reference's global bounds, unscaled), fp64_binned or mixed_bf16x3."""
+
+    def __init__(self, lam, tree: Tree, families: FamilySet, max_family_size: int, max_root_family_size: int,
+                 error_model: Optional[ErrorModel] = None, precision: str = "fp64_ref", dedupe: bool = True,
+                 ctx: Optional[Context] = None):
+        self.ctx = ctx or default_context()
+        self.lam = lam
+        self.tree = tree
+        self.families = families
+        self.max_family_size = max_family_size
+        self.max_root_family_size = max_root_family_size
+        self.error_model = error_model
+        self.precision = precision
+        self.dedupe = dedupe
+        lam_idx = lambda_index_of_nodes(tree, lam.lambda_tree) if isinstance(lam, MultipleLambda) else None
+        self.tree_id = self.ctx.upload_tree(tree, lam_idx)
+        self.set_id = self.ctx.upload_families(self.tree_id, families.counts)
+        self.results: Optional[np.ndarray] = None
+        self.category_results: Optional[np.ndarray] = None
+        self.last: Optional[ScoreResult] = None
+
+    def _common(self, prior: RootPrior):
+        n = max(self.max_root_family_size, 1) + 8
+        self.ctx.set_prior(prior.vector(max(n, len(prior.vector()))))
+        self.ctx.set_error_model(self.error_model.table() if self.error_model else None)
+
+    def _kw(self):
+        ref = self.precision == "fp64_ref"
+        return dict(use_error_model=self.error_model is not None, S=self.max_family_size if ref else 0,
+                    R=self.max_root_family_size if ref else 0, precision=self.precision)
+
+    def infer_family_likelihoods(self, prior: RootPrior, lam=None) -> float:
+        lam = lam or self.lam
+        self._common(prior)
+        r = self.ctx.score(self.tree_id, self.set_id, lam.values, model=_lib.MODEL_BASE, lambda_kind=lam.kind,
+                           dedupe=self.dedupe, **self._kw())
+        self.last = r
+        self.results = r.family_lnl
+        return r.total
+
+
+class GammaModel(BaseModel):
+    def __init__(self, lam, tree, families, max_family_size, max_root_family_size, n_gamma_cats: int = 0,
+                 fixed_alpha: float = -1.0, error_model=None, cat_probs=None, multipliers=None, **kw):
+        super().__init__(lam, tree, families, max_family_size, max_root_family_size, error_model, **kw)
+        if multipliers is not None:
+            self.cat_probs, self.multipliers = list(cat_probs), list(multipliers)
+            self.alpha = fixed_alpha
+        else:
+            self.cat_probs, self.multipliers = [1.0] * n_gamma_cats, [1.0] * n_gamma_cats
+            self.set_alpha(fixed_alpha)
+
+    def set_alpha(self, alpha: float):
+        """gamma_model::set_alpha (src/gamma_core.cpp:61-67)."""
+        self.alpha = alpha
+        if len(self.cat_probs) > 1:
+            self.cat_probs, self.multipliers = discrete_gamma(alpha, len(self.cat_probs))
+
+    def infer_family_likelihoods(self, prior: RootPrior, lam=None) -> float:
+        lam = lam or self.lam
+        if self.alpha is not None and self.alpha < 0 and len(self.cat_probs) > 1 and self.multipliers == [1.0] * len(self.cat_probs):
+            return math.inf
+        self._common(prior)
+        r = self.ctx.score(self.tree_id, self.set_id, lam.values, model=_lib.MODEL_GAMMA, lambda_kind=lam.kind,
+                           multipliers=self.multipliers, cat_probs=self.cat_probs, want_categories=True,
+                           **self._kw())
+        self.last = r
+        self.results = r.family_lnl
+        self.category_results = r.category_lnl
+        return r.total
+
+
+class InferenceOptimizerScorer:
+    """inference_optimizer_scorer::calculate_score: prepare, infer, NaN -> inf."""
+
+    def __init__(self, lam, model: BaseModel, prior: RootPrior):
+        self.lam, self.model, self.prior = lam, model, prior
+
+    def prepare_calculation(self, values):
+        raise NotImplementedError
+
+    def calculate_score(self, values) -> float:
+        self.prepare_calculation(values)
+        score = self.model.infer_family_likelihoods(self.prior, self.lam)
+        return math.inf if math.isnan(score) else score
+
+
+class LambdaOptimizerScorer(InferenceOptimizerScorer):
+    def __init__(self, lam, model, prior, longest_branch: float):
+        super().__init__(lam, model, prior)
+        self.longest_branch = longest_branch
+
+    def initial_guesses(self, rng: np.random.Generator) -> List[float]:
+        """lambda_optimizer::initial_guesses (src/optimizer_scorer.cpp:40-55)."""
+        distmean = 0.002 / (1.0 / self.longest_branch)
+        out = []
+        for _ in range(self.lam.count()):
+            x = -1.0
+            while x < 0:
+                x = 1.0 / self.longest_branch * rng.normal(distmean, 0.2)
+            out.append(x)
+        return out
+
+    def prepare_calculation(self, values):
+        self.lam.update(values)
+
+
+class GammaLambdaOptimizerScorer(LambdaOptimizerScorer):
+    """gamma_lambda_optimizer: lambdas then alpha."""
+
+    def initial_guesses(self, rng):
+        return super().initial_guesses(rng) + [float(rng.gamma(4.0, 0.25))]
+
+    def prepare_calculation(self, values):
+        n = self.lam.count()
+        self.lam.update(values[:n])
+        self.model.set_alpha(float(values[n]))
+
+
+class LambdaEpsilonOptimizerScorer(LambdaOptimizerScorer):
+    """lambda_epsilon_optimizer: lambdas then epsilons, replaced in the error
+    model (src/optimizer_scorer.cpp:72-109)."""
+
+    def __init__(self, lam, model, prior, longest_branch, error_model: ErrorModel):
+        super().__init__(lam, model, prior, longest_branch)
+        self.error_model = error_model
+        self.current = error_model.get_epsilons()
+
+    def initial_guesses(self, rng):
+        return super().initial_guesses(rng) + list(self.current)
+
+    def prepare_calculation(self, values):
+        n = self.lam.count()
+        self.lam.update(values[:n])
+        repl = {}
+        for i, old in enumerate(self.current):
+            repl[old] = float(values[n + i])
+            self.current[i] = float(values[n + i])
+        self.error_model.replace_epsilons(repl)

@@ -24,7 +24,8 @@ import numpy as np
 
 from .tree import Tree
 
-DEFAULT_BINS = (32, 64, 96, 128, 192, 256)
+# bin widths shared with the library (kDefaultBins in csrc/cafe_abi.cu)
+DEFAULT_BINS = (32, 64, 96, 128, 192, 256, 384, 512, 768, 1024)
 
 
 @dataclass

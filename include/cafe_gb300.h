@@ -1,0 +1,177 @@
+/* cafe_gb300.h -- C ABI of the GB300 (sm_103a) CAFE5 likelihood path.
+ *
+ * Drop-in boundary for CAFE5's likelihood hot path: transition-matrix
+ * construction (matrix_cache / probability.cpp) and Felsenstein pruning of
+ * every gene family (inference_prune) as called by the base and gamma
+ * models and, through them, by optimizer_scorer. Plain C types only.
+ *
+ * Every entry point returns a cafe_status. No call throws, and no pointer
+ * handed back to the host aliases device memory. A context owns all
+ * device-resident state (trees, family counts, prior, error model and the
+ * transition-matrix cache); callers own every host buffer they pass.
+ *
+ * Reference interfaces each entry point replaces are cited per function
+ * (paths relative to the CAFE5 project).
+ */
+#ifndef CAFE_GB300_H
+#define CAFE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    CAFE_OK = 0,
+    CAFE_ERR_OOM = 1,            /* device allocation refused */
+    CAFE_ERR_MISSING_MATRIX = 2, /* matrix_cache::get_matrix on an absent key */
+    CAFE_ERR_SATURATED = 3,      /* reported in cafe_result.status only */
+    CAFE_ERR_UNDERFLOW = 4,      /* reported in cafe_result.status only */
+    CAFE_ERR_TIMEOUT = 5,        /* a bounded wait ran out */
+    CAFE_ERR_INVALID = 6,        /* malformed argument */
+    CAFE_ERR_CUDA = 7,           /* CUDA runtime error; see cafe_last_error */
+    CAFE_ERR_BUSY = 8,           /* request not finished / not admitted yet */
+    CAFE_ERR_NOT_FOUND = 9       /* unknown tree / family-set / ticket id */
+} cafe_status;
+
+typedef enum { CAFE_MODEL_BASE = 0, CAFE_MODEL_GAMMA = 1 } cafe_model;
+typedef enum { CAFE_LAMBDA_SINGLE = 0, CAFE_LAMBDA_MULTIPLE = 1 } cafe_lambda_kind;
+
+/* Arithmetic of the pruning step. Matrices, root weighting and the final
+ * log-likelihood sums are FP64 in every mode.
+ *   FP64_REF     reference semantics: one global state bound S and root
+ *                bound R, unscaled FP64 (underflow behaves as in CAFE5)
+ *   FP64_BINNED  per-family S bins, FP64 with per-node power-of-two rescale
+ *   MIXED_BF16X3 per-family S bins, tensor-core split-BF16 products with FP32
+ *                accumulation and integer-exponent rescale; families whose
+ *                node vectors lose range are recomputed in FP64_BINNED */
+typedef enum {
+    CAFE_PREC_FP64_REF = 0,
+    CAFE_PREC_FP64_BINNED = 1,
+    CAFE_PREC_MIXED_BF16X3 = 2
+} cafe_precision;
+
+typedef struct cafe_ctx cafe_ctx;
+
+typedef struct {
+    int device;                  /* CUDA device ordinal */
+    size_t matrix_cache_bytes;   /* cap on cached matrices; 0 = 25% of free HBM */
+    int n_streams;               /* concurrent request streams for cafe_submit; 0 = 4 */
+    int max_bins;                /* reserved, 0 */
+} cafe_config;
+
+/* One score request: one infer_family_likelihoods call
+ * (model::infer_family_likelihoods, src/core.h:174). */
+typedef struct {
+    int tree_id;
+    int set_id;
+    int model;                   /* cafe_model */
+    int lambda_kind;             /* cafe_lambda_kind */
+    int n_lambdas;
+    const double* lambdas;       /* host; lambda per lambda index */
+    int n_categories;            /* gamma: K; base: ignored (1) */
+    const double* multipliers;   /* host; gamma lambda multipliers m_k */
+    const double* cat_probs;     /* host; gamma category probabilities */
+    int use_error_model;         /* leaves from the context's error model */
+    int max_family_size;         /* FP64_REF: global S; binned modes: 0 */
+    int max_root_family_size;    /* FP64_REF: global R; binned modes: 0 */
+    int precision;               /* cafe_precision */
+    int dedupe;                  /* prune identical count rows once (base model) */
+} cafe_request;
+
+typedef struct {
+    double* family_lnl;          /* host, n_families, or NULL */
+    double* category_lnl;        /* host, n_families * K (natural log), or NULL */
+    double total_neg_lnl;        /* -sum lnL; +inf on the reference's rejection paths */
+    int status;                  /* CAFE_OK / CAFE_ERR_SATURATED / CAFE_ERR_UNDERFLOW */
+    int64_t n_failed;            /* gamma: families whose category root vector summed to 0 */
+    int64_t n_fallback;          /* mixed: families recomputed in FP64 */
+    double device_ms;            /* device time of the request (CUDA events) */
+} cafe_result;
+
+/* ---- context --------------------------------------------------------- */
+int cafe_ctx_create(const cafe_config* cfg, cafe_ctx** out);
+int cafe_ctx_destroy(cafe_ctx* ctx);
+const char* cafe_last_error(const cafe_ctx* ctx);
+const char* cafe_status_string(int status);
+int cafe_version(void);
+
+/* ---- inputs ---------------------------------------------------------- */
+/* Species tree (clade, src/clade.h:25-121). Nodes are numbered so that the
+ * children of every node appear in increasing index (Newick order), which
+ * is the descendant order used for the product over children. parent[i]
+ * is -1 for the root. lambda_index[i] (0-based) selects the rate of the
+ * branch above node i (multiple_lambda, src/lambda.cpp:32-40); NULL means
+ * all 0. Leaves are the nodes without children, in increasing index; that
+ * order is the column order of the counts passed to cafe_families_upload. */
+int cafe_tree_upload(cafe_ctx* ctx, int n_nodes, const int32_t* parent, const double* branch_length,
+                     const int32_t* lambda_index, int* tree_id);
+
+/* Gene families (gene_family, src/gene_family.h) as an int32 matrix
+ * counts[n_families][n_leaves], kept resident on the device. */
+int cafe_families_upload(cafe_ctx* ctx, int tree_id, const int32_t* counts, int64_t n_families, int n_leaves,
+                         int* set_id);
+/* Replace the counts of an existing set in place (same shape). */
+int cafe_families_update(cafe_ctx* ctx, int set_id, const int32_t* counts);
+int cafe_families_free(cafe_ctx* ctx, int set_id);
+
+/* Root prior: prior[j] = root_equilibrium_distribution::compute(j)
+ * (src/root_equilibrium_distribution.cpp:81-87), already rounded to float
+ * by the caller, for root-vector index j; 0 beyond n. */
+int cafe_prior_set(cafe_ctx* ctx, const double* prior, int n);
+
+/* Error model (error_model::get_probs, src/error_model.cpp:52-57): rows of
+ * n_dev probabilities per observed count; counts past the last row use the
+ * last row. n_rows = 0 clears it. */
+int cafe_error_model_set(cafe_ctx* ctx, const double* rows, int n_rows, int n_dev);
+
+/* ---- matrix cache (matrix_cache, src/matrix_cache.h:70-96) ------------ */
+/* precalculate_matrices (src/matrix_cache.cpp:113-163): build every missing
+ * (lambda, t) matrix of the given size, keyed and computed at
+ * lambda truncated to 1e-9 and t truncated to 1e-3. */
+int cafe_matrices_build(cafe_ctx* ctx, const double* lambdas, int n_lambdas, const double* branch_lengths,
+                        int n_branch_lengths, int matrix_size);
+/* get_matrix (src/matrix_cache.cpp:88-105): copy one cached matrix
+ * (row-major size x size) to host memory; CAFE_ERR_MISSING_MATRIX if the
+ * key was never built. */
+int cafe_matrix_get(cafe_ctx* ctx, double lambda, double branch_length, int matrix_size, double* out);
+int cafe_matrix_cache_size(cafe_ctx* ctx, int64_t* n_matrices);
+int cafe_matrix_cache_clear(cafe_ctx* ctx);
+/* is_saturated (src/matrix_cache.cpp:107-111). */
+int cafe_is_saturated(double branch_length, double lambda);
+
+/* ---- scoring --------------------------------------------------------- */
+/* Synchronous infer_family_likelihoods (src/base_model.cpp:53-100,
+ * src/gamma_core.cpp:168-237): results copied into the caller's host
+ * buffers. Rejections the reference reports as a score (invalid lambda,
+ * saturation, gamma underflow) return CAFE_OK with total_neg_lnl = +inf
+ * and result->status set. */
+int cafe_score(cafe_ctx* ctx, const cafe_request* req, cafe_result* res);
+
+/* Device-resident variant: enqueues the whole evaluation on `stream`
+ * (a cudaStream_t; NULL = the context's stream) and writes per-family lnL
+ * to d_family_lnl (device, n_families doubles, may be NULL) and the total
+ * to d_total (device, one double, may be NULL) without any host sync.
+ * res->status and counters are not filled. */
+int cafe_score_device(cafe_ctx* ctx, const cafe_request* req, double* d_family_lnl, double* d_total,
+                      void* stream);
+
+/* Continuous-batching request loop for many concurrent optimizers: submit
+ * returns at once with a ticket; the request is admitted when a stream and
+ * enough device memory are free, runs concurrently with other admitted
+ * requests, and fills `res` (host buffers must stay valid until done).
+ * poll returns CAFE_OK when finished, CAFE_ERR_BUSY while pending;
+ * wait_ms < 0 waits without limit, otherwise at most wait_ms. */
+int cafe_submit(cafe_ctx* ctx, const cafe_request* req, cafe_result* res, uint64_t* ticket);
+int cafe_poll(cafe_ctx* ctx, uint64_t ticket, int wait_ms);
+
+/* Serving statistics since context creation: completed requests, p50 and
+ * p99 latency (ms, submit -> done), current in-flight count. */
+int cafe_serving_stats(cafe_ctx* ctx, int64_t* completed, double* p50_ms, double* p99_ms, int* in_flight);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

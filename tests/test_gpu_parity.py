@@ -1,0 +1,196 @@
+"""GPU parity through the C ABI: the FP64 path against the reference's own
+outputs (committed fixtures) and against the CPU oracle.
+
+Tolerances (stated per test):
+  * transition matrices: relative 1e-12 per entry >= 1e-280 (the GPU builds
+    them with an O(S^2) recurrence, the reference with per-term exp/pow);
+  * -lnL and per-family lnL: relative 1e-10 (the parity bar for the plain
+    FP64 path).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from golden_cases import load_cases, load_json
+
+pytestmark = pytest.mark.gpu
+
+CASES = load_cases()
+REL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from cafe5_gb300.engine import Context
+    c = Context()
+    yield c
+    c.close()
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+
+
+def test_matrices_match_reference_bits(ctx):
+    d = load_json("ref_matrices.json")
+    for m in d["matrices"]:
+        ctx.matrices_build([m["lambda"]], [m["t"]], m["size"])
+        ours = ctx.matrix_get(m["lambda"], m["t"], m["size"])
+        ref = np.array([[float.fromhex(x) for x in row] for row in m["hex"]])
+        mask = ref >= 1e-280
+        assert np.all(rel_err(ours[mask], ref[mask]) <= 1e-12), (m["lambda"], m["t"])
+        assert np.all(np.abs(ours[~mask]) <= 1e-270)
+
+
+@pytest.mark.parametrize("lam,t,size", [(0.002, 1.0, 200), (0.0005, 150.0, 257), (0.01, 68.71, 150),
+                                         (0.0113, 44.0, 96), (0.3, 1.5, 40), (0.0025, 0.001, 64),
+                                         (0.05, 25.0, 12), (0.02, 0.5, 601)])
+def test_matrix_build_vs_oracle(ctx, lam, t, size):
+    ctx.matrices_build([lam], [t], size)
+    ours = ctx.matrix_get(lam, t, size)
+    ref = oracle.fill_matrix(lam, t, size)
+    mask = ref >= 1e-280
+    assert np.all(rel_err(ours[mask], ref[mask]) <= 1e-12)
+    assert np.all(ours[~mask] <= 1e-270)
+    assert ours[0, 0] == 1.0 and np.all(ours[0, 1:] == 0)
+
+
+def test_missing_matrix_is_reported(ctx):
+    from cafe5_gb300._lib import CafeError
+    with pytest.raises(CafeError) as e:
+        ctx.matrix_get(0.123456, 9.87, 17)
+    assert e.value.code == 2
+
+
+def _score_case(ctx, case, precision="fp64_ref", prior=None, **kw):
+    tid = ctx.upload_tree(case.tree, case.lambda_of_node)
+    sid = ctx.upload_families(tid, case.counts)
+    ctx.set_prior(case.prior if prior is None else prior)
+    ctx.set_error_model(case.err_rows)
+    r = ctx.score(tid, sid, case.lambdas, model=case.model, lambda_kind=case.lambda_kind,
+                  multipliers=case.multipliers, cat_probs=case.cat_probs, use_error_model=case.err_rows is not None,
+                  S=case.S if precision == "fp64_ref" else 0, R=case.R if precision == "fp64_ref" else 0,
+                  precision=precision, want_categories=True, **kw)
+    ctx.free_families(sid)
+    return r
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c.name for c in CASES])
+@pytest.mark.parametrize("dedupe", [False, True])
+def test_fp64_ref_matches_reference(ctx, case, dedupe):
+    """Plain FP64 path vs the reference's own -lnL and per-family lnL
+    (tolerance: 1e-10 relative)."""
+    r = _score_case(ctx, case, dedupe=dedupe)
+    if math.isinf(case.total):
+        assert r.total == math.inf
+        return
+    assert abs(r.total - case.total) <= REL * abs(case.total), (r.total, case.total)
+    if case.model == 0:
+        exp = np.array(case.fam_lnl)
+        fin = np.isfinite(exp)
+        assert np.all(rel_err(r.family_lnl[fin], exp[fin]) <= REL)
+        assert np.all(r.family_lnl[~fin] == exp[~fin])
+    else:
+        for f, cats in enumerate(case.cat):
+            fam_lh = float.fromhex(cats[0]["fam_lh"])
+            assert abs(r.family_lnl[f] - math.log(fam_lh)) <= REL * abs(math.log(fam_lh))
+            for k, c in enumerate(cats):
+                lc = math.log(float.fromhex(c["cat_lh"]))
+                assert abs(r.category_lnl[f, k] - lc) <= REL * abs(lc)
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if not math.isinf(c.total) or c.name == "syn_base_underflow"],
+                         ids=lambda c: c.name)
+def test_fp64_binned_matches_scaled_oracle(ctx, case):
+    """Per-family S-bins with power-of-two rescale vs the rescaled oracle at
+    the same bins (tolerance: 1e-10 relative)."""
+    from cafe5_gb300.families import FamilySet, bin_families
+    fams = FamilySet([str(i) for i in range(len(case.counts))], case.counts)
+    W, S, R = bin_families(fams)
+    ta = oracle.TreeArrays.from_tree(case.tree, case.lambda_of_node)
+    prior = np.zeros(int(W.max()) + 8)
+    prior[:len(case.prior)] = case.prior[:len(prior)]
+    tot, fam, cat = oracle.score(ta, case.counts, case.lambdas, lambda_kind=case.lambda_kind, model=case.model,
+                                 multipliers=case.multipliers, cat_probs=case.cat_probs, prior=prior,
+                                 err_rows=case.err_rows, fam_S=S, fam_R=R, scaled=True, dedupe=False)
+    r = _score_case(ctx, case, precision="fp64_binned", prior=prior)
+    if math.isinf(tot):
+        assert r.total == math.inf
+        return
+    assert abs(r.total - tot) <= REL * abs(tot)
+    assert np.all(rel_err(r.family_lnl, fam) <= REL)
+
+
+def test_reference_config0_workload_vs_oracle(ctx):
+    """1,000 families, 12 taxa: FP64_REF vs the oracle with the reference's
+    global bounds."""
+    from cafe5_gb300.families import global_bounds
+    from cafe5_gb300.inputs import RootPrior
+    from cafe5_gb300.synth import workload
+    w = workload(0)
+    S, R = global_bounds(w.families)
+    prior = RootPrior.uniform(R).vector()
+    ta = oracle.TreeArrays.from_tree(w.tree)
+    tot, fam, _ = oracle.score(ta, w.families.counts, [0.0025], prior=prior, S=S, R=R)
+    tid = ctx.upload_tree(w.tree)
+    sid = ctx.upload_families(tid, w.families.counts)
+    ctx.set_prior(prior)
+    ctx.set_error_model(None)
+    r = ctx.score(tid, sid, [0.0025], S=S, R=R, precision="fp64_ref")
+    assert abs(r.total - tot) <= REL * abs(tot)
+    assert np.all(rel_err(r.family_lnl, fam) <= REL)
+
+
+def test_rejections_are_scores(ctx):
+    """Invalid lambda and gamma saturation return +inf (base_model.cpp:56-60,
+    gamma_core.cpp:174-178) without an error."""
+    case = [c for c in CASES if c.name == "syn_base_12taxa"][0]
+    tid = ctx.upload_tree(case.tree)
+    sid = ctx.upload_families(tid, case.counts)
+    ctx.set_prior(case.prior)
+    ctx.set_error_model(None)
+    r = ctx.score(tid, sid, [0.0], S=case.S, R=case.R)
+    assert r.total == math.inf
+    r = ctx.score(tid, sid, [-1.0], S=case.S, R=case.R)
+    assert r.total == math.inf
+    r = ctx.score(tid, sid, [5.0], model=1, multipliers=[0.5, 1.5], cat_probs=[0.5, 0.5], S=case.S, R=case.R)
+    assert r.total == math.inf and r.status == 3
+
+
+def test_invalid_arguments_fail_loudly(ctx):
+    from cafe5_gb300._lib import CafeError
+    case = [c for c in CASES if c.name == "syn_base_12taxa"][0]
+    tid = ctx.upload_tree(case.tree)
+    with pytest.raises(CafeError):
+        ctx.upload_families(tid, case.counts[:, :5])        # wrong column count
+    sid = ctx.upload_families(tid, case.counts)
+    with pytest.raises(CafeError):
+        ctx.score(tid, sid, [0.01], S=3, R=30)             # a count exceeds S
+    with pytest.raises(CafeError):
+        ctx.score(tid, 999, [0.01], S=case.S, R=case.R)    # unknown set
+
+
+def test_serving_results_equal_alone_and_in_the_mix(ctx):
+    """Requests from several 'optimizers' submitted together give the same
+    results as the same requests scored alone."""
+    from cafe5_gb300.synth import workload
+    from cafe5_gb300.families import global_bounds
+    from cafe5_gb300.inputs import RootPrior
+    w = workload(0, n_families=300, seed=11)
+    S, R = global_bounds(w.families)
+    tid = ctx.upload_tree(w.tree)
+    sid = ctx.upload_families(tid, w.families.counts)
+    ctx.set_prior(RootPrior.uniform(R).vector())
+    ctx.set_error_model(None)
+    lams = [0.001 * (1 + i) for i in range(12)]
+    alone = [ctx.score(tid, sid, [l], S=S, R=R) for l in lams]
+    handles = [ctx.submit(tid, sid, [l], S=S, R=R) for l in lams]
+    mixed = [ctx.poll(h, -1) for h in handles]
+    for a, m in zip(alone, mixed):
+        assert m.total == a.total
+        assert np.array_equal(m.family_lnl, a.family_lnl)
+    st = ctx.serving_stats()
+    assert st["completed"] >= len(lams) and st["p99_ms"] >= st["p50_ms"] > 0
