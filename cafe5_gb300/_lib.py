@@ -24,7 +24,8 @@ EXPORTS = [
     "cafe_tree_upload", "cafe_families_upload", "cafe_families_update", "cafe_families_free",
     "cafe_prior_set", "cafe_error_model_set", "cafe_matrices_build", "cafe_matrix_get",
     "cafe_matrix_cache_size", "cafe_matrix_cache_clear", "cafe_is_saturated", "cafe_score",
-    "cafe_score_device", "cafe_submit", "cafe_poll", "cafe_serving_stats",
+    "cafe_score_device", "cafe_submit", "cafe_poll", "cafe_serving_stats", "cafe_profile_enable",
+    "cafe_profile_read",
 ]
 
 
@@ -45,6 +46,12 @@ class Result(C.Structure):
     _fields_ = [("family_lnl", C.c_void_p), ("category_lnl", C.c_void_p), ("total_neg_lnl", C.c_double),
                 ("status", C.c_int), ("n_failed", C.c_int64), ("n_fallback", C.c_int64),
                 ("device_ms", C.c_double)]
+
+
+class Timings(C.Structure):
+    _fields_ = [("matrix_ms", C.c_double), ("prune_ms", C.c_double), ("finish_ms", C.c_double),
+                ("other_ms", C.c_double), ("prune_flops", C.c_double), ("launches", C.c_int64),
+                ("prune_launches", C.c_int64), ("matrices_built", C.c_int64)]
 
 
 _lib = None
@@ -87,6 +94,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
         "cafe_submit": (i, [p, P(Request), P(Result), P(C.c_uint64)]),
         "cafe_poll": (i, [p, C.c_uint64, i]),
         "cafe_serving_stats": (i, [p, P(i64), P(d), P(d), P(i)]),
+        "cafe_profile_enable": (i, [p, i]),
+        "cafe_profile_read": (i, [p, P(Timings)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -75,6 +75,47 @@ int Workspace::init(int device) {
     return CAFE_OK;
 }
 
+cudaEvent_t Profiler::get() {
+    if (!pool.empty()) {
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+void Profiler::begin(int kind, cudaStream_t s, cudaEvent_t* a) {
+    (void)kind;
+    *a = nullptr;
+    if (!on) return;
+    *a = get();
+    cudaEventRecord(*a, s);
+}
+void Profiler::end(int kind, cudaStream_t s, cudaEvent_t a) {
+    acc.launches++;
+    if (!on || !a) return;
+    cudaEvent_t b = get();
+    cudaEventRecord(b, s);
+    pending.push_back({kind, {a, b}});
+}
+void Profiler::collect() {
+    for (auto& p : pending) {
+        cudaEventSynchronize(p.second.second);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+        switch (p.first) {
+            case 0: acc.matrix_ms += ms; break;
+            case 1: acc.prune_ms += ms; acc.prune_launches++; break;
+            case 2: acc.finish_ms += ms; break;
+            default: acc.other_ms += ms; break;
+        }
+        pool.push_back(p.second.first);
+        pool.push_back(p.second.second);
+    }
+    pending.clear();
+}
+
 cudaError_t launch_fill(double* p, int64_t n, double v, cudaStream_t s);
 cudaError_t launch_fill_i32(int32_t* p, int64_t n, int32_t v, cudaStream_t s);
 
@@ -333,7 +374,14 @@ int cache_build(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
         cur += (size_t)k.size * k.size * sizeof(double);
     }
     CK(cudaMemcpyAsync(ws.jobs.p, J, n * sizeof(MatrixJob), cudaMemcpyHostToDevice, ws.stream), "jobs");
+    const bool prof = (&ws == C->ws[0].get());
+    cudaEvent_t ev;
+    if (prof) C->prof.begin(0, ws.stream, &ev);
     CK(launch_matrix_build(ws.jobs.as<MatrixJob>(), (int)n, max_size, ws.stream), "matrix build");
+    if (prof) {
+        C->prof.end(0, ws.stream, ev);
+        C->prof.acc.matrices_built += (int64_t)n;
+    }
     // the pinned job buffer is reused by the next request on this stream
     CK(cudaStreamSynchronize(ws.stream), "matrix build");
     P.keys.clear();
@@ -537,7 +585,29 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_f
     }
     a.tile_families = TFm;
     a.W = W;
+    const bool prof = (&ws == C->ws[0].get());
+    cudaEvent_t ev;
+    if (prof) {
+        C->prof.begin(1, ws.stream, &ev);
+        // algorithmic flops of this launch
+        double fl = 0;
+        for (const PruneTile& t : tiles) {
+            double per = 0;
+            for (size_t ii = 0; ii < T.internal.size(); ++ii) {
+                const int v = T.internal[ii];
+                const int rows = (v == T.root) ? t.R : t.S + 1;
+                const int nch = T.cstart[ii + 1] - T.cstart[ii];
+                for (int ci = T.cstart[ii]; ci < T.cstart[ii + 1]; ++ci)
+                    if (!T.children[T.child[ci]].empty()) per += 2.0 * rows * (t.S + 1);
+                    else if (R->use_error_model) per += 6.0 * rows;
+                per += (double)(nch - 1) * rows;
+            }
+            fl += per * t.count;
+        }
+        C->prof.acc.prune_flops += fl;
+    }
     CK(launch_prune64(a, n_ctas, ws.stream), "prune");
+    if (prof) C->prof.end(1, ws.stream, ev);
 
     FinishArgs fa{};
     fa.F = F;
@@ -549,7 +619,9 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_f
     fa.family_lnl = d_fam;
     fa.total = d_total;
     fa.n_failed = ws.nfail.as<int32_t>();
+    if (prof) C->prof.begin(2, ws.stream, &ev);
     CK(launch_finish(fa, ws.stream), "finish");
+    if (prof) C->prof.end(2, ws.stream, ev);
     return CAFE_OK;
 }
 
@@ -897,6 +969,23 @@ int cafe_score(cafe_ctx* C, const cafe_request* req, cafe_result* res) {
     std::lock_guard<std::mutex> lk(C->mu);
     cudaSetDevice(C->device);
     return score_sync(C, *C->ws[0], req, res);
+}
+
+int cafe_profile_enable(cafe_ctx* C, int enable) {
+    if (!C) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->mu);
+    C->prof.on = enable != 0;
+    return CAFE_OK;
+}
+
+int cafe_profile_read(cafe_ctx* C, cafe_timings* out) {
+    if (!C || !out) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    C->prof.collect();
+    *out = C->prof.acc;
+    C->prof.acc = cafe_timings{};
+    return CAFE_OK;
 }
 
 int cafe_score_device(cafe_ctx* C, const cafe_request* req, double* d_family_lnl, double* d_total, void* stream) {

@@ -239,9 +239,9 @@ __global__ void __launch_bounds__(NT) k_prune64(Prune64Args a) {
 // compensated reduction (one block).
 __global__ void __launch_bounds__(1024) k_finish(FinishArgs a) {
     __shared__ double ssum[1024], scomp[1024];
-    __shared__ int sfail[1024];
+    __shared__ int sfail[1024], sinf[1024];
     double sum = 0.0, comp = 0.0;
-    int fail = 0;
+    int fail = 0, ninf = 0;   // ninf: families with lnL = -inf (log of an underflowed 0)
     for (int64_t f = threadIdx.x; f < a.F; f += blockDim.x) {
         const int64_t r = a.ref ? a.ref[f] : f;
         double lnl;
@@ -273,7 +273,9 @@ __global__ void __launch_bounds__(1024) k_finish(FinishArgs a) {
             fail += bad;
         }
         a.family_lnl[f] = lnl;
-        if (!isnan(lnl)) {
+        if (isinf(lnl)) {
+            ninf++;
+        } else if (!isnan(lnl)) {
             // Neumaier summation
             const double tt = sum + lnl;
             if (fabs(sum) >= fabs(lnl)) comp += (sum - tt) + lnl;
@@ -284,10 +286,11 @@ __global__ void __launch_bounds__(1024) k_finish(FinishArgs a) {
     ssum[threadIdx.x] = sum;
     scomp[threadIdx.x] = comp;
     sfail[threadIdx.x] = fail;
+    sinf[threadIdx.x] = ninf;
     __syncthreads();
     if (threadIdx.x == 0) {
         double s = 0.0, c = 0.0;
-        int fl = 0;
+        int fl = 0, ni = 0;
         for (int i = 0; i < (int)blockDim.x; ++i) {
             const double x = ssum[i];
             const double tt = s + x;
@@ -296,9 +299,11 @@ __global__ void __launch_bounds__(1024) k_finish(FinishArgs a) {
             s = tt;
             c += scomp[i];
             fl += sfail[i];
+            ni += sinf[i];
         }
         *a.n_failed = fl;
-        *a.total = fl ? INFINITY : -(s + c);
+        // -sum lnL: +inf on gamma failure or when any family's lnL is -inf
+        *a.total = (fl || ni) ? INFINITY : -(s + c);
     }
 }
 

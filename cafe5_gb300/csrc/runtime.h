@@ -102,6 +102,18 @@ struct Workspace {
 
 struct Request;   // serving-loop request record
 
+// Event pairs recorded around launches when profiling is on.
+struct Profiler {
+    bool on = false;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;   // (kind, events)
+    std::vector<cudaEvent_t> pool;
+    cafe_timings acc{};
+    cudaEvent_t get();
+    void begin(int kind, cudaStream_t s, cudaEvent_t* a);
+    void end(int kind, cudaStream_t s, cudaEvent_t a);
+    void collect();
+};
+
 }  // namespace cafe
 
 struct cafe_ctx {
@@ -135,4 +147,5 @@ struct cafe_ctx {
     int in_flight = 0;
     std::vector<double> latencies_ms;
     int64_t completed = 0;
+    cafe::Profiler prof;
 };

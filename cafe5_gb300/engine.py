@@ -146,7 +146,7 @@ class Context:
 
     def score(self, tree_id, set_id, lambdas, *, want_categories=False, **kw) -> ScoreResult:
         req, keep = self.make_request(tree_id, set_id, lambdas, **kw)
-        F = self._set_shape[set_id][0]
+        F = self._set_shape.get(set_id, (0,))[0]     # unknown ids are reported by the library
         K = req.n_categories
         fam = np.zeros(F)
         cat = np.zeros((F, K)) if want_categories else None
@@ -179,6 +179,14 @@ class Context:
         r = handle["res"]
         return ScoreResult(r.total_neg_lnl, handle["fam"], handle["cat"], r.status, r.n_failed, r.n_fallback,
                            r.device_ms)
+
+    def profile(self, enable: bool = True):
+        self._check(self.lib.cafe_profile_enable(self.h, 1 if enable else 0))
+
+    def profile_read(self) -> dict:
+        t = _lib.Timings()
+        self._check(self.lib.cafe_profile_read(self.h, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in _lib.Timings._fields_}
 
     def serving_stats(self):
         n = C.c_int64()

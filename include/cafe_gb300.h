@@ -167,6 +167,26 @@ int cafe_score_device(cafe_ctx* ctx, const cafe_request* req, double* d_family_l
 int cafe_submit(cafe_ctx* ctx, const cafe_request* req, cafe_result* res, uint64_t* ticket);
 int cafe_poll(cafe_ctx* ctx, uint64_t ticket, int wait_ms);
 
+/* Per-kernel device timing for measurement. When enabled, the library
+ * records CUDA events around each kernel it launches on the synchronous
+ * workspace stream (cafe_score / cafe_score_device) and accumulates their
+ * durations; cafe_profile_read waits for that stream, returns the sums
+ * since the previous read and resets them. `prune_flops` is the
+ * algorithmic flop count of the pruning launches (2 x rows x states per
+ * internal-child contraction, rows x states per extra child product). */
+typedef struct {
+    double matrix_ms;            /* K1 transition-matrix builds */
+    double prune_ms;             /* pruning + root weighting (FP64 or tensor core) */
+    double finish_ms;            /* per-family lnL and the total */
+    double other_ms;             /* conversion / fallback launches */
+    double prune_flops;
+    int64_t launches;            /* kernels launched */
+    int64_t prune_launches;
+    int64_t matrices_built;
+} cafe_timings;
+int cafe_profile_enable(cafe_ctx* ctx, int enable);
+int cafe_profile_read(cafe_ctx* ctx, cafe_timings* out);
+
 /* Serving statistics since context creation: completed requests, p50 and
  * p99 latency (ms, submit -> done), current in-flight count. */
 int cafe_serving_stats(cafe_ctx* ctx, int64_t* completed, double* p50_ms, double* p99_ms, int* in_flight);
