@@ -223,7 +223,10 @@ def run_ours(args):
     ctx.set_error_model(None)
     kw = dict(model=1, multipliers=w.multipliers, cat_probs=w.cat_probs, precision=prec,
               S=S if prec == "fp64_ref" else 0, R=R if prec == "fp64_ref" else 0)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: the legacy default stream has handle 0, which the
+    # C ABI reads as "the context's own stream"
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     d_fam = torch.empty(F, dtype=torch.float64, device=dev)
     d_tot = torch.empty(1, dtype=torch.float64, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > 129 MB L2
