@@ -25,7 +25,7 @@ EXPORTS = [
     "cafe_prior_set", "cafe_error_model_set", "cafe_matrices_build", "cafe_matrix_get",
     "cafe_matrix_cache_size", "cafe_matrix_cache_clear", "cafe_is_saturated", "cafe_score",
     "cafe_score_device", "cafe_submit", "cafe_poll", "cafe_serving_stats", "cafe_profile_enable",
-    "cafe_profile_read",
+    "cafe_profile_read", "cafe_prune_fp64_noalloc",
 ]
 
 
@@ -96,6 +96,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
         "cafe_serving_stats": (i, [p, P(i64), P(d), P(d), P(i)]),
         "cafe_profile_enable": (i, [p, i]),
         "cafe_profile_read": (i, [p, P(Timings)]),
+        "cafe_prune_fp64_noalloc": (i, [i, p, p, i, p, i64, i, i, i, p, i, i, p, p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -187,6 +187,36 @@ typedef struct {
 int cafe_profile_enable(cafe_ctx* ctx, int enable);
 int cafe_profile_read(cafe_ctx* ctx, cafe_timings* out);
 
+/* No-allocation FP64 pruning, for callers that cannot call cudaMalloc (a
+ * host framework that owns every device allocation through its own pool, a
+ * serving loop that must not allocate per request, a plug-in living inside
+ * another allocator). No counterpart in the reference: it is an extra entry
+ * point of this library. It runs the same pruning kernel as cafe_score in
+ * FP64 for the base model (per-family lnL = max_j log L_root[j] + log
+ * prior[j], src/base_model.cpp:77-95) with one global state bound, and takes
+ * every input and output as the caller's memory:
+ *   parent[n_nodes]         host, tree as in cafe_tree_upload
+ *   node_matrix[n_nodes]    host array of device pointers: the FP64
+ *                           matrix_size x matrix_size matrix of the branch
+ *                           above each node (root entry ignored)
+ *   d_counts                device int32 [n_families][n_leaves]
+ *   d_prior                 device, n_prior doubles (float-rounded prior)
+ *   scaled                  0 = reference arithmetic, 1 = per-node rescale
+ *   d_family_lnl            device output, n_families doubles
+ *   stream                  cudaStream_t the work is enqueued on
+ * It allocates nothing: its working space is one static device array of
+ * 40 MiB that the library reserves on every GPU that loads it until the
+ * process exits. Limits: n_families <= 262,144, n_nodes <= 512, and
+ * (internal-node slots) x max(S+1, R) x 32 doubles must fit in 32 MiB;
+ * larger calls return CAFE_ERR_INVALID without launching anything. The
+ * first call on each device looks up the array's device address (with that
+ * device current), so make it before any stream capture. All calls share
+ * the array: calls whose GPU work overlaps race and must be serialised. */
+int cafe_prune_fp64_noalloc(int n_nodes, const int32_t* parent, const double* const* node_matrix,
+                            int matrix_size, const int32_t* d_counts, int64_t n_families, int n_leaves,
+                            int max_family_size, int max_root_family_size, const double* d_prior, int n_prior,
+                            int scaled, double* d_family_lnl, void* stream);
+
 /* Serving statistics since context creation: completed requests, p50 and
  * p99 latency (ms, submit -> done), current in-flight count. */
 int cafe_serving_stats(cafe_ctx* ctx, int64_t* completed, double* p50_ms, double* p99_ms, int* in_flight);
