@@ -16,7 +16,7 @@ STATUS = {0: "ok", 1: "oom", 2: "missing matrix", 3: "saturated", 4: "underflow"
           6: "invalid", 7: "cuda", 8: "busy", 9: "not found"}
 MODEL_BASE, MODEL_GAMMA = 0, 1
 LAMBDA_SINGLE, LAMBDA_MULTIPLE = 0, 1
-PREC_FP64_REF, PREC_FP64_BINNED, PREC_MIXED_BF16X3 = 0, 1, 2
+PREC_FP64_REF, PREC_FP64_BINNED, PREC_MIXED_TF32X3 = 0, 1, 2
 
 # every symbol the header declares
 EXPORTS = [

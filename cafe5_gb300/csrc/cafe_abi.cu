@@ -410,7 +410,310 @@ struct ScoreInfo {
     int reject_status = CAFE_OK;
     bool scaled = false;
     size_t footprint = 0;
+    int64_t n_fallback = 0;
 };
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// 2D FP32 tensor map [rows][cols], 32 x 32 boxes, 128-byte swizzle.
+int encode_map(cafe_ctx* C, CUtensorMap* m, const float* base, int64_t rows, int cols) {
+    static EncodeTiledFn enc = nullptr;
+    if (!enc) {
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", (void**)&enc, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            !enc) {
+            enc = nullptr;
+            return fail(C, CAFE_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+        }
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)cols * sizeof(float)};
+    cuuint32_t box[2] = {32, 32};
+    cuuint32_t es[2] = {1, 1};
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(C, CAFE_ERR_CUDA, "tensor map encode failed (%d)", (int)r);
+    return CAFE_OK;
+}
+
+// Launch k_prune64 (per-node rescaled FP64) for the given 32-family tiles.
+int launch_fp64_tiles(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T, FamSet& S, int K,
+                      const std::vector<PruneTile>& tiles, DevBuf& d_tiles, PinnedBuf& h_tiles, const int64_t* d_perm,
+                      int W, int msize, double* out, int prof_kind) {
+    if (tiles.empty()) return CAFE_OK;
+    const int n = (int)tiles.size();
+    CK(h_tiles.reserve(n * sizeof(PruneTile)), "tiles");
+    CK(d_tiles.reserve(n * sizeof(PruneTile)), "tiles");
+    std::memcpy(h_tiles.p, tiles.data(), n * sizeof(PruneTile));
+    CK(cudaMemcpyAsync(d_tiles.p, h_tiles.p, n * sizeof(PruneTile), cudaMemcpyHostToDevice, ws.stream), "tiles");
+    const int n_ctas = std::max(1, std::min(n, C->n_ctas));
+    const int64_t per_cta = (int64_t)T.n_slots * W * 32;
+    CK(ws.scratch.reserve((size_t)n_ctas * per_cta * sizeof(double)), "scratch");
+    Prune64Args a{};
+    a.plan = T.plan;
+    a.tiles = d_tiles.as<PruneTile>();
+    a.n_tiles = n;
+    a.counts = S.d_counts.as<int32_t>();
+    a.perm = d_perm;
+    a.mats = ws.mats.as<const double*>();
+    a.ld_mat = msize;
+    a.prior = C->d_prior.as<double>();
+    a.n_prior = (int)C->prior.size();
+    a.err = R->use_error_model ? C->d_err.as<double>() : nullptr;
+    a.err_rows = C->err_rows;
+    a.err_ndev = C->err_ndev;
+    a.fam_R = S.bins.d_famR.as<int32_t>();
+    a.scratch = ws.scratch.as<double>();
+    a.scratch_per_cta = per_cta;
+    a.scaled = 1;
+    a.model = R->model == CAFE_MODEL_GAMMA ? 1 : 0;
+    a.out = out;
+    a.K = K;
+    a.cat_probs = ws.catp.as<double>();
+    a.tile_families = 32;
+    a.W = W;
+    const bool prof = (&ws == C->ws[0].get());
+    cudaEvent_t ev;
+    if (prof) C->prof.begin(prof_kind, ws.stream, &ev);
+    CK(launch_prune64(a, n_ctas, ws.stream), "prune fp64");
+    if (prof) C->prof.end(prof_kind, ws.stream, ev);
+    return CAFE_OK;
+}
+
+double tile_flops(const TreeHost& T, const PruneTile& t, bool err) {
+    double per = 0;
+    for (size_t ii = 0; ii < T.internal.size(); ++ii) {
+        const int v = T.internal[ii];
+        const int rows = (v == T.root) ? t.R : t.S + 1;
+        const int nch = T.cstart[ii + 1] - T.cstart[ii];
+        for (int ci = T.cstart[ii]; ci < T.cstart[ii + 1]; ++ci)
+            if (!T.children[T.child[ci]].empty()) per += 2.0 * rows * (t.S + 1);
+            else if (err) per += 6.0 * rows;
+        per += (double)(nch - 1) * rows;
+    }
+    return per * t.count;
+}
+
+// MIXED_TF32X3: tensor-core tiles for bins <= 256 states, FP64 tiles for
+// wider bins and for families the tensor-core pass flags. Caller holds C->mu;
+// hm holds the FP64 matrix of every (category, node).
+int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T, FamSet& S, int K, double** hm,
+                  double* d_fam, double* d_total, ScoreInfo* info) {
+    const bool gamma = R->model == CAFE_MODEL_GAMMA;
+    const int64_t F = S.F;
+    const BinPlan& B = S.bins;
+    const int msize = B.W_max;
+    int Wm = 0;
+    for (int w : B.widths)
+        if (w <= 256) Wm = std::max(Wm, w);
+    info->scaled = true;
+
+    // request-local matrix list and conversion to TF32 operands
+    std::vector<int32_t> mat_index((size_t)K * T.n_nodes, -1);
+    std::vector<ConvertJob> jobs;
+    std::unordered_map<const double*, int> seen;
+    for (int k = 0; k < K; ++k)
+        for (int v = 0; v < T.n_nodes; ++v) {
+            const double* m = hm[(size_t)k * T.n_nodes + v];
+            if (!m) continue;
+            auto it = seen.find(m);
+            int idx;
+            if (it == seen.end()) {
+                idx = (int)jobs.size();
+                seen[m] = idx;
+                jobs.push_back(ConvertJob{m, msize, idx});
+            } else {
+                idx = it->second;
+            }
+            mat_index[(size_t)k * T.n_nodes + v] = idx;
+        }
+    const int n_mat = (int)jobs.size();
+
+    // category probabilities (device) for both kernels
+    if (gamma) {
+        CK(ws.h_catp.reserve((size_t)K * sizeof(double)), "cat probs");
+        CK(ws.catp.reserve((size_t)K * sizeof(double)), "cat probs");
+        std::memcpy(ws.h_catp.p, R->cat_probs, K * sizeof(double));
+        CK(cudaMemcpyAsync(ws.catp.p, ws.h_catp.p, K * sizeof(double), cudaMemcpyHostToDevice, ws.stream), "cat probs");
+    } else {
+        CK(ws.h_catp.reserve(sizeof(double)), "cat probs");
+        CK(ws.catp.reserve(sizeof(double)), "cat probs");
+        *ws.h_catp.as<double>() = 1.0;
+        CK(cudaMemcpyAsync(ws.catp.p, ws.h_catp.p, sizeof(double), cudaMemcpyHostToDevice, ws.stream), "cat probs");
+    }
+    CK(ws.mats.reserve((size_t)K * T.n_nodes * sizeof(double*)), "mats");
+    CK(cudaMemcpyAsync(ws.mats.p, hm, (size_t)K * T.n_nodes * sizeof(double*), cudaMemcpyHostToDevice, ws.stream), "mats");
+    CK(ws.cat.reserve((size_t)std::max<int64_t>(F, 1) * K * sizeof(double)), "category buffer");
+    CK(ws.nfail.reserve(sizeof(int32_t)), "fail counter");
+    CK(ws.flags.reserve((size_t)std::max<int64_t>(F, 1) * sizeof(int32_t) + 64), "flags");
+    int32_t* d_flags = ws.flags.as<int32_t>();
+    int32_t* d_status = d_flags + std::max<int64_t>(F, 1);
+    CK(cudaMemsetAsync(ws.flags.p, 0, (size_t)std::max<int64_t>(F, 1) * sizeof(int32_t) + 64, ws.stream), "flags");
+
+    // tiles: 128 families (tensor cores) or 32 families (FP64, wide bins)
+    std::vector<PruneTile> tc_tiles, wide_tiles;
+    for (int k = 0; k < K; ++k)
+        for (size_t b = 0; b < B.widths.size(); ++b) {
+            const int w = B.widths[b];
+            const int step = w <= 256 ? 128 : 32;
+            for (int64_t i = 0; i < B.bin_count[b]; i += step) {
+                PruneTile t{};
+                t.first = (int)(B.bin_first[b] + i);
+                t.count = (int)std::min<int64_t>(step, B.bin_count[b] - i);
+                t.k = k;
+                t.S = w - 1;
+                t.R = w - 1;
+                (w <= 256 ? tc_tiles : wide_tiles).push_back(t);
+            }
+        }
+    const bool prof = (&ws == C->ws[0].get());
+    cudaEvent_t ev;
+    if (!tc_tiles.empty()) {
+        const size_t fl = (size_t)n_mat * Wm * Wm;
+        CK(ws.tc_hi.reserve(fl * sizeof(float)), "tc matrices");
+        CK(ws.tc_lo.reserve(fl * sizeof(float)), "tc matrices");
+        CK(ws.tc_ct.reserve(fl * sizeof(float)), "tc matrices");
+        CK(ws.tc_ce.reserve((size_t)n_mat * Wm * sizeof(int32_t)), "tc matrices");
+        CK(ws.h_conv.reserve(jobs.size() * sizeof(ConvertJob)), "convert jobs");
+        CK(ws.conv.reserve(jobs.size() * sizeof(ConvertJob)), "convert jobs");
+        std::memcpy(ws.h_conv.p, jobs.data(), jobs.size() * sizeof(ConvertJob));
+        CK(cudaMemcpyAsync(ws.conv.p, ws.h_conv.p, jobs.size() * sizeof(ConvertJob), cudaMemcpyHostToDevice, ws.stream),
+           "convert jobs");
+        CK(ws.tc_mi.reserve(mat_index.size() * sizeof(int32_t)), "mat index");
+        CK(ws.h_mi.reserve(mat_index.size() * sizeof(int32_t)), "mat index");
+        std::memcpy(ws.h_mi.p, mat_index.data(), mat_index.size() * sizeof(int32_t));
+        CK(cudaMemcpyAsync(ws.tc_mi.p, ws.h_mi.p, mat_index.size() * sizeof(int32_t), cudaMemcpyHostToDevice, ws.stream),
+           "mat index");
+        TcBuffers tb{ws.tc_hi.as<float>(), ws.tc_lo.as<float>(), ws.tc_ct.as<float>(), ws.tc_ce.as<int32_t>(), Wm};
+        if (prof) C->prof.begin(3, ws.stream, &ev);
+        CK(launch_convert_tc(ws.conv.as<ConvertJob>(), n_mat, tb, ws.stream), "convert");
+        if (prof) C->prof.end(3, ws.stream, ev);
+
+        // occupancy: shared memory and 512 TMEM columns per SM
+        const int tmem_cols = 2 * Wm <= 64 ? 64 : (2 * Wm <= 128 ? 128 : (2 * Wm <= 256 ? 256 : 512));
+        size_t smem = prune_tc_smem_bytes(Wm, T.n_slots);
+        const int by_tmem = 512 / tmem_cols;
+        int by_smem = (int)((227 * 1024) / smem);
+        if (by_smem < 1) return fail(C, CAFE_ERR_INVALID, "tensor-core tile does not fit shared memory");
+        int per_sm = std::min(by_tmem, by_smem);
+        // request enough shared memory that no more CTAs than TMEM allows share an SM
+        smem = std::max(smem, (size_t)((227 * 1024) / per_sm) - 1024);
+        const int n_tc = (int)tc_tiles.size();
+        const int n_ctas = std::max(1, std::min(n_tc, C->sm_count * per_sm));
+        const int64_t vrows = (int64_t)n_ctas * T.n_slots * 128;
+        CK(ws.tc_vhi.reserve((size_t)vrows * Wm * sizeof(float)), "tc vectors");
+        CK(ws.tc_vlo.reserve((size_t)vrows * Wm * sizeof(float)), "tc vectors");
+        TcMaps maps;
+        int rc = encode_map(C, &maps.mat_hi, ws.tc_hi.as<float>(), (int64_t)n_mat * Wm, Wm);
+        if (!rc) rc = encode_map(C, &maps.mat_lo, ws.tc_lo.as<float>(), (int64_t)n_mat * Wm, Wm);
+        if (!rc) rc = encode_map(C, &maps.vec_hi, ws.tc_vhi.as<float>(), vrows, Wm);
+        if (!rc) rc = encode_map(C, &maps.vec_lo, ws.tc_vlo.as<float>(), vrows, Wm);
+        if (rc) return rc;
+        CK(ws.tiles.reserve(n_tc * sizeof(PruneTile)), "tiles");
+        CK(ws.h_tiles.reserve(n_tc * sizeof(PruneTile)), "tiles");
+        std::memcpy(ws.h_tiles.p, tc_tiles.data(), n_tc * sizeof(PruneTile));
+        CK(cudaMemcpyAsync(ws.tiles.p, ws.h_tiles.p, n_tc * sizeof(PruneTile), cudaMemcpyHostToDevice, ws.stream),
+           "tiles");
+        PruneTcArgs a{};
+        a.plan = T.plan;
+        a.tiles = ws.tiles.as<PruneTile>();
+        a.n_tiles = n_tc;
+        a.counts = S.d_counts.as<int32_t>();
+        a.perm = B.d_perm.as<int64_t>();
+        a.mat_index = ws.tc_mi.as<int32_t>();
+        a.ct = ws.tc_ct.as<float>();
+        a.ce = ws.tc_ce.as<int32_t>();
+        a.Wm = Wm;
+        a.vec_hi = ws.tc_vhi.as<float>();
+        a.vec_lo = ws.tc_vlo.as<float>();
+        a.n_slots = T.n_slots;
+        a.prior = C->d_prior.as<double>();
+        a.n_prior = (int)C->prior.size();
+        a.err = R->use_error_model ? C->d_err.as<double>() : nullptr;
+        a.err_rows = C->err_rows;
+        a.err_ndev = C->err_ndev;
+        a.fam_R = B.d_famR.as<int32_t>();
+        a.out = ws.cat.as<double>();
+        a.K = K;
+        a.cat_probs = ws.catp.as<double>();
+        a.flags = d_flags;
+        a.status = d_status;
+        a.tmem_cols = tmem_cols;
+        if (prof) {
+            C->prof.begin(1, ws.stream, &ev);
+            for (const PruneTile& t : tc_tiles) C->prof.acc.prune_flops += tile_flops(T, t, R->use_error_model);
+        }
+        CK(launch_prune_tc(maps, a, n_ctas, smem, ws.stream), "prune tc");
+        if (prof) C->prof.end(1, ws.stream, ev);
+    }
+    int rc = launch_fp64_tiles(C, ws, R, T, S, K, wide_tiles, ws.tiles64, ws.h_tiles64, B.d_perm.as<int64_t>(), msize,
+                               msize, ws.cat.as<double>(), 3);
+    if (rc) return rc;
+
+    // families the tensor-core pass could not represent: FP64 recompute
+    int64_t n_fb = 0;
+    if (!tc_tiles.empty()) {
+        CK(ws.h_flags.reserve((size_t)std::max<int64_t>(F, 1) * sizeof(int32_t) + 64), "flags");
+        CK(cudaMemcpyAsync(ws.h_flags.p, ws.flags.p, (size_t)std::max<int64_t>(F, 1) * sizeof(int32_t) + 64,
+                           cudaMemcpyDeviceToHost, ws.stream),
+           "flags");
+        CK(cudaStreamSynchronize(ws.stream), "prune tc");
+        const int32_t* hf = ws.h_flags.as<int32_t>();
+        const int32_t st = hf[std::max<int64_t>(F, 1)];
+        if (st) return fail(C, CAFE_ERR_TIMEOUT, "tensor-core pruning gave up waiting (status %d)", st);
+        // flagged families, grouped by bin in the bin order of the permutation
+        std::vector<int64_t> fb_perm;
+        std::vector<PruneTile> fb_tiles;
+        std::vector<int64_t> perm_h;   // host copy of the bin permutation
+        perm_h.resize(F);
+        CK(cudaMemcpy(perm_h.data(), B.d_perm.p, F * sizeof(int64_t), cudaMemcpyDeviceToHost), "perm");
+        for (size_t b = 0; b < B.widths.size(); ++b) {
+            if (B.widths[b] > 256) continue;
+            const int64_t start = (int64_t)fb_perm.size();
+            for (int64_t i = B.bin_first[b]; i < B.bin_first[b] + B.bin_count[b]; ++i)
+                if (hf[perm_h[i]]) fb_perm.push_back(perm_h[i]);
+            const int64_t cnt = (int64_t)fb_perm.size() - start;
+            for (int k = 0; k < K; ++k)
+                for (int64_t i = 0; i < cnt; i += 32) {
+                    PruneTile t{};
+                    t.first = (int)(start + i);
+                    t.count = (int)std::min<int64_t>(32, cnt - i);
+                    t.k = k;
+                    t.S = B.widths[b] - 1;
+                    t.R = B.widths[b] - 1;
+                    fb_tiles.push_back(t);
+                }
+        }
+        n_fb = (int64_t)fb_perm.size();
+        if (n_fb) {
+            CK(ws.fb_perm.reserve(n_fb * sizeof(int64_t)), "fallback");
+            CK(cudaMemcpy(ws.fb_perm.p, fb_perm.data(), n_fb * sizeof(int64_t), cudaMemcpyHostToDevice), "fallback");
+            rc = launch_fp64_tiles(C, ws, R, T, S, K, fb_tiles, ws.tiles_fb, ws.h_tiles_fb, ws.fb_perm.as<int64_t>(),
+                                   msize, msize, ws.cat.as<double>(), 3);
+            if (rc) return rc;
+        }
+    }
+    info->n_fallback = n_fb;
+
+    FinishArgs fa{};
+    fa.F = F;
+    fa.K = K;
+    fa.model = gamma ? 1 : 0;
+    fa.scaled = 1;
+    fa.cat = ws.cat.as<double>();
+    fa.ref = nullptr;
+    fa.family_lnl = d_fam;
+    fa.total = d_total;
+    fa.n_failed = ws.nfail.as<int32_t>();
+    if (prof) C->prof.begin(2, ws.stream, &ev);
+    CK(launch_finish(fa, ws.stream), "finish");
+    if (prof) C->prof.end(2, ws.stream, ev);
+    return CAFE_OK;
+}
 
 // Enqueue one evaluation on ws.stream. Caller holds C->mu.
 int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_fam, double* d_total,
@@ -433,8 +736,8 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_f
     if (gamma && (K < 1 || !R->multipliers || !R->cat_probs)) return fail(C, CAFE_ERR_INVALID, "gamma needs K >= 1");
     if (C->prior.empty()) return fail(C, CAFE_ERR_INVALID, "no prior set (cafe_prior_set)");
     if (R->use_error_model && C->err_rows == 0) return fail(C, CAFE_ERR_INVALID, "no error model set");
-    if (R->precision == CAFE_PREC_MIXED_BF16X3) return fail(C, CAFE_ERR_INVALID, "mixed precision path not built");
-    if (R->precision != CAFE_PREC_FP64_REF && R->precision != CAFE_PREC_FP64_BINNED)
+    if (R->precision != CAFE_PREC_FP64_REF && R->precision != CAFE_PREC_FP64_BINNED &&
+        R->precision != CAFE_PREC_MIXED_TF32X3)
         return fail(C, CAFE_ERR_INVALID, "bad precision %d", R->precision);
     const int64_t F = S.F;
     info->F = F;
@@ -501,6 +804,27 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_f
     for (int k = 0; k < K; ++k)
         for (int v = 0; v < T.n_nodes; ++v)
             hm[(size_t)k * T.n_nodes + v] = T.parent[v] < 0 ? nullptr : cache_lookup(C, node_key[(size_t)k * T.n_nodes + v]);
+    if (R->precision == CAFE_PREC_MIXED_TF32X3) {
+        // saturated keys (1 - 2a < 0) and wide polytomies stay on the FP64 path
+        bool to_fp64 = false;
+        for (int k = 0; k < K && !to_fp64; ++k)
+            for (int v = 0; v < T.n_nodes; ++v)
+                if (T.parent[v] >= 0) {
+                    const MatKey& key = node_key[(size_t)k * T.n_nodes + v];
+                    const double lq = (double)key.lq / 1000000000.0, tq = (double)key.tq / 1000.0;
+                    const double al = lq * tq / (1 + lq * tq), co = 1 - 2 * al;
+                    if (!(co > 0 && co != 1)) to_fp64 = true;
+                }
+        int max_int = 0;
+        for (int v = 0; v < T.n_nodes; ++v) {
+            int ni = 0;
+            for (int c : T.children[v]) ni += !T.children[c].empty();
+            max_int = std::max(max_int, ni);
+        }
+        if (T.max_children > 8 || max_int > 2) to_fp64 = true;
+        if (!to_fp64) return enqueue_mixed(C, ws, R, T, S, K, hm, d_fam, d_total, info);
+        info->n_fallback = F;
+    }
 
     // tiles
     std::vector<PruneTile>& tiles = ws.tile_vec;
@@ -674,7 +998,7 @@ int score_complete(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_resul
     res->device_ms = ms;
     res->total_neg_lnl = *h_total;
     res->n_failed = info.rejected ? 0 : *h_fail;
-    res->n_fallback = 0;
+    res->n_fallback = info.n_fallback;
     if (res->family_lnl && F) std::memcpy(res->family_lnl, h_fam, F * sizeof(double));
     if (res->category_lnl && F) {
         const bool gamma = R->model == CAFE_MODEL_GAMMA;

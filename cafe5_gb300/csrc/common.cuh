@@ -1,6 +1,7 @@
 // Shared definitions of the GB300 CAFE5 likelihood kernels.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -101,5 +102,58 @@ struct FinishArgs {
 };
 
 cudaError_t launch_finish(const FinishArgs& a, cudaStream_t s);
+
+// ---- tensor-core (TF32x3) path ----
+// Conversion of one cached FP64 matrix into the tensor-core operands.
+struct ConvertJob {
+    const double* src;   // FP64 row-major, leading dimension `ld`
+    int ld;
+    int mat;             // index into the request's converted arrays
+};
+
+struct TcBuffers {
+    float* hi;           // [n_mat][Wm][Wm] TF32 hi part, row-major M[s][c]
+    float* lo;           // [n_mat][Wm][Wm] TF32 lo part
+    float* ct;           // [n_mat][Wm][Wm] transposed, column-normalised: ct[n][s] = M[s][n] 2^-ce[n]
+    int32_t* ce;         // [n_mat][Wm]
+    int Wm;
+};
+
+cudaError_t launch_convert_tc(const ConvertJob* d_jobs, int n_jobs, TcBuffers b, cudaStream_t s);
+
+struct PruneTcArgs {
+    TreePlan plan;
+    const PruneTile* tiles;      // 128-family tiles; S = W - 1 of the tile's bin
+    int n_tiles;
+    const int32_t* counts;
+    const int64_t* perm;
+    const int32_t* mat_index;    // [K][n_nodes] converted-matrix index (-1 for the root)
+    const float* ct;
+    const int32_t* ce;
+    int Wm;                      // pitch of matrices and node vectors (elements)
+    float* vec_hi;               // node vectors, rows = CTA x slot x 128 families
+    float* vec_lo;
+    int n_slots;
+    const double* prior;
+    int n_prior;
+    const double* err;
+    int err_rows;
+    int err_ndev;
+    const int32_t* fam_R;
+    double* out;                 // [F][K] natural log of each category term
+    int K;
+    const double* cat_probs;
+    int32_t* flags;              // [F] set when a family must be recomputed in FP64
+    int32_t* status;             // [1] nonzero when a bounded wait gave up
+    int tmem_cols;
+};
+
+// Tensor maps travel by value (__grid_constant__); the host encodes them.
+struct TcMaps {
+    CUtensorMap mat_hi, mat_lo, vec_hi, vec_lo;
+};
+
+cudaError_t launch_prune_tc(const TcMaps& maps, const PruneTcArgs& a, int n_ctas, size_t smem, cudaStream_t s);
+size_t prune_tc_smem_bytes(int Wm, int n_slots);
 
 }  // namespace cafe

@@ -28,7 +28,7 @@ from .inputs import ErrorModel, RootPrior, discrete_gamma
 from .tree import Tree, lambda_index_of_nodes
 
 PREC = {"fp64_ref": _lib.PREC_FP64_REF, "fp64_binned": _lib.PREC_FP64_BINNED,
-        "mixed_bf16x3": _lib.PREC_MIXED_BF16X3}
+        "mixed_tf32x3": _lib.PREC_MIXED_TF32X3}
 
 
 def _p(a: Optional[np.ndarray]):
@@ -277,7 +277,7 @@ class MultipleLambda:
 
 class BaseModel:
     """base_model over the GPU path. `precision` selects fp64_ref (the
-    reference's global bounds, unscaled), fp64_binned or mixed_bf16x3."""
+    reference's global bounds, unscaled), fp64_binned or mixed_tf32x3."""
 
     def __init__(self, lam, tree: Tree, families: FamilySet, max_family_size: int, max_root_family_size: int,
                  error_model: Optional[ErrorModel] = None, precision: str = "fp64_ref", dedupe: bool = True,

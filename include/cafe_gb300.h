@@ -44,13 +44,16 @@ typedef enum { CAFE_LAMBDA_SINGLE = 0, CAFE_LAMBDA_MULTIPLE = 1 } cafe_lambda_ki
  *   FP64_REF     reference semantics: one global state bound S and root
  *                bound R, unscaled FP64 (underflow behaves as in CAFE5)
  *   FP64_BINNED  per-family S bins, FP64 with per-node power-of-two rescale
- *   MIXED_BF16X3 per-family S bins, tensor-core split-BF16 products with FP32
- *                accumulation and integer-exponent rescale; families whose
- *                node vectors lose range are recomputed in FP64_BINNED */
+ *   MIXED_TF32X3 per-family S bins on the tensor cores (tcgen05, kind::tf32):
+ *                each operand is split into two TF32 parts (hi, lo), products
+ *                hi*hi + hi*lo + lo*hi accumulate in FP32, node vectors carry
+ *                integer power-of-two exponents; bins wider than 256 states,
+ *                saturated categories and families whose factors lose range
+ *                are computed in FP64_BINNED */
 typedef enum {
     CAFE_PREC_FP64_REF = 0,
     CAFE_PREC_FP64_BINNED = 1,
-    CAFE_PREC_MIXED_BF16X3 = 2
+    CAFE_PREC_MIXED_TF32X3 = 2
 } cafe_precision;
 
 typedef struct cafe_ctx cafe_ctx;

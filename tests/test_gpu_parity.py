@@ -198,3 +198,94 @@ def test_serving_results_equal_alone_and_in_the_mix(ctx):
         assert np.array_equal(m.family_lnl, a.family_lnl)
     st = ctx.serving_stats()
     assert st["completed"] >= len(lams) and st["p99_ms"] >= st["p50_ms"] > 0
+
+
+# ---------------------------------------------------------------- tensor cores
+MIXED_REL = 1e-6    # |dlnL| / |lnL| per family against FP64 at the same bins
+
+
+def _both(ctx, tree, counts, lambdas, lam_idx=None, kind=0, model=0, mult=(1.0,), probs=(1.0,), err=None, prior=None):
+    tid = ctx.upload_tree(tree, lam_idx)
+    sid = ctx.upload_families(tid, counts)
+    if prior is None:
+        from cafe5_gb300.inputs import RootPrior
+        prior = RootPrior.uniform(1100).vector()
+    ctx.set_prior(prior)
+    ctx.set_error_model(err)
+    kw = dict(model=model, lambda_kind=kind, multipliers=list(mult), cat_probs=list(probs),
+              use_error_model=err is not None, want_categories=True)
+    a = ctx.score(tid, sid, lambdas, precision="fp64_binned", **kw)
+    b = ctx.score(tid, sid, lambdas, precision="mixed_tf32x3", **kw)
+    ctx.free_families(sid)
+    return a, b
+
+
+def _check_mixed(a, b):
+    fin = np.isfinite(a.family_lnl)
+    assert np.array_equal(fin, np.isfinite(b.family_lnl))
+    rel = np.abs(b.family_lnl[fin] - a.family_lnl[fin]) / np.abs(a.family_lnl[fin])
+    assert rel.max() <= MIXED_REL, f"max rel dlnL {rel.max():.3e}"
+    if math.isfinite(a.total):
+        assert abs(b.total - a.total) <= MIXED_REL * abs(a.total)
+    else:
+        assert b.total == a.total
+
+
+@pytest.mark.parametrize("lam", [0.002, 0.0007, 0.0035])
+def test_mixed_gamma_config1_shape(ctx, lam):
+    from cafe5_gb300.synth import workload
+    w = workload(1, n_families=3000, seed=21)
+    a, b = _both(ctx, w.tree, w.families.counts, [lam], model=1, mult=w.multipliers, probs=w.cat_probs)
+    _check_mixed(a, b)
+
+
+def test_mixed_base_config0(ctx):
+    from cafe5_gb300.synth import workload
+    w = workload(0, seed=22)
+    a, b = _both(ctx, w.tree, w.families.counts, [0.0025])
+    _check_mixed(a, b)
+    assert b.n_fallback == 0
+
+
+def test_mixed_error_model_two_lambdas(ctx):
+    case = [c for c in CASES if c.name == "syn_multilambda_error_32taxa"][0]
+    a, b = _both(ctx, case.tree, case.counts, case.lambdas, lam_idx=case.lambda_of_node, kind=1, err=case.err_rows)
+    _check_mixed(a, b)
+
+
+def test_mixed_polytomy_and_underflow_cases(ctx):
+    for name in ["syn_polytomy", "syn_base_underflow", "syn_base_zero_family", "syn_gamma_24taxa_k4"]:
+        case = [c for c in CASES if c.name == name][0]
+        a, b = _both(ctx, case.tree, case.counts, case.lambdas, model=case.model, mult=case.multipliers,
+                     probs=case.cat_probs)
+        _check_mixed(a, b)
+
+
+def test_mixed_saturated_category_matches_fp64(ctx):
+    """The largest K=8 category saturates: the request runs on the FP64 path
+    and both agree on +inf."""
+    case = [c for c in CASES if c.name == "syn_gamma_24taxa_k8_small_cat"][0]
+    a, b = _both(ctx, case.tree, case.counts, case.lambdas, model=1, mult=case.multipliers, probs=case.cat_probs)
+    assert a.total == b.total == math.inf
+
+
+def test_mixed_wide_bins_hybrid(ctx):
+    """Families needing more than 256 states run on FP64 tiles in the same
+    request; the rest on the tensor cores."""
+    from cafe5_gb300.synth import workload
+    w = workload(0, n_families=600, seed=23)
+    counts = w.families.counts.copy()
+    counts[:7] += 230            # bins 384 (counts ~240-260)
+    a, b = _both(ctx, w.tree, counts, [0.0025])
+    _check_mixed(a, b)
+
+
+def test_mixed_results_do_not_depend_on_batch_composition(ctx):
+    """Per-family results are identical whether a family is scored with
+    10,000 others or with 100."""
+    from cafe5_gb300.synth import workload
+    w = workload(1, n_families=4000, seed=24)
+    a, b = _both(ctx, w.tree, w.families.counts, [0.002], model=1, mult=w.multipliers, probs=w.cat_probs)
+    sub = w.families.counts[:300]
+    c, d = _both(ctx, w.tree, sub, [0.002], model=1, mult=w.multipliers, probs=w.cat_probs)
+    assert np.array_equal(d.family_lnl, b.family_lnl[:300])
