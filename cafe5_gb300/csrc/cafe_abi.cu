@@ -66,12 +66,24 @@ Workspace::~Workspace() {
     if (stream) cudaStreamDestroy(stream);
     if (ev_start) cudaEventDestroy(ev_start);
     if (ev_stop) cudaEventDestroy(ev_stop);
+    if (ev_staged) cudaEventDestroy(ev_staged);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    for (int q = 0; q < kAux; ++q) {
+        if (aux[q]) cudaStreamDestroy(aux[q]);
+        if (ev_join[q]) cudaEventDestroy(ev_join[q]);
+    }
 }
 int Workspace::init(int device) {
     (void)device;
     if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return CAFE_ERR_CUDA;
     if (cudaEventCreate(&ev_start) != cudaSuccess) return CAFE_ERR_CUDA;
     if (cudaEventCreate(&ev_stop) != cudaSuccess) return CAFE_ERR_CUDA;
+    if (cudaEventCreateWithFlags(&ev_staged, cudaEventDisableTiming) != cudaSuccess) return CAFE_ERR_CUDA;
+    if (cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming) != cudaSuccess) return CAFE_ERR_CUDA;
+    for (int q = 0; q < kAux; ++q) {
+        if (cudaStreamCreateWithFlags(&aux[q], cudaStreamNonBlocking) != cudaSuccess) return CAFE_ERR_CUDA;
+        if (cudaEventCreateWithFlags(&ev_join[q], cudaEventDisableTiming) != cudaSuccess) return CAFE_ERR_CUDA;
+    }
     return CAFE_OK;
 }
 
@@ -322,6 +334,15 @@ struct PendingJobs {
     std::vector<double> lam, t;
 };
 
+void cache_reset(cafe_ctx* C) {
+    for (auto& sl : C->slabs) cudaFree(sl.p);
+    C->slabs.clear();
+    for (cudaEvent_t e : C->batch_events) cudaEventDestroy(e);
+    C->batch_events.clear();
+    C->cache.clear();
+    C->cache_bytes = 0;
+}
+
 double* cache_lookup(cafe_ctx* C, const MatKey& k) {
     auto it = C->cache.find(k);
     return it == C->cache.end() ? nullptr : it->second.d;
@@ -346,15 +367,25 @@ int cache_build(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
         // over the cap: start a fresh cache (the reference's cache lives for
         // one evaluation; keeping matrices across calls is only a speed-up)
         cudaDeviceSynchronize();
-        for (void* p : C->chunks) cudaFree(p);
-        C->chunks.clear();
-        C->cache.clear();
-        C->cache_bytes = 0;
+        cache_reset(C);
     }
-    void* chunk = nullptr;
-    CK(cudaMalloc(&chunk, total), "matrix cache");
-    C->chunks.push_back(chunk);
+    // bump allocation from large slabs (no cudaMalloc per evaluation)
+    const size_t need = (total + 255) & ~(size_t)255;
+    if (C->slabs.empty() || C->slabs.back().used + need > C->slabs.back().size) {
+        Slab sl;
+        sl.size = std::max(need, (size_t)256 << 20);
+        CK(cudaMalloc(&sl.p, sl.size), "matrix cache");
+        sl.used = 0;
+        C->slabs.push_back(sl);
+    }
+    Slab& slab = C->slabs.back();
+    void* chunk = static_cast<char*>(slab.p) + slab.used;
+    slab.used += need;
     C->cache_bytes += total;
+    cudaEvent_t ready = nullptr;
+    CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), "event");
+    C->batch_events.push_back(ready);
+    const int batch = (int)C->batch_events.size() - 1;
     CK(ws.h_jobs.reserve(n * sizeof(MatrixJob)), "jobs");
     CK(ws.jobs.reserve(n * sizeof(MatrixJob)), "jobs");
     MatrixJob* J = ws.h_jobs.as<MatrixJob>();
@@ -369,7 +400,7 @@ int cache_build(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
         J[i] = j;
         MatEntry e;
         e.d = j.dst;
-        e.chunk = (int)C->chunks.size() - 1;
+        e.chunk = batch;
         C->cache[k] = e;
         cur += (size_t)k.size * k.size * sizeof(double);
     }
@@ -382,9 +413,23 @@ int cache_build(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
         C->prof.end(0, ws.stream, ev);
         C->prof.acc.matrices_built += (int64_t)n;
     }
-    // the pinned job buffer is reused by the next request on this stream
-    CK(cudaStreamSynchronize(ws.stream), "matrix build");
+    // requests on other streams order themselves after this build
+    CK(cudaEventRecord(ready, ws.stream), "event");
     P.keys.clear();
+    return CAFE_OK;
+}
+
+// Make ws.stream wait for the builds of every matrix it is about to read.
+int cache_wait_ready(cafe_ctx* C, Workspace& ws, const std::vector<MatKey>& keys) {
+    std::vector<int> seen;
+    for (const MatKey& k : keys) {
+        auto it = C->cache.find(k);
+        if (it == C->cache.end()) continue;
+        const int b = it->second.chunk;
+        if (std::find(seen.begin(), seen.end(), b) != seen.end()) continue;
+        seen.push_back(b);
+        CK(cudaStreamWaitEvent(ws.stream, C->batch_events[b], 0), "event");
+    }
     return CAFE_OK;
 }
 
@@ -411,6 +456,7 @@ struct ScoreInfo {
     bool scaled = false;
     size_t footprint = 0;
     int64_t n_fallback = 0;
+    const int32_t* d_tail = nullptr;   // tensor-core pass: [status, fallback families, fallback tiles]
 };
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -437,6 +483,22 @@ int encode_map(cafe_ctx* C, CUtensorMap* m, const float* base, int64_t rows, int
                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(C, CAFE_ERR_CUDA, "tensor map encode failed (%d)", (int)r);
+    return CAFE_OK;
+}
+
+int cached_map(cafe_ctx* C, Workspace& ws, int slot, CUtensorMap* out, const float* base, int64_t rows, int cols) {
+    Workspace::MapCache& mc = ws.map_cache[slot];
+    if (mc.ptr != base || mc.rows != rows || mc.cols != cols) {
+        int rc = encode_map(C, &mc.map, base, rows, cols);
+        if (rc) {
+            mc.ptr = nullptr;
+            return rc;
+        }
+        mc.ptr = base;
+        mc.rows = rows;
+        mc.cols = cols;
+    }
+    *out = mc.map;
     return CAFE_OK;
 }
 
@@ -593,26 +655,58 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         CK(launch_convert_tc(ws.conv.as<ConvertJob>(), n_mat, tb, ws.stream), "convert");
         if (prof) C->prof.end(3, ws.stream, ev);
 
-        // occupancy: shared memory and 512 TMEM columns per SM
-        const int tmem_cols = 2 * Wm <= 64 ? 64 : (2 * Wm <= 128 ? 128 : (2 * Wm <= 256 ? 256 : 512));
-        size_t smem = prune_tc_smem_bytes(Wm, T.n_slots);
-        const int by_tmem = 512 / tmem_cols;
-        int by_smem = (int)((227 * 1024) / smem);
-        if (by_smem < 1) return fail(C, CAFE_ERR_INVALID, "tensor-core tile does not fit shared memory");
-        int per_sm = std::min(by_tmem, by_smem);
-        // request enough shared memory that no more CTAs than TMEM allows share an SM
-        smem = std::max(smem, (size_t)((227 * 1024) / per_sm) - 1024);
-        const int n_tc = (int)tc_tiles.size();
-        const int n_ctas = std::max(1, std::min(n_tc, C->sm_count * per_sm));
-        const int64_t vrows = (int64_t)n_ctas * T.n_slots * 128;
+        // one launch per S-bin, each sized for its own width, run
+        // concurrently: TMEM (512 columns per SM) and shared memory set how
+        // many tiles of a bin share an SM
+        struct BinLaunch {
+            int W, tmem_cols, stages, per_sm, n_ctas;
+            size_t smem;
+            int64_t first_tile, n_tiles, vrow_base;
+        };
+        std::vector<BinLaunch> launches;
+        std::stable_sort(tc_tiles.begin(), tc_tiles.end(),
+                         [](const PruneTile& x, const PruneTile& y) { return x.S < y.S; });
+        int64_t vrows = 0;
+        for (size_t i = 0; i < tc_tiles.size();) {
+            size_t j = i;
+            while (j < tc_tiles.size() && tc_tiles[j].S == tc_tiles[i].S) ++j;
+            BinLaunch L{};
+            L.W = tc_tiles[i].S + 1;
+            L.tmem_cols = 32;
+            while (L.tmem_cols < 2 * L.W) L.tmem_cols *= 2;
+            const int by_tmem = 512 / L.tmem_cols;
+            int best_per = 0;
+            for (int st = 2; st >= 1; --st) {
+                const size_t sm = prune_tc_smem_bytes(L.W, T.n_slots, st);
+                const int by_smem = (int)((227 * 1024) / (sm + 1024));
+                const int per = std::min(by_tmem, by_smem);
+                if (per > best_per) {
+                    best_per = per;
+                    L.stages = st;
+                    L.smem = sm;
+                }
+            }
+            if (best_per < 1) return fail(C, CAFE_ERR_INVALID, "tensor-core tile does not fit shared memory");
+            L.per_sm = best_per;
+            // pad shared memory so no more CTAs of this launch than TMEM allows share an SM
+            L.smem = std::max(L.smem, (size_t)((227 * 1024) / L.per_sm) - 2048);
+            L.first_tile = (int64_t)i;
+            L.n_tiles = (int64_t)(j - i);
+            L.n_ctas = (int)std::max<int64_t>(1, std::min<int64_t>(L.n_tiles, (int64_t)C->sm_count * L.per_sm));
+            L.vrow_base = vrows;
+            vrows += (int64_t)L.n_ctas * T.n_slots * 128;
+            launches.push_back(L);
+            i = j;
+        }
         CK(ws.tc_vhi.reserve((size_t)vrows * Wm * sizeof(float)), "tc vectors");
         CK(ws.tc_vlo.reserve((size_t)vrows * Wm * sizeof(float)), "tc vectors");
         TcMaps maps;
-        int rc = encode_map(C, &maps.mat_hi, ws.tc_hi.as<float>(), (int64_t)n_mat * Wm, Wm);
-        if (!rc) rc = encode_map(C, &maps.mat_lo, ws.tc_lo.as<float>(), (int64_t)n_mat * Wm, Wm);
-        if (!rc) rc = encode_map(C, &maps.vec_hi, ws.tc_vhi.as<float>(), vrows, Wm);
-        if (!rc) rc = encode_map(C, &maps.vec_lo, ws.tc_vlo.as<float>(), vrows, Wm);
+        int rc = cached_map(C, ws, 0, &maps.mat_hi, ws.tc_hi.as<float>(), (int64_t)n_mat * Wm, Wm);
+        if (!rc) rc = cached_map(C, ws, 1, &maps.mat_lo, ws.tc_lo.as<float>(), (int64_t)n_mat * Wm, Wm);
+        if (!rc) rc = cached_map(C, ws, 2, &maps.vec_hi, ws.tc_vhi.as<float>(), vrows, Wm);
+        if (!rc) rc = cached_map(C, ws, 3, &maps.vec_lo, ws.tc_vlo.as<float>(), vrows, Wm);
         if (rc) return rc;
+        const int n_tc = (int)tc_tiles.size();
         CK(ws.tiles.reserve(n_tc * sizeof(PruneTile)), "tiles");
         CK(ws.h_tiles.reserve(n_tc * sizeof(PruneTile)), "tiles");
         std::memcpy(ws.h_tiles.p, tc_tiles.data(), n_tc * sizeof(PruneTile));
@@ -620,8 +714,6 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
            "tiles");
         PruneTcArgs a{};
         a.plan = T.plan;
-        a.tiles = ws.tiles.as<PruneTile>();
-        a.n_tiles = n_tc;
         a.counts = S.d_counts.as<int32_t>();
         a.perm = B.d_perm.as<int64_t>();
         a.mat_index = ws.tc_mi.as<int32_t>();
@@ -642,62 +734,111 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         a.cat_probs = ws.catp.as<double>();
         a.flags = d_flags;
         a.status = d_status;
-        a.tmem_cols = tmem_cols;
+        a.phase_clocks = nullptr;
+        static const bool phase_env = getenv("CAFE_TC_PHASES") != nullptr;
+        if (phase_env) {
+            CK(ws.phase.reserve(4 * sizeof(unsigned long long)), "phase clocks");
+            CK(cudaMemsetAsync(ws.phase.p, 0, 4 * sizeof(unsigned long long), ws.stream), "phase clocks");
+            a.phase_clocks = ws.phase.as<unsigned long long>();
+        }
         if (prof) {
             C->prof.begin(1, ws.stream, &ev);
             for (const PruneTile& t : tc_tiles) C->prof.acc.prune_flops += tile_flops(T, t, R->use_error_model);
         }
-        CK(launch_prune_tc(maps, a, n_ctas, smem, ws.stream), "prune tc");
+        // fork: bins run on the auxiliary streams after everything queued so far
+        const bool fork = launches.size() > 1;
+        if (fork) {
+            CK(cudaEventRecord(ws.ev_fork, ws.stream), "fork");
+            for (int q = 0; q < Workspace::kAux; ++q) CK(cudaStreamWaitEvent(ws.aux[q], ws.ev_fork, 0), "fork");
+        }
+        for (size_t li = 0; li < launches.size(); ++li) {
+            const BinLaunch& L = launches[li];
+            PruneTcArgs b = a;
+            b.tiles = ws.tiles.as<PruneTile>() + L.first_tile;
+            b.n_tiles = (int)L.n_tiles;
+            b.tmem_cols = L.tmem_cols;
+            b.Ws = L.W;
+            b.stages = L.stages;
+            b.vrow_base = L.vrow_base;
+            cudaStream_t st = fork ? ws.aux[li % Workspace::kAux] : ws.stream;
+            CK(launch_prune_tc(maps, b, L.n_ctas, L.smem, st), "prune tc");
+        }
+        if (fork) {
+            for (int q = 0; q < Workspace::kAux; ++q) {
+                CK(cudaEventRecord(ws.ev_join[q], ws.aux[q]), "join");
+                CK(cudaStreamWaitEvent(ws.stream, ws.ev_join[q], 0), "join");
+            }
+        }
+        if (phase_env) {
+            unsigned long long h[4];
+            CK(cudaMemcpyAsync(h, ws.phase.p, sizeof(h), cudaMemcpyDeviceToHost, ws.stream), "phase clocks");
+            CK(cudaStreamSynchronize(ws.stream), "phase clocks");
+            const double tot = (double)(h[0] + h[1] + h[2] + h[3]) + 1e-9;
+            fprintf(stderr, "k_prune_tc phases (CTA-summed SM clocks): gemm %.1f%% passA %.1f%% passB %.1f%% sync %.1f%% total %.3g\n",
+                    100 * h[0] / tot, 100 * h[1] / tot, 100 * h[2] / tot, 100 * h[3] / tot, tot);
+        }
         if (prof) C->prof.end(1, ws.stream, ev);
     }
     int rc = launch_fp64_tiles(C, ws, R, T, S, K, wide_tiles, ws.tiles64, ws.h_tiles64, B.d_perm.as<int64_t>(), msize,
                                msize, ws.cat.as<double>(), 3);
     if (rc) return rc;
 
-    // families the tensor-core pass could not represent: FP64 recompute
-    int64_t n_fb = 0;
+    // families the tensor-core pass could not represent: planned on the
+    // device and recomputed in FP64 without a host round trip
     if (!tc_tiles.empty()) {
-        CK(ws.h_flags.reserve((size_t)std::max<int64_t>(F, 1) * sizeof(int32_t) + 64), "flags");
-        CK(cudaMemcpyAsync(ws.h_flags.p, ws.flags.p, (size_t)std::max<int64_t>(F, 1) * sizeof(int32_t) + 64,
-                           cudaMemcpyDeviceToHost, ws.stream),
-           "flags");
-        CK(cudaStreamSynchronize(ws.stream), "prune tc");
-        const int32_t* hf = ws.h_flags.as<int32_t>();
-        const int32_t st = hf[std::max<int64_t>(F, 1)];
-        if (st) return fail(C, CAFE_ERR_TIMEOUT, "tensor-core pruning gave up waiting (status %d)", st);
-        // flagged families, grouped by bin in the bin order of the permutation
-        std::vector<int64_t> fb_perm;
-        std::vector<PruneTile> fb_tiles;
-        std::vector<int64_t> perm_h;   // host copy of the bin permutation
-        perm_h.resize(F);
-        CK(cudaMemcpy(perm_h.data(), B.d_perm.p, F * sizeof(int64_t), cudaMemcpyDeviceToHost), "perm");
-        for (size_t b = 0; b < B.widths.size(); ++b) {
+        FallbackPlanArgs fp{};
+        fp.flags = d_flags;
+        fp.perm = B.d_perm.as<int64_t>();
+        fp.n_bins = 0;
+        for (size_t b = 0; b < B.widths.size() && fp.n_bins < 16; ++b) {
             if (B.widths[b] > 256) continue;
-            const int64_t start = (int64_t)fb_perm.size();
-            for (int64_t i = B.bin_first[b]; i < B.bin_first[b] + B.bin_count[b]; ++i)
-                if (hf[perm_h[i]]) fb_perm.push_back(perm_h[i]);
-            const int64_t cnt = (int64_t)fb_perm.size() - start;
-            for (int k = 0; k < K; ++k)
-                for (int64_t i = 0; i < cnt; i += 32) {
-                    PruneTile t{};
-                    t.first = (int)(start + i);
-                    t.count = (int)std::min<int64_t>(32, cnt - i);
-                    t.k = k;
-                    t.S = B.widths[b] - 1;
-                    t.R = B.widths[b] - 1;
-                    fb_tiles.push_back(t);
-                }
+            fp.bin_width[fp.n_bins] = B.widths[b];
+            fp.bin_first[fp.n_bins] = B.bin_first[b];
+            fp.bin_count[fp.n_bins] = B.bin_count[b];
+            fp.n_bins++;
         }
-        n_fb = (int64_t)fb_perm.size();
-        if (n_fb) {
-            CK(ws.fb_perm.reserve(n_fb * sizeof(int64_t)), "fallback");
-            CK(cudaMemcpy(ws.fb_perm.p, fb_perm.data(), n_fb * sizeof(int64_t), cudaMemcpyHostToDevice), "fallback");
-            rc = launch_fp64_tiles(C, ws, R, T, S, K, fb_tiles, ws.tiles_fb, ws.h_tiles_fb, ws.fb_perm.as<int64_t>(),
-                                   msize, msize, ws.cat.as<double>(), 3);
-            if (rc) return rc;
-        }
+        fp.K = K;
+        const int64_t max_tiles = (int64_t)K * (F / 32 + fp.n_bins + 1);
+        CK(ws.fb_perm.reserve((size_t)std::max<int64_t>(F, 1) * sizeof(int64_t)), "fallback");
+        CK(ws.tiles_fb.reserve((size_t)max_tiles * sizeof(PruneTile)), "fallback");
+        fp.fb_perm = ws.fb_perm.as<int64_t>();
+        fp.fb_tiles = ws.tiles_fb.as<PruneTile>();
+        fp.out_counts = d_status + 1;     // [families, tiles]
+        if (prof) C->prof.begin(3, ws.stream, &ev);
+        CK(launch_fallback_plan(fp, ws.stream), "fallback plan");
+        if (prof) C->prof.end(3, ws.stream, ev);
+        const int n_ctas = C->n_ctas;
+        const int64_t per_cta = (int64_t)T.n_slots * msize * 32;
+        CK(ws.scratch.reserve((size_t)n_ctas * per_cta * sizeof(double)), "scratch");
+        Prune64Args a{};
+        a.plan = T.plan;
+        a.tiles = fp.fb_tiles;
+        a.n_tiles = 0;
+        a.n_tiles_dev = d_status + 2;
+        a.counts = S.d_counts.as<int32_t>();
+        a.perm = fp.fb_perm;
+        a.mats = ws.mats.as<const double*>();
+        a.ld_mat = msize;
+        a.prior = C->d_prior.as<double>();
+        a.n_prior = (int)C->prior.size();
+        a.err = R->use_error_model ? C->d_err.as<double>() : nullptr;
+        a.err_rows = C->err_rows;
+        a.err_ndev = C->err_ndev;
+        a.fam_R = B.d_famR.as<int32_t>();
+        a.scratch = ws.scratch.as<double>();
+        a.scratch_per_cta = per_cta;
+        a.scaled = 1;
+        a.model = gamma ? 1 : 0;
+        a.out = ws.cat.as<double>();
+        a.K = K;
+        a.cat_probs = ws.catp.as<double>();
+        a.tile_families = 32;
+        a.W = msize;
+        if (prof) C->prof.begin(3, ws.stream, &ev);
+        CK(launch_prune64(a, n_ctas, ws.stream), "fallback prune");
+        if (prof) C->prof.end(3, ws.stream, ev);
+        info->d_tail = d_status;     // [status, fallback families, fallback tiles]
     }
-    info->n_fallback = n_fb;
 
     FinishArgs fa{};
     fa.F = F;
@@ -709,6 +850,10 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
     fa.family_lnl = d_fam;
     fa.total = d_total;
     fa.n_failed = ws.nfail.as<int32_t>();
+    CK(ws.parts.reserve((size_t)finish_parts(F) * 2 * (sizeof(double) + sizeof(int32_t))), "finish");
+    fa.part_sum = ws.parts.as<double>();
+    fa.part_cnt = reinterpret_cast<int32_t*>(fa.part_sum + 2 * finish_parts(F));
+    fa.status = tc_tiles.empty() ? nullptr : d_status;
     if (prof) C->prof.begin(2, ws.stream, &ev);
     CK(launch_finish(fa, ws.stream), "finish");
     if (prof) C->prof.end(2, ws.stream, ev);
@@ -719,6 +864,12 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
 int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_fam, double* d_total,
                   ScoreInfo* info) {
     if (!R) return fail(C, CAFE_ERR_INVALID, "null request");
+    // pinned staging buffers of this workspace are rewritten below: the
+    // previous request's copies out of them must have run
+    if (ws.staged) {
+        CK(cudaEventSynchronize(ws.ev_staged), "staging");
+        ws.staged = false;
+    }
     auto ti = C->trees.find(R->tree_id);
     if (ti == C->trees.end()) return fail(C, CAFE_ERR_NOT_FOUND, "unknown tree id %d", R->tree_id);
     auto si = C->sets.find(R->set_id);
@@ -798,6 +949,8 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_f
     }
     int rc = cache_build(C, ws, P);
     if (rc) return rc;
+    rc = cache_wait_ready(C, ws, node_key);
+    if (rc) return rc;
     CK(ws.h_mats.reserve((size_t)K * T.n_nodes * sizeof(double*)), "mats");
     CK(ws.mats.reserve((size_t)K * T.n_nodes * sizeof(double*)), "mats");
     double** hm = ws.h_mats.as<double*>();
@@ -821,7 +974,7 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_f
             for (int c : T.children[v]) ni += !T.children[c].empty();
             max_int = std::max(max_int, ni);
         }
-        if (T.max_children > 8 || max_int > 2) to_fp64 = true;
+        if (T.max_children > 2) to_fp64 = true;   // polytomies stay on FP64
         if (!to_fp64) return enqueue_mixed(C, ws, R, T, S, K, hm, d_fam, d_total, info);
         info->n_fallback = F;
     }
@@ -943,6 +1096,10 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_f
     fa.family_lnl = d_fam;
     fa.total = d_total;
     fa.n_failed = ws.nfail.as<int32_t>();
+    CK(ws.parts.reserve((size_t)finish_parts(F) * 2 * (sizeof(double) + sizeof(int32_t))), "finish");
+    fa.part_sum = ws.parts.as<double>();
+    fa.part_cnt = reinterpret_cast<int32_t*>(fa.part_sum + 2 * finish_parts(F));
+    fa.status = nullptr;
     if (prof) C->prof.begin(2, ws.stream, &ev);
     CK(launch_finish(fa, ws.stream), "finish");
     if (prof) C->prof.end(2, ws.stream, ev);
@@ -960,11 +1117,16 @@ int score_enqueue(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_result
     CK(cudaEventRecord(ws.ev_start, ws.stream), "event");
     int rc = enqueue_score(C, ws, R, ws.fam_lnl.as<double>(), ws.total.as<double>(), info);
     if (rc) return rc;
+    CK(cudaEventRecord(ws.ev_staged, ws.stream), "event");
+    ws.staged = true;
     CK(cudaEventRecord(ws.ev_stop, ws.stream), "event");
     const int K = info->K;
     const size_t out_bytes = sizeof(double) + sizeof(int32_t) + (size_t)F * sizeof(double) +
                              (res && res->category_lnl ? (size_t)F * K * sizeof(double) : 0);
     CK(ws.h_out.reserve(out_bytes + 64), "host staging");
+    CK(ws.h_tail.reserve(64), "host staging");
+    if (info->d_tail)
+        CK(cudaMemcpyAsync(ws.h_tail.p, info->d_tail, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, ws.stream), "d2h");
     char* h = static_cast<char*>(ws.h_out.p);
     double* h_total = reinterpret_cast<double*>(h);
     int32_t* h_fail = reinterpret_cast<int32_t*>(h + 8);
@@ -999,6 +1161,11 @@ int score_complete(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_resul
     res->total_neg_lnl = *h_total;
     res->n_failed = info.rejected ? 0 : *h_fail;
     res->n_fallback = info.n_fallback;
+    if (info.d_tail) {
+        const int32_t* tail = ws.h_tail.as<int32_t>();
+        if (tail[0]) return fail(C, CAFE_ERR_TIMEOUT, "tensor-core pruning gave up waiting (status %d)", tail[0]);
+        res->n_fallback = tail[1];
+    }
     if (res->family_lnl && F) std::memcpy(res->family_lnl, h_fam, F * sizeof(double));
     if (res->category_lnl && F) {
         const bool gamma = R->model == CAFE_MODEL_GAMMA;
@@ -1099,8 +1266,7 @@ int cafe_ctx_destroy(cafe_ctx* C) {
     cudaSetDevice(C->device);
     cafe_serving_stop(C);
     cudaDeviceSynchronize();
-    for (void* p : C->chunks) cudaFree(p);
-    C->chunks.clear();
+    cache_reset(C);
     delete C;
     return CAFE_OK;
 }
@@ -1281,10 +1447,7 @@ int cafe_matrix_cache_clear(cafe_ctx* C) {
     std::lock_guard<std::mutex> lk(C->mu);
     cudaSetDevice(C->device);
     cudaDeviceSynchronize();
-    for (void* p : C->chunks) cudaFree(p);
-    C->chunks.clear();
-    C->cache.clear();
-    C->cache_bytes = 0;
+    cache_reset(C);
     return CAFE_OK;
 }
 
@@ -1332,6 +1495,8 @@ int cafe_score_device(cafe_ctx* C, const cafe_request* req, double* d_family_lnl
     int rc = enqueue_score(C, ws, req, d_family_lnl ? d_family_lnl : ws.fam_lnl.as<double>(),
                            d_total ? d_total : ws.total.as<double>(), &info);
     if (rc) return rc;
+    CK(cudaEventRecord(ws.ev_staged, ws.stream), "event");
+    ws.staged = true;
     if (user) {
         CK(cudaEventRecord(ws.ev_stop, ws.stream), "event");
         CK(cudaStreamWaitEvent(user, ws.ev_stop, 0), "event");

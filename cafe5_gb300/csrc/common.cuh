@@ -85,6 +85,7 @@ struct Prune64Args {
     const double* cat_probs;     // [K]
     int tile_families;           // families per tile (<= 32)
     int W;                       // max vector length over tiles (S + 1 or R)
+    const int32_t* n_tiles_dev;  // optional: tile count read from device memory
 };
 
 cudaError_t launch_prune64(const Prune64Args& a, int n_ctas, cudaStream_t s);
@@ -99,8 +100,12 @@ struct FinishArgs {
     double* family_lnl;          // [F] out
     double* total;               // [1] out
     int32_t* n_failed;           // [1] out
+    double* part_sum;            // [2 * finish_parts(F)] workspace
+    int32_t* part_cnt;           // [2 * finish_parts(F)] workspace
+    const int32_t* status;       // optional: nonzero -> total = NaN
 };
 
+int finish_parts(int64_t F);
 cudaError_t launch_finish(const FinishArgs& a, cudaStream_t s);
 
 // ---- tensor-core (TF32x3) path ----
@@ -146,6 +151,11 @@ struct PruneTcArgs {
     int32_t* flags;              // [F] set when a family must be recomputed in FP64
     int32_t* status;             // [1] nonzero when a bounded wait gave up
     int tmem_cols;
+    int Ws;                      // widest bin of this launch (shared-memory B rows)
+    int stages;                  // shared-memory stages (1 or 2)
+    int64_t vrow_base;           // first node-vector row of this launch
+    unsigned long long* phase_clocks;   // optional [4]: SM clocks spent in GEMM wait,
+                                        // epilogue pass A, pass B, end-of-node barrier
 };
 
 // Tensor maps travel by value (__grid_constant__); the host encodes them.
@@ -154,6 +164,24 @@ struct TcMaps {
 };
 
 cudaError_t launch_prune_tc(const TcMaps& maps, const PruneTcArgs& a, int n_ctas, size_t smem, cudaStream_t s);
-size_t prune_tc_smem_bytes(int Wm, int n_slots);
+size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages);
+
+// Device-side plan of the FP64 recompute of flagged families: compacts the
+// flagged families of each listed bin (in permutation order) into fb_perm
+// and writes 32-family tiles for every category; out_counts[0] = families,
+// out_counts[1] = tiles.
+struct FallbackPlanArgs {
+    const int32_t* flags;        // [F]
+    const int64_t* perm;         // [F] bin order
+    int n_bins;
+    int bin_width[16];
+    int64_t bin_first[16];
+    int64_t bin_count[16];
+    int K;
+    int64_t* fb_perm;            // [F]
+    PruneTile* fb_tiles;         // [K * (F / 32 + n_bins)]
+    int32_t* out_counts;         // [2]
+};
+cudaError_t launch_fallback_plan(const FallbackPlanArgs& a, cudaStream_t s);
 
 }  // namespace cafe

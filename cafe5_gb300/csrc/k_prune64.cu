@@ -55,7 +55,8 @@ __global__ void __launch_bounds__(NT) k_prune64(Prune64Args a) {
     double* base = a.scratch + (size_t)blockIdx.x * a.scratch_per_cta;
     const int W = a.W;
 
-    for (int t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
+    const int n_tiles = a.n_tiles_dev ? *a.n_tiles_dev : a.n_tiles;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
         const PruneTile tile = a.tiles[t];
         const int cnt = tile.count, S = tile.S, R = tile.R, k = tile.k;
         if (tid < TF) fam[tid] = tid < cnt ? a.perm[tile.first + tid] : -1;
@@ -235,14 +236,22 @@ __global__ void __launch_bounds__(NT) k_prune64(Prune64Args a) {
     }
 }
 
-// Per-family lnL from category values, and -sum lnL with a deterministic
-// compensated reduction (one block).
-__global__ void __launch_bounds__(1024) k_finish(FinishArgs a) {
-    __shared__ double ssum[1024], scomp[1024];
-    __shared__ int sfail[1024], sinf[1024];
+// Per-family lnL from category values (many blocks), then -sum lnL with a
+// deterministic compensated reduction: Neumaier sums per thread, combined
+// in a fixed order per block and then across blocks.
+__device__ __forceinline__ void neumaier_add(double& sum, double& comp, double x) {
+    const double tt = sum + x;
+    if (fabs(sum) >= fabs(x)) comp += (sum - tt) + x;
+    else comp += (x - tt) + sum;
+    sum = tt;
+}
+
+__global__ void __launch_bounds__(256) k_finish_fam(FinishArgs a) {
+    __shared__ double ssum[256], scomp[256];
+    __shared__ int sfail[256], sinf[256];
     double sum = 0.0, comp = 0.0;
     int fail = 0, ninf = 0;   // ninf: families with lnL = -inf (log of an underflowed 0)
-    for (int64_t f = threadIdx.x; f < a.F; f += blockDim.x) {
+    for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < a.F; f += (int64_t)gridDim.x * blockDim.x) {
         const int64_t r = a.ref ? a.ref[f] : f;
         double lnl;
         if (a.model == 0) {
@@ -273,15 +282,8 @@ __global__ void __launch_bounds__(1024) k_finish(FinishArgs a) {
             fail += bad;
         }
         a.family_lnl[f] = lnl;
-        if (isinf(lnl)) {
-            ninf++;
-        } else if (!isnan(lnl)) {
-            // Neumaier summation
-            const double tt = sum + lnl;
-            if (fabs(sum) >= fabs(lnl)) comp += (sum - tt) + lnl;
-            else comp += (lnl - tt) + sum;
-            sum = tt;
-        }
+        if (isinf(lnl)) ninf++;
+        else if (!isnan(lnl)) neumaier_add(sum, comp, lnl);
     }
     ssum[threadIdx.x] = sum;
     scomp[threadIdx.x] = comp;
@@ -292,19 +294,34 @@ __global__ void __launch_bounds__(1024) k_finish(FinishArgs a) {
         double s = 0.0, c = 0.0;
         int fl = 0, ni = 0;
         for (int i = 0; i < (int)blockDim.x; ++i) {
-            const double x = ssum[i];
-            const double tt = s + x;
-            if (fabs(s) >= fabs(x)) c += (s - tt) + x;
-            else c += (x - tt) + s;
-            s = tt;
+            neumaier_add(s, c, ssum[i]);
             c += scomp[i];
             fl += sfail[i];
             ni += sinf[i];
         }
-        *a.n_failed = fl;
-        // -sum lnL: +inf on gamma failure or when any family's lnL is -inf
-        *a.total = (fl || ni) ? INFINITY : -(s + c);
+        a.part_sum[2 * blockIdx.x] = s;
+        a.part_sum[2 * blockIdx.x + 1] = c;
+        a.part_cnt[2 * blockIdx.x] = fl;
+        a.part_cnt[2 * blockIdx.x + 1] = ni;
     }
+}
+
+__global__ void k_finish_total(FinishArgs a, int n_parts) {
+    if (threadIdx.x != 0) return;
+    double s = 0.0, c = 0.0;
+    int fl = 0, ni = 0;
+    for (int i = 0; i < n_parts; ++i) {
+        neumaier_add(s, c, a.part_sum[2 * i]);
+        c += a.part_sum[2 * i + 1];
+        fl += a.part_cnt[2 * i];
+        ni += a.part_cnt[2 * i + 1];
+    }
+    *a.n_failed = fl;
+    // -sum lnL: +inf on gamma failure or when any family's lnL is -inf;
+    // NaN if the tensor-core pass reported a time-out
+    double t = (fl || ni) ? INFINITY : -(s + c);
+    if (a.status && *a.status) t = NAN;
+    *a.total = t;
 }
 
 __global__ void k_fill(double* p, int64_t n, double v) {
@@ -331,14 +348,18 @@ cudaError_t launch_fill_i32(int32_t* p, int64_t n, int32_t v, cudaStream_t s) {
 }
 
 cudaError_t launch_prune64(const Prune64Args& a, int n_ctas, cudaStream_t s) {
-    if (a.n_tiles <= 0) return cudaSuccess;
+    if (a.n_tiles <= 0 && !a.n_tiles_dev) return cudaSuccess;
     size_t smem = sizeof(int) * (size_t)a.plan.n_slots * TF;
     k_prune64<<<n_ctas, NT, smem, s>>>(a);
     return cudaGetLastError();
 }
 
+int finish_parts(int64_t F) { return (int)std::max<int64_t>(1, std::min<int64_t>((F + 255) / 256, 512)); }
+
 cudaError_t launch_finish(const FinishArgs& a, cudaStream_t s) {
-    k_finish<<<1, 1024, 0, s>>>(a);
+    const int parts = finish_parts(a.F);
+    k_finish_fam<<<parts, 256, 0, s>>>(a);
+    k_finish_total<<<1, 32, 0, s>>>(a, parts);
     return cudaGetLastError();
 }
 

@@ -44,8 +44,9 @@ namespace {
 constexpr int TM = 128;   // families per tile = MMA M = TMEM lanes
 constexpr int KC = 32;    // K per stage: 32 fp32 = one 128-byte swizzle row
 constexpr int NTHREADS = 128;
+constexpr int CW = 16;    // epilogue columns per TMEM load
 
-__host__ __device__ inline size_t stage_bytes(int Wm) { return (size_t)(2 * TM + 2 * Wm) * KC * sizeof(float); }
+__host__ __device__ inline size_t stage_bytes(int Ws) { return (size_t)(2 * TM + 2 * Ws) * KC * sizeof(float); }
 
 __device__ __forceinline__ int bexp(float y) {
     // binary exponent e with y = m 2^e, m in [0.5, 1); zero -> very negative
@@ -66,7 +67,322 @@ struct ChildInfo {
     int tcol;       // TMEM column base for internal children
 };
 
-__global__ void __launch_bounds__(NTHREADS, 1)
+// Per-child source of the factor: TMEM columns (internal child) or up to
+// three weighted rows of the column-normalised matrix copy (leaf).
+struct Src {
+    bool leaf;      // also true for the unit factor of an absent second child
+    bool unit;
+    uint32_t taddr;
+    const float* row[3];
+    float w[3];
+};
+
+template <int NC>
+struct NodeSrc {
+    Src s[NC];
+    int Eacc;     // sum of the children's power-of-two exponents
+    bool flag;
+};
+
+// Child sources of one node for this thread's family; issued before the
+// GEMM wait so the count / exponent loads overlap the tensor-core work.
+template <int NC>
+__device__ __forceinline__ void setup_src(const PruneTcArgs& a, const ChildInfo* ch, int nch, const int* Esh,
+                                          uint32_t tmem_lane, int64_t fam, int tid, int S, int Wm,
+                                          NodeSrc<NC>& ns) {
+    ns.Eacc = 0;
+    ns.flag = false;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        Src& sc = ns.s[c];
+        sc.unit = c >= nch;
+        if (sc.unit) {
+            sc.leaf = true;
+            sc.taddr = 0;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                sc.row[d] = nullptr;
+                sc.w[d] = 0.0f;
+            }
+            continue;
+        }
+        const ChildInfo ci = ch[c];
+        sc.leaf = ci.leaf_col >= 0;
+        sc.taddr = tmem_lane + (uint32_t)(ci.tcol > 0 ? ci.tcol : 0);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            sc.row[d] = nullptr;
+            sc.w[d] = 0.0f;
+        }
+        if (ci.leaf_col >= 0) {
+            const int n = fam >= 0 ? __ldg(a.counts + (size_t)fam * a.plan.n_leaves + ci.leaf_col) : 0;
+            const int32_t* ce = a.ce + (size_t)ci.mat * Wm;
+            const float* ct = a.ct + (size_t)ci.mat * Wm * Wm;
+            if (a.err) {
+                // error-model leaf: weights p_d 2^(ce_d - ce_max) over columns n-1, n, n+1
+                const double* pr = a.err + (size_t)(n < a.err_rows ? n : a.err_rows - 1) * a.err_ndev;
+                const int off = n - (a.err_ndev - 1) / 2;
+                int cmax = -100000;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const int col = off + d;
+                    if (d < a.err_ndev && col >= 0 && col <= S && pr[d] > 0) cmax = max(cmax, __ldg(ce + col));
+                }
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const int col = off + d;
+                    if (d < a.err_ndev && col >= 0 && col <= S && pr[d] > 0) {
+                        sc.row[d] = ct + (size_t)col * Wm;
+                        sc.w[d] = (float)pr[d] * pow2f(__ldg(ce + col) - cmax);
+                    }
+                }
+                if (cmax == -100000) ns.flag = true;
+                else ns.Eacc += cmax;
+            } else if (n >= 0 && n <= S) {
+                sc.row[0] = ct + (size_t)n * Wm;
+                sc.w[0] = 1.0f;
+                ns.Eacc += __ldg(ce + n);
+            } else {
+                ns.flag = true;
+            }
+        } else {
+            ns.Eacc += Esh[a.plan.slot[ci.node] * TM + tid];
+        }
+    }
+}
+
+// 16 values of a leaf factor starting at column col0.
+__device__ __forceinline__ void load_leaf(const Src& c, int col0, uint32_t (&out)[CW]) {
+    if (c.unit) {
+#pragma unroll
+        for (int j = 0; j < CW; ++j) out[j] = __float_as_uint(1.0f);
+        return;
+    }
+    float y[CW];
+#pragma unroll
+    for (int j = 0; j < CW; ++j) y[j] = 0.0f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (!c.row[d]) continue;
+        const float4* src = reinterpret_cast<const float4*>(c.row[d] + col0);
+        const float w = c.w[d];
+#pragma unroll
+        for (int q = 0; q < CW / 4; ++q) {
+            const float4 x = __ldg(src + q);
+            y[4 * q + 0] = fmaf(w, x.x, y[4 * q + 0]);
+            y[4 * q + 1] = fmaf(w, x.y, y[4 * q + 1]);
+            y[4 * q + 2] = fmaf(w, x.z, y[4 * q + 2]);
+            y[4 * q + 3] = fmaf(w, x.w, y[4 * q + 3]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < CW; ++j) out[j] = __float_as_uint(y[j]);
+}
+
+struct EpiOut {
+    int E;
+    bool flag;
+    double best;            // root: max_j L[j] prior[j] (in units of 2^E)
+};
+
+__device__ __forceinline__ void store_tf32x2(float* __restrict__ hi, float* __restrict__ lo, int col0,
+                                             const float (&p)[CW]) {
+#pragma unroll
+    for (int q = 0; q < CW / 4; ++q) {
+        float4 h, l;
+        h.x = tc::round_tf32(p[4 * q + 0]);
+        h.y = tc::round_tf32(p[4 * q + 1]);
+        h.z = tc::round_tf32(p[4 * q + 2]);
+        h.w = tc::round_tf32(p[4 * q + 3]);
+        l.x = tc::round_tf32(p[4 * q + 0] - h.x);
+        l.y = tc::round_tf32(p[4 * q + 1] - h.y);
+        l.z = tc::round_tf32(p[4 * q + 2] - h.z);
+        l.w = tc::round_tf32(p[4 * q + 3] - h.w);
+        reinterpret_cast<float4*>(hi + col0)[q] = h;
+        reinterpret_cast<float4*>(lo + col0)[q] = l;
+    }
+}
+
+// Fast epilogue: one pass. Every factor is <= 1 (rows of M sum to <= 1,
+// node vectors and normalised leaf columns are <= 1), so the plain product
+// cannot overflow; its maximum is tracked and the stored row is rescaled
+// only if it drifts below 2^-32. Leaf loads run one chunk ahead.
+// `need_exact` is set when the product underflowed (max < 2^-120, or an
+// all-zero weighted root) so the exact two-pass epilogue must redo it.
+template <int NC>
+__device__ __forceinline__ void epi_fast(const NodeSrc<NC>& ns, int W, bool is_root, int Rf, const float* prior_f,
+                                         float* __restrict__ rowhi, float* __restrict__ rowlo, EpiOut& out,
+                                         bool& need_exact) {
+    float maxp = 0.0f;
+    float best_f = 0.0f, best_p = 0.0f, best_q = 0.0f;
+    uint32_t lf[NC][CW];
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+        if (ns.s[c].leaf) load_leaf(ns.s[c], 0, lf[c]);
+    for (int col0 = 0; col0 < W; col0 += CW) {
+        uint32_t r[NC][CW];
+        bool any_tmem = false;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            if (!ns.s[c].leaf) {
+                tc::tmem_ld16_issue(ns.s[c].taddr + (uint32_t)col0, r[c]);
+                any_tmem = true;
+            } else {
+#pragma unroll
+                for (int j = 0; j < CW; ++j) r[c][j] = lf[c][j];
+                if (col0 + CW < W) load_leaf(ns.s[c], col0 + CW, lf[c]);   // next chunk, in flight
+            }
+        }
+        if (any_tmem) tc::tmem_wait();
+        float p[CW];
+#pragma unroll
+        for (int j = 0; j < CW; ++j) p[j] = 1.0f;
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+#pragma unroll
+            for (int j = 0; j < CW; ++j) p[j] *= __uint_as_float(r[c][j]);
+        if (!is_root) {
+#pragma unroll
+            for (int j = 0; j < CW; ++j) maxp = fmaxf(maxp, p[j]);
+            store_tf32x2(rowhi, rowlo, col0, p);
+        } else {
+#pragma unroll
+            for (int j = 0; j < CW; ++j) {
+                const int s = col0 + j;
+                if (s >= 1 && s <= Rf) {
+                    const float q = prior_f[s - 1];
+                    const float v = p[j] * q;
+                    if (v > best_f) {
+                        best_f = v;
+                        best_p = p[j];
+                        best_q = q;
+                    }
+                }
+            }
+        }
+    }
+    int E = ns.Eacc;
+    need_exact = false;
+    if (!is_root && maxp < 0x1p-32f) {
+        if (!(maxp >= 0x1p-120f)) {
+            need_exact = true;
+        } else {
+            // bring this row's maximum back to [0.5, 1)
+            const int k = -bexp(maxp);
+            const float sc = pow2f(k);
+            for (int col0 = 0; col0 < W; col0 += 4) {
+                float4 h = *reinterpret_cast<const float4*>(rowhi + col0);
+                float4 l = *reinterpret_cast<const float4*>(rowlo + col0);
+                float v[4] = {(h.x + l.x) * sc, (h.y + l.y) * sc, (h.z + l.z) * sc, (h.w + l.w) * sc};
+                h.x = tc::round_tf32(v[0]);
+                h.y = tc::round_tf32(v[1]);
+                h.z = tc::round_tf32(v[2]);
+                h.w = tc::round_tf32(v[3]);
+                l.x = tc::round_tf32(v[0] - h.x);
+                l.y = tc::round_tf32(v[1] - h.y);
+                l.z = tc::round_tf32(v[2] - h.z);
+                l.w = tc::round_tf32(v[3] - h.w);
+                *reinterpret_cast<float4*>(rowhi + col0) = h;
+                *reinterpret_cast<float4*>(rowlo + col0) = l;
+            }
+            E -= k;
+        }
+    }
+    if (is_root && !(best_f > 0.0f)) need_exact = true;
+    out.E = E;
+    out.flag = ns.flag;
+    out.best = (double)best_p * (double)best_q;
+}
+
+// Exact epilogue (warp-collective: every lane runs it when any lane needs
+// it): pass A finds the largest per-state sum of the factors' binary
+// exponents, pass B forms the product rescaled by it, so the product's
+// maximum is in [2^-NC, 1) and nothing underflows unless the factors are
+// more than 2^250 apart. Results are stored only where `write` is set.
+template <int NC>
+__device__ __noinline__ void epi_exact(const NodeSrc<NC>& ns, int W, bool is_root, int Rf, const float* prior_f,
+                                       float* __restrict__ rowhi, float* __restrict__ rowlo, bool write,
+                                       EpiOut& out) {
+    const int s_lo = is_root ? 1 : 0;
+    const int s_hi = is_root ? Rf + 1 : W;
+    int maxe = -100000;
+    for (int col0 = 0; col0 < W; col0 += CW) {
+        int ex[CW];
+#pragma unroll
+        for (int j = 0; j < CW; ++j) ex[j] = 0;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            uint32_t r[CW];
+            if (!ns.s[c].leaf) {
+                tc::tmem_ld16_issue(ns.s[c].taddr + (uint32_t)col0, r);
+                tc::tmem_wait();
+            } else {
+                load_leaf(ns.s[c], col0, r);
+            }
+#pragma unroll
+            for (int j = 0; j < CW; ++j) ex[j] += bexp(__uint_as_float(r[j]));
+        }
+#pragma unroll
+        for (int j = 0; j < CW; ++j) {
+            const int s = col0 + j;
+            if (s >= s_lo && s < s_hi && ex[j] > maxe) maxe = ex[j];
+        }
+    }
+    bool flag = ns.flag;
+    if (maxe < -250) {
+        flag = true;     // factors too far apart (or all zero): FP64 recomputes this family
+        maxe = 0;
+    }
+    float scl[NC];
+    {
+        const int sh = -maxe;
+        const int part = sh / NC;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) scl[c] = pow2f(part + (c == 0 ? sh - part * NC : 0));
+    }
+    float best_f = 0.0f, best_p = 0.0f, best_q = 0.0f;
+    for (int col0 = 0; col0 < W; col0 += CW) {
+        float p[CW];
+#pragma unroll
+        for (int j = 0; j < CW; ++j) p[j] = 1.0f;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            uint32_t r[CW];
+            if (!ns.s[c].leaf) {
+                tc::tmem_ld16_issue(ns.s[c].taddr + (uint32_t)col0, r);
+                tc::tmem_wait();
+            } else {
+                load_leaf(ns.s[c], col0, r);
+            }
+#pragma unroll
+            for (int j = 0; j < CW; ++j) p[j] *= __uint_as_float(r[j]) * scl[c];
+        }
+        if (!is_root) {
+            if (write) store_tf32x2(rowhi, rowlo, col0, p);
+        } else {
+#pragma unroll
+            for (int j = 0; j < CW; ++j) {
+                const int s = col0 + j;
+                if (s >= 1 && s <= Rf) {
+                    const float q = prior_f[s - 1];
+                    const float v = p[j] * q;
+                    if (v > best_f) {
+                        best_f = v;
+                        best_p = p[j];
+                        best_q = q;
+                    }
+                }
+            }
+        }
+    }
+    if (write) {
+        out.E = ns.Eacc + maxe;
+        out.flag = flag;
+        out.best = (double)best_p * (double)best_q;
+    }
+}
+
+__global__ void __launch_bounds__(NTHREADS, 4)
     k_prune_tc(const __grid_constant__ CUtensorMap map_mhi, const __grid_constant__ CUtensorMap map_mlo,
                const __grid_constant__ CUtensorMap map_vhi, const __grid_constant__ CUtensorMap map_vlo,
                const PruneTcArgs a) {
@@ -76,13 +392,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     __shared__ uint32_t tmem_sh;
     __shared__ int abort_sh;
     __shared__ ChildInfo ch_sh[8];
+    __shared__ float prior_f[256];
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int Wm = a.Wm;
+    const int NS = a.stages;
     const TreePlan& P = a.plan;
-    const size_t sbytes = stage_bytes(Wm);
-    int* Esh = reinterpret_cast<int*>(smem + 2 * sbytes);   // [n_slots][TM]
+    const size_t sbytes = stage_bytes(a.Ws);
+    int* Esh = reinterpret_cast<int*>(smem + NS * sbytes);   // [n_slots][TM]
 
+    for (int j = tid; j < 256; j += NTHREADS) prior_f[j] = j < a.n_prior ? (float)a.prior[j] : 0.0f;
     if (warp == 0) tc::tmem_alloc(&tmem_sh, (uint32_t)a.tmem_cols);
     if (tid == 0) {
         tc::mbar_init(&bar_full[0], 1);
@@ -103,7 +422,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     uint32_t dn = 0;         // completions of bar_done observed (all threads)
     int last_full = -1;      // stage of the last issued TMA (thread 0)
     uint32_t last_full_parity = 0;
-    const int64_t vrow_cta = (int64_t)blockIdx.x * a.n_slots * TM;
+    const int64_t vrow_cta = a.vrow_base + (int64_t)blockIdx.x * a.n_slots * TM;
+    unsigned long long ph[4] = {0, 0, 0, 0};
+    const bool timing = a.phase_clocks != nullptr && tid == 0;
 
     for (int t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
         const PruneTile tile = a.tiles[t];
@@ -134,8 +455,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             __syncthreads();
             int nint = 0;
             for (int c = 0; c < nch; ++c) nint += ch_sh[c].leaf_col < 0;
+            // child sources (count / exponent loads) overlap the GEMM below
+            NodeSrc<2> ns2;
+            setup_src<2>(a, ch_sh, nch, Esh, tmem + lane_base, fam, tid, S, Wm, ns2);
 
             // ---------------- GEMMs of the internal children ----------------
+            long long t0 = timing ? clock64() : 0;
             if (nint > 0) {
                 if (tid == 0 && !abort_sh) {
                     const int kpc = W / KC;             // K chunks per child
@@ -151,8 +476,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     };
                     auto issue = [&](int i) -> bool {
                         const uint32_t ci = g + (uint32_t)i;
-                        const int st = ci & 1;
-                        const uint32_t u = ci >> 1;
+                        const int st = (int)(ci % (uint32_t)NS);
+                        const uint32_t u = ci / (uint32_t)NS;
                         if (u >= 1 && !tc::mbar_wait(&bar_empty[st], (u - 1) & 1)) return false;
                         const ChildInfo& c = child_of(i / kpc);
                         const int kc = i % kpc;
@@ -160,7 +485,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         float* Ahi = reinterpret_cast<float*>(base);
                         float* Alo = Ahi + TM * KC;
                         float* Bhi = Alo + TM * KC;
-                        float* Blo = Bhi + Wm * KC;
+                        float* Blo = Bhi + a.Ws * KC;
                         tc::mbar_expect_tx(&bar_full[st], (uint32_t)((2 * TM + 2 * W) * KC * sizeof(float)));
                         const int vrow = (int)(vrow_cta + (int64_t)P.slot[c.node] * TM);
                         for (int r = 0; r < TM / 32; ++r) {
@@ -178,10 +503,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     };
                     bool ok = issue(0);
                     for (int i = 0; i < total && ok; ++i) {
-                        if (i + 1 < total) ok = issue(i + 1);
+                        // with two stages the next chunk's TMA overlaps this chunk's MMAs
+                        if (NS > 1 && i + 1 < total) ok = issue(i + 1);
                         const uint32_t ci = g + (uint32_t)i;
-                        const int st = ci & 1;
-                        if (ok) ok = tc::mbar_wait(&bar_full[st], (ci >> 1) & 1);
+                        const int st = (int)(ci % (uint32_t)NS);
+                        if (ok) ok = tc::mbar_wait(&bar_full[st], (ci / (uint32_t)NS) & 1);
                         if (!ok) break;
                         tc::fence_after();
                         const ChildInfo& c = child_of(i / kpc);
@@ -190,7 +516,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         const float* Ahi = reinterpret_cast<const float*>(base);
                         const float* Alo = Ahi + TM * KC;
                         const float* Bhi = Alo + TM * KC;
-                        const float* Blo = Bhi + Wm * KC;
+                        const float* Blo = Bhi + a.Ws * KC;
                         const uint32_t d = tmem + (uint32_t)c.tcol;
 #pragma unroll
                         for (int ks = 0; ks < KC / 8; ++ks) {
@@ -201,6 +527,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                             tc::mma_tf32(d, al, bh, idesc, 1);
                         }
                         tc::mma_commit(&bar_empty[st]);
+                        if (NS == 1 && i + 1 < total) ok = issue(i + 1);
                     }
                     if (ok) {
                         tc::mma_commit(&bar_done);
@@ -222,170 +549,48 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             __syncthreads();
             if (abort_sh) break;
+            long long t1 = timing ? clock64() : 0;
 
             // ---------------- epilogue: product over children ----------------
-            int Eacc = 0;
-            int lcol[8];
-            float lw[8][3];
-            int lrow[8][3];
-            for (int c = 0; c < nch; ++c) {
-                const ChildInfo& ci = ch_sh[c];
-                if (ci.leaf_col >= 0) {
-                    const int n = fam >= 0 ? a.counts[(size_t)fam * P.n_leaves + ci.leaf_col] : 0;
-                    const int32_t* ce = a.ce + (size_t)ci.mat * Wm;
-                    if (a.err) {
-                        // error-model leaf: weights p_d 2^(ce_d - ce_max) over columns n-1, n, n+1
-                        const double* pr = a.err + (size_t)(n < a.err_rows ? n : a.err_rows - 1) * a.err_ndev;
-                        const int off = n - (a.err_ndev - 1) / 2;
-                        int cmax = -100000;
-                        for (int d = 0; d < 3 && d < a.err_ndev; ++d) {
-                            const int col = off + d;
-                            if (col >= 0 && col <= S && pr[d] > 0) cmax = max(cmax, ce[col]);
-                        }
-                        for (int d = 0; d < 3; ++d) {
-                            const int col = off + d;
-                            const bool use = d < a.err_ndev && col >= 0 && col <= S && pr[d] > 0;
-                            lrow[c][d] = use ? col : -1;
-                            lw[c][d] = use ? (float)(pr[d] * exp2((double)(ce[col] - cmax))) : 0.0f;
-                        }
-                        Eacc += cmax > -100000 ? cmax : 0;
-                        if (cmax == -100000) flag = true;
-                    } else {
-                        const bool use = n >= 0 && n <= S;
-                        lrow[c][0] = use ? n : -1;
-                        lw[c][0] = 1.0f;
-                        lrow[c][1] = lrow[c][2] = -1;
-                        lw[c][1] = lw[c][2] = 0.0f;
-                        Eacc += use ? ce[n] : 0;
-                        if (!use) flag = true;
-                    }
-                    lcol[c] = 0;
-                } else {
-                    Eacc += Esh[P.slot[ci.node] * TM + tid];
-                    lcol[c] = ci.tcol;
-                }
-            }
-            const int s_lo = is_root ? 1 : 0;
-            const int s_hi = is_root ? Rf + 1 : W;   // exclusive
-
-            auto load_factor = [&](int c, int col0, float (&y)[32]) {
-                const ChildInfo& ci = ch_sh[c];
-                if (ci.leaf_col < 0) {
-                    tc::tmem_ld32(tmem + lane_base + (uint32_t)(lcol[c] + col0), y);
-                } else {
-                    const float* ct = a.ct + (size_t)ci.mat * Wm * Wm;
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) y[j] = 0.0f;
-                    for (int d = 0; d < 3; ++d) {
-                        if (lrow[c][d] < 0) continue;
-                        const float4* src = reinterpret_cast<const float4*>(ct + (size_t)lrow[c][d] * Wm + col0);
-                        const float w = lw[c][d];
-#pragma unroll
-                        for (int q = 0; q < 8; ++q) {
-                            const float4 x = __ldg(src + q);
-                            y[4 * q + 0] = fmaf(w, x.x, y[4 * q + 0]);
-                            y[4 * q + 1] = fmaf(w, x.y, y[4 * q + 1]);
-                            y[4 * q + 2] = fmaf(w, x.z, y[4 * q + 2]);
-                            y[4 * q + 3] = fmaf(w, x.w, y[4 * q + 3]);
-                        }
-                    }
-                }
-            };
-
-            // pass A: largest per-state sum of binary exponents
-            int maxe = -100000;
-            for (int col0 = 0; col0 < W; col0 += 32) {
-                int ex[32];
-#pragma unroll
-                for (int j = 0; j < 32; ++j) ex[j] = 0;
-                for (int c = 0; c < nch; ++c) {
-                    float y[32];
-                    load_factor(c, col0, y);
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) ex[j] += bexp(y[j]);
-                }
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int s = col0 + j;
-                    if (s >= s_lo && s < s_hi && ex[j] > maxe) maxe = ex[j];
-                }
-            }
-            if (maxe < -250) {
-                flag = true;     // factors too far apart (or all zero): FP64 recomputes this family
-                maxe = 0;
-            }
-            // split the rescale over the children so no factor overflows
-            int shift[8];
-            {
-                const int sh = -maxe;
-                const int part = sh / nch;
-                for (int c = 0; c < nch; ++c) shift[c] = part;
-                shift[0] += sh - part * nch;
-            }
-
-            // pass B: product, then store (internal node) or weight by the prior (root)
-            double best = 0.0;
+            EpiOut eo;
             float* rowhi = a.vec_hi + (size_t)(vrow_cta + (int64_t)vs * TM + tid) * Wm;
             float* rowlo = a.vec_lo + (size_t)(vrow_cta + (int64_t)vs * TM + tid) * Wm;
-            for (int col0 = 0; col0 < W; col0 += 32) {
-                float p[32];
-#pragma unroll
-                for (int j = 0; j < 32; ++j) p[j] = 1.0f;
-                for (int c = 0; c < nch; ++c) {
-                    float y[32];
-                    load_factor(c, col0, y);
-                    const float sc = pow2f(shift[c]);
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) p[j] *= y[j] * sc;
-                }
-                if (!is_root) {
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        float4 h, l;
-                        h.x = tc::round_tf32(p[4 * q + 0]);
-                        h.y = tc::round_tf32(p[4 * q + 1]);
-                        h.z = tc::round_tf32(p[4 * q + 2]);
-                        h.w = tc::round_tf32(p[4 * q + 3]);
-                        l.x = tc::round_tf32(p[4 * q + 0] - h.x);
-                        l.y = tc::round_tf32(p[4 * q + 1] - h.y);
-                        l.z = tc::round_tf32(p[4 * q + 2] - h.z);
-                        l.w = tc::round_tf32(p[4 * q + 3] - h.w);
-                        reinterpret_cast<float4*>(rowhi + col0)[q] = h;
-                        reinterpret_cast<float4*>(rowlo + col0)[q] = l;
-                    }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        const int s = col0 + j;
-                        if (s >= 1 && s <= Rf) {
-                            const int jr = s - 1;
-                            const double eq = jr < a.n_prior ? a.prior[jr] : 0.0;
-                            const double vv = (double)p[j] * eq;
-                            best = vv > best ? vv : best;
-                        }
-                    }
-                }
-            }
-            const int E = Eacc + maxe;
+            bool need;
+            epi_fast<2>(ns2, W, is_root, Rf, prior_f, rowhi, rowlo, eo, need);
+            if (__any_sync(0xffffffffu, need)) epi_exact<2>(ns2, W, is_root, Rf, prior_f, rowhi, rowlo, need, eo);
+            long long t2 = timing ? clock64() : 0;
+            flag |= eo.flag;
             if (!is_root) {
-                Esh[vs * TM + tid] = E;
+                Esh[vs * TM + tid] = eo.E;
             } else if (fam >= 0) {
                 double o = NAN;
-                if (best > 0.0 && !flag) o = log(best * a.cat_probs[k]) + (double)E * 0.69314718055994530942;
+                if (eo.best > 0.0 && !flag)
+                    o = log(eo.best * a.cat_probs[k]) + (double)eo.E * 0.69314718055994530942;
                 else flag = true;
                 a.out[(size_t)fam * a.K + k] = o;
             }
             // node vectors are read back by TMA (async proxy) for the parent
+            long long t3 = timing ? clock64() : 0;
+            if (timing) t2 = t3;
             tc::fence_proxy_async_global();
             tc::fence_before();
             __syncthreads();
             tc::fence_after();
+            if (timing) {
+                const long long t4 = clock64();
+                ph[0] += t1 - t0;
+                ph[1] += t2 - t1;
+                ph[2] += t3 - t2;
+                ph[3] += t4 - t3;
+            }
         }
         if (flag && fam >= 0) atomicOr(&a.flags[fam], 1);
         __syncthreads();
         if (abort_sh) break;
     }
 
+    if (timing)
+        for (int q = 0; q < 4; ++q) atomicAdd(&a.phase_clocks[q], ph[q]);
     // teardown: no copy of ours may still be landing when TMEM goes away
     tc::fence_before();
     __syncthreads();
@@ -421,9 +626,73 @@ __global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict
     }
 }
 
+// One block: flagged families of each bin, compacted in permutation order
+// (a block-wide prefix sum per 256-family chunk), then tiles bin by bin.
+__global__ void __launch_bounds__(256) k_fallback_plan(FallbackPlanArgs a) {
+    __shared__ int scan[256];
+    __shared__ int64_t base_sh;
+    __shared__ int n_tiles_sh;
+    if (threadIdx.x == 0) {
+        base_sh = 0;
+        n_tiles_sh = 0;
+    }
+    __syncthreads();
+    for (int b = 0; b < a.n_bins; ++b) {
+        const int64_t start = base_sh;
+        for (int64_t i0 = 0; i0 < a.bin_count[b]; i0 += 256) {
+            const int64_t i = i0 + threadIdx.x;
+            int64_t fam = -1;
+            int f = 0;
+            if (i < a.bin_count[b]) {
+                fam = a.perm[a.bin_first[b] + i];
+                f = a.flags[fam] != 0;
+            }
+            scan[threadIdx.x] = f;
+            __syncthreads();
+            for (int off = 1; off < 256; off <<= 1) {
+                const int add = threadIdx.x >= off ? scan[threadIdx.x - off] : 0;
+                __syncthreads();
+                scan[threadIdx.x] += add;
+                __syncthreads();
+            }
+            if (f) a.fb_perm[base_sh + scan[threadIdx.x] - 1] = fam;
+            const int total = scan[255];
+            __syncthreads();
+            if (threadIdx.x == 0) base_sh += total;
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            const int64_t cnt = base_sh - start;
+            for (int k = 0; k < a.K; ++k)
+                for (int64_t i = 0; i < cnt; i += 32) {
+                    PruneTile t;
+                    t.first = (int)(start + i);
+                    t.count = (int)(cnt - i < 32 ? cnt - i : 32);
+                    t.k = k;
+                    t.S = a.bin_width[b] - 1;
+                    t.R = a.bin_width[b] - 1;
+                    t.pad[0] = t.pad[1] = t.pad[2] = 0;
+                    a.fb_tiles[n_tiles_sh++] = t;
+                }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        a.out_counts[0] = (int32_t)base_sh;
+        a.out_counts[1] = n_tiles_sh;
+    }
+}
+
 }  // namespace
 
-size_t prune_tc_smem_bytes(int Wm, int n_slots) { return 2 * stage_bytes(Wm) + (size_t)n_slots * TM * sizeof(int) + 1024; }
+cudaError_t launch_fallback_plan(const FallbackPlanArgs& a, cudaStream_t s) {
+    k_fallback_plan<<<1, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages) {
+    return (size_t)stages * stage_bytes(Ws) + (size_t)n_slots * TM * sizeof(int) + 1024;
+}
 
 cudaError_t launch_convert_tc(const ConvertJob* d_jobs, int n_jobs, TcBuffers b, cudaStream_t s) {
     if (n_jobs <= 0) return cudaSuccess;

@@ -86,18 +86,35 @@ struct MatKeyHash {
 
 struct MatEntry {
     double* d = nullptr;       // FP64 row-major size x size
-    int chunk = -1;
+    int chunk = -1;            // build batch (index of its ready event)
+};
+
+struct Slab {
+    void* p = nullptr;
+    size_t size = 0, used = 0;
 };
 
 // Per-request device workspace (one per stream).
 struct Workspace {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    cudaEvent_t ev_staged = nullptr;   // after the last request's host->device staging copies
+    bool staged = false;
+    static constexpr int kAux = 3;     // streams for concurrent per-bin launches
+    cudaStream_t aux[kAux] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_join[kAux] = {nullptr, nullptr, nullptr};
+    struct MapCache {
+        const void* ptr = nullptr;
+        int64_t rows = 0;
+        int cols = 0;
+        CUtensorMap map;
+    } map_cache[4];
     DevBuf scratch, tiles, mats, cat, fam_lnl, total, nfail, jobs, catp;
     PinnedBuf h_tiles, h_mats, h_jobs, h_out, h_catp;
     // tensor-core path
-    DevBuf tc_hi, tc_lo, tc_ct, tc_ce, tc_mi, tc_vhi, tc_vlo, conv, flags, fb_perm, tiles64, tiles_fb;
-    PinnedBuf h_conv, h_mi, h_flags, h_tiles64, h_tiles_fb;
+    DevBuf tc_hi, tc_lo, tc_ct, tc_ce, tc_mi, tc_vhi, tc_vlo, conv, flags, fb_perm, tiles64, tiles_fb, parts, fb_count, phase;
+    PinnedBuf h_conv, h_mi, h_flags, h_tiles64, h_tiles_fb, h_tail;
     std::vector<PruneTile> tile_vec;
     ~Workspace();
     int init(int device);
@@ -133,7 +150,8 @@ struct cafe_ctx {
     cafe::DevBuf d_err;
     // matrix cache
     std::unordered_map<cafe::MatKey, cafe::MatEntry, cafe::MatKeyHash> cache;
-    std::vector<void*> chunks;
+    std::vector<cafe::Slab> slabs;
+    std::vector<cudaEvent_t> batch_events;
     size_t cache_bytes = 0, cache_cap = 0;
     // workspaces: [0] for synchronous calls, [1..] for the serving loop
     std::vector<std::unique_ptr<cafe::Workspace>> ws;
