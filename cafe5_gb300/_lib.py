@@ -25,8 +25,10 @@ EXPORTS = [
     "cafe_prior_set", "cafe_error_model_set", "cafe_matrices_build", "cafe_matrix_get",
     "cafe_matrix_cache_size", "cafe_matrix_cache_clear", "cafe_is_saturated", "cafe_score",
     "cafe_score_device", "cafe_submit", "cafe_poll", "cafe_serving_stats", "cafe_profile_enable",
-    "cafe_profile_read", "cafe_prune_fp64_noalloc",
+    "cafe_profile_read", "cafe_prune_fp64_noalloc", "cafe_optimize", "cafe_discrete_gamma",
+    "cafe_nelder_mead",
 ]
+OPT_LAMBDA, OPT_LAMBDA_ALPHA, OPT_LAMBDA_EPSILON, OPT_ALPHA = 0, 1, 2, 3
 
 
 class Config(C.Structure):
@@ -52,6 +54,19 @@ class Timings(C.Structure):
     _fields_ = [("matrix_ms", C.c_double), ("prune_ms", C.c_double), ("finish_ms", C.c_double),
                 ("other_ms", C.c_double), ("prune_flops", C.c_double), ("launches", C.c_int64),
                 ("prune_launches", C.c_int64), ("matrices_built", C.c_int64)]
+
+
+class OptConfig(C.Structure):
+    _fields_ = [("kind", C.c_int), ("n_params", C.c_int), ("initial", C.c_void_p), ("max_iterations", C.c_int),
+                ("reflection", C.c_double), ("expansion", C.c_double)]
+
+
+OBJECTIVE = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.c_int, C.c_void_p)
+
+
+class OptResult(C.Structure):
+    _fields_ = [("values", C.c_void_p), ("score", C.c_double), ("iterations", C.c_int),
+                ("evaluations", C.c_int), ("converged", C.c_int)]
 
 
 _lib = None
@@ -97,6 +112,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
         "cafe_profile_enable": (i, [p, i]),
         "cafe_profile_read": (i, [p, P(Timings)]),
         "cafe_prune_fp64_noalloc": (i, [i, p, p, i, p, i64, i, i, i, p, i, i, p, p]),
+        "cafe_optimize": (i, [p, P(Request), P(OptConfig), P(OptResult)]),
+        "cafe_discrete_gamma": (i, [i, d, p, p]),
+        "cafe_nelder_mead": (i, [P(OptConfig), OBJECTIVE, p, P(OptResult)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

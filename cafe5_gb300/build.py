@@ -15,7 +15,10 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcafe_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Host code is compiled without floating-point contraction so that it rounds
+# identically on x86-64 and on Arm (where FMA is always available).
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+         "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr", "-I", os.path.join(HERE, "..", "include")]
 
 
@@ -34,6 +37,7 @@ def _compile(src: str, extra) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     deps = [src] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     deps.append(os.path.join(HERE, "..", "include", "cafe_gb300.h"))
+    deps.append(os.path.abspath(__file__))
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc()] + ARCH + FLAGS + list(extra) + ["-c", src, "-o", obj]

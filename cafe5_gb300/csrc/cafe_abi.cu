@@ -804,10 +804,11 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         fp.fb_perm = ws.fb_perm.as<int64_t>();
         fp.fb_tiles = ws.tiles_fb.as<PruneTile>();
         fp.out_counts = d_status + 1;     // [families, tiles]
+        fp.any_flag = d_status + 3;
         if (prof) C->prof.begin(3, ws.stream, &ev);
         CK(launch_fallback_plan(fp, ws.stream), "fallback plan");
         if (prof) C->prof.end(3, ws.stream, ev);
-        const int n_ctas = C->n_ctas;
+        const int n_ctas = C->sm_count;
         const int64_t per_cta = (int64_t)T.n_slots * msize * 32;
         CK(ws.scratch.reserve((size_t)n_ctas * per_cta * sizeof(double)), "scratch");
         Prune64Args a{};

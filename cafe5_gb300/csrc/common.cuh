@@ -181,6 +181,7 @@ struct FallbackPlanArgs {
     int64_t* fb_perm;            // [F]
     PruneTile* fb_tiles;         // [K * (F / 32 + n_bins)]
     int32_t* out_counts;         // [2]
+    const int32_t* any_flag;     // optional: zero means no family is flagged
 };
 cudaError_t launch_fallback_plan(const FallbackPlanArgs& a, cudaStream_t s);
 

@@ -246,9 +246,11 @@ __device__ __forceinline__ void neumaier_add(double& sum, double& comp, double x
     sum = tt;
 }
 
-__global__ void __launch_bounds__(256) k_finish_fam(FinishArgs a) {
-    __shared__ double ssum[256], scomp[256];
-    __shared__ int sfail[256], sinf[256];
+constexpr int kFinishThreads = 64;
+
+__global__ void __launch_bounds__(kFinishThreads) k_finish_fam(FinishArgs a) {
+    __shared__ double ssum[kFinishThreads], scomp[kFinishThreads];
+    __shared__ int sfail[kFinishThreads], sinf[kFinishThreads];
     double sum = 0.0, comp = 0.0;
     int fail = 0, ninf = 0;   // ninf: families with lnL = -inf (log of an underflowed 0)
     for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < a.F; f += (int64_t)gridDim.x * blockDim.x) {
@@ -306,15 +308,34 @@ __global__ void __launch_bounds__(256) k_finish_fam(FinishArgs a) {
     }
 }
 
-__global__ void k_finish_total(FinishArgs a, int n_parts) {
-    if (threadIdx.x != 0) return;
+__global__ void __launch_bounds__(256) k_finish_total(FinishArgs a, int n_parts) {
+    // fixed partition (thread i takes parts i, i + 256, ...), then a fixed
+    // sequential combine: deterministic for a given family count
+    __shared__ double ssum[256], scomp[256];
+    __shared__ int sfail[256], sinf[256];
     double s = 0.0, c = 0.0;
     int fl = 0, ni = 0;
-    for (int i = 0; i < n_parts; ++i) {
+    for (int i = threadIdx.x; i < n_parts; i += blockDim.x) {
         neumaier_add(s, c, a.part_sum[2 * i]);
         c += a.part_sum[2 * i + 1];
         fl += a.part_cnt[2 * i];
         ni += a.part_cnt[2 * i + 1];
+    }
+    ssum[threadIdx.x] = s;
+    scomp[threadIdx.x] = c;
+    sfail[threadIdx.x] = fl;
+    sinf[threadIdx.x] = ni;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    s = 0.0;
+    c = 0.0;
+    fl = 0;
+    ni = 0;
+    for (int i = 0; i < (int)blockDim.x; ++i) {
+        neumaier_add(s, c, ssum[i]);
+        c += scomp[i];
+        fl += sfail[i];
+        ni += sinf[i];
     }
     *a.n_failed = fl;
     // -sum lnL: +inf on gamma failure or when any family's lnL is -inf;
@@ -354,12 +375,14 @@ cudaError_t launch_prune64(const Prune64Args& a, int n_ctas, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-int finish_parts(int64_t F) { return (int)std::max<int64_t>(1, std::min<int64_t>((F + 255) / 256, 512)); }
+int finish_parts(int64_t F) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>((F + kFinishThreads - 1) / kFinishThreads, 2048));
+}
 
 cudaError_t launch_finish(const FinishArgs& a, cudaStream_t s) {
     const int parts = finish_parts(a.F);
-    k_finish_fam<<<parts, 256, 0, s>>>(a);
-    k_finish_total<<<1, 32, 0, s>>>(a, parts);
+    k_finish_fam<<<parts, kFinishThreads, 0, s>>>(a);
+    k_finish_total<<<1, 256, 0, s>>>(a, parts);
     return cudaGetLastError();
 }
 

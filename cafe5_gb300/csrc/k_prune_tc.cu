@@ -584,7 +584,10 @@ __global__ void __launch_bounds__(NTHREADS, 4)
                 ph[3] += t4 - t3;
             }
         }
-        if (flag && fam >= 0) atomicOr(&a.flags[fam], 1);
+        if (flag && fam >= 0) {
+            atomicOr(&a.flags[fam], 1);
+            atomicOr(a.status + 3, 1);     // "some family is flagged"
+        }
         __syncthreads();
         if (abort_sh) break;
     }
@@ -632,6 +635,13 @@ __global__ void __launch_bounds__(256) k_fallback_plan(FallbackPlanArgs a) {
     __shared__ int scan[256];
     __shared__ int64_t base_sh;
     __shared__ int n_tiles_sh;
+    if (a.any_flag && *a.any_flag == 0) {     // nothing flagged: no work
+        if (threadIdx.x == 0) {
+            a.out_counts[0] = 0;
+            a.out_counts[1] = 0;
+        }
+        return;
+    }
     if (threadIdx.x == 0) {
         base_sh = 0;
         n_tiles_sh = 0;

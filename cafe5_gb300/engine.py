@@ -308,11 +308,13 @@ class BaseModel:
         return dict(use_error_model=self.error_model is not None, S=self.max_family_size if ref else 0,
                     R=self.max_root_family_size if ref else 0, precision=self.precision)
 
+    def _score_kw(self, lam):
+        return dict(model=_lib.MODEL_BASE, lambda_kind=lam.kind, dedupe=self.dedupe, **self._kw())
+
     def infer_family_likelihoods(self, prior: RootPrior, lam=None) -> float:
         lam = lam or self.lam
         self._common(prior)
-        r = self.ctx.score(self.tree_id, self.set_id, lam.values, model=_lib.MODEL_BASE, lambda_kind=lam.kind,
-                           dedupe=self.dedupe, **self._kw())
+        r = self.ctx.score(self.tree_id, self.set_id, lam.values, **self._score_kw(lam))
         self.last = r
         self.results = r.family_lnl
         return r.total
@@ -330,19 +332,26 @@ class GammaModel(BaseModel):
             self.set_alpha(fixed_alpha)
 
     def set_alpha(self, alpha: float):
-        """gamma_model::set_alpha (src/gamma_core.cpp:61-67)."""
+        """gamma_model::set_alpha (src/gamma_core.cpp:61-67). An alpha <= 0
+        leaves unit multipliers; can_infer then rejects it (score +inf)."""
         self.alpha = alpha
-        if len(self.cat_probs) > 1:
-            self.cat_probs, self.multipliers = discrete_gamma(alpha, len(self.cat_probs))
+        K = len(self.cat_probs)
+        if K > 1:
+            if alpha > 0:
+                self.cat_probs, self.multipliers = discrete_gamma(alpha, K)
+            else:
+                self.cat_probs, self.multipliers = [1.0 / K] * K, [1.0] * K
+
+    def _score_kw(self, lam):
+        return dict(model=_lib.MODEL_GAMMA, lambda_kind=lam.kind, multipliers=self.multipliers,
+                    cat_probs=self.cat_probs, **self._kw())
 
     def infer_family_likelihoods(self, prior: RootPrior, lam=None) -> float:
         lam = lam or self.lam
-        if self.alpha is not None and self.alpha < 0 and len(self.cat_probs) > 1 and self.multipliers == [1.0] * len(self.cat_probs):
+        if self.alpha is not None and self.alpha <= 0 and len(self.cat_probs) > 1 and self.multipliers == [1.0] * len(self.cat_probs):
             return math.inf
         self._common(prior)
-        r = self.ctx.score(self.tree_id, self.set_id, lam.values, model=_lib.MODEL_GAMMA, lambda_kind=lam.kind,
-                           multipliers=self.multipliers, cat_probs=self.cat_probs, want_categories=True,
-                           **self._kw())
+        r = self.ctx.score(self.tree_id, self.set_id, lam.values, want_categories=True, **self._score_kw(lam))
         self.last = r
         self.results = r.family_lnl
         self.category_results = r.category_lnl
@@ -383,6 +392,9 @@ class LambdaOptimizerScorer(InferenceOptimizerScorer):
     def prepare_calculation(self, values):
         self.lam.update(values)
 
+    def finalize(self, values):
+        self.lam.update(values)
+
 
 class GammaLambdaOptimizerScorer(LambdaOptimizerScorer):
     """gamma_lambda_optimizer: lambdas then alpha."""
@@ -394,6 +406,9 @@ class GammaLambdaOptimizerScorer(LambdaOptimizerScorer):
         n = self.lam.count()
         self.lam.update(values[:n])
         self.model.set_alpha(float(values[n]))
+
+    def finalize(self, values):
+        self.prepare_calculation(values)
 
 
 class LambdaEpsilonOptimizerScorer(LambdaOptimizerScorer):
@@ -416,3 +431,74 @@ class LambdaEpsilonOptimizerScorer(LambdaOptimizerScorer):
             repl[old] = float(values[n + i])
             self.current[i] = float(values[n + i])
         self.error_model.replace_epsilons(repl)
+
+    def finalize(self, values):
+        """lambda_epsilon_optimizer::finalize: lambdas, then the first epsilon
+        through error_model::update_single_epsilon."""
+        n = self.lam.count()
+        self.lam.update(values[:n])
+        self.error_model.replace_epsilons({self.current[0]: float(values[n])})
+        self.current = self.error_model.get_epsilons()
+
+
+class GammaOptimizerScorer(InferenceOptimizerScorer):
+    """gamma_optimizer: alpha only, lambdas fixed (src/optimizer_scorer.cpp:112-150)."""
+
+    def initial_guesses(self, rng):
+        return [float(rng.gamma(4.0, 0.25))]
+
+    def prepare_calculation(self, values):
+        self.model.set_alpha(float(values[0]))
+
+    def finalize(self, values):
+        self.model.set_alpha(float(values[0]))
+
+
+@dataclass
+class OptimizerResult:
+    values: List[float]
+    score: float
+    num_iterations: int
+    evaluations: int
+    converged: bool
+
+
+class Optimizer:
+    """optimizer (src/optimizer.h, src/optimizer.cpp:537-560) with the
+    Standard Nelder-Mead strategy. The simplex search runs natively in the
+    library (cafe_optimize): the host C++ loop proposes points and each
+    objective evaluation is one GPU score of the scorer's model, exactly as
+    the scorer's calculate_score would compute it."""
+
+    def __init__(self, scorer: InferenceOptimizerScorer):
+        self.scorer = scorer
+
+    def _kind(self):
+        sc = self.scorer
+        if isinstance(sc, LambdaEpsilonOptimizerScorer):
+            return _lib.OPT_LAMBDA_EPSILON
+        if isinstance(sc, GammaLambdaOptimizerScorer):
+            return _lib.OPT_LAMBDA_ALPHA
+        if isinstance(sc, GammaOptimizerScorer):
+            return _lib.OPT_ALPHA
+        if isinstance(sc, LambdaOptimizerScorer):
+            return _lib.OPT_LAMBDA
+        raise TypeError(f"no native search for {type(sc).__name__}")
+
+    def optimize(self, initial: Optional[Sequence[float]] = None, rng: Optional[np.random.Generator] = None,
+                 max_iterations: int = 300, expansion: float = 2.0, reflection: float = 1.0) -> OptimizerResult:
+        sc = self.scorer
+        model = sc.model
+        if initial is None:
+            initial = sc.initial_guesses(rng or np.random.default_rng())
+        x0 = np.ascontiguousarray(initial, dtype=np.float64)
+        kind = self._kind()
+        model._common(sc.prior)
+        if kind == _lib.OPT_LAMBDA_EPSILON:
+            model.ctx.set_error_model(sc.error_model.table())
+        req, keep = model.ctx.make_request(model.tree_id, model.set_id, sc.lam.values, **model._score_kw(sc.lam))
+        cfg = _lib.OptConfig(kind, len(x0), _p(x0), int(max_iterations), float(reflection), float(expansion))
+        best = np.zeros(len(x0))
+        res = _lib.OptResult(_p(best), 0.0, 0, 0, 0)
+        model.ctx._check(model.ctx.lib.cafe_optimize(model.ctx.h, C.byref(req), C.byref(cfg), C.byref(res)))
+        return OptimizerResult(best.tolist(), res.score, res.iterations, res.evaluations, bool(res.converged))

@@ -104,14 +104,14 @@ class ErrorModel:
         def near(x, y):
             return abs(x - y) <= 0.01 * abs(x)
         vec = list(self.rows[0])
-        for old, new in new_eps.items():
+        for old, new in sorted(new_eps.items()):
             if near(old, vec[-1]):
                 vec[-1] = new
                 vec[1] = 1 - new
                 self.set_probabilities(0, vec)
         for i in range(1, len(self.rows)):
             vec = list(self.rows[i])
-            for old, new in new_eps.items():
+            for old, new in sorted(new_eps.items()):
                 if near(old, vec[-1]):
                     vec[-1] = new
                     vec[0] = new
@@ -144,20 +144,18 @@ class ErrorModel:
         return em
 
 
-def _gamma_quantile(p: float, shape: float) -> float:
-    """Quantile of Gamma(shape, scale=1): inverse of the regularised lower
-    incomplete gamma function (scipy.special.gammaincinv)."""
-    from scipy.special import gammaincinv
-    return float(gammaincinv(shape, p))
-
-
 def discrete_gamma(alpha: float, K: int) -> (List[float], List[float]):
-    """(category probabilities, rate multipliers) for K median categories."""
+    """(category probabilities, rate multipliers) for K median categories of
+    a mean-1 Gamma(alpha) (get_gamma, src/gamma.cpp:225-241), computed by the
+    library's restatement of the reference's AS 91 / AS 32 / AS 70 routines
+    so that the multipliers match the reference's bit for bit."""
     if K <= 1:
         return [1.0], [1.0]
-    # Gamma(alpha, rate=alpha): quantile = Gamma(alpha,1) quantile / alpha
-    r = [_gamma_quantile((2 * k + 1) / (2.0 * K), alpha) / alpha for k in range(K)]
-    t = sum(r)
-    factor = alpha / alpha * K
-    mult = [x * factor / t for x in r]
-    return [1.0 / K] * K, mult
+    import ctypes
+    from . import _lib
+    probs = (ctypes.c_double * K)()
+    mult = (ctypes.c_double * K)()
+    rc = _lib.load().cafe_discrete_gamma(K, float(alpha), ctypes.addressof(probs), ctypes.addressof(mult))
+    if rc != 0:
+        raise ValueError(f"discrete gamma needs alpha > 0 (got {alpha})")
+    return list(probs), list(mult)

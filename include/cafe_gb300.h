@@ -224,6 +224,68 @@ int cafe_prune_fp64_noalloc(int n_nodes, const int32_t* parent, const double* co
  * p99 latency (ms, submit -> done), current in-flight count. */
 int cafe_serving_stats(cafe_ctx* ctx, int64_t* completed, double* p50_ms, double* p99_ms, int* in_flight);
 
+/* ---- parameter search (src/optimizer.cpp, src/optimizer_scorer.cpp) ---- */
+/* Which parameters the search varies (the scorer classes of
+ * src/optimizer_scorer.h:28-150):
+ *   LAMBDA          lambdas only (lambda_optimizer; base model, or gamma
+ *                   with the request's fixed categories)
+ *   ALPHA           alpha only, lambdas fixed at the request's (gamma_optimizer)
+ *   LAMBDA_ALPHA    lambdas + alpha (gamma_lambda_optimizer); the request's
+ *                   multipliers and cat_probs are recomputed from alpha each
+ *                   evaluation by cafe_discrete_gamma
+ *   LAMBDA_EPSILON  lambdas + the error model's distinct epsilons
+ *                   (lambda_epsilon_optimizer); the context's error model
+ *                   (3 deviations per row) is rewritten by
+ *                   error_model::replace_epsilons each evaluation and left
+ *                   at the last evaluated values */
+typedef enum {
+    CAFE_OPT_LAMBDA = 0,
+    CAFE_OPT_LAMBDA_ALPHA = 1,
+    CAFE_OPT_LAMBDA_EPSILON = 2,
+    CAFE_OPT_ALPHA = 3,
+} cafe_opt_kind;
+
+typedef struct {
+    int kind;                    /* cafe_opt_kind */
+    int n_params;                /* n_lambdas (+1 alpha | + number of epsilons); ALPHA: 1 */
+    const double* initial;       /* starting point, n_params (optimizer_scorer::initial_guesses) */
+    int max_iterations;          /* <= 0: 300 (optimizer_parameters::neldermead_iterations) */
+    double reflection;           /* <= 0: 1 (Nelder-Mead rho) */
+    double expansion;            /* <= 0: 2 (Nelder-Mead chi) */
+} cafe_opt_config;
+
+typedef struct {
+    double* values;              /* host, n_params: best point found */
+    double score;                /* -lnL there (+inf if every point was rejected) */
+    int iterations;
+    int evaluations;             /* objective (= cafe_score) calls */
+    int converged;               /* 1 if tolx/tolf were reached before max_iterations */
+} cafe_opt_result;
+
+/* optimizer::optimize with the Standard Nelder-Mead strategy
+ * (src/optimizer.cpp:60-73, 156-322, 430-487): simplex start 5 % away from
+ * `initial` per coordinate (0.00025 for a zero coordinate), tolx = tolf =
+ * 1e-6, reflection/expansion/contraction/shrink 1/2/0.5/0.5. Each objective
+ * evaluation scores `base` through cafe_score with the candidate
+ * parameters substituted; NaN scores count as +inf. As in
+ * optimizer::get_initial_guesses (src/optimizer.cpp:343-360) the initial
+ * point is scored first; if that is +inf the call returns
+ * CAFE_ERR_INVALID without searching. `evaluations` counts that call. */
+int cafe_optimize(cafe_ctx* ctx, const cafe_request* base, const cafe_opt_config* cfg, cafe_opt_result* out);
+
+/* fminsearch_min (src/optimizer.cpp:281-322) over a caller-supplied
+ * objective, for scorers that are not likelihoods (the reference's
+ * optimizer_scorer interface, src/optimizer_scorer.h:13-20): the same
+ * simplex rules and defaults as cafe_optimize (`kind` is ignored), without
+ * the initial-point check; `evaluations` counts objective calls. */
+int cafe_nelder_mead(const cafe_opt_config* cfg, double (*objective)(const double* x, int n, void* user), void* user,
+                     cafe_opt_result* out);
+
+/* gamma_model::set_alpha (src/gamma.cpp:15-52, 225-241): K equal-probability
+ * rate categories of a mean-1 Gamma(alpha) distribution, each represented
+ * by its median, rescaled so the multipliers average 1. */
+int cafe_discrete_gamma(int K, double alpha, double* probs, double* multipliers);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,6 +7,8 @@
 //   gamma_model::infer_family_likelihoods  (src/gamma_core.cpp:168-237)
 //   matrix_cache::precalculate_matrices    (src/matrix_cache.cpp:113-163)
 //   inference_prune                        (src/core.cpp:134-145)
+//   fminsearch_min over the optimizer scorers (src/optimizer.cpp:281-322,
+//                                           src/optimizer_scorer.cpp:22-180)
 //
 // It reads the reference's own file formats (Newick tree, CAFE family
 // table, error-model file) through the reference's own readers
@@ -15,7 +17,9 @@
 // that the parity tests compare bit patterns, not printed decimals.
 //
 // Nothing in the product links or runs this file.
+#include <algorithm>
 #include <chrono>
+#include <limits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -41,6 +45,8 @@
 #include "io.h"
 #include "lambda.h"
 #include "matrix_cache.h"
+#include "optimizer.h"
+#include "optimizer_scorer.h"
 #include "probability.h"
 #include "root_equilibrium_distribution.h"
 
@@ -79,13 +85,70 @@ std::vector<double> parse_list(const std::string& s) {
     return v;
 }
 
+// Analytic objectives for the Nelder-Mead known-answer runs. The parity
+// tests evaluate the same expressions in the same order.
+struct analytic_scorer : public optimizer_scorer {
+    std::string fn;
+    int n;
+    int evaluations = 0;
+    analytic_scorer(std::string f, int n_) : fn(std::move(f)), n(n_) {}
+    std::vector<double> initial_guesses() override { return std::vector<double>(n, 1.0); }
+    double calculate_score(const double* x) override {
+        ++evaluations;
+        if (fn == "rosen" || fn == "wall") {
+            if (fn == "wall" && x[0] > 1.0) return std::numeric_limits<double>::infinity();
+            double s = 0;
+            for (int i = 0; i + 1 < n; ++i) {
+                const double a = x[i + 1] - x[i] * x[i], b = 1 - x[i];
+                s += 100 * a * a + b * b;
+            }
+            return s;
+        }
+        if (fn == "bowl") {
+            double s = 0;
+            for (int i = 0; i < n; ++i) {
+                const double d = x[i] - (i + 1);
+                s += d * d * (i + 1);
+            }
+            return s;
+        }
+        if (fn == "product") {
+            double s = 1.0;
+            for (int i = 0; i < n; ++i) s *= x[i];
+            return s;
+        }
+        throw std::runtime_error("unknown objective " + fn);
+    }
+};
+
+// Counts the objective calls of a likelihood scorer.
+struct counting_scorer : public optimizer_scorer {
+    inference_optimizer_scorer* inner;
+    int evaluations = 0;
+    explicit counting_scorer(inference_optimizer_scorer* s) : inner(s) {}
+    std::vector<double> initial_guesses() override { return inner->initial_guesses(); }
+    double calculate_score(const double* x) override {
+        ++evaluations;
+        return inner->calculate_score(x);
+    }
+};
+
+void print_search(FMinSearch* pfm, int evaluations) {
+    candidate* best = get_best_result(pfm);
+    std::printf("best");
+    for (double v : best->values) std::printf(" %a", v);
+    std::printf("\nscore %a\niters %d\nevals %d\n", best->score, pfm->iters, evaluations);
+}
+
 void usage() {
     std::fprintf(stderr,
         "cafe_ref_harness --tree T.nwk --families F.tab --lambdas l1[,l2..]\n"
         "   [--lambda-tree L.nwk] [--error E.txt]\n"
         "   [--gamma-alpha A --gamma-k K] [--gamma-mult m1,.. --gamma-prob p1,..]\n"
         "   [--max-family S --max-root R] [--prior uniform|uniform:N|poisson:X|rootdist:s=n,..]\n"
-        "   [--repeat N] [--quiet]\n");
+        "   [--repeat N] [--quiet]\n"
+        "   [--optimize lambda|alpha|lambda_alpha|lambda_epsilon --initial x1,..]\n"
+        "cafe_ref_harness nm rosen|wall|bowl|product <maxiters> x1,..\n");
 }
 
 }  // namespace
@@ -131,7 +194,23 @@ int main(int argc, char** argv) {
         return 0;
     }
 
-    std::string tree_path, fam_path, lambda_tree_path, err_path, prior_spec = "uniform";
+    // "nm <objective> <maxiters> x1,..": fminsearch_min on an analytic
+    // objective with the Standard strategy's tolerances.
+    if (argc == 5 && std::string(argv[1]) == "nm") {
+        std::vector<double> x0 = parse_list(argv[4]);
+        analytic_scorer sc(argv[2], (int)x0.size());
+        FMinSearch* pfm = fminsearch_new_with_eq(&sc, (int)x0.size());
+        pfm->maxiters = std::stoi(argv[3]);
+        pfm->tolx = 1e-6;
+        pfm->tolf = 1e-6;
+        fminsearch_min(pfm, x0.data());
+        print_search(pfm, sc.evaluations);
+        fminsearch_free(pfm);
+        return 0;
+    }
+
+    std::string tree_path, fam_path, lambda_tree_path, err_path, prior_spec = "uniform", opt_kind;
+    std::vector<double> opt_initial;
     std::vector<double> lambdas, gmult, gprob;
     double alpha = -1;
     int gk = 0, S = -1, R = -1, repeat = 1;
@@ -156,6 +235,8 @@ int main(int argc, char** argv) {
         else if (a == "--prior") prior_spec = next();
         else if (a == "--repeat") repeat = std::stoi(next());
         else if (a == "--quiet") quiet = true;
+        else if (a == "--optimize") opt_kind = next();
+        else if (a == "--initial") opt_initial = parse_list(next());
         else { usage(); return 2; }
     }
     if (tree_path.empty() || fam_path.empty() || lambdas.empty()) { usage(); return 2; }
@@ -227,6 +308,37 @@ int main(int argc, char** argv) {
         } else {
             pb = new probe_base(lam.get(), tree.get(), &families, max_fam, max_root, em.get());
             m.reset(pb);
+        }
+
+        if (!opt_kind.empty()) {
+            // optimizer::optimize with the Standard strategy from a given
+            // starting point: the initial-point check of get_initial_guesses,
+            // then fminsearch_min (src/optimizer.cpp:343-360, 366-385).
+            auto lengths = tree->get_branch_lengths();
+            double longest = *std::max_element(lengths.begin(), lengths.end());
+            std::unique_ptr<inference_optimizer_scorer> sc;
+            if (opt_kind == "lambda") sc.reset(new lambda_optimizer(lam.get(), m.get(), prior.get(), longest));
+            else if (opt_kind == "alpha" && pg) sc.reset(new gamma_optimizer(pg, prior.get()));
+            else if (opt_kind == "lambda_alpha" && pg)
+                sc.reset(new gamma_lambda_optimizer(lam.get(), pg, prior.get(), longest));
+            else if (opt_kind == "lambda_epsilon" && em) {
+                auto* le = new lambda_epsilon_optimizer(m.get(), em.get(), prior.get(), std::map<int, int>(), lam.get(),
+                                                        longest);
+                le->initial_guesses();   // records the current epsilons
+                sc.reset(le);
+            } else throw std::runtime_error("bad --optimize " + opt_kind);
+            sc->quiet = true;
+            counting_scorer cs(sc.get());
+            const double first = cs.calculate_score(opt_initial.data());
+            std::printf("first %a\n", first);
+            FMinSearch* pfm = fminsearch_new_with_eq(&cs, (int)opt_initial.size());
+            pfm->maxiters = 300;
+            pfm->tolx = 1e-6;
+            pfm->tolf = 1e-6;
+            fminsearch_min(pfm, opt_initial.data());
+            print_search(pfm, cs.evaluations);
+            fminsearch_free(pfm);
+            return 0;
         }
 
         double total = 0;

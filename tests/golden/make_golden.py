@@ -7,6 +7,8 @@ tests, and stores inputs plus hex-float outputs:
 
   ref_cases.json     end-to-end infer_family_likelihoods cases
   ref_matrices.json  transition matrices from matrix_cache
+  ref_optimizer.json Nelder-Mead searches (fminsearch_min) over analytic
+                     objectives and over the likelihood scorers
 
 Only this script reads the reference (it needs /root/reference and the
 built harness); the tests read the committed JSON. Usage:
@@ -63,8 +65,22 @@ def lambda_tree_newick(tree, lam_idx):
     return rec(tree.root) + ";"
 
 
+def parse_search(out: str):
+    res = {}
+    for ln in out.splitlines():
+        tok = ln.split()
+        if tok[0] == "best":
+            res["best_hex"] = tok[1:]
+        elif tok[0] in ("score", "first"):
+            res[tok[0] + "_hex"] = tok[1]
+        elif tok[0] in ("iters", "evals"):
+            res[tok[0]] = int(tok[1])
+    return res
+
+
 def make_case(name, tree, fams, lambdas, *, lam_idx=None, model="base", mult=None, probs=None,
-              err=None, S=None, R=None, prior="uniform", note=""):
+              err=None, S=None, R=None, prior="uniform", note="", alpha=None, K=None, optimize=None,
+              initial=None):
     with tempfile.TemporaryDirectory() as d:
         tp, fp = os.path.join(d, "t.nwk"), os.path.join(d, "f.tab")
         nwk = tree.to_newick()
@@ -84,10 +100,15 @@ def make_case(name, tree, fams, lambdas, *, lam_idx=None, model="base", mult=Non
             err_text = err
             open(ep, "w").write(err)
             args += ["--error", ep]
-        if model == "gamma":
+        if model == "gamma" and alpha is not None:
+            args += ["--gamma-alpha", repr(alpha), "--gamma-k", str(K)]
+        elif model == "gamma":
             args += ["--gamma-mult", ",".join(repr(x) for x in mult), "--gamma-prob", ",".join(repr(x) for x in probs)]
         if S is not None:
             args += ["--max-family", str(S), "--max-root", str(R)]
+        if optimize is not None:
+            search = parse_search(run(args + ["--optimize", optimize, "--initial",
+                                              ",".join(repr(x) for x in initial)]))
         out = parse_output(run(args))
     case = {
         "name": name, "note": note, "newick": nwk, "lambda_newick": lnwk, "taxa": tree.leaf_names,
@@ -95,9 +116,14 @@ def make_case(name, tree, fams, lambdas, *, lam_idx=None, model="base", mult=Non
         "model": model, "multipliers": None if mult is None else [float(x).hex() for x in mult],
         "cat_probs": None if probs is None else [float(x).hex() for x in probs],
         "error_model": err_text, "prior": prior, "S": out["S"], "R": out["R"],
+        "alpha": alpha, "K": K,
         "expected": {"total_hex": out["total_hex"], "fam_lnl_hex": [out["fam"].get(i) for i in fams.ids],
                      "cat": [out["cat"].get(i) for i in fams.ids] if model == "gamma" else None},
     }
+    if optimize is not None:
+        case["optimize"] = optimize
+        case["initial"] = [float(x).hex() for x in initial]
+        case["search"] = search
     return case
 
 
@@ -165,6 +191,28 @@ def main():
         gam.append({"K": k, "alpha": a, "probs": [r[0] for r in rows], "multipliers": [r[1] for r in rows]})
     json.dump({"generator": "tests/golden/make_golden.py", "matrices": mats, "gamma": gam},
               open(os.path.join(HERE, "ref_matrices.json"), "w"))
+
+    # -- Nelder-Mead: analytic objectives and likelihood searches ------------
+    analytic = []
+    for fn, it, x0 in [("rosen", 300, [-1.2, 1.0]), ("wall", 300, [0.99, 0.5]), ("bowl", 300, [0.0, 0.0, 0.0]),
+                       ("product", 5, [5.0, 3.0]), ("rosen", 40, [0.5, 0.5, 0.5, 0.5])]:
+        r = parse_search(run(["nm", fn, str(it), ",".join(repr(x) for x in x0)]))
+        analytic.append({"objective": fn, "max_iterations": it, "initial": x0, **r})
+    searches = []
+    searches.append(make_case("opt_lambda_base_12taxa", w0.tree, w0.families, [0.003], optimize="lambda",
+                              initial=[0.003], note="lambda_optimizer, config-0 shape"))
+    searches.append(make_case("opt_two_lambdas_base_32taxa", w2.tree, f2, [0.0015, 0.006], lam_idx=w2.lambda_of_node,
+                              optimize="lambda", initial=[0.002, 0.004], note="two lambdas"))
+    searches.append(make_case("opt_lambda_epsilon_32taxa", w2.tree, f2, [0.0015, 0.006], lam_idx=w2.lambda_of_node,
+                              err=err, optimize="lambda_epsilon", initial=[0.0015, 0.006, 0.05],
+                              note="lambda_epsilon_optimizer, one epsilon"))
+    f1 = FamilySet(w1.families.ids[:60], w1.families.counts[:60])
+    searches.append(make_case("opt_lambda_alpha_gamma_24taxa", w1.tree, f1, [0.002], model="gamma", alpha=0.5, K=4,
+                              optimize="lambda_alpha", initial=[0.002, 0.5], note="gamma_lambda_optimizer, K=4"))
+    searches.append(make_case("opt_alpha_gamma_24taxa", w1.tree, f1, [0.0025], model="gamma", alpha=0.5, K=4,
+                              optimize="alpha", initial=[0.8], note="gamma_optimizer, lambda fixed"))
+    json.dump({"generator": "tests/golden/make_golden.py", "analytic": analytic, "searches": searches},
+              open(os.path.join(HERE, "ref_optimizer.json"), "w"), indent=1)
 
 
 if __name__ == "__main__":

@@ -60,33 +60,39 @@ def prior_from_spec(spec: str, R: int) -> RootPrior:
     raise ValueError(spec)
 
 
+def case_from_json(c) -> Case:
+    tree = parse_newick(c["newick"])
+    assert tree.leaf_names == c["taxa"]
+    lam_idx = [0] * tree.n_nodes
+    kind = 0
+    if c["lambda_newick"]:
+        lam_idx = lambda_index_of_nodes(tree, parse_newick(c["lambda_newick"], lambda_tree=True))
+        kind = 1
+    err = None
+    if c["error_model"]:
+        err = ErrorModel.parse(c["error_model"]).table()
+    prior = prior_from_spec(c["prior"], c["R"]).vector()
+    model = 1 if c["model"] == "gamma" else 0
+    cat = None
+    if c["expected"]["cat"] is not None:
+        cat = c["expected"]["cat"]
+    return Case(
+        name=c["name"], tree=tree, lambda_of_node=lam_idx, lambda_kind=kind,
+        counts=np.asarray(c["counts"], dtype=np.int32).reshape(len(c["ids"]), len(c["taxa"])),
+        lambdas=[hexf(x) for x in c["lambdas"]], model=model,
+        multipliers=[hexf(x) for x in c["multipliers"]] if c["multipliers"] else [1.0],
+        cat_probs=[hexf(x) for x in c["cat_probs"]] if c["cat_probs"] else [1.0],
+        prior=prior, err_rows=err, S=c["S"], R=c["R"],
+        total=float.fromhex(c["expected"]["total_hex"]) if "x" in c["expected"]["total_hex"]
+        else float(c["expected"]["total_hex"]),
+        fam_lnl=[hexf(x) if x is not None else None for x in c["expected"]["fam_lnl_hex"]],
+        cat=cat)
+
+
 def load_cases() -> List[Case]:
-    out = []
-    for c in load_json("ref_cases.json")["cases"]:
-        tree = parse_newick(c["newick"])
-        assert tree.leaf_names == c["taxa"]
-        lam_idx = [0] * tree.n_nodes
-        kind = 0
-        if c["lambda_newick"]:
-            lam_idx = lambda_index_of_nodes(tree, parse_newick(c["lambda_newick"], lambda_tree=True))
-            kind = 1
-        err = None
-        if c["error_model"]:
-            err = ErrorModel.parse(c["error_model"]).table()
-        prior = prior_from_spec(c["prior"], c["R"]).vector()
-        model = 1 if c["model"] == "gamma" else 0
-        cat = None
-        if c["expected"]["cat"] is not None:
-            cat = c["expected"]["cat"]
-        out.append(Case(
-            name=c["name"], tree=tree, lambda_of_node=lam_idx, lambda_kind=kind,
-            counts=np.asarray(c["counts"], dtype=np.int32).reshape(len(c["ids"]), len(c["taxa"])),
-            lambdas=[hexf(x) for x in c["lambdas"]], model=model,
-            multipliers=[hexf(x) for x in c["multipliers"]] if c["multipliers"] else [1.0],
-            cat_probs=[hexf(x) for x in c["cat_probs"]] if c["cat_probs"] else [1.0],
-            prior=prior, err_rows=err, S=c["S"], R=c["R"],
-            total=float.fromhex(c["expected"]["total_hex"]) if "x" in c["expected"]["total_hex"]
-            else float(c["expected"]["total_hex"]),
-            fam_lnl=[hexf(x) if x is not None else None for x in c["expected"]["fam_lnl_hex"]],
-            cat=cat))
-    return out
+    return [case_from_json(c) for c in load_json("ref_cases.json")["cases"]]
+
+
+def load_searches():
+    """(raw json, Case) per likelihood search of ref_optimizer.json."""
+    return [(c, case_from_json(c)) for c in load_json("ref_optimizer.json")["searches"]]
