@@ -451,7 +451,10 @@ void schedule(cafe_ctx* C, PendingJobs& P, const MatKey& k) {
 struct ScoreInfo {
     int64_t F = 0;
     int K = 1;
-    bool rejected = false;
+    int B = 1;                          // candidates scored together
+    std::vector<char> cand_rejected;    // per candidate: +inf without pruning
+    std::vector<int> cand_status;       // per candidate rejection status
+    bool rejected = false;              // every candidate rejected
     int reject_status = CAFE_OK;
     bool scaled = false;
     size_t footprint = 0;
@@ -499,6 +502,55 @@ int cached_map(cafe_ctx* C, Workspace& ws, int slot, CUtensorMap* out, const flo
         mc.cols = cols;
     }
     *out = mc.map;
+    return CAFE_OK;
+}
+
+// Category probabilities of every (candidate, category) index, and the list
+// of indices that are pruned (candidates not rejected), staged to the device.
+int stage_cat_probs(cafe_ctx* C, Workspace& ws, const cafe_request* R, int K, int NB) {
+    const int CT = NB * K;
+    CK(ws.h_catp.reserve((size_t)CT * sizeof(double)), "cat probs");
+    CK(ws.catp.reserve((size_t)CT * sizeof(double)), "cat probs");
+    double* h = ws.h_catp.as<double>();
+    for (int b = 0; b < NB; ++b)
+        for (int k = 0; k < K; ++k) h[b * K + k] = R[b].model == CAFE_MODEL_GAMMA ? R[b].cat_probs[k] : 1.0;
+    CK(cudaMemcpyAsync(ws.catp.p, h, (size_t)CT * sizeof(double), cudaMemcpyHostToDevice, ws.stream), "cat probs");
+    return CAFE_OK;
+}
+
+// Per-family lnL and the total of every candidate, then +inf / NaN for
+// the candidates rejected before pruning.
+int finish_batch(cafe_ctx* C, Workspace& ws, const ScoreInfo* info, bool gamma, bool scaled, const int64_t* d_ref,
+                 const int32_t* d_status, double* d_fam, double* d_total) {
+    const int64_t F = info->F;
+    const int NB = info->B;
+    FinishArgs fa{};
+    fa.F = F;
+    fa.K = info->K;
+    fa.n_cand = NB;
+    fa.model = gamma ? 1 : 0;
+    fa.scaled = scaled ? 1 : 0;
+    fa.cat = ws.cat.as<double>();
+    fa.ref = d_ref;
+    fa.family_lnl = d_fam;
+    fa.total = d_total;
+    fa.n_failed = ws.nfail.as<int32_t>();
+    const size_t parts = (size_t)finish_parts(F) * NB;
+    CK(ws.parts.reserve(parts * 2 * (sizeof(double) + sizeof(int32_t))), "finish");
+    fa.part_sum = ws.parts.as<double>();
+    fa.part_cnt = reinterpret_cast<int32_t*>(fa.part_sum + 2 * parts);
+    fa.status = d_status;
+    const bool prof = (&ws == C->ws[0].get());
+    cudaEvent_t ev;
+    if (prof) C->prof.begin(2, ws.stream, &ev);
+    CK(launch_finish(fa, ws.stream), "finish");
+    if (prof) C->prof.end(2, ws.stream, ev);
+    for (int b = 0; b < NB; ++b) {
+        if (!info->cand_rejected[b]) continue;
+        if (d_total) CK(launch_fill(d_total + b, 1, INFINITY, ws.stream), "fill");
+        if (d_fam && F) CK(launch_fill(d_fam + (size_t)b * F, F, NAN, ws.stream), "fill");
+        CK(launch_fill_i32(ws.nfail.as<int32_t>() + b, 1, 0, ws.stream), "fill");
+    }
     return CAFE_OK;
 }
 
@@ -563,9 +615,11 @@ double tile_flops(const TreeHost& T, const PruneTile& t, bool err) {
 // MIXED_TF32X3: tensor-core tiles for bins <= 256 states, FP64 tiles for
 // wider bins and for families the tensor-core pass flags. Caller holds C->mu;
 // hm holds the FP64 matrix of every (category, node).
-int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T, FamSet& S, int K, double** hm,
-                  double* d_fam, double* d_total, ScoreInfo* info) {
+int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T, FamSet& S, int K, int CT,
+                  const std::vector<int32_t>& active, double** hm, double* d_fam, double* d_total, ScoreInfo* info) {
     const bool gamma = R->model == CAFE_MODEL_GAMMA;
+    const int KC = K;    // categories per candidate
+    K = CT;              // below, K counts the combined (candidate, category) indices
     const int64_t F = S.F;
     const BinPlan& B = S.bins;
     const int msize = B.W_max;
@@ -596,17 +650,8 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
     const int n_mat = (int)jobs.size();
 
     // category probabilities (device) for both kernels
-    if (gamma) {
-        CK(ws.h_catp.reserve((size_t)K * sizeof(double)), "cat probs");
-        CK(ws.catp.reserve((size_t)K * sizeof(double)), "cat probs");
-        std::memcpy(ws.h_catp.p, R->cat_probs, K * sizeof(double));
-        CK(cudaMemcpyAsync(ws.catp.p, ws.h_catp.p, K * sizeof(double), cudaMemcpyHostToDevice, ws.stream), "cat probs");
-    } else {
-        CK(ws.h_catp.reserve(sizeof(double)), "cat probs");
-        CK(ws.catp.reserve(sizeof(double)), "cat probs");
-        *ws.h_catp.as<double>() = 1.0;
-        CK(cudaMemcpyAsync(ws.catp.p, ws.h_catp.p, sizeof(double), cudaMemcpyHostToDevice, ws.stream), "cat probs");
-    }
+    int rc0 = stage_cat_probs(C, ws, R, KC, CT / KC);
+    if (rc0) return rc0;
     CK(ws.mats.reserve((size_t)K * T.n_nodes * sizeof(double*)), "mats");
     CK(cudaMemcpyAsync(ws.mats.p, hm, (size_t)K * T.n_nodes * sizeof(double*), cudaMemcpyHostToDevice, ws.stream), "mats");
     CK(ws.cat.reserve((size_t)std::max<int64_t>(F, 1) * K * sizeof(double)), "category buffer");
@@ -618,7 +663,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
 
     // tiles: 128 families (tensor cores) or 32 families (FP64, wide bins)
     std::vector<PruneTile> tc_tiles, wide_tiles;
-    for (int k = 0; k < K; ++k)
+    for (int k : active)
         for (size_t b = 0; b < B.widths.size(); ++b) {
             const int w = B.widths[b];
             const int step = w <= 256 ? 128 : 32;
@@ -797,8 +842,9 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             fp.bin_count[fp.n_bins] = B.bin_count[b];
             fp.n_bins++;
         }
-        fp.K = K;
-        const int64_t max_tiles = (int64_t)K * (F / 32 + fp.n_bins + 1);
+        fp.cats = ws.catids.as<int32_t>();
+        fp.n_cats = (int)active.size();
+        const int64_t max_tiles = (int64_t)active.size() * (F / 32 + fp.n_bins + 1);
         CK(ws.fb_perm.reserve((size_t)std::max<int64_t>(F, 1) * sizeof(int64_t)), "fallback");
         CK(ws.tiles_fb.reserve((size_t)max_tiles * sizeof(PruneTile)), "fallback");
         fp.fb_perm = ws.fb_perm.as<int64_t>();
@@ -841,30 +887,18 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         info->d_tail = d_status;     // [status, fallback families, fallback tiles]
     }
 
-    FinishArgs fa{};
-    fa.F = F;
-    fa.K = K;
-    fa.model = gamma ? 1 : 0;
-    fa.scaled = 1;
-    fa.cat = ws.cat.as<double>();
-    fa.ref = nullptr;
-    fa.family_lnl = d_fam;
-    fa.total = d_total;
-    fa.n_failed = ws.nfail.as<int32_t>();
-    CK(ws.parts.reserve((size_t)finish_parts(F) * 2 * (sizeof(double) + sizeof(int32_t))), "finish");
-    fa.part_sum = ws.parts.as<double>();
-    fa.part_cnt = reinterpret_cast<int32_t*>(fa.part_sum + 2 * finish_parts(F));
-    fa.status = tc_tiles.empty() ? nullptr : d_status;
-    if (prof) C->prof.begin(2, ws.stream, &ev);
-    CK(launch_finish(fa, ws.stream), "finish");
-    if (prof) C->prof.end(2, ws.stream, ev);
-    return CAFE_OK;
+    return finish_batch(C, ws, info, gamma, true, nullptr, tc_tiles.empty() ? nullptr : d_status, d_fam, d_total);
 }
 
-// Enqueue one evaluation on ws.stream. Caller holds C->mu.
-int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_fam, double* d_total,
+// Enqueue the evaluation of NB candidate requests (same tree, family set,
+// model, categories and precision; own lambdas, multipliers and category
+// probabilities) on ws.stream. Candidate b, category k is pruned as the
+// combined category b * K + k. d_fam is [NB][F], d_total [NB]. Caller
+// holds C->mu.
+int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, double* d_fam, double* d_total,
                   ScoreInfo* info) {
-    if (!R) return fail(C, CAFE_ERR_INVALID, "null request");
+    if (!Rs || NB < 1) return fail(C, CAFE_ERR_INVALID, "null request");
+    const cafe_request* R = Rs;
     // pinned staging buffers of this workspace are rewritten below: the
     // previous request's copies out of them must have run
     if (ws.staged) {
@@ -878,44 +912,74 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_f
     TreeHost& T = *ti->second;
     FamSet& S = *si->second;
     if (S.tree_id != R->tree_id) return fail(C, CAFE_ERR_INVALID, "family set %d belongs to tree %d", R->set_id, S.tree_id);
-    if (R->n_lambdas < 1 || !R->lambdas) return fail(C, CAFE_ERR_INVALID, "no lambdas");
-    for (int v = 0; v < T.n_nodes; ++v)
-        if (T.parent[v] >= 0 && (T.lambda_index[v] < 0 || T.lambda_index[v] >= R->n_lambdas))
-            return fail(C, CAFE_ERR_INVALID, "lambda index %d out of range at node %d", T.lambda_index[v], v);
     const bool gamma = R->model == CAFE_MODEL_GAMMA;
     if (R->model != CAFE_MODEL_BASE && !gamma) return fail(C, CAFE_ERR_INVALID, "bad model %d", R->model);
     const int K = gamma ? R->n_categories : 1;
-    if (gamma && (K < 1 || !R->multipliers || !R->cat_probs)) return fail(C, CAFE_ERR_INVALID, "gamma needs K >= 1");
     if (C->prior.empty()) return fail(C, CAFE_ERR_INVALID, "no prior set (cafe_prior_set)");
     if (R->use_error_model && C->err_rows == 0) return fail(C, CAFE_ERR_INVALID, "no error model set");
     if (R->precision != CAFE_PREC_FP64_REF && R->precision != CAFE_PREC_FP64_BINNED &&
         R->precision != CAFE_PREC_MIXED_TF32X3)
         return fail(C, CAFE_ERR_INVALID, "bad precision %d", R->precision);
+    for (int b = 0; b < NB; ++b) {
+        const cafe_request& Q = Rs[b];
+        if (Q.tree_id != R->tree_id || Q.set_id != R->set_id || Q.model != R->model ||
+            Q.precision != R->precision || Q.use_error_model != R->use_error_model ||
+            Q.lambda_kind != R->lambda_kind || Q.dedupe != R->dedupe ||
+            (R->precision == CAFE_PREC_FP64_REF &&
+             (Q.max_family_size != R->max_family_size || Q.max_root_family_size != R->max_root_family_size)) ||
+            (gamma && Q.n_categories != K))
+            return fail(C, CAFE_ERR_INVALID, "batched request %d differs from request 0 in more than its parameters", b);
+        if (Q.n_lambdas < 1 || !Q.lambdas) return fail(C, CAFE_ERR_INVALID, "request %d has no lambdas", b);
+        for (int v = 0; v < T.n_nodes; ++v)
+            if (T.parent[v] >= 0 && (T.lambda_index[v] < 0 || T.lambda_index[v] >= Q.n_lambdas))
+                return fail(C, CAFE_ERR_INVALID, "lambda index %d out of range at node %d", T.lambda_index[v], v);
+        if (gamma && (K < 1 || !Q.multipliers || !Q.cat_probs))
+            return fail(C, CAFE_ERR_INVALID, "gamma needs K >= 1 with multipliers and probabilities");
+    }
     const int64_t F = S.F;
     info->F = F;
     info->K = K;
+    info->B = NB;
+    info->cand_rejected.assign(NB, 0);
+    info->cand_status.assign(NB, CAFE_OK);
 
-    // lambda::is_valid (src/lambda.h:58-60, src/lambda.cpp:172-175)
-    bool valid = true;
-    double largest = R->lambdas[0];
-    for (int i = 0; i < R->n_lambdas; ++i) {
-        const double l = R->lambdas[i];
-        if (R->lambda_kind == CAFE_LAMBDA_SINGLE ? !(l > 0) : (l < 0)) valid = false;
-        largest = std::max(largest, l);
+    // lambda::is_valid (src/lambda.h:58-60, src/lambda.cpp:172-175) and
+    // gamma_model::can_infer (src/gamma_core.cpp:123-141), per candidate
+    int n_rej = 0;
+    for (int b = 0; b < NB; ++b) {
+        const cafe_request& Q = Rs[b];
+        bool valid = true;
+        double largest = Q.lambdas[0];
+        for (int i = 0; i < Q.n_lambdas; ++i) {
+            const double l = Q.lambdas[i];
+            if (Q.lambda_kind == CAFE_LAMBDA_SINGLE ? !(l > 0) : (l < 0)) valid = false;
+            largest = std::max(largest, l);
+        }
+        bool reject = !valid;
+        if (!reject && gamma && T.longest_branch > 0) {
+            const double al = largest * T.longest_branch / (1 + largest * T.longest_branch);
+            if ((1 - 2 * al) < 0) reject = true;
+        }
+        if (reject) {
+            info->cand_rejected[b] = 1;
+            info->cand_status[b] = valid ? CAFE_ERR_SATURATED : CAFE_OK;
+            n_rej++;
+        }
     }
-    bool reject = !valid;
-    // gamma_model::can_infer (src/gamma_core.cpp:123-141)
-    if (!reject && gamma && T.longest_branch > 0) {
-        const double a = largest * T.longest_branch / (1 + largest * T.longest_branch);
-        if ((1 - 2 * a) < 0) reject = true;
-    }
-    if (reject) {
+    CK(ws.nfail.reserve((size_t)NB * sizeof(int32_t)), "fail counter");
+    if (n_rej == NB) {
         info->rejected = true;
-        info->reject_status = valid ? CAFE_ERR_SATURATED : CAFE_OK;
-        if (d_total) CK(launch_fill(d_total, 1, INFINITY, ws.stream), "fill");
-        if (d_fam && F) CK(launch_fill(d_fam, F, NAN, ws.stream), "fill");
+        info->reject_status = info->cand_status[0];
+        if (d_total) CK(launch_fill(d_total, NB, INFINITY, ws.stream), "fill");
+        if (d_fam && F) CK(launch_fill(d_fam, (int64_t)NB * F, NAN, ws.stream), "fill");
+        CK(launch_fill_i32(ws.nfail.as<int32_t>(), NB, 0, ws.stream), "fill");
         return CAFE_OK;
     }
+    const int CT = NB * K;
+    std::vector<int32_t> active;
+    for (int b = 0; b < NB; ++b)
+        if (!info->cand_rejected[b])
+            for (int k = 0; k < K; ++k) active.push_back(b * K + k);
 
     const bool ref_mode = R->precision == CAFE_PREC_FP64_REF;
     const bool scaled = !ref_mode;
@@ -935,48 +999,56 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_f
         W = S.bins.W_max;
     }
 
-    // matrices for every (category, non-root node)
+    // matrices for every (candidate, category, non-root node)
     PendingJobs P;
-    std::vector<MatKey> node_key((size_t)K * T.n_nodes);
-    for (int k = 0; k < K; ++k) {
-        const double m = gamma ? R->multipliers[k] : 1.0;
+    std::vector<MatKey> node_key((size_t)CT * T.n_nodes);
+    std::vector<MatKey> wait_keys;
+    for (int c : active) {
+        const cafe_request& Q = Rs[c / K];
+        const double m = gamma ? Q.multipliers[c % K] : 1.0;
         for (int v = 0; v < T.n_nodes; ++v) {
             if (T.parent[v] < 0) continue;
-            const double lam = R->lambdas[T.lambda_index[v]] * m;
+            const double lam = Q.lambdas[T.lambda_index[v]] * m;
             const MatKey key = make_key(msize, lam, T.branch_length[v]);
-            node_key[(size_t)k * T.n_nodes + v] = key;
+            node_key[(size_t)c * T.n_nodes + v] = key;
+            wait_keys.push_back(key);
             schedule(C, P, key);
         }
     }
     int rc = cache_build(C, ws, P);
     if (rc) return rc;
-    rc = cache_wait_ready(C, ws, node_key);
+    rc = cache_wait_ready(C, ws, wait_keys);
     if (rc) return rc;
-    CK(ws.h_mats.reserve((size_t)K * T.n_nodes * sizeof(double*)), "mats");
-    CK(ws.mats.reserve((size_t)K * T.n_nodes * sizeof(double*)), "mats");
+    CK(ws.h_mats.reserve((size_t)CT * T.n_nodes * sizeof(double*)), "mats");
+    CK(ws.mats.reserve((size_t)CT * T.n_nodes * sizeof(double*)), "mats");
     double** hm = ws.h_mats.as<double*>();
-    for (int k = 0; k < K; ++k)
+    std::fill(hm, hm + (size_t)CT * T.n_nodes, nullptr);
+    for (int c : active)
         for (int v = 0; v < T.n_nodes; ++v)
-            hm[(size_t)k * T.n_nodes + v] = T.parent[v] < 0 ? nullptr : cache_lookup(C, node_key[(size_t)k * T.n_nodes + v]);
+            if (T.parent[v] >= 0) hm[(size_t)c * T.n_nodes + v] = cache_lookup(C, node_key[(size_t)c * T.n_nodes + v]);
+    CK(ws.cat.reserve((size_t)std::max<int64_t>(F, 1) * CT * sizeof(double)), "category buffer");
     if (R->precision == CAFE_PREC_MIXED_TF32X3) {
-        // saturated keys (1 - 2a < 0) and wide polytomies stay on the FP64 path
-        bool to_fp64 = false;
-        for (int k = 0; k < K && !to_fp64; ++k)
+        // saturated keys (1 - 2a < 0) and polytomies stay on the FP64 path
+        bool to_fp64 = T.max_children > 2;
+        for (int c : active) {
+            if (to_fp64) break;
             for (int v = 0; v < T.n_nodes; ++v)
                 if (T.parent[v] >= 0) {
-                    const MatKey& key = node_key[(size_t)k * T.n_nodes + v];
+                    const MatKey& key = node_key[(size_t)c * T.n_nodes + v];
                     const double lq = (double)key.lq / 1000000000.0, tq = (double)key.tq / 1000.0;
                     const double al = lq * tq / (1 + lq * tq), co = 1 - 2 * al;
                     if (!(co > 0 && co != 1)) to_fp64 = true;
                 }
-        int max_int = 0;
-        for (int v = 0; v < T.n_nodes; ++v) {
-            int ni = 0;
-            for (int c : T.children[v]) ni += !T.children[c].empty();
-            max_int = std::max(max_int, ni);
         }
-        if (T.max_children > 2) to_fp64 = true;   // polytomies stay on FP64
-        if (!to_fp64) return enqueue_mixed(C, ws, R, T, S, K, hm, d_fam, d_total, info);
+        if (!to_fp64) {
+            CK(ws.catids.reserve(active.size() * sizeof(int32_t)), "categories");
+            CK(ws.h_catids.reserve(active.size() * sizeof(int32_t)), "categories");
+            std::memcpy(ws.h_catids.p, active.data(), active.size() * sizeof(int32_t));
+            CK(cudaMemcpyAsync(ws.catids.p, ws.h_catids.p, active.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                               ws.stream),
+               "categories");
+            return enqueue_mixed(C, ws, Rs, T, S, K, CT, active, hm, d_fam, d_total, info);
+        }
         info->n_fallback = F;
     }
 
@@ -990,12 +1062,12 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_f
     if (ref_mode) {
         const int64_t nf = dedupe ? (int64_t)S.unique.size() : F;
         d_perm = dedupe ? S.d_unique.as<int64_t>() : S.d_identity.as<int64_t>();
-        for (int k = 0; k < K; ++k)
+        for (int c : active)
             for (int64_t i = 0; i < nf; i += TFm) {
                 PruneTile t{};
                 t.first = (int)i;
                 t.count = (int)std::min<int64_t>(TFm, nf - i);
-                t.k = k;
+                t.k = c;
                 t.S = Sg;
                 t.R = Rg;
                 tiles.push_back(t);
@@ -1003,13 +1075,13 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_f
     } else {
         d_perm = S.bins.d_perm.as<int64_t>();
         d_famR = S.bins.d_famR.as<int32_t>();
-        for (int k = 0; k < K; ++k)
+        for (int c : active)
             for (size_t b = 0; b < S.bins.widths.size(); ++b)
                 for (int64_t i = 0; i < S.bins.bin_count[b]; i += TFm) {
                     PruneTile t{};
                     t.first = (int)(S.bins.bin_first[b] + i);
                     t.count = (int)std::min<int64_t>(TFm, S.bins.bin_count[b] - i);
-                    t.k = k;
+                    t.k = c;
                     t.S = S.bins.widths[b] - 1;
                     t.R = S.bins.widths[b] - 1;
                     tiles.push_back(t);
@@ -1023,15 +1095,15 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_f
     const int n_ctas = std::max(1, std::min(n_tiles, C->n_ctas));
     const int64_t per_cta = (int64_t)T.n_slots * W * TFm;
     CK(ws.scratch.reserve((size_t)n_ctas * per_cta * sizeof(double)), "scratch");
-    CK(ws.cat.reserve((size_t)std::max<int64_t>(F, 1) * K * sizeof(double)), "category buffer");
-    CK(ws.nfail.reserve(sizeof(int32_t)), "fail counter");
-    info->footprint = (size_t)n_ctas * per_cta * sizeof(double) + (size_t)F * K * sizeof(double);
+    info->footprint = (size_t)n_ctas * per_cta * sizeof(double) + (size_t)F * CT * sizeof(double);
 
     CK(cudaMemcpyAsync(ws.tiles.p, ws.h_tiles.p, n_tiles * sizeof(PruneTile), cudaMemcpyHostToDevice, ws.stream),
        "tiles");
-    CK(cudaMemcpyAsync(ws.mats.p, hm, (size_t)K * T.n_nodes * sizeof(double*), cudaMemcpyHostToDevice, ws.stream),
+    CK(cudaMemcpyAsync(ws.mats.p, hm, (size_t)CT * T.n_nodes * sizeof(double*), cudaMemcpyHostToDevice, ws.stream),
        "mats");
-    if (gamma && !scaled) CK(launch_fill(ws.cat.as<double>(), F * K, 0.0, ws.stream), "fill");
+    if (gamma && !scaled) CK(launch_fill(ws.cat.as<double>(), F * CT, 0.0, ws.stream), "fill");
+    rc = stage_cat_probs(C, ws, Rs, K, NB);
+    if (rc) return rc;
 
     Prune64Args a{};
     a.plan = T.plan;
@@ -1052,148 +1124,119 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* R, double* d_f
     a.scaled = scaled ? 1 : 0;
     a.model = gamma ? 1 : 0;
     a.out = ws.cat.as<double>();
-    a.K = K;
-    a.cat_probs = nullptr;
-    if (gamma) {
-        CK(ws.h_catp.reserve((size_t)K * sizeof(double)), "cat probs");
-        CK(ws.catp.reserve((size_t)K * sizeof(double)), "cat probs");
-        std::memcpy(ws.h_catp.p, R->cat_probs, K * sizeof(double));
-        CK(cudaMemcpyAsync(ws.catp.p, ws.h_catp.p, K * sizeof(double), cudaMemcpyHostToDevice, ws.stream), "cat probs");
-        a.cat_probs = ws.catp.as<double>();
-    }
+    a.K = CT;
+    a.cat_probs = ws.catp.as<double>();
     a.tile_families = TFm;
     a.W = W;
     const bool prof = (&ws == C->ws[0].get());
     cudaEvent_t ev;
     if (prof) {
         C->prof.begin(1, ws.stream, &ev);
-        // algorithmic flops of this launch
-        double fl = 0;
-        for (const PruneTile& t : tiles) {
-            double per = 0;
-            for (size_t ii = 0; ii < T.internal.size(); ++ii) {
-                const int v = T.internal[ii];
-                const int rows = (v == T.root) ? t.R : t.S + 1;
-                const int nch = T.cstart[ii + 1] - T.cstart[ii];
-                for (int ci = T.cstart[ii]; ci < T.cstart[ii + 1]; ++ci)
-                    if (!T.children[T.child[ci]].empty()) per += 2.0 * rows * (t.S + 1);
-                    else if (R->use_error_model) per += 6.0 * rows;
-                per += (double)(nch - 1) * rows;
-            }
-            fl += per * t.count;
-        }
-        C->prof.acc.prune_flops += fl;
+        for (const PruneTile& t : tiles) C->prof.acc.prune_flops += tile_flops(T, t, R->use_error_model);
     }
     CK(launch_prune64(a, n_ctas, ws.stream), "prune");
     if (prof) C->prof.end(1, ws.stream, ev);
-
-    FinishArgs fa{};
-    fa.F = F;
-    fa.K = K;
-    fa.model = gamma ? 1 : 0;
-    fa.scaled = scaled ? 1 : 0;
-    fa.cat = ws.cat.as<double>();
-    fa.ref = dedupe ? S.d_ref.as<int64_t>() : nullptr;
-    fa.family_lnl = d_fam;
-    fa.total = d_total;
-    fa.n_failed = ws.nfail.as<int32_t>();
-    CK(ws.parts.reserve((size_t)finish_parts(F) * 2 * (sizeof(double) + sizeof(int32_t))), "finish");
-    fa.part_sum = ws.parts.as<double>();
-    fa.part_cnt = reinterpret_cast<int32_t*>(fa.part_sum + 2 * finish_parts(F));
-    fa.status = nullptr;
-    if (prof) C->prof.begin(2, ws.stream, &ev);
-    CK(launch_finish(fa, ws.stream), "finish");
-    if (prof) C->prof.end(2, ws.stream, ev);
-    return CAFE_OK;
+    return finish_batch(C, ws, info, gamma, scaled, dedupe ? S.d_ref.as<int64_t>() : nullptr, nullptr, d_fam, d_total);
 }
 
-// Phase 1 of a host-visible score: enqueue the evaluation and the copies
-// back into pinned staging (caller holds C->mu).
-int score_enqueue(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_result* res, ScoreInfo* info) {
+// Phase 1 of a host-visible score of NB batched candidates: enqueue the
+// evaluation and the copies back into pinned staging (caller holds C->mu).
+// Host staging: totals [NB], fail counts [NB], family lnL [NB][F], then
+// category values [F][NB * K] when any result asks for them.
+int score_enqueue(cafe_ctx* C, Workspace& ws, const cafe_request* R, int NB, cafe_result* res, ScoreInfo* info) {
     auto si = C->sets.find(R ? R->set_id : -1);
     if (si == C->sets.end()) return fail(C, CAFE_ERR_NOT_FOUND, "unknown family set");
+    if (NB < 1) return fail(C, CAFE_ERR_INVALID, "empty batch");
     const int64_t F = si->second->F;
-    CK(ws.fam_lnl.reserve(std::max<int64_t>(F, 1) * sizeof(double)), "family buffer");
-    CK(ws.total.reserve(sizeof(double)), "total");
+    CK(ws.fam_lnl.reserve((size_t)std::max<int64_t>(F, 1) * NB * sizeof(double)), "family buffer");
+    CK(ws.total.reserve((size_t)NB * sizeof(double)), "total");
     CK(cudaEventRecord(ws.ev_start, ws.stream), "event");
-    int rc = enqueue_score(C, ws, R, ws.fam_lnl.as<double>(), ws.total.as<double>(), info);
+    int rc = enqueue_score(C, ws, R, NB, ws.fam_lnl.as<double>(), ws.total.as<double>(), info);
     if (rc) return rc;
     CK(cudaEventRecord(ws.ev_staged, ws.stream), "event");
     ws.staged = true;
     CK(cudaEventRecord(ws.ev_stop, ws.stream), "event");
     const int K = info->K;
-    const size_t out_bytes = sizeof(double) + sizeof(int32_t) + (size_t)F * sizeof(double) +
-                             (res && res->category_lnl ? (size_t)F * K * sizeof(double) : 0);
+    bool any_cat = false;
+    for (int b = 0; b < NB && res; ++b) any_cat |= res[b].category_lnl != nullptr;
+    const size_t head = (size_t)NB * (sizeof(double) + sizeof(int32_t));
+    const size_t head8 = (head + 7) & ~(size_t)7;
+    const size_t out_bytes = head8 + (size_t)NB * F * sizeof(double) + (any_cat ? (size_t)F * NB * K * sizeof(double) : 0);
     CK(ws.h_out.reserve(out_bytes + 64), "host staging");
     CK(ws.h_tail.reserve(64), "host staging");
     if (info->d_tail)
         CK(cudaMemcpyAsync(ws.h_tail.p, info->d_tail, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, ws.stream), "d2h");
     char* h = static_cast<char*>(ws.h_out.p);
     double* h_total = reinterpret_cast<double*>(h);
-    int32_t* h_fail = reinterpret_cast<int32_t*>(h + 8);
-    double* h_fam = reinterpret_cast<double*>(h + 16);
-    double* h_cat = h_fam + F;
-    CK(cudaMemcpyAsync(h_total, ws.total.p, sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");
-    if (!info->rejected) CK(cudaMemcpyAsync(h_fail, ws.nfail.p, sizeof(int32_t), cudaMemcpyDeviceToHost, ws.stream), "d2h");
-    else *h_fail = 0;
-    if (F) CK(cudaMemcpyAsync(h_fam, ws.fam_lnl.p, F * sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");
-    const bool want_cat = res && res->category_lnl && !info->rejected;
-    if (want_cat && F)
-        CK(cudaMemcpyAsync(h_cat, ws.cat.p, (size_t)F * K * sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");
+    int32_t* h_fail = reinterpret_cast<int32_t*>(h + (size_t)NB * sizeof(double));
+    double* h_fam = reinterpret_cast<double*>(h + head8);
+    double* h_cat = h_fam + (size_t)NB * F;
+    CK(cudaMemcpyAsync(h_total, ws.total.p, (size_t)NB * sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");
+    CK(cudaMemcpyAsync(h_fail, ws.nfail.p, (size_t)NB * sizeof(int32_t), cudaMemcpyDeviceToHost, ws.stream), "d2h");
+    if (F) CK(cudaMemcpyAsync(h_fam, ws.fam_lnl.p, (size_t)NB * F * sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");
+    if (any_cat && F && !info->rejected)
+        CK(cudaMemcpyAsync(h_cat, ws.cat.p, (size_t)F * NB * K * sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");
     return CAFE_OK;
 }
 
-// Phase 2: wait for the stream and fill the result (no context lock needed:
-// the workspace belongs to the caller).
-int score_complete(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_result* res, const ScoreInfo& info) {
+// Phase 2: wait for the stream and fill the results (no context lock
+// needed: the workspace belongs to the caller).
+int score_complete(cafe_ctx* C, Workspace& ws, const cafe_request* R, int NB, cafe_result* res, const ScoreInfo& info) {
     CK(cudaStreamSynchronize(ws.stream), "score");
     if (!res) return CAFE_OK;
     const int64_t F = info.F;
     const int K = info.K;
+    const size_t head = (size_t)NB * (sizeof(double) + sizeof(int32_t));
+    const size_t head8 = (head + 7) & ~(size_t)7;
     char* h = static_cast<char*>(ws.h_out.p);
-    double* h_total = reinterpret_cast<double*>(h);
-    int32_t* h_fail = reinterpret_cast<int32_t*>(h + 8);
-    double* h_fam = reinterpret_cast<double*>(h + 16);
-    double* h_cat = h_fam + F;
-    const bool want_cat = res->category_lnl && !info.rejected;
+    const double* h_total = reinterpret_cast<const double*>(h);
+    const int32_t* h_fail = reinterpret_cast<const int32_t*>(h + (size_t)NB * sizeof(double));
+    const double* h_fam = reinterpret_cast<const double*>(h + head8);
+    const double* h_cat = h_fam + (size_t)NB * F;
     float ms = 0;
     cudaEventElapsedTime(&ms, ws.ev_start, ws.ev_stop);
-    res->device_ms = ms;
-    res->total_neg_lnl = *h_total;
-    res->n_failed = info.rejected ? 0 : *h_fail;
-    res->n_fallback = info.n_fallback;
+    int64_t n_fb = info.n_fallback;
     if (info.d_tail) {
         const int32_t* tail = ws.h_tail.as<int32_t>();
         if (tail[0]) return fail(C, CAFE_ERR_TIMEOUT, "tensor-core pruning gave up waiting (status %d)", tail[0]);
-        res->n_fallback = tail[1];
+        n_fb = tail[1];
     }
-    if (res->family_lnl && F) std::memcpy(res->family_lnl, h_fam, F * sizeof(double));
-    if (res->category_lnl && F) {
-        const bool gamma = R->model == CAFE_MODEL_GAMMA;
-        for (int64_t f = 0; f < F; ++f)
-            for (int k = 0; k < K; ++k) {
-                double v = NAN;
-                if (want_cat && gamma) {
-                    const double c = h_cat[f * K + k];
-                    v = info.scaled ? c : (c < 0 ? NAN : std::log(c));
-                } else if (want_cat) {
-                    v = h_fam[f];
+    const bool gamma = R->model == CAFE_MODEL_GAMMA;
+    for (int b = 0; b < NB; ++b) {
+        cafe_result& r = res[b];
+        const bool rej = info.cand_rejected.empty() ? info.rejected : info.cand_rejected[b] != 0;
+        r.device_ms = ms;
+        r.total_neg_lnl = h_total[b];
+        r.n_failed = rej ? 0 : h_fail[b];
+        r.n_fallback = n_fb;
+        if (r.family_lnl && F) std::memcpy(r.family_lnl, h_fam + (size_t)b * F, F * sizeof(double));
+        if (r.category_lnl && F) {
+            const bool want_cat = !rej;
+            for (int64_t f = 0; f < F; ++f)
+                for (int k = 0; k < K; ++k) {
+                    double v = NAN;
+                    if (want_cat && gamma) {
+                        const double c = h_cat[(size_t)f * NB * K + (size_t)b * K + k];
+                        v = info.scaled ? c : (c < 0 ? NAN : std::log(c));
+                    } else if (want_cat) {
+                        v = h_fam[(size_t)b * F + f];
+                    }
+                    r.category_lnl[f * K + k] = v;
                 }
-                res->category_lnl[f * K + k] = v;
-            }
+        }
+        if (rej) r.status = info.cand_status.empty() ? info.reject_status : info.cand_status[b];
+        else if (r.n_failed) r.status = CAFE_ERR_SATURATED;
+        else if (std::isinf(r.total_neg_lnl)) r.status = CAFE_ERR_UNDERFLOW;
+        else r.status = CAFE_OK;
     }
-    if (info.rejected) res->status = info.reject_status;
-    else if (res->n_failed) res->status = CAFE_ERR_SATURATED;
-    else if (std::isinf(res->total_neg_lnl)) res->status = CAFE_ERR_UNDERFLOW;
-    else res->status = CAFE_OK;
     return CAFE_OK;
 }
 
-int score_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_result* res) {
+int score_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, int NB, cafe_result* res) {
     ScoreInfo info;
-    int rc = score_enqueue(C, ws, R, res, &info);
+    int rc = score_enqueue(C, ws, R, NB, res, &info);
     if (rc) return rc;
-    return score_complete(C, ws, R, res, info);
+    return score_complete(C, ws, R, NB, res, info);
 }
 
 }  // namespace
@@ -1456,7 +1499,14 @@ int cafe_score(cafe_ctx* C, const cafe_request* req, cafe_result* res) {
     if (!C) return CAFE_ERR_INVALID;
     std::lock_guard<std::mutex> lk(C->mu);
     cudaSetDevice(C->device);
-    return score_sync(C, *C->ws[0], req, res);
+    return score_sync(C, *C->ws[0], req, 1, res);
+}
+
+int cafe_score_batch(cafe_ctx* C, const cafe_request* reqs, int n, cafe_result* results) {
+    if (!C || !reqs || n < 1 || !results) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    return score_sync(C, *C->ws[0], reqs, n, results);
 }
 
 int cafe_profile_enable(cafe_ctx* C, int enable) {
@@ -1493,7 +1543,8 @@ int cafe_score_device(cafe_ctx* C, const cafe_request* req, double* d_family_lnl
         CK(cudaEventRecord(ws.ev_start, user), "event");
         CK(cudaStreamWaitEvent(ws.stream, ws.ev_start, 0), "event");
     }
-    int rc = enqueue_score(C, ws, req, d_family_lnl ? d_family_lnl : ws.fam_lnl.as<double>(),
+    CK(ws.nfail.reserve(sizeof(int32_t)), "fail counter");
+    int rc = enqueue_score(C, ws, req, 1, d_family_lnl ? d_family_lnl : ws.fam_lnl.as<double>(),
                            d_total ? d_total : ws.total.as<double>(), &info);
     if (rc) return rc;
     CK(cudaEventRecord(ws.ev_staged, ws.stream), "event");
@@ -1543,9 +1594,9 @@ void server_loop(cafe_ctx* C, int wi) {
             // enqueue under the context lock; the GPU work of this request
             // then overlaps with requests running on the other streams
             std::unique_lock<std::mutex> lk(C->mu);
-            rc = score_enqueue(C, ws, &r->req, r->res, &info);
+            rc = score_enqueue(C, ws, &r->req, 1, r->res, &info);
         }
-        if (rc == CAFE_OK) rc = score_complete(C, ws, &r->req, r->res, info);
+        if (rc == CAFE_OK) rc = score_complete(C, ws, &r->req, 1, r->res, info);
         const double ms =
             std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - r->t_submit).count();
         {

@@ -80,8 +80,8 @@ struct Prune64Args {
     int64_t scratch_per_cta;
     int scaled;                  // per-node power-of-two rescale
     int model;                   // 0 base, 1 gamma
-    double* out;                 // base: [F] lnl; gamma: [F][K] category value
-    int K;
+    double* out;                 // [F][K]: base lnl, gamma category value
+    int K;                       // categories (all candidates' categories of a batch)
     const double* cat_probs;     // [K]
     int tile_families;           // families per tile (<= 32)
     int W;                       // max vector length over tiles (S + 1 or R)
@@ -92,16 +92,17 @@ cudaError_t launch_prune64(const Prune64Args& a, int n_ctas, cudaStream_t s);
 
 struct FinishArgs {
     int64_t F;
-    int K;
+    int K;                       // categories per candidate (1 for the base model)
+    int n_cand;                  // candidates scored together (>= 1)
     int model;
     int scaled;
-    const double* cat;           // gamma: [F][K] (linear if !scaled, log if scaled); base: [F] lnl
+    const double* cat;           // [F][n_cand][K]: gamma terms (linear if !scaled, log if scaled); base: lnl
     const int64_t* ref;          // dedupe reference per family, or null
-    double* family_lnl;          // [F] out
-    double* total;               // [1] out
-    int32_t* n_failed;           // [1] out
-    double* part_sum;            // [2 * finish_parts(F)] workspace
-    int32_t* part_cnt;           // [2 * finish_parts(F)] workspace
+    double* family_lnl;          // [n_cand][F] out, or null
+    double* total;               // [n_cand] out, or null
+    int32_t* n_failed;           // [n_cand] out
+    double* part_sum;            // [n_cand][2 * finish_parts(F)] workspace
+    int32_t* part_cnt;           // [n_cand][2 * finish_parts(F)] workspace
     const int32_t* status;       // optional: nonzero -> total = NaN
 };
 
@@ -168,7 +169,7 @@ size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages);
 
 // Device-side plan of the FP64 recompute of flagged families: compacts the
 // flagged families of each listed bin (in permutation order) into fb_perm
-// and writes 32-family tiles for every category; out_counts[0] = families,
+// and writes 32-family tiles for every listed category; out_counts[0] = families,
 // out_counts[1] = tiles.
 struct FallbackPlanArgs {
     const int32_t* flags;        // [F]
@@ -177,9 +178,10 @@ struct FallbackPlanArgs {
     int bin_width[16];
     int64_t bin_first[16];
     int64_t bin_count[16];
-    int K;
+    const int32_t* cats;         // [n_cats] category indices to recompute
+    int n_cats;
     int64_t* fb_perm;            // [F]
-    PruneTile* fb_tiles;         // [K * (F / 32 + n_bins)]
+    PruneTile* fb_tiles;         // [n_cats * (F / 32 + n_bins + 1)]
     int32_t* out_counts;         // [2]
     const int32_t* any_flag;     // optional: zero means no family is flagged
 };

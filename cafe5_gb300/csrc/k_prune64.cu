@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(NT) k_prune64(Prune64Args a) {
                     if (!got || x > b) b = x;
                     got = true;
                 }
-                a.out[f] = b + (double)s_exp[rs * TF + i] * 0.69314718055994530942;
+                a.out[(size_t)f * a.K + k] = b + (double)s_exp[rs * TF + i] * 0.69314718055994530942;
             }
         } else {
             double mx = 0.0;
@@ -248,22 +248,30 @@ __device__ __forceinline__ void neumaier_add(double& sum, double& comp, double x
 
 constexpr int kFinishThreads = 64;
 
+// Candidate b (blockIdx.y here, blockIdx.x in k_finish_total) reads
+// category k of family row r at cat[r * K * n_cand + b * K + k] and writes
+// family_lnl[b * F + f], total[b], n_failed[b].
 __global__ void __launch_bounds__(kFinishThreads) k_finish_fam(FinishArgs a) {
     __shared__ double ssum[kFinishThreads], scomp[kFinishThreads];
     __shared__ int sfail[kFinishThreads], sinf[kFinishThreads];
+    const int b = blockIdx.y;
+    const size_t stride = (size_t)a.K * a.n_cand;
+    const double* cat = a.cat + (size_t)b * a.K;
+    double* fam_out = a.family_lnl ? a.family_lnl + (size_t)b * a.F : nullptr;
     double sum = 0.0, comp = 0.0;
     int fail = 0, ninf = 0;   // ninf: families with lnL = -inf (log of an underflowed 0)
     for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < a.F; f += (int64_t)gridDim.x * blockDim.x) {
         const int64_t r = a.ref ? a.ref[f] : f;
+        const double* c_r = cat + (size_t)r * stride;
         double lnl;
         if (a.model == 0) {
-            lnl = a.cat[r];
+            lnl = c_r[0];
         } else if (!a.scaled) {
             // gamma_core.cpp:196-207: family likelihood = sum_k category terms
             double lh = 0.0;
             bool bad = false;
             for (int k = 0; k < a.K; ++k) {
-                const double c = a.cat[(size_t)r * a.K + k];
+                const double c = c_r[k];
                 if (c < 0) bad = true;
                 lh += c;
             }
@@ -273,17 +281,17 @@ __global__ void __launch_bounds__(kFinishThreads) k_finish_fam(FinishArgs a) {
             double mx = -INFINITY;
             bool bad = false;
             for (int k = 0; k < a.K; ++k) {
-                const double c = a.cat[(size_t)r * a.K + k];
+                const double c = c_r[k];
                 if (isnan(c)) bad = true;
                 else mx = c > mx ? c : mx;
             }
             double acc = 0.0;
             if (!bad && mx > -INFINITY)
-                for (int k = 0; k < a.K; ++k) acc += exp(a.cat[(size_t)r * a.K + k] - mx);
+                for (int k = 0; k < a.K; ++k) acc += exp(c_r[k] - mx);
             lnl = bad ? NAN : (mx > -INFINITY ? mx + log(acc) : -INFINITY);
             fail += bad;
         }
-        a.family_lnl[f] = lnl;
+        if (fam_out) fam_out[f] = lnl;
         if (isinf(lnl)) ninf++;
         else if (!isnan(lnl)) neumaier_add(sum, comp, lnl);
     }
@@ -301,10 +309,11 @@ __global__ void __launch_bounds__(kFinishThreads) k_finish_fam(FinishArgs a) {
             fl += sfail[i];
             ni += sinf[i];
         }
-        a.part_sum[2 * blockIdx.x] = s;
-        a.part_sum[2 * blockIdx.x + 1] = c;
-        a.part_cnt[2 * blockIdx.x] = fl;
-        a.part_cnt[2 * blockIdx.x + 1] = ni;
+        const size_t p = (size_t)b * gridDim.x + blockIdx.x;
+        a.part_sum[2 * p] = s;
+        a.part_sum[2 * p + 1] = c;
+        a.part_cnt[2 * p] = fl;
+        a.part_cnt[2 * p + 1] = ni;
     }
 }
 
@@ -313,13 +322,16 @@ __global__ void __launch_bounds__(256) k_finish_total(FinishArgs a, int n_parts)
     // sequential combine: deterministic for a given family count
     __shared__ double ssum[256], scomp[256];
     __shared__ int sfail[256], sinf[256];
+    const int b = blockIdx.x;
+    const double* ps = a.part_sum + (size_t)2 * b * n_parts;
+    const int32_t* pc = a.part_cnt + (size_t)2 * b * n_parts;
     double s = 0.0, c = 0.0;
     int fl = 0, ni = 0;
     for (int i = threadIdx.x; i < n_parts; i += blockDim.x) {
-        neumaier_add(s, c, a.part_sum[2 * i]);
-        c += a.part_sum[2 * i + 1];
-        fl += a.part_cnt[2 * i];
-        ni += a.part_cnt[2 * i + 1];
+        neumaier_add(s, c, ps[2 * i]);
+        c += ps[2 * i + 1];
+        fl += pc[2 * i];
+        ni += pc[2 * i + 1];
     }
     ssum[threadIdx.x] = s;
     scomp[threadIdx.x] = c;
@@ -337,12 +349,12 @@ __global__ void __launch_bounds__(256) k_finish_total(FinishArgs a, int n_parts)
         fl += sfail[i];
         ni += sinf[i];
     }
-    *a.n_failed = fl;
+    a.n_failed[b] = fl;
     // -sum lnL: +inf on gamma failure or when any family's lnL is -inf;
     // NaN if the tensor-core pass reported a time-out
     double t = (fl || ni) ? INFINITY : -(s + c);
     if (a.status && *a.status) t = NAN;
-    *a.total = t;
+    if (a.total) a.total[b] = t;
 }
 
 __global__ void k_fill(double* p, int64_t n, double v) {
@@ -381,8 +393,11 @@ int finish_parts(int64_t F) {
 
 cudaError_t launch_finish(const FinishArgs& a, cudaStream_t s) {
     const int parts = finish_parts(a.F);
-    k_finish_fam<<<parts, kFinishThreads, 0, s>>>(a);
-    k_finish_total<<<1, 256, 0, s>>>(a, parts);
+    const int nc = a.n_cand > 0 ? a.n_cand : 1;
+    FinishArgs b = a;
+    b.n_cand = nc;
+    k_finish_fam<<<dim3(parts, nc), kFinishThreads, 0, s>>>(b);
+    k_finish_total<<<nc, 256, 0, s>>>(b, parts);
     return cudaGetLastError();
 }
 

@@ -673,8 +673,9 @@ __global__ void __launch_bounds__(256) k_fallback_plan(FallbackPlanArgs a) {
         }
         if (threadIdx.x == 0) {
             const int64_t cnt = base_sh - start;
-            for (int k = 0; k < a.K; ++k)
+            for (int q = 0; q < a.n_cats; ++q)
                 for (int64_t i = 0; i < cnt; i += 32) {
+                    const int k = a.cats[q];
                     PruneTile t;
                     t.first = (int)(start + i);
                     t.count = (int)(cnt - i < 32 ? cnt - i : 32);

@@ -154,6 +154,29 @@ class Context:
         self._check(self.lib.cafe_score(self.h, C.byref(req), C.byref(res)))
         return ScoreResult(res.total_neg_lnl, fam, cat, res.status, res.n_failed, res.n_fallback, res.device_ms)
 
+    def score_batch(self, tree_id, set_id, candidates, *, want_categories=False, **kw) -> List[ScoreResult]:
+        """cafe_score_batch: candidates is a sequence of dicts with `lambdas`
+        (and for the gamma model `multipliers`, `cat_probs`); every other
+        request field is shared (keyword arguments as for score())."""
+        reqs, keep = [], []
+        for cand in candidates:
+            ck = dict(kw)
+            for key in ("multipliers", "cat_probs"):
+                if key in cand:
+                    ck[key] = cand[key]
+            r, k = self.make_request(tree_id, set_id, cand["lambdas"], **ck)
+            reqs.append(r)
+            keep.append(k)
+        n = len(reqs)
+        arr = (_lib.Request * n)(*reqs)
+        F = self._set_shape.get(set_id, (0,))[0]
+        fams = [np.zeros(F) for _ in range(n)]
+        cats = [np.zeros((F, r.n_categories)) if want_categories else None for r in reqs]
+        res = (_lib.Result * n)(*[_lib.Result(_p(fams[i]), _p(cats[i]), 0.0, 0, 0, 0, 0.0) for i in range(n)])
+        self._check(self.lib.cafe_score_batch(self.h, C.cast(arr, C.c_void_p), n, C.cast(res, C.c_void_p)))
+        return [ScoreResult(res[i].total_neg_lnl, fams[i], cats[i], res[i].status, res[i].n_failed, res[i].n_fallback,
+                            res[i].device_ms) for i in range(n)]
+
     def score_device(self, tree_id, set_id, lambdas, d_family_lnl=0, d_total=0, stream=0, **kw):
         req, keep = self.make_request(tree_id, set_id, lambdas, **kw)
         self._check(self.lib.cafe_score_device(self.h, C.byref(req), d_family_lnl or None, d_total or None,

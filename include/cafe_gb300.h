@@ -153,6 +153,17 @@ int cafe_is_saturated(double branch_length, double lambda);
  * and result->status set. */
 int cafe_score(cafe_ctx* ctx, const cafe_request* req, cafe_result* res);
 
+/* Batched candidates (many optimizer steps, or the B candidate vectors of
+ * one search round, scored together): n requests that share tree, family
+ * set, model, category count, precision, error-model use and (FP64_REF)
+ * bounds, each with its own lambdas, multipliers and category
+ * probabilities. Every (candidate, category) pair is pruned in the same
+ * launches; results[i] is exactly what cafe_score(reqs[i]) reports, within
+ * the precision's tolerance (bit-identical for the FP64 modes). A
+ * candidate the reference would reject scores +inf without affecting the
+ * others. */
+int cafe_score_batch(cafe_ctx* ctx, const cafe_request* reqs, int n, cafe_result* results);
+
 /* Device-resident variant: enqueues the whole evaluation on `stream`
  * (a cudaStream_t; NULL = the context's stream) and writes per-family lnL
  * to d_family_lnl (device, n_families doubles, may be NULL) and the total

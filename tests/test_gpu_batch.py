@@ -1,0 +1,158 @@
+"""Batched candidate scoring (cafe_score_batch): B candidate parameter
+vectors over one tree and family set in the same launches.
+
+Bars (stated per test):
+  * FP64_REF and FP64_BINNED: each batched result is bit-identical to the
+    same request scored alone, and the reference's golden -lnL is met to
+    1e-10 relative;
+  * MIXED_TF32X3: each batched result is within 1e-6 relative per family of
+    the FP64_BINNED value; a candidate's results equal its results alone
+    except for families that another candidate flagged for the FP64
+    recompute (then within 1e-6);
+  * a candidate the reference rejects (lambda <= 0, saturation) scores +inf
+    and leaves the others unchanged."""
+import math
+
+import numpy as np
+import pytest
+
+from golden_cases import load_cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = {c.name: c for c in load_cases()}
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from cafe5_gb300.engine import Context
+    c = Context()
+    yield c
+    c.close()
+
+
+def _setup(ctx, tree, counts, lam_idx=None, prior=None, err=None):
+    tid = ctx.upload_tree(tree, lam_idx)
+    sid = ctx.upload_families(tid, counts)
+    if prior is not None:
+        ctx.set_prior(prior)
+    ctx.set_error_model(err)
+    return tid, sid
+
+
+def _alone(ctx, tid, sid, cand, **kw):
+    ck = dict(kw)
+    for key in ("multipliers", "cat_probs"):
+        if key in cand:
+            ck[key] = cand[key]
+    return ctx.score(tid, sid, cand["lambdas"], **ck)
+
+
+@pytest.mark.parametrize("name,dedupe", [("syn_gamma_24taxa_k4", False), ("syn_base_12taxa", True),
+                                         ("syn_multilambda_error_32taxa", False)])
+@pytest.mark.parametrize("precision", ["fp64_ref", "fp64_binned"])
+def test_fp64_batch_is_bit_identical_to_alone(ctx, name, dedupe, precision):
+    case = CASES[name]
+    gamma = case.model == 1
+    prior = np.zeros(max(len(case.prior), 700))
+    prior[:len(case.prior)] = case.prior
+    tid, sid = _setup(ctx, case.tree, case.counts, case.lambda_of_node, prior, case.err_rows)
+    kw = dict(model=case.model, lambda_kind=case.lambda_kind, use_error_model=case.err_rows is not None,
+              precision=precision, dedupe=dedupe)
+    if precision == "fp64_ref":
+        kw.update(S=case.S, R=case.R)
+    base = dict(lambdas=case.lambdas)
+    if gamma:
+        base.update(multipliers=case.multipliers, cat_probs=case.cat_probs)
+    cands = [base]
+    for f in (0.7, 1.3, -1.0, 1.05):
+        c = dict(base)
+        c["lambdas"] = [x * f for x in case.lambdas]
+        cands.append(c)
+    if gamma:
+        c = dict(base)
+        c["multipliers"] = [m * 1.1 for m in case.multipliers]
+        cands.append(c)
+    got = ctx.score_batch(tid, sid, cands, want_categories=True, **kw)
+    for i, cand in enumerate(cands):
+        one = _alone(ctx, tid, sid, cand, want_categories=True, **kw)
+        if cand["lambdas"][0] < 0:
+            assert got[i].total == math.inf and one.total == math.inf
+            continue
+        assert got[i].total == one.total or (math.isnan(got[i].total) and math.isnan(one.total)), i
+        assert np.array_equal(got[i].family_lnl, one.family_lnl, equal_nan=True), i
+        assert np.array_equal(got[i].category_lnl, one.category_lnl, equal_nan=True), i
+        assert got[i].status == one.status
+    if precision == "fp64_ref" and not math.isinf(case.total):
+        assert abs(got[0].total - case.total) <= 1e-10 * abs(case.total)
+    ctx.free_families(sid)
+
+
+def test_mixed_batch_config3_shape(ctx):
+    """16 candidate (lambda, alpha) vectors x K=8 x 1,500 families on the
+    48-taxon tree (the config-3 shape at test size)."""
+    from cafe5_gb300.inputs import RootPrior, discrete_gamma
+    from cafe5_gb300.synth import workload
+    w = workload(3, n_families=1500, seed=31)
+    prior = RootPrior.uniform(400).vector()
+    tid, sid = _setup(ctx, w.tree, w.families.counts, prior=prior)
+    rng = np.random.default_rng(5)
+    cands = []
+    # lambda x (largest multiplier) x (longest branch, ~157) stays below 1:
+    # a saturated category would make every family fail (+inf)
+    for _ in range(16):
+        lam = float(0.0008 * np.exp(rng.normal(0, 0.2)))
+        alpha = float(0.8 * np.exp(rng.normal(0, 0.2)))
+        p, m = discrete_gamma(alpha, 8)
+        cands.append(dict(lambdas=[lam], multipliers=m, cat_probs=p))
+    kw = dict(model=1)
+    mixed = ctx.score_batch(tid, sid, cands, precision="mixed_tf32x3", **kw)
+    fp64 = ctx.score_batch(tid, sid, cands, precision="fp64_binned", **kw)
+    for i, cand in enumerate(cands):
+        a, b = fp64[i], mixed[i]
+        fin = np.isfinite(a.family_lnl)
+        rel = np.abs(b.family_lnl[fin] - a.family_lnl[fin]) / np.abs(a.family_lnl[fin])
+        assert rel.max() <= 1e-6, (i, rel.max())
+        assert abs(b.total - a.total) <= 1e-6 * abs(a.total)
+        alone = _alone(ctx, tid, sid, cand, precision="mixed_tf32x3", **kw)
+        d = np.abs(alone.family_lnl - b.family_lnl) / np.abs(a.family_lnl)
+        assert d.max() <= 1e-6
+        same = alone.family_lnl == b.family_lnl
+        assert same.mean() >= 0.99
+    ctx.free_families(sid)
+
+
+def test_mixed_batch_with_a_rejected_candidate(ctx):
+    from cafe5_gb300.inputs import RootPrior
+    from cafe5_gb300.synth import workload
+    w = workload(1, n_families=800, seed=32)
+    tid, sid = _setup(ctx, w.tree, w.families.counts, prior=RootPrior.uniform(400).vector())
+    good = dict(lambdas=[0.002], multipliers=w.multipliers, cat_probs=w.cat_probs)
+    sat = dict(lambdas=[0.5], multipliers=w.multipliers, cat_probs=w.cat_probs)      # lambda * t > 1
+    neg = dict(lambdas=[-0.001], multipliers=w.multipliers, cat_probs=w.cat_probs)
+    got = ctx.score_batch(tid, sid, [sat, good, neg], model=1, precision="mixed_tf32x3")
+    one = _alone(ctx, tid, sid, good, model=1, precision="mixed_tf32x3")
+    assert got[0].total == math.inf and got[0].status == 3
+    assert got[2].total == math.inf
+    assert np.array_equal(got[1].family_lnl, one.family_lnl)
+    assert got[1].total == one.total
+    ctx.free_families(sid)
+
+
+def test_batch_rejects_mismatched_requests(ctx):
+    from cafe5_gb300._lib import CafeError
+    from cafe5_gb300.inputs import RootPrior
+    from cafe5_gb300.synth import workload
+    w = workload(0, n_families=100, seed=33)
+    tid, sid = _setup(ctx, w.tree, w.families.counts, prior=RootPrior.uniform(100).vector())
+    reqs = [dict(lambdas=[0.002]), dict(lambdas=[0.003])]
+    with pytest.raises(CafeError):
+        # FP64_REF bounds differ between the two requests
+        from cafe5_gb300 import _lib
+        import ctypes as C
+        r0, k0 = ctx.make_request(tid, sid, [0.002], S=80, R=40)
+        r1, k1 = ctx.make_request(tid, sid, [0.003], S=90, R=40)
+        arr = (_lib.Request * 2)(r0, r1)
+        res = (_lib.Result * 2)()
+        ctx._check(ctx.lib.cafe_score_batch(ctx.h, C.cast(arr, C.c_void_p), 2, C.cast(res, C.c_void_p)))
+    ctx.free_families(sid)
