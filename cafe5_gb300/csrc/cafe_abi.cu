@@ -16,6 +16,7 @@
 #include <cstring>
 #include <functional>
 #include <numeric>
+#include <unordered_set>
 
 #include "runtime.h"
 
@@ -331,6 +332,7 @@ int prepare_set(cafe_ctx* C, FamSet& S) {
 // Matrix cache: look up or schedule (size, lambda, t). Caller holds C->mu.
 struct PendingJobs {
     std::vector<MatKey> keys;
+    std::unordered_set<MatKey, MatKeyHash> seen;
     std::vector<double> lam, t;
 };
 
@@ -416,6 +418,7 @@ int cache_build(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
     // requests on other streams order themselves after this build
     CK(cudaEventRecord(ready, ws.stream), "event");
     P.keys.clear();
+    P.seen.clear();
     return CAFE_OK;
 }
 
@@ -443,8 +446,7 @@ MatKey make_key(int size, double lambda, double t) {
 
 void schedule(cafe_ctx* C, PendingJobs& P, const MatKey& k) {
     if (cache_lookup(C, k)) return;
-    for (auto& q : P.keys)
-        if (q == k) return;
+    if (!P.seen.insert(k).second) return;
     P.keys.push_back(k);
 }
 
@@ -683,8 +685,6 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         const size_t fl = (size_t)n_mat * Wm * Wm;
         CK(ws.tc_hi.reserve(fl * sizeof(float)), "tc matrices");
         CK(ws.tc_lo.reserve(fl * sizeof(float)), "tc matrices");
-        CK(ws.tc_ct.reserve(fl * sizeof(float)), "tc matrices");
-        CK(ws.tc_ce.reserve((size_t)n_mat * Wm * sizeof(int32_t)), "tc matrices");
         CK(ws.h_conv.reserve(jobs.size() * sizeof(ConvertJob)), "convert jobs");
         CK(ws.conv.reserve(jobs.size() * sizeof(ConvertJob)), "convert jobs");
         std::memcpy(ws.h_conv.p, jobs.data(), jobs.size() * sizeof(ConvertJob));
@@ -695,7 +695,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         std::memcpy(ws.h_mi.p, mat_index.data(), mat_index.size() * sizeof(int32_t));
         CK(cudaMemcpyAsync(ws.tc_mi.p, ws.h_mi.p, mat_index.size() * sizeof(int32_t), cudaMemcpyHostToDevice, ws.stream),
            "mat index");
-        TcBuffers tb{ws.tc_hi.as<float>(), ws.tc_lo.as<float>(), ws.tc_ct.as<float>(), ws.tc_ce.as<int32_t>(), Wm};
+        TcBuffers tb{ws.tc_hi.as<float>(), ws.tc_lo.as<float>(), Wm};
         if (prof) C->prof.begin(3, ws.stream, &ev);
         CK(launch_convert_tc(ws.conv.as<ConvertJob>(), n_mat, tb, ws.stream), "convert");
         if (prof) C->prof.end(3, ws.stream, ev);
@@ -762,8 +762,6 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         a.counts = S.d_counts.as<int32_t>();
         a.perm = B.d_perm.as<int64_t>();
         a.mat_index = ws.tc_mi.as<int32_t>();
-        a.ct = ws.tc_ct.as<float>();
-        a.ce = ws.tc_ce.as<int32_t>();
         a.Wm = Wm;
         a.vec_hi = ws.tc_vhi.as<float>();
         a.vec_lo = ws.tc_vlo.as<float>();
@@ -782,8 +780,8 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         a.phase_clocks = nullptr;
         static const bool phase_env = getenv("CAFE_TC_PHASES") != nullptr;
         if (phase_env) {
-            CK(ws.phase.reserve(4 * sizeof(unsigned long long)), "phase clocks");
-            CK(cudaMemsetAsync(ws.phase.p, 0, 4 * sizeof(unsigned long long), ws.stream), "phase clocks");
+            CK(ws.phase.reserve(6 * sizeof(unsigned long long)), "phase clocks");
+            CK(cudaMemsetAsync(ws.phase.p, 0, 6 * sizeof(unsigned long long), ws.stream), "phase clocks");
             a.phase_clocks = ws.phase.as<unsigned long long>();
         }
         if (prof) {
@@ -815,13 +813,14 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             }
         }
         if (phase_env) {
-            unsigned long long h[4];
+            unsigned long long h[6];
             CK(cudaMemcpyAsync(h, ws.phase.p, sizeof(h), cudaMemcpyDeviceToHost, ws.stream), "phase clocks");
             CK(cudaStreamSynchronize(ws.stream), "phase clocks");
-            const double tot = (double)(h[0] + h[1] + h[2] + h[3]) + 1e-9;
-            fprintf(stderr, "k_prune_tc phases (CTA-summed SM clocks): gemm %.1f%% passA %.1f%% passB %.1f%% sync %.1f%% total %.3g\n",
-                    100 * h[0] / tot, 100 * h[1] / tot, 100 * h[2] / tot, 100 * h[3] / tot, tot);
+            const double n = (double)h[5] + 1e-9;
+            fprintf(stderr, "k_prune_tc clocks per tile-node: setup %.0f gemm %.0f epilogue %.0f root %.0f sync %.0f (%llu tile-nodes)\n",
+                    h[0] / n, h[1] / n, h[2] / n, h[3] / n, h[4] / n, h[5]);
         }
+
         if (prof) C->prof.end(1, ws.stream, ev);
     }
     int rc = launch_fp64_tiles(C, ws, R, T, S, K, wide_tiles, ws.tiles64, ws.h_tiles64, B.d_perm.as<int64_t>(), msize,
@@ -1527,7 +1526,12 @@ int cafe_profile_read(cafe_ctx* C, cafe_timings* out) {
 }
 
 int cafe_score_device(cafe_ctx* C, const cafe_request* req, double* d_family_lnl, double* d_total, void* stream) {
-    if (!C) return CAFE_ERR_INVALID;
+    return cafe_score_batch_device(C, req, 1, d_family_lnl, d_total, stream);
+}
+
+int cafe_score_batch_device(cafe_ctx* C, const cafe_request* req, int n, double* d_family_lnl, double* d_total,
+                            void* stream) {
+    if (!C || n < 1) return CAFE_ERR_INVALID;
     std::lock_guard<std::mutex> lk(C->mu);
     cudaSetDevice(C->device);
     Workspace& ws = *C->ws[0];
@@ -1536,15 +1540,14 @@ int cafe_score_device(cafe_ctx* C, const cafe_request* req, double* d_family_lnl
     auto si = C->sets.find(req ? req->set_id : -1);
     if (si == C->sets.end()) return fail(C, CAFE_ERR_NOT_FOUND, "unknown family set");
     const int64_t F = si->second->F;
-    CK(ws.fam_lnl.reserve(std::max<int64_t>(F, 1) * sizeof(double)), "family buffer");
-    CK(ws.total.reserve(sizeof(double)), "total");
+    CK(ws.fam_lnl.reserve((size_t)std::max<int64_t>(F, 1) * n * sizeof(double)), "family buffer");
+    CK(ws.total.reserve((size_t)n * sizeof(double)), "total");
     if (user) {
         // order the workspace stream after the caller's stream, and back
         CK(cudaEventRecord(ws.ev_start, user), "event");
         CK(cudaStreamWaitEvent(ws.stream, ws.ev_start, 0), "event");
     }
-    CK(ws.nfail.reserve(sizeof(int32_t)), "fail counter");
-    int rc = enqueue_score(C, ws, req, 1, d_family_lnl ? d_family_lnl : ws.fam_lnl.as<double>(),
+    int rc = enqueue_score(C, ws, req, n, d_family_lnl ? d_family_lnl : ws.fam_lnl.as<double>(),
                            d_total ? d_total : ws.total.as<double>(), &info);
     if (rc) return rc;
     CK(cudaEventRecord(ws.ev_staged, ws.stream), "event");

@@ -120,8 +120,6 @@ struct ConvertJob {
 struct TcBuffers {
     float* hi;           // [n_mat][Wm][Wm] TF32 hi part, row-major M[s][c]
     float* lo;           // [n_mat][Wm][Wm] TF32 lo part
-    float* ct;           // [n_mat][Wm][Wm] transposed, column-normalised: ct[n][s] = M[s][n] 2^-ce[n]
-    int32_t* ce;         // [n_mat][Wm]
     int Wm;
 };
 
@@ -134,8 +132,6 @@ struct PruneTcArgs {
     const int32_t* counts;
     const int64_t* perm;
     const int32_t* mat_index;    // [K][n_nodes] converted-matrix index (-1 for the root)
-    const float* ct;
-    const int32_t* ce;
     int Wm;                      // pitch of matrices and node vectors (elements)
     float* vec_hi;               // node vectors, rows = CTA x slot x 128 families
     float* vec_lo;
@@ -155,8 +151,8 @@ struct PruneTcArgs {
     int Ws;                      // widest bin of this launch (shared-memory B rows)
     int stages;                  // shared-memory stages (1 or 2)
     int64_t vrow_base;           // first node-vector row of this launch
-    unsigned long long* phase_clocks;   // optional [4]: SM clocks spent in GEMM wait,
-                                        // epilogue pass A, pass B, end-of-node barrier
+    unsigned long long* phase_clocks;   // optional [6]: SM clocks of thread 0 in child setup, GEMMs,
+                                        // epilogue, root bookkeeping, end-of-node barrier; tile-nodes
 };
 
 // Tensor maps travel by value (__grid_constant__); the host encodes them.

@@ -17,9 +17,13 @@
 //    staged by TMA into two shared-memory stages; one thread issues TMA and
 //    tcgen05.mma; the accumulators of up to two children sit side by side in
 //    TMEM.
-//  * Leaf child: its factor is the matrix column of the observed count,
-//    read from an FP32 column-normalised transposed copy (with the column's
-//    power-of-two exponent), or the three-column error-model sum.
+//  * Leaf child: its factor is the matrix column of the observed count (or
+//    the error model's weighted sum of three columns), computed as the same
+//    GEMM with a one-hot (or three-hot) A tile that the threads write into
+//    shared memory in the swizzled operand layout: D = A (B_hi + B_lo), plus
+//    A_lo B_hi for error-model weights. Only the K chunks that hold a count
+//    of the tile are issued. Every child's factor then sits in TMEM and the
+//    epilogue reads no global memory.
 //  * Epilogue (thread f owns family f = TMEM lane f): the product over
 //    children is rescaled by the largest per-state sum of the factors'
 //    binary exponents, so the product's maximum is ~1 and nothing
@@ -44,7 +48,13 @@ namespace {
 constexpr int TM = 128;   // families per tile = MMA M = TMEM lanes
 constexpr int KC = 32;    // K per stage: 32 fp32 = one 128-byte swizzle row
 constexpr int NTHREADS = 128;
-constexpr int CW = 16;    // epilogue columns per TMEM load
+#ifndef CAFE_TC_CW
+#define CAFE_TC_CW 16
+#endif
+#ifndef CAFE_TC_MINB
+#define CAFE_TC_MINB 4
+#endif
+constexpr int CW = CAFE_TC_CW;   // epilogue columns per TMEM load
 
 __host__ __device__ inline size_t stage_bytes(int Ws) { return (size_t)(2 * TM + 2 * Ws) * KC * sizeof(float); }
 
@@ -64,187 +74,145 @@ struct ChildInfo {
     int node;
     int leaf_col;   // >= 0: leaf
     int mat;
-    int tcol;       // TMEM column base for internal children
+    int tcol;       // TMEM column base of the child's factor
 };
 
-// Per-child source of the factor: TMEM columns (internal child) or up to
-// three weighted rows of the column-normalised matrix copy (leaf).
+// Per-child source of the factor: TMEM columns, or the unit factor of an
+// absent second child.
 struct Src {
-    bool leaf;      // also true for the unit factor of an absent second child
     bool unit;
     uint32_t taddr;
-    const float* row[3];
-    float w[3];
 };
 
 template <int NC>
 struct NodeSrc {
     Src s[NC];
-    int Eacc;     // sum of the children's power-of-two exponents
+    int Eacc;     // sum of the internal children's power-of-two exponents
     bool flag;
 };
 
-// Child sources of one node for this thread's family; issued before the
-// GEMM wait so the count / exponent loads overlap the tensor-core work.
+// Leaf weights of this thread's family: up to three (column, weight) pairs
+// (one-hot column n, or the error model's columns n-1, n, n+1).
+struct LeafW {
+    int col[3];
+    float hi[3], lo[3];
+};
+
 template <int NC>
 __device__ __forceinline__ void setup_src(const PruneTcArgs& a, const ChildInfo* ch, int nch, const int* Esh,
-                                          uint32_t tmem_lane, int64_t fam, int tid, int S, int Wm,
-                                          NodeSrc<NC>& ns) {
+                                          uint32_t tmem_lane, int64_t fam, int tid, int S, NodeSrc<NC>& ns,
+                                          LeafW (&lw)[NC], int* cmask_sh) {
     ns.Eacc = 0;
     ns.flag = false;
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
         Src& sc = ns.s[c];
-        sc.unit = c >= nch;
-        if (sc.unit) {
-            sc.leaf = true;
-            sc.taddr = 0;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                sc.row[d] = nullptr;
-                sc.w[d] = 0.0f;
-            }
-            continue;
-        }
-        const ChildInfo ci = ch[c];
-        sc.leaf = ci.leaf_col >= 0;
-        sc.taddr = tmem_lane + (uint32_t)(ci.tcol > 0 ? ci.tcol : 0);
+        LeafW& L = lw[c];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            sc.row[d] = nullptr;
-            sc.w[d] = 0.0f;
+            L.col[d] = -1;
+            L.hi[d] = 0.0f;
+            L.lo[d] = 0.0f;
         }
-        if (ci.leaf_col >= 0) {
-            const int n = fam >= 0 ? __ldg(a.counts + (size_t)fam * a.plan.n_leaves + ci.leaf_col) : 0;
-            const int32_t* ce = a.ce + (size_t)ci.mat * Wm;
-            const float* ct = a.ct + (size_t)ci.mat * Wm * Wm;
-            if (a.err) {
-                // error-model leaf: weights p_d 2^(ce_d - ce_max) over columns n-1, n, n+1
-                const double* pr = a.err + (size_t)(n < a.err_rows ? n : a.err_rows - 1) * a.err_ndev;
-                const int off = n - (a.err_ndev - 1) / 2;
-                int cmax = -100000;
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    const int col = off + d;
-                    if (d < a.err_ndev && col >= 0 && col <= S && pr[d] > 0) cmax = max(cmax, __ldg(ce + col));
-                }
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    const int col = off + d;
-                    if (d < a.err_ndev && col >= 0 && col <= S && pr[d] > 0) {
-                        sc.row[d] = ct + (size_t)col * Wm;
-                        sc.w[d] = (float)pr[d] * pow2f(__ldg(ce + col) - cmax);
-                    }
-                }
-                if (cmax == -100000) ns.flag = true;
-                else ns.Eacc += cmax;
-            } else if (n >= 0 && n <= S) {
-                sc.row[0] = ct + (size_t)n * Wm;
-                sc.w[0] = 1.0f;
-                ns.Eacc += __ldg(ce + n);
-            } else {
-                ns.flag = true;
-            }
-        } else {
+        sc.unit = c >= nch;
+        sc.taddr = 0;
+        if (sc.unit) continue;
+        const ChildInfo ci = ch[c];
+        sc.taddr = tmem_lane + (uint32_t)ci.tcol;
+        if (ci.leaf_col < 0) {
             ns.Eacc += Esh[a.plan.slot[ci.node] * TM + tid];
+            continue;
         }
-    }
-}
-
-// 16 values of a leaf factor starting at column col0.
-__device__ __forceinline__ void load_leaf(const Src& c, int col0, uint32_t (&out)[CW]) {
-    if (c.unit) {
+        if (fam < 0) continue;        // padding row: zero factor
+        const int n = __ldg(a.counts + (size_t)fam * a.plan.n_leaves + ci.leaf_col);
+        unsigned bits = 0;
+        if (a.err) {
+            const double* pr = a.err + (size_t)(n < a.err_rows ? n : a.err_rows - 1) * a.err_ndev;
+            const int off = n - (a.err_ndev - 1) / 2;
 #pragma unroll
-        for (int j = 0; j < CW; ++j) out[j] = __float_as_uint(1.0f);
-        return;
-    }
-    float y[CW];
-#pragma unroll
-    for (int j = 0; j < CW; ++j) y[j] = 0.0f;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        if (!c.row[d]) continue;
-        const float4* src = reinterpret_cast<const float4*>(c.row[d] + col0);
-        const float w = c.w[d];
-#pragma unroll
-        for (int q = 0; q < CW / 4; ++q) {
-            const float4 x = __ldg(src + q);
-            y[4 * q + 0] = fmaf(w, x.x, y[4 * q + 0]);
-            y[4 * q + 1] = fmaf(w, x.y, y[4 * q + 1]);
-            y[4 * q + 2] = fmaf(w, x.z, y[4 * q + 2]);
-            y[4 * q + 3] = fmaf(w, x.w, y[4 * q + 3]);
+            for (int d = 0; d < 3; ++d) {
+                const int col = off + d;
+                if (d < a.err_ndev && col >= 0 && col <= S && pr[d] > 0) {
+                    const float w = (float)pr[d];
+                    L.col[d] = col;
+                    L.hi[d] = tc::round_tf32(w);
+                    L.lo[d] = tc::round_tf32(w - L.hi[d]);
+                    bits |= 1u << (col / KC);
+                }
+            }
+        } else if (n >= 0 && n <= S) {
+            L.col[0] = n;
+            L.hi[0] = 1.0f;
+            bits = 1u << (n / KC);
         }
-    }
-#pragma unroll
-    for (int j = 0; j < CW; ++j) out[j] = __float_as_uint(y[j]);
-}
-
-struct EpiOut {
-    int E;
-    bool flag;
-    double best;            // root: max_j L[j] prior[j] (in units of 2^E)
-};
-
-__device__ __forceinline__ void store_tf32x2(float* __restrict__ hi, float* __restrict__ lo, int col0,
-                                             const float (&p)[CW]) {
-#pragma unroll
-    for (int q = 0; q < CW / 4; ++q) {
-        float4 h, l;
-        h.x = tc::round_tf32(p[4 * q + 0]);
-        h.y = tc::round_tf32(p[4 * q + 1]);
-        h.z = tc::round_tf32(p[4 * q + 2]);
-        h.w = tc::round_tf32(p[4 * q + 3]);
-        l.x = tc::round_tf32(p[4 * q + 0] - h.x);
-        l.y = tc::round_tf32(p[4 * q + 1] - h.y);
-        l.z = tc::round_tf32(p[4 * q + 2] - h.z);
-        l.w = tc::round_tf32(p[4 * q + 3] - h.w);
-        reinterpret_cast<float4*>(hi + col0)[q] = h;
-        reinterpret_cast<float4*>(lo + col0)[q] = l;
+        if (!bits) ns.flag = true;
+        else atomicOr(cmask_sh + c, (int)bits);
     }
 }
 
-// Fast epilogue: one pass. Every factor is <= 1 (rows of M sum to <= 1,
-// node vectors and normalised leaf columns are <= 1), so the plain product
-// cannot overflow; its maximum is tracked and the stored row is rescaled
-// only if it drifts below 2^-32. Leaf loads run one chunk ahead.
-// `need_exact` is set when the product underflowed (max < 2^-120, or an
-// all-zero weighted root) so the exact two-pass epilogue must redo it.
+// This thread's row of the leaf A tile for K chunk kc (columns
+// [kc KC, kc KC + KC)), written into the 128-byte-swizzled K-major layout
+// the MMA descriptor reads: row r of an 8-row, 1024-byte atom keeps its
+// 16-byte piece j at position j ^ (r % 8).
+__device__ __forceinline__ void write_leaf_row(float* tile, int r, const LeafW& L, int kc, bool lo) {
+    uint8_t* row = reinterpret_cast<uint8_t*>(tile) + (size_t)(r >> 3) * 1024 + (size_t)(r & 7) * 128;
+    const int c0 = kc * KC;
+#pragma unroll
+    for (int j = 0; j < KC / 4; ++j) {
+        float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int q = L.col[d] - c0 - 4 * j;
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (q == e) v[e] = lo ? L.lo[d] : L.hi[d];
+        }
+        *reinterpret_cast<float4*>(row + ((j ^ (r & 7)) << 4)) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+}
+
+// CW values of a child's factor starting at column col0 (issue only for
+// TMEM children; the unit factor is filled at once).
+__device__ __forceinline__ void load_unit(uint32_t (&out)[CW]) {
+#pragma unroll
+    for (int j = 0; j < CW; ++j) out[j] = __float_as_uint(1.0f);
+}
+
+
+// Loads CW columns (from col0) of every child's factor.
 template <int NC>
-__device__ __forceinline__ void epi_fast(const NodeSrc<NC>& ns, int W, bool is_root, int Rf, const float* prior_f,
-                                         float* __restrict__ rowhi, float* __restrict__ rowlo, EpiOut& out,
-                                         bool& need_exact) {
-    float maxp = 0.0f;
-    float best_f = 0.0f, best_p = 0.0f, best_q = 0.0f;
-    uint32_t lf[NC][CW];
+__device__ __forceinline__ void load_children(const NodeSrc<NC>& ns, int col0, uint32_t (&r)[NC][CW]) {
 #pragma unroll
-    for (int c = 0; c < NC; ++c)
-        if (ns.s[c].leaf) load_leaf(ns.s[c], 0, lf[c]);
+    for (int c = 0; c < NC; ++c) {
+        if (!ns.s[c].unit) tc::tmem_ld_issue(ns.s[c].taddr + (uint32_t)col0, r[c]);
+        else load_unit(r[c]);
+    }
+    tc::tmem_wait();
+}
+
+// Pass 1 over the product of the children's factors, each scaled by
+// scl[c]: its maximum over the states (inner node), or the largest
+// prior-weighted value over root rows 1..Rf (root; index j = state j + 1).
+// Warp-collective (TMEM loads).
+template <int NC>
+__device__ __forceinline__ void epi_scan(const NodeSrc<NC>& ns, int W, bool is_root, int Rf, const float* prior_f,
+                                         const float (&scl)[NC], float& maxp, float& best_f, float& best_p,
+                                         float& best_q) {
+    maxp = 0.0f;
+    best_f = best_p = best_q = 0.0f;
     for (int col0 = 0; col0 < W; col0 += CW) {
         uint32_t r[NC][CW];
-        bool any_tmem = false;
-#pragma unroll
-        for (int c = 0; c < NC; ++c) {
-            if (!ns.s[c].leaf) {
-                tc::tmem_ld16_issue(ns.s[c].taddr + (uint32_t)col0, r[c]);
-                any_tmem = true;
-            } else {
-#pragma unroll
-                for (int j = 0; j < CW; ++j) r[c][j] = lf[c][j];
-                if (col0 + CW < W) load_leaf(ns.s[c], col0 + CW, lf[c]);   // next chunk, in flight
-            }
-        }
-        if (any_tmem) tc::tmem_wait();
+        load_children(ns, col0, r);
         float p[CW];
 #pragma unroll
         for (int j = 0; j < CW; ++j) p[j] = 1.0f;
 #pragma unroll
         for (int c = 0; c < NC; ++c)
 #pragma unroll
-            for (int j = 0; j < CW; ++j) p[j] *= __uint_as_float(r[c][j]);
+            for (int j = 0; j < CW; ++j) p[j] *= __uint_as_float(r[c][j]) * scl[c];
         if (!is_root) {
 #pragma unroll
             for (int j = 0; j < CW; ++j) maxp = fmaxf(maxp, p[j]);
-            store_tf32x2(rowhi, rowlo, col0, p);
         } else {
 #pragma unroll
             for (int j = 0; j < CW; ++j) {
@@ -261,128 +229,88 @@ __device__ __forceinline__ void epi_fast(const NodeSrc<NC>& ns, int W, bool is_r
             }
         }
     }
-    int E = ns.Eacc;
-    need_exact = false;
-    if (!is_root && maxp < 0x1p-32f) {
-        if (!(maxp >= 0x1p-120f)) {
-            need_exact = true;
-        } else {
-            // bring this row's maximum back to [0.5, 1)
-            const int k = -bexp(maxp);
-            const float sc = pow2f(k);
-            for (int col0 = 0; col0 < W; col0 += 4) {
-                float4 h = *reinterpret_cast<const float4*>(rowhi + col0);
-                float4 l = *reinterpret_cast<const float4*>(rowlo + col0);
-                float v[4] = {(h.x + l.x) * sc, (h.y + l.y) * sc, (h.z + l.z) * sc, (h.w + l.w) * sc};
-                h.x = tc::round_tf32(v[0]);
-                h.y = tc::round_tf32(v[1]);
-                h.z = tc::round_tf32(v[2]);
-                h.w = tc::round_tf32(v[3]);
-                l.x = tc::round_tf32(v[0] - h.x);
-                l.y = tc::round_tf32(v[1] - h.y);
-                l.z = tc::round_tf32(v[2] - h.z);
-                l.w = tc::round_tf32(v[3] - h.w);
-                *reinterpret_cast<float4*>(rowhi + col0) = h;
-                *reinterpret_cast<float4*>(rowlo + col0) = l;
-            }
-            E -= k;
-        }
-    }
-    if (is_root && !(best_f > 0.0f)) need_exact = true;
-    out.E = E;
-    out.flag = ns.flag;
-    out.best = (double)best_p * (double)best_q;
 }
 
-// Exact epilogue (warp-collective: every lane runs it when any lane needs
-// it): pass A finds the largest per-state sum of the factors' binary
-// exponents, pass B forms the product rescaled by it, so the product's
-// maximum is in [2^-NC, 1) and nothing underflows unless the factors are
-// more than 2^250 apart. Results are stored only where `write` is set.
+// Exact path (warp-collective; lanes that do not need it ignore the
+// result): the largest per-state sum of the factors' binary exponents over
+// states [s_lo, s_hi). Arguments travel by value so the caller's copies
+// stay in registers.
 template <int NC>
-__device__ __noinline__ void epi_exact(const NodeSrc<NC>& ns, int W, bool is_root, int Rf, const float* prior_f,
-                                       float* __restrict__ rowhi, float* __restrict__ rowlo, bool write,
-                                       EpiOut& out) {
-    const int s_lo = is_root ? 1 : 0;
-    const int s_hi = is_root ? Rf + 1 : W;
+__device__ __noinline__ int epi_maxexp(const NodeSrc<NC> ns, int W, int s_lo, int s_hi) {
     int maxe = -100000;
     for (int col0 = 0; col0 < W; col0 += CW) {
+        uint32_t r[NC][CW];
+        load_children(ns, col0, r);
         int ex[CW];
 #pragma unroll
         for (int j = 0; j < CW; ++j) ex[j] = 0;
 #pragma unroll
-        for (int c = 0; c < NC; ++c) {
-            uint32_t r[CW];
-            if (!ns.s[c].leaf) {
-                tc::tmem_ld16_issue(ns.s[c].taddr + (uint32_t)col0, r);
-                tc::tmem_wait();
-            } else {
-                load_leaf(ns.s[c], col0, r);
-            }
+        for (int c = 0; c < NC; ++c)
 #pragma unroll
-            for (int j = 0; j < CW; ++j) ex[j] += bexp(__uint_as_float(r[j]));
-        }
+            for (int j = 0; j < CW; ++j) ex[j] += bexp(__uint_as_float(r[c][j]));
 #pragma unroll
         for (int j = 0; j < CW; ++j) {
             const int s = col0 + j;
             if (s >= s_lo && s < s_hi && ex[j] > maxe) maxe = ex[j];
         }
     }
-    bool flag = ns.flag;
-    if (maxe < -250) {
-        flag = true;     // factors too far apart (or all zero): FP64 recomputes this family
-        maxe = 0;
-    }
-    float scl[NC];
-    {
-        const int sh = -maxe;
-        const int part = sh / NC;
-#pragma unroll
-        for (int c = 0; c < NC; ++c) scl[c] = pow2f(part + (c == 0 ? sh - part * NC : 0));
-    }
-    float best_f = 0.0f, best_p = 0.0f, best_q = 0.0f;
-    for (int col0 = 0; col0 < W; col0 += CW) {
-        float p[CW];
-#pragma unroll
-        for (int j = 0; j < CW; ++j) p[j] = 1.0f;
-#pragma unroll
-        for (int c = 0; c < NC; ++c) {
-            uint32_t r[CW];
-            if (!ns.s[c].leaf) {
-                tc::tmem_ld16_issue(ns.s[c].taddr + (uint32_t)col0, r);
-                tc::tmem_wait();
-            } else {
-                load_leaf(ns.s[c], col0, r);
-            }
-#pragma unroll
-            for (int j = 0; j < CW; ++j) p[j] *= __uint_as_float(r[j]) * scl[c];
+    return maxe;
+}
+
+// Pass 2 (inner nodes; every thread of the CTA): the scaled product as
+// TF32 hi/lo into a staging tile in the 128-byte-swizzled layout, 32
+// columns at a time, written to the node's vector rows by TMA stores.
+template <int NC>
+__device__ __forceinline__ void epi_store(const NodeSrc<NC>& ns, int W, const float (&scl)[NC], float* stg_hi,
+                                          float* stg_lo, int tid, const CUtensorMap* map_hi, const CUtensorMap* map_lo,
+                                          int vrow) {
+    uint8_t* row_hi = reinterpret_cast<uint8_t*>(stg_hi) + (size_t)(tid >> 3) * 1024 + (size_t)(tid & 7) * 128;
+    uint8_t* row_lo = reinterpret_cast<uint8_t*>(stg_lo) + (size_t)(tid >> 3) * 1024 + (size_t)(tid & 7) * 128;
+    for (int c32 = 0; c32 < W; c32 += KC) {
+        if (c32 > 0) {
+            if (tid == 0) tc::bulk_wait_read0();     // the previous chunk's stores have read the tile
+            __syncthreads();
         }
-        if (!is_root) {
-            if (write) store_tf32x2(rowhi, rowlo, col0, p);
-        } else {
+        for (int col0 = c32; col0 < c32 + KC; col0 += CW) {
+            uint32_t r[NC][CW];
+            load_children(ns, col0, r);
+            float p[CW];
 #pragma unroll
-            for (int j = 0; j < CW; ++j) {
-                const int s = col0 + j;
-                if (s >= 1 && s <= Rf) {
-                    const float q = prior_f[s - 1];
-                    const float v = p[j] * q;
-                    if (v > best_f) {
-                        best_f = v;
-                        best_p = p[j];
-                        best_q = q;
-                    }
-                }
+            for (int j = 0; j < CW; ++j) p[j] = 1.0f;
+#pragma unroll
+            for (int c = 0; c < NC; ++c)
+#pragma unroll
+                for (int j = 0; j < CW; ++j) p[j] *= __uint_as_float(r[c][j]) * scl[c];
+#pragma unroll
+            for (int q = 0; q < CW / 4; ++q) {
+                float4 h, l;
+                h.x = tc::round_tf32(p[4 * q + 0]);
+                h.y = tc::round_tf32(p[4 * q + 1]);
+                h.z = tc::round_tf32(p[4 * q + 2]);
+                h.w = tc::round_tf32(p[4 * q + 3]);
+                l.x = tc::round_tf32(p[4 * q + 0] - h.x);
+                l.y = tc::round_tf32(p[4 * q + 1] - h.y);
+                l.z = tc::round_tf32(p[4 * q + 2] - h.z);
+                l.w = tc::round_tf32(p[4 * q + 3] - h.w);
+                const int j = ((col0 - c32) >> 2) + q;          // 16-byte piece of the 128-byte row
+                const int off = (j ^ (tid & 7)) << 4;
+                *reinterpret_cast<float4*>(row_hi + off) = h;
+                *reinterpret_cast<float4*>(row_lo + off) = l;
             }
         }
-    }
-    if (write) {
-        out.E = ns.Eacc + maxe;
-        out.flag = flag;
-        out.best = (double)best_p * (double)best_q;
+        tc::fence_proxy_async_shared();
+        __syncthreads();
+        if (tid == 0) {
+            for (int r = 0; r < TM / 32; ++r) {
+                tc::tma_store_2d(map_hi, c32, vrow + 32 * r, stg_hi + r * 32 * KC);
+                tc::tma_store_2d(map_lo, c32, vrow + 32 * r, stg_lo + r * 32 * KC);
+            }
+            tc::bulk_commit();
+        }
     }
 }
 
-__global__ void __launch_bounds__(NTHREADS, 4)
+__global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
     k_prune_tc(const __grid_constant__ CUtensorMap map_mhi, const __grid_constant__ CUtensorMap map_mlo,
                const __grid_constant__ CUtensorMap map_vhi, const __grid_constant__ CUtensorMap map_vlo,
                const PruneTcArgs a) {
@@ -392,6 +320,7 @@ __global__ void __launch_bounds__(NTHREADS, 4)
     __shared__ uint32_t tmem_sh;
     __shared__ int abort_sh;
     __shared__ ChildInfo ch_sh[8];
+    __shared__ int cmask_sh[2];     // per child: K chunks holding a leaf column of the tile
     __shared__ float prior_f[256];
 
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -418,12 +347,12 @@ __global__ void __launch_bounds__(NTHREADS, 4)
     const uint32_t tmem = tmem_sh;
     const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
 
-    uint32_t g = 0;          // chunks issued so far (thread 0)
+    uint32_t g = 0;          // chunks issued so far (same in every thread)
     uint32_t dn = 0;         // completions of bar_done observed (all threads)
     int last_full = -1;      // stage of the last issued TMA (thread 0)
     uint32_t last_full_parity = 0;
     const int64_t vrow_cta = a.vrow_base + (int64_t)blockIdx.x * a.n_slots * TM;
-    unsigned long long ph[4] = {0, 0, 0, 0};
+    unsigned long long ph[6] = {0, 0, 0, 0, 0, 0};
     const bool timing = a.phase_clocks != nullptr && tid == 0;
 
     for (int t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
@@ -441,102 +370,111 @@ __global__ void __launch_bounds__(NTHREADS, 4)
             const int vs = P.slot[v];
             const int c0 = P.cstart[ii], c1 = P.cstart[ii + 1];
             const int nch = c1 - c0;
+            const long long ts = timing ? clock64() : 0;
             if (tid == 0) {
-                int nint = 0;
                 for (int c = c0; c < c1; ++c) {
                     ChildInfo ci;
                     ci.node = P.child[c];
                     ci.leaf_col = P.leaf_col[ci.node];
                     ci.mat = mi[ci.node];
-                    ci.tcol = ci.leaf_col < 0 ? (nint++) * W : -1;
+                    ci.tcol = (c - c0) * W;
                     ch_sh[c - c0] = ci;
                 }
+                cmask_sh[0] = 0;
+                cmask_sh[1] = 0;
             }
             __syncthreads();
-            int nint = 0;
-            for (int c = 0; c < nch; ++c) nint += ch_sh[c].leaf_col < 0;
-            // child sources (count / exponent loads) overlap the GEMM below
+            // child sources; leaf weights and the K chunks they touch
             NodeSrc<2> ns2;
-            setup_src<2>(a, ch_sh, nch, Esh, tmem + lane_base, fam, tid, S, Wm, ns2);
+            LeafW lw[2];
+            setup_src<2>(a, ch_sh, nch, Esh, tmem + lane_base, fam, tid, S, ns2, lw, cmask_sh);
+            __syncthreads();
 
-            // ---------------- GEMMs of the internal children ----------------
+            // ---------------- one GEMM per child into TMEM ----------------
             long long t0 = timing ? clock64() : 0;
-            if (nint > 0) {
-                if (tid == 0 && !abort_sh) {
-                    const int kpc = W / KC;             // K chunks per child
-                    const int total = nint * kpc;
-                    auto child_of = [&](int j) -> const ChildInfo& {
-                        int seen = 0;
-                        for (int c = 0; c < nch; ++c)
-                            if (ch_sh[c].leaf_col < 0) {
-                                if (seen == j) return ch_sh[c];
-                                ++seen;
-                            }
-                        return ch_sh[0];
-                    };
-                    auto issue = [&](int i) -> bool {
-                        const uint32_t ci = g + (uint32_t)i;
-                        const int st = (int)(ci % (uint32_t)NS);
-                        const uint32_t u = ci / (uint32_t)NS;
-                        if (u >= 1 && !tc::mbar_wait(&bar_empty[st], (u - 1) & 1)) return false;
-                        const ChildInfo& c = child_of(i / kpc);
-                        const int kc = i % kpc;
+            // the previous nodes' TMA stores must be complete: their staging
+            // tile is about to be overwritten and their rows may be read back
+            if (tid == 0) tc::bulk_wait0();
+            {
+                const int kpc = W / KC;             // K chunks per child
+                int ci = 0;                         // chunks issued for this node
+                for (int c = 0; c < nch; ++c) {
+                    const ChildInfo chi = ch_sh[c];
+                    const bool leaf = chi.leaf_col >= 0;
+                    unsigned mask = leaf ? (unsigned)cmask_sh[c] : ((1u << kpc) - 1);
+                    if (!mask) mask = 1;            // all-zero leaf tile: still initialise D
+                    bool first = true;
+                    for (int kc = 0; kc < kpc; ++kc) {
+                        if (!((mask >> kc) & 1u)) continue;
+                        const uint32_t cg = g + (uint32_t)ci;
+                        const int st = (int)(cg % (uint32_t)NS);
+                        const uint32_t u = cg / (uint32_t)NS;
                         uint8_t* base = smem + st * sbytes;
                         float* Ahi = reinterpret_cast<float*>(base);
                         float* Alo = Ahi + TM * KC;
                         float* Bhi = Alo + TM * KC;
                         float* Blo = Bhi + a.Ws * KC;
-                        tc::mbar_expect_tx(&bar_full[st], (uint32_t)((2 * TM + 2 * W) * KC * sizeof(float)));
-                        const int vrow = (int)(vrow_cta + (int64_t)P.slot[c.node] * TM);
-                        for (int r = 0; r < TM / 32; ++r) {
-                            tc::tma_load_2d(Ahi + r * 32 * KC, &map_vhi, kc * KC, vrow + 32 * r, &bar_full[st]);
-                            tc::tma_load_2d(Alo + r * 32 * KC, &map_vlo, kc * KC, vrow + 32 * r, &bar_full[st]);
+                        const bool with_lo = !leaf || a.err != nullptr;
+                        if (leaf) {
+                            // the stage must be free before the threads write its A tile;
+                            // on a time-out every thread still walks the same barriers
+                            if (tid == 0 && !abort_sh && u >= 1 && !tc::mbar_wait(&bar_empty[st], (u - 1) & 1)) {
+                                atomicExch(a.status, 1);
+                                abort_sh = 1;
+                            }
+                            __syncthreads();
+                            if (!abort_sh) {
+                                write_leaf_row(Ahi, tid, lw[c], kc, false);
+                                if (with_lo) write_leaf_row(Alo, tid, lw[c], kc, true);
+                                tc::fence_proxy_async_shared();
+                            }
+                            __syncthreads();
                         }
-                        const int mrow = c.mat * Wm;
-                        for (int r = 0; r < W / 32; ++r) {
-                            tc::tma_load_2d(Bhi + r * 32 * KC, &map_mhi, kc * KC, mrow + 32 * r, &bar_full[st]);
-                            tc::tma_load_2d(Blo + r * 32 * KC, &map_mlo, kc * KC, mrow + 32 * r, &bar_full[st]);
-                        }
-                        last_full = st;
-                        last_full_parity = u & 1;
-                        return true;
-                    };
-                    bool ok = issue(0);
-                    for (int i = 0; i < total && ok; ++i) {
-                        // with two stages the next chunk's TMA overlaps this chunk's MMAs
-                        if (NS > 1 && i + 1 < total) ok = issue(i + 1);
-                        const uint32_t ci = g + (uint32_t)i;
-                        const int st = (int)(ci % (uint32_t)NS);
-                        if (ok) ok = tc::mbar_wait(&bar_full[st], (ci / (uint32_t)NS) & 1);
-                        if (!ok) break;
-                        tc::fence_after();
-                        const ChildInfo& c = child_of(i / kpc);
-                        const int kc = i % kpc;
-                        uint8_t* base = smem + st * sbytes;
-                        const float* Ahi = reinterpret_cast<const float*>(base);
-                        const float* Alo = Ahi + TM * KC;
-                        const float* Bhi = Alo + TM * KC;
-                        const float* Blo = Bhi + a.Ws * KC;
-                        const uint32_t d = tmem + (uint32_t)c.tcol;
+                        if (tid == 0 && !abort_sh) {
+                            bool ok = true;
+                            if (!leaf && u >= 1) ok = tc::mbar_wait(&bar_empty[st], (u - 1) & 1);
+                            if (ok) {
+                                const uint32_t bytes = (uint32_t)((leaf ? 0 : 2 * TM) + 2 * W) * KC * sizeof(float);
+                                tc::mbar_expect_tx(&bar_full[st], bytes);
+                                if (!leaf) {
+                                    const int vrow = (int)(vrow_cta + (int64_t)P.slot[chi.node] * TM);
+                                    for (int r = 0; r < TM / 32; ++r) {
+                                        tc::tma_load_2d(Ahi + r * 32 * KC, &map_vhi, kc * KC, vrow + 32 * r, &bar_full[st]);
+                                        tc::tma_load_2d(Alo + r * 32 * KC, &map_vlo, kc * KC, vrow + 32 * r, &bar_full[st]);
+                                    }
+                                }
+                                const int mrow = chi.mat * Wm;
+                                for (int r = 0; r < W / 32; ++r) {
+                                    tc::tma_load_2d(Bhi + r * 32 * KC, &map_mhi, kc * KC, mrow + 32 * r, &bar_full[st]);
+                                    tc::tma_load_2d(Blo + r * 32 * KC, &map_mlo, kc * KC, mrow + 32 * r, &bar_full[st]);
+                                }
+                                last_full = st;
+                                last_full_parity = u & 1;
+                                ok = tc::mbar_wait(&bar_full[st], u & 1);
+                            }
+                            if (ok) {
+                                tc::fence_after();
+                                const uint32_t d = tmem + (uint32_t)chi.tcol;
 #pragma unroll
-                        for (int ks = 0; ks < KC / 8; ++ks) {
-                            const uint64_t ah = tc::desc_sw128(Ahi + ks * 8), al = tc::desc_sw128(Alo + ks * 8);
-                            const uint64_t bh = tc::desc_sw128(Bhi + ks * 8), bl = tc::desc_sw128(Blo + ks * 8);
-                            tc::mma_tf32(d, ah, bh, idesc, (kc | ks) != 0);
-                            tc::mma_tf32(d, ah, bl, idesc, 1);
-                            tc::mma_tf32(d, al, bh, idesc, 1);
+                                for (int ks = 0; ks < KC / 8; ++ks) {
+                                    const uint64_t ah = tc::desc_sw128(Ahi + ks * 8), al = tc::desc_sw128(Alo + ks * 8);
+                                    const uint64_t bh = tc::desc_sw128(Bhi + ks * 8), bl = tc::desc_sw128(Blo + ks * 8);
+                                    tc::mma_tf32(d, ah, bh, idesc, (first && ks == 0) ? 0u : 1u);
+                                    tc::mma_tf32(d, ah, bl, idesc, 1);
+                                    if (with_lo) tc::mma_tf32(d, al, bh, idesc, 1);
+                                }
+                                tc::mma_commit(&bar_empty[st]);
+                            } else {
+                                atomicExch(a.status, 1);
+                                abort_sh = 1;
+                            }
                         }
-                        tc::mma_commit(&bar_empty[st]);
-                        if (NS == 1 && i + 1 < total) ok = issue(i + 1);
-                    }
-                    if (ok) {
-                        tc::mma_commit(&bar_done);
-                        g += (uint32_t)total;
-                    } else {
-                        atomicExch(a.status, 1);
-                        abort_sh = 1;
+                        first = false;
+                        ++ci;
                     }
                 }
+                if (tid == 0 && !abort_sh) tc::mma_commit(&bar_done);
+                g += (uint32_t)ci;        // every thread tracks the stage sequence
                 __syncthreads();
                 if (!abort_sh) {
                     if (!tc::mbar_wait(&bar_done, dn & 1)) {
@@ -552,36 +490,70 @@ __global__ void __launch_bounds__(NTHREADS, 4)
             long long t1 = timing ? clock64() : 0;
 
             // ---------------- epilogue: product over children ----------------
-            EpiOut eo;
-            float* rowhi = a.vec_hi + (size_t)(vrow_cta + (int64_t)vs * TM + tid) * Wm;
-            float* rowlo = a.vec_lo + (size_t)(vrow_cta + (int64_t)vs * TM + tid) * Wm;
-            bool need;
-            epi_fast<2>(ns2, W, is_root, Rf, prior_f, rowhi, rowlo, eo, need);
-            if (__any_sync(0xffffffffu, need)) epi_exact<2>(ns2, W, is_root, Rf, prior_f, rowhi, rowlo, need, eo);
+            float scl[2] = {1.0f, 1.0f};
+            int E = ns2.Eacc;
+            bool nflag = ns2.flag;
+            float maxp, bf, bp, bq;
+            epi_scan<2>(ns2, W, is_root, Rf, prior_f, scl, maxp, bf, bp, bq);
+            const bool need = is_root ? !(bf > 0.0f) : !(maxp >= 0x1p-120f);
+            if (!is_root && !need && maxp < 0x1p-32f) {
+                // bring this row's maximum back to [0.5, 1)
+                const int kk = -bexp(maxp);
+                scl[0] = pow2f(kk);
+                E -= kk;
+            }
+            if (__any_sync(0xffffffffu, need)) {
+                // underflow: rescale by the largest per-state exponent sum, so the
+                // product's maximum is in [2^-2, 1) unless the factors are more
+                // than 2^250 apart (then FP64 recomputes the family)
+                int maxe = epi_maxexp<2>(ns2, W, is_root ? 1 : 0, is_root ? Rf + 1 : W);
+                if (need) {
+                    if (maxe < -250) {
+                        nflag = true;
+                        maxe = 0;
+                    }
+                    const int sh = -maxe, part = sh / 2;
+                    scl[0] = pow2f(part + (sh - part * 2));
+                    scl[1] = pow2f(part);
+                    E = ns2.Eacc + maxe;
+                }
+                if (is_root) {
+                    float m2, f2, p2, q2;
+                    epi_scan<2>(ns2, W, true, Rf, prior_f, scl, m2, f2, p2, q2);
+                    if (need) {
+                        bf = f2;
+                        bp = p2;
+                        bq = q2;
+                    }
+                }
+            }
             long long t2 = timing ? clock64() : 0;
-            flag |= eo.flag;
+            flag |= nflag;
             if (!is_root) {
-                Esh[vs * TM + tid] = eo.E;
+                float* stg_hi = reinterpret_cast<float*>(smem);               // stage 0 as staging tile
+                float* stg_lo = stg_hi + TM * KC;
+                epi_store<2>(ns2, W, scl, stg_hi, stg_lo, tid, &map_vhi, &map_vlo, (int)(vrow_cta + (int64_t)vs * TM));
+                Esh[vs * TM + tid] = E;
             } else if (fam >= 0) {
                 double o = NAN;
-                if (eo.best > 0.0 && !flag)
-                    o = log(eo.best * a.cat_probs[k]) + (double)eo.E * 0.69314718055994530942;
+                const double best = (double)bp * (double)bq;
+                if (best > 0.0 && !flag)
+                    o = log(best * a.cat_probs[k]) + (double)E * 0.69314718055994530942;
                 else flag = true;
                 a.out[(size_t)fam * a.K + k] = o;
             }
-            // node vectors are read back by TMA (async proxy) for the parent
             long long t3 = timing ? clock64() : 0;
-            if (timing) t2 = t3;
-            tc::fence_proxy_async_global();
             tc::fence_before();
             __syncthreads();
             tc::fence_after();
             if (timing) {
                 const long long t4 = clock64();
-                ph[0] += t1 - t0;
-                ph[1] += t2 - t1;
-                ph[2] += t3 - t2;
-                ph[3] += t4 - t3;
+                ph[0] += t0 - ts;     // child setup
+                ph[1] += t1 - t0;     // GEMMs (issue, TMA and MMA latency)
+                ph[2] += t2 - t1;     // epilogue scan (and exact rescale)
+                ph[3] += t3 - t2;     // epilogue store (TMA) or root weighting
+                ph[4] += t4 - t3;     // end-of-node fence and barrier
+                ph[5] += 1;           // tile-nodes
             }
         }
         if (flag && fam >= 0) {
@@ -593,8 +565,9 @@ __global__ void __launch_bounds__(NTHREADS, 4)
     }
 
     if (timing)
-        for (int q = 0; q < 4; ++q) atomicAdd(&a.phase_clocks[q], ph[q]);
+        for (int q = 0; q < 6; ++q) atomicAdd(&a.phase_clocks[q], ph[q]);
     // teardown: no copy of ours may still be landing when TMEM goes away
+    if (tid == 0) tc::bulk_wait0();
     tc::fence_before();
     __syncthreads();
     if (abort_sh && tid == 0 && last_full >= 0) tc::mbar_wait(&bar_full[last_full], last_full_parity, 1 << 20);
@@ -602,8 +575,7 @@ __global__ void __launch_bounds__(NTHREADS, 4)
     if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)a.tmem_cols);
 }
 
-// FP64 matrix -> TF32 hi/lo operands (row-major) and the FP32
-// column-normalised transposed copy used for leaf columns.
+// FP64 matrix -> TF32 hi/lo operands (row-major, pitch Wm).
 __global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict__ jobs, TcBuffers b) {
     const ConvertJob J = jobs[blockIdx.x];
     const int Wm = b.Wm;
@@ -614,18 +586,6 @@ __global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict
         const float h = tc::round_tf32(x);
         b.hi[base + idx] = h;
         b.lo[base + idx] = tc::round_tf32(x - h);
-    }
-    for (int c = threadIdx.x; c < Wm; c += blockDim.x) {
-        double mx = 0.0;
-        for (int s = 0; s < Wm; ++s) {
-            const double x = J.src[(size_t)s * J.ld + c];
-            mx = x > mx ? x : mx;
-        }
-        int e = 0;
-        if (mx > 0.0) frexp(mx, &e);
-        b.ce[(size_t)J.mat * Wm + c] = e;
-        float* row = b.ct + base + (size_t)c * Wm;
-        for (int s = 0; s < Wm; ++s) row[s] = (float)scalbn(J.src[(size_t)s * J.ld + c], -e);
     }
 }
 

@@ -44,7 +44,21 @@ CAFE_DEV void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint6
         "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
         : "memory");
 }
+// 2D TMA tile store from shared memory (bulk-group completion).
+CAFE_DEV void tma_store_2d(const CUtensorMap* map, int x, int y, const void* src) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"((uint64_t)map),
+                 "r"(x), "r"(y), "r"(smem_u32(src))
+                 : "memory");
+}
+CAFE_DEV void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// The shared-memory sources of this thread's bulk stores may be reused.
+CAFE_DEV void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// This thread's bulk stores are complete in global memory.
+CAFE_DEV void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 CAFE_DEV void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+// Generic-proxy writes to this CTA's shared memory become visible to the
+// async proxy (TMA, tcgen05.mma operand reads).
+CAFE_DEV void fence_proxy_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms
 // 1024 bytes apart (stride byte offset), descriptor version 1.
@@ -114,6 +128,13 @@ CAFE_DEV void tmem_ld16_issue(uint32_t taddr, uint32_t (&r)[16]) {
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
           "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
+}
+CAFE_DEV void tmem_ld_issue(uint32_t taddr, uint32_t (&r)[16]) { tmem_ld16_issue(taddr, r); }
+// 32 lanes x 8 consecutive columns, issue only.
+CAFE_DEV void tmem_ld_issue(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
 }
 CAFE_DEV void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 

@@ -158,6 +158,18 @@ class Context:
         """cafe_score_batch: candidates is a sequence of dicts with `lambdas`
         (and for the gamma model `multipliers`, `cat_probs`); every other
         request field is shared (keyword arguments as for score())."""
+        arr, keep = self._batch_requests(tree_id, set_id, candidates, kw)
+        reqs = list(arr)
+        n = len(reqs)
+        F = self._set_shape.get(set_id, (0,))[0]
+        fams = [np.zeros(F) for _ in range(n)]
+        cats = [np.zeros((F, r.n_categories)) if want_categories else None for r in reqs]
+        res = (_lib.Result * n)(*[_lib.Result(_p(fams[i]), _p(cats[i]), 0.0, 0, 0, 0, 0.0) for i in range(n)])
+        self._check(self.lib.cafe_score_batch(self.h, C.cast(arr, C.c_void_p), n, C.cast(res, C.c_void_p)))
+        return [ScoreResult(res[i].total_neg_lnl, fams[i], cats[i], res[i].status, res[i].n_failed, res[i].n_fallback,
+                            res[i].device_ms) for i in range(n)]
+
+    def _batch_requests(self, tree_id, set_id, candidates, kw):
         reqs, keep = [], []
         for cand in candidates:
             ck = dict(kw)
@@ -167,15 +179,13 @@ class Context:
             r, k = self.make_request(tree_id, set_id, cand["lambdas"], **ck)
             reqs.append(r)
             keep.append(k)
-        n = len(reqs)
-        arr = (_lib.Request * n)(*reqs)
-        F = self._set_shape.get(set_id, (0,))[0]
-        fams = [np.zeros(F) for _ in range(n)]
-        cats = [np.zeros((F, r.n_categories)) if want_categories else None for r in reqs]
-        res = (_lib.Result * n)(*[_lib.Result(_p(fams[i]), _p(cats[i]), 0.0, 0, 0, 0, 0.0) for i in range(n)])
-        self._check(self.lib.cafe_score_batch(self.h, C.cast(arr, C.c_void_p), n, C.cast(res, C.c_void_p)))
-        return [ScoreResult(res[i].total_neg_lnl, fams[i], cats[i], res[i].status, res[i].n_failed, res[i].n_fallback,
-                            res[i].device_ms) for i in range(n)]
+        return (_lib.Request * len(reqs))(*reqs), keep
+
+    def score_batch_device(self, tree_id, set_id, candidates, d_family_lnl=0, d_total=0, stream=0, **kw):
+        """cafe_score_batch_device: d_family_lnl [n][F], d_total [n] (device pointers)."""
+        arr, keep = self._batch_requests(tree_id, set_id, candidates, kw)
+        self._check(self.lib.cafe_score_batch_device(self.h, C.cast(arr, C.c_void_p), len(arr), d_family_lnl or None,
+                                                     d_total or None, stream or None))
 
     def score_device(self, tree_id, set_id, lambdas, d_family_lnl=0, d_total=0, stream=0, **kw):
         req, keep = self.make_request(tree_id, set_id, lambdas, **kw)

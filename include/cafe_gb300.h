@@ -171,6 +171,10 @@ int cafe_score_batch(cafe_ctx* ctx, const cafe_request* reqs, int n, cafe_result
  * res->status and counters are not filled. */
 int cafe_score_device(cafe_ctx* ctx, const cafe_request* req, double* d_family_lnl, double* d_total,
                       void* stream);
+/* Device-resident batch (the requests of cafe_score_batch): d_family_lnl
+ * is [n][n_families], d_total [n]. */
+int cafe_score_batch_device(cafe_ctx* ctx, const cafe_request* reqs, int n, double* d_family_lnl, double* d_total,
+                            void* stream);
 
 /* Continuous-batching request loop for many concurrent optimizers: submit
  * returns at once with a ticket; the request is admitted when a stream and
