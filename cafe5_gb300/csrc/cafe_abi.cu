@@ -468,8 +468,10 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-// 2D FP32 tensor map [rows][cols], 32 x 32 boxes, 128-byte swizzle.
-int encode_map(cafe_ctx* C, CUtensorMap* m, const float* base, int64_t rows, int cols) {
+// 2D FP32 tensor map [rows][cols] with 32-row boxes: box_cols = 16 uses the
+// 64-byte swizzle (operand loads), box_cols = 32 the 128-byte swizzle
+// (node-vector stores).
+int encode_map(cafe_ctx* C, CUtensorMap* m, const float* base, int64_t rows, int cols, int box_cols) {
     static EncodeTiledFn enc = nullptr;
     if (!enc) {
         cudaDriverEntryPointQueryResult q;
@@ -482,19 +484,21 @@ int encode_map(cafe_ctx* C, CUtensorMap* m, const float* base, int64_t rows, int
     }
     cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)cols * sizeof(float)};
-    cuuint32_t box[2] = {32, 32};
+    cuuint32_t box[2] = {(cuuint32_t)box_cols, 32};
     cuuint32_t es[2] = {1, 1};
+    const CUtensorMapSwizzle sw = box_cols == 16 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B;
     const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, es,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(C, CAFE_ERR_CUDA, "tensor map encode failed (%d)", (int)r);
     return CAFE_OK;
 }
 
-int cached_map(cafe_ctx* C, Workspace& ws, int slot, CUtensorMap* out, const float* base, int64_t rows, int cols) {
+int cached_map(cafe_ctx* C, Workspace& ws, int slot, CUtensorMap* out, const float* base, int64_t rows, int cols,
+               int box_cols) {
     Workspace::MapCache& mc = ws.map_cache[slot];
-    if (mc.ptr != base || mc.rows != rows || mc.cols != cols) {
-        int rc = encode_map(C, &mc.map, base, rows, cols);
+    if (mc.ptr != base || mc.rows != rows || mc.cols != cols || mc.box != box_cols) {
+        int rc = encode_map(C, &mc.map, base, rows, cols, box_cols);
         if (rc) {
             mc.ptr = nullptr;
             return rc;
@@ -502,6 +506,7 @@ int cached_map(cafe_ctx* C, Workspace& ws, int slot, CUtensorMap* out, const flo
         mc.ptr = base;
         mc.rows = rows;
         mc.cols = cols;
+        mc.box = box_cols;
     }
     *out = mc.map;
     return CAFE_OK;
@@ -720,9 +725,10 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             L.tmem_cols = 32;
             while (L.tmem_cols < 2 * L.W) L.tmem_cols *= 2;
             const int by_tmem = 512 / L.tmem_cols;
+            // most CTAs per SM first, then the deepest pipeline that keeps them
             int best_per = 0;
-            for (int st = 2; st >= 1; --st) {
-                const size_t sm = prune_tc_smem_bytes(L.W, T.n_slots, st);
+            for (int st = 4; st >= 1; --st) {
+                const size_t sm = prune_tc_smem_bytes(L.W, T.n_slots, st, (int)T.internal.size());
                 const int by_smem = (int)((227 * 1024) / (sm + 1024));
                 const int per = std::min(by_tmem, by_smem);
                 if (per > best_per) {
@@ -746,10 +752,13 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         CK(ws.tc_vhi.reserve((size_t)vrows * Wm * sizeof(float)), "tc vectors");
         CK(ws.tc_vlo.reserve((size_t)vrows * Wm * sizeof(float)), "tc vectors");
         TcMaps maps;
-        int rc = cached_map(C, ws, 0, &maps.mat_hi, ws.tc_hi.as<float>(), (int64_t)n_mat * Wm, Wm);
-        if (!rc) rc = cached_map(C, ws, 1, &maps.mat_lo, ws.tc_lo.as<float>(), (int64_t)n_mat * Wm, Wm);
-        if (!rc) rc = cached_map(C, ws, 2, &maps.vec_hi, ws.tc_vhi.as<float>(), vrows, Wm);
-        if (!rc) rc = cached_map(C, ws, 3, &maps.vec_lo, ws.tc_vlo.as<float>(), vrows, Wm);
+        const int kbox = prune_tc_kchunk();
+        int rc = cached_map(C, ws, 0, &maps.mat_hi, ws.tc_hi.as<float>(), (int64_t)n_mat * Wm, Wm, kbox);
+        if (!rc) rc = cached_map(C, ws, 1, &maps.mat_lo, ws.tc_lo.as<float>(), (int64_t)n_mat * Wm, Wm, kbox);
+        if (!rc) rc = cached_map(C, ws, 2, &maps.vec_hi, ws.tc_vhi.as<float>(), vrows, Wm, kbox);
+        if (!rc) rc = cached_map(C, ws, 3, &maps.vec_lo, ws.tc_vlo.as<float>(), vrows, Wm, kbox);
+        if (!rc) rc = cached_map(C, ws, 4, &maps.vst_hi, ws.tc_vhi.as<float>(), vrows, Wm, 32);
+        if (!rc) rc = cached_map(C, ws, 5, &maps.vst_lo, ws.tc_vlo.as<float>(), vrows, Wm, 32);
         if (rc) return rc;
         const int n_tc = (int)tc_tiles.size();
         CK(ws.tiles.reserve(n_tc * sizeof(PruneTile)), "tiles");

@@ -149,19 +149,23 @@ struct PruneTcArgs {
     int32_t* status;             // [1] nonzero when a bounded wait gave up
     int tmem_cols;
     int Ws;                      // widest bin of this launch (shared-memory B rows)
-    int stages;                  // shared-memory stages (1 or 2)
+    int stages;                  // pipeline stages (1 to 4)
     int64_t vrow_base;           // first node-vector row of this launch
     unsigned long long* phase_clocks;   // optional [6]: SM clocks of thread 0 in child setup, GEMMs,
                                         // epilogue, root bookkeeping, end-of-node barrier; tile-nodes
 };
 
 // Tensor maps travel by value (__grid_constant__); the host encodes them.
+// Operand loads use prune_tc_kchunk()-column boxes (mat_*, vec_*; 128-byte
+// swizzle for 32 columns, 64-byte for 16); the epilogue stores node vectors
+// in 32-column boxes in the 128-byte swizzle (vst_*). Boxes are 32 rows.
 struct TcMaps {
-    CUtensorMap mat_hi, mat_lo, vec_hi, vec_lo;
+    CUtensorMap mat_hi, mat_lo, vec_hi, vec_lo, vst_hi, vst_lo;
 };
 
 cudaError_t launch_prune_tc(const TcMaps& maps, const PruneTcArgs& a, int n_ctas, size_t smem, cudaStream_t s);
-size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages);
+size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages, int n_internal);
+int prune_tc_kchunk();   // K columns per operand box of k_prune_tc (its load maps' box width)
 
 // Device-side plan of the FP64 recompute of flagged families: compacts the
 // flagged families of each listed bin (in permutation order) into fb_perm

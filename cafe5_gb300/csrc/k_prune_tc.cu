@@ -46,7 +46,16 @@ namespace cafe {
 namespace {
 
 constexpr int TM = 128;   // families per tile = MMA M = TMEM lanes
-constexpr int KC = 32;    // K per stage: 32 fp32 = one 128-byte swizzle row
+#ifndef CAFE_TC_KC
+#define CAFE_TC_KC 32
+#endif
+// K per stage: 32 fp32 = one 128-byte swizzle row, or 16 fp32 = one 64-byte
+// swizzle row. Shared memory bounds the operand bytes in flight per SM
+// either way; 32-column chunks halve the per-chunk issue and barrier costs.
+constexpr int KC = CAFE_TC_KC;
+static_assert(KC == 32 || KC == 16, "K chunk of 16 or 32 columns");
+constexpr int SC = 32;    // columns per staging tile of the epilogue's TMA stores (128-byte swizzle)
+constexpr int MAXST = 4;  // pipeline stages at most
 constexpr int NTHREADS = 128;
 #ifndef CAFE_TC_CW
 #define CAFE_TC_CW 16
@@ -57,6 +66,13 @@ constexpr int NTHREADS = 128;
 constexpr int CW = CAFE_TC_CW;   // epilogue columns per TMEM load
 
 __host__ __device__ inline size_t stage_bytes(int Ws) { return (size_t)(2 * TM + 2 * Ws) * KC * sizeof(float); }
+__device__ __forceinline__ uint64_t desc_k(const void* p) { return KC == 32 ? tc::desc_sw128(p) : tc::desc_sw64(p); }
+
+// Pipeline stages, also home of the epilogue's 32 KB staging tile.
+__host__ __device__ inline size_t stages_region(int Ws, int stages) {
+    const size_t st = (size_t)stages * stage_bytes(Ws), stg = (size_t)2 * TM * SC * sizeof(float);
+    return st > stg ? st : stg;
+}
 
 __device__ __forceinline__ int bexp(float y) {
     // binary exponent e with y = m 2^e, m in [0.5, 1); zero -> very negative
@@ -71,10 +87,21 @@ __device__ __forceinline__ float pow2f(int a) {
 }
 
 struct ChildInfo {
-    int node;
+    int slot;       // scratch slot of an internal child's vector
     int leaf_col;   // >= 0: leaf
     int mat;
-    int tcol;       // TMEM column base of the child's factor
+    int tcol;       // TMEM column base of the child's factor, in units of W
+};
+
+// One internal node of the post-order walk, as the tile's table in shared
+// memory holds it (filled once per tile: the matrices depend on the tile's
+// category).
+struct NodeInfo {
+    int slot;
+    int nch;
+    int is_root;
+    int pad;
+    ChildInfo c[2];
 };
 
 // Per-child source of the factor: TMEM columns, or the unit factor of an
@@ -100,8 +127,8 @@ struct LeafW {
 
 template <int NC>
 __device__ __forceinline__ void setup_src(const PruneTcArgs& a, const ChildInfo* ch, int nch, const int* Esh,
-                                          uint32_t tmem_lane, int64_t fam, int tid, int S, NodeSrc<NC>& ns,
-                                          LeafW (&lw)[NC], int* cmask_sh) {
+                                          uint32_t tmem_lane, int64_t fam, int tid, int S, int W,
+                                          const int (&count)[NC], NodeSrc<NC>& ns, LeafW (&lw)[NC], int* cmask_sh) {
     ns.Eacc = 0;
     ns.flag = false;
 #pragma unroll
@@ -118,13 +145,13 @@ __device__ __forceinline__ void setup_src(const PruneTcArgs& a, const ChildInfo*
         sc.taddr = 0;
         if (sc.unit) continue;
         const ChildInfo ci = ch[c];
-        sc.taddr = tmem_lane + (uint32_t)ci.tcol;
+        sc.taddr = tmem_lane + (uint32_t)(ci.tcol * W);
         if (ci.leaf_col < 0) {
-            ns.Eacc += Esh[a.plan.slot[ci.node] * TM + tid];
+            ns.Eacc += Esh[ci.slot * TM + tid];
             continue;
         }
         if (fam < 0) continue;        // padding row: zero factor
-        const int n = __ldg(a.counts + (size_t)fam * a.plan.n_leaves + ci.leaf_col);
+        const int n = count[c];
         unsigned bits = 0;
         if (a.err) {
             const double* pr = a.err + (size_t)(n < a.err_rows ? n : a.err_rows - 1) * a.err_ndev;
@@ -151,11 +178,11 @@ __device__ __forceinline__ void setup_src(const PruneTcArgs& a, const ChildInfo*
 }
 
 // This thread's row of the leaf A tile for K chunk kc (columns
-// [kc KC, kc KC + KC)), written into the 128-byte-swizzled K-major layout
-// the MMA descriptor reads: row r of an 8-row, 1024-byte atom keeps its
-// 16-byte piece j at position j ^ (r % 8).
+// [kc KC, kc KC + KC)), written into the swizzled K-major layout the MMA
+// descriptor reads: a 128-byte row r keeps its 16-byte piece j at
+// j ^ (r % 8); a 64-byte row at j ^ ((r >> 1) % 4).
 __device__ __forceinline__ void write_leaf_row(float* tile, int r, const LeafW& L, int kc, bool lo) {
-    uint8_t* row = reinterpret_cast<uint8_t*>(tile) + (size_t)(r >> 3) * 1024 + (size_t)(r & 7) * 128;
+    uint8_t* row = reinterpret_cast<uint8_t*>(tile) + (size_t)r * (KC * sizeof(float));
     const int c0 = kc * KC;
 #pragma unroll
     for (int j = 0; j < KC / 4; ++j) {
@@ -167,7 +194,8 @@ __device__ __forceinline__ void write_leaf_row(float* tile, int r, const LeafW& 
             for (int e = 0; e < 4; ++e)
                 if (q == e) v[e] = lo ? L.lo[d] : L.hi[d];
         }
-        *reinterpret_cast<float4*>(row + ((j ^ (r & 7)) << 4)) = make_float4(v[0], v[1], v[2], v[3]);
+        const int pj = KC == 32 ? (j ^ (r & 7)) : (j ^ ((r >> 1) & 3));
+        *reinterpret_cast<float4*>(row + (pj << 4)) = make_float4(v[0], v[1], v[2], v[3]);
     }
 }
 
@@ -266,12 +294,12 @@ __device__ __forceinline__ void epi_store(const NodeSrc<NC>& ns, int W, const fl
                                           int vrow) {
     uint8_t* row_hi = reinterpret_cast<uint8_t*>(stg_hi) + (size_t)(tid >> 3) * 1024 + (size_t)(tid & 7) * 128;
     uint8_t* row_lo = reinterpret_cast<uint8_t*>(stg_lo) + (size_t)(tid >> 3) * 1024 + (size_t)(tid & 7) * 128;
-    for (int c32 = 0; c32 < W; c32 += KC) {
+    for (int c32 = 0; c32 < W; c32 += SC) {
         if (c32 > 0) {
             if (tid == 0) tc::bulk_wait_read0();     // the previous chunk's stores have read the tile
             __syncthreads();
         }
-        for (int col0 = c32; col0 < c32 + KC; col0 += CW) {
+        for (int col0 = c32; col0 < c32 + SC; col0 += CW) {
             uint32_t r[NC][CW];
             load_children(ns, col0, r);
             float p[CW];
@@ -302,8 +330,8 @@ __device__ __forceinline__ void epi_store(const NodeSrc<NC>& ns, int W, const fl
         __syncthreads();
         if (tid == 0) {
             for (int r = 0; r < TM / 32; ++r) {
-                tc::tma_store_2d(map_hi, c32, vrow + 32 * r, stg_hi + r * 32 * KC);
-                tc::tma_store_2d(map_lo, c32, vrow + 32 * r, stg_lo + r * 32 * KC);
+                tc::tma_store_2d(map_hi, c32, vrow + 32 * r, stg_hi + r * 32 * SC);
+                tc::tma_store_2d(map_lo, c32, vrow + 32 * r, stg_lo + r * 32 * SC);
             }
             tc::bulk_commit();
         }
@@ -313,14 +341,14 @@ __device__ __forceinline__ void epi_store(const NodeSrc<NC>& ns, int W, const fl
 __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
     k_prune_tc(const __grid_constant__ CUtensorMap map_mhi, const __grid_constant__ CUtensorMap map_mlo,
                const __grid_constant__ CUtensorMap map_vhi, const __grid_constant__ CUtensorMap map_vlo,
+               const __grid_constant__ CUtensorMap map_shi, const __grid_constant__ CUtensorMap map_slo,
                const PruneTcArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    __shared__ __align__(8) uint64_t bar_full[2], bar_empty[2], bar_done;
+    __shared__ __align__(8) uint64_t bar_full[MAXST], bar_empty[MAXST], bar_done;
     __shared__ uint32_t tmem_sh;
     __shared__ int abort_sh;
-    __shared__ ChildInfo ch_sh[8];
-    __shared__ int cmask_sh[2];     // per child: K chunks holding a leaf column of the tile
+    __shared__ int cmask_sh[2][2];  // [node parity][child]: K chunks holding a leaf column of the tile
     __shared__ float prior_f[256];
 
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -328,15 +356,16 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
     const int NS = a.stages;
     const TreePlan& P = a.plan;
     const size_t sbytes = stage_bytes(a.Ws);
-    int* Esh = reinterpret_cast<int*>(smem + NS * sbytes);   // [n_slots][TM]
+    int* Esh = reinterpret_cast<int*>(smem + stages_region(a.Ws, NS));   // [n_slots][TM]
+    NodeInfo* nodes = reinterpret_cast<NodeInfo*>(Esh + (size_t)a.n_slots * TM);   // [n_internal]
 
     for (int j = tid; j < 256; j += NTHREADS) prior_f[j] = j < a.n_prior ? (float)a.prior[j] : 0.0f;
     if (warp == 0) tc::tmem_alloc(&tmem_sh, (uint32_t)a.tmem_cols);
     if (tid == 0) {
-        tc::mbar_init(&bar_full[0], 1);
-        tc::mbar_init(&bar_full[1], 1);
-        tc::mbar_init(&bar_empty[0], 1);
-        tc::mbar_init(&bar_empty[1], 1);
+        for (int q = 0; q < MAXST; ++q) {
+            tc::mbar_init(&bar_full[q], 1);
+            tc::mbar_init(&bar_empty[q], 1);
+        }
         tc::mbar_init(&bar_done, 1);
         tc::mbar_init_fence();
         abort_sh = 0;
@@ -349,8 +378,8 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
 
     uint32_t g = 0;          // chunks issued so far (same in every thread)
     uint32_t dn = 0;         // completions of bar_done observed (all threads)
-    int last_full = -1;      // stage of the last issued TMA (thread 0)
-    uint32_t last_full_parity = 0;
+    int last_full[MAXST] = {0, 0, 0, 0};            // thread 0: stage has a TMA not yet waited for
+    uint32_t last_full_parity[MAXST] = {0, 0, 0, 0};
     const int64_t vrow_cta = a.vrow_base + (int64_t)blockIdx.x * a.n_slots * TM;
     unsigned long long ph[6] = {0, 0, 0, 0, 0, 0};
     const bool timing = a.phase_clocks != nullptr && tid == 0;
@@ -364,49 +393,92 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
         const uint32_t idesc = tc::idesc_tf32(TM, W);
         bool flag = false;
 
-        for (int ii = 0; ii < P.n_internal; ++ii) {
+        // the tile's walk: children, matrices and slots of every internal node
+        for (int ii = tid; ii < P.n_internal; ii += NTHREADS) {
             const int v = P.internal[ii];
-            const bool is_root = (v == P.root);
-            const int vs = P.slot[v];
-            const int c0 = P.cstart[ii], c1 = P.cstart[ii + 1];
-            const int nch = c1 - c0;
-            const long long ts = timing ? clock64() : 0;
-            if (tid == 0) {
-                for (int c = c0; c < c1; ++c) {
-                    ChildInfo ci;
-                    ci.node = P.child[c];
-                    ci.leaf_col = P.leaf_col[ci.node];
-                    ci.mat = mi[ci.node];
-                    ci.tcol = (c - c0) * W;
-                    ch_sh[c - c0] = ci;
+            NodeInfo e;
+            e.slot = P.slot[v];
+            e.is_root = v == P.root;
+            e.nch = P.cstart[ii + 1] - P.cstart[ii];
+            e.pad = 0;
+            for (int c = 0; c < 2; ++c) {
+                ChildInfo ci{0, -1, 0, c};
+                if (c < e.nch) {
+                    const int ch = P.child[P.cstart[ii] + c];
+                    ci.slot = P.slot[ch];
+                    ci.leaf_col = P.leaf_col[ch];
+                    ci.mat = mi[ch];
                 }
-                cmask_sh[0] = 0;
-                cmask_sh[1] = 0;
+                e.c[c] = ci;
             }
-            __syncthreads();
+            nodes[ii] = e;
+        }
+        if (tid == 0) {
+            cmask_sh[0][0] = cmask_sh[0][1] = 0;
+            cmask_sh[1][0] = cmask_sh[1][1] = 0;
+        }
+        __syncthreads();
+        const int32_t* fam_counts = a.counts + (size_t)(fam >= 0 ? fam : 0) * P.n_leaves;
+        int cnt_next[2] = {0, 0};
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+            if (fam >= 0 && c < nodes[0].nch && nodes[0].c[c].leaf_col >= 0)
+                cnt_next[c] = __ldg(fam_counts + nodes[0].c[c].leaf_col);
+
+        for (int ii = 0; ii < P.n_internal; ++ii) {
+            const NodeInfo nd = nodes[ii];
+            const bool is_root = nd.is_root != 0;
+            const int vs = nd.slot;
+            const int nch = nd.nch;
+            int* cmask = cmask_sh[ii & 1];
+            const long long ts = timing ? clock64() : 0;
+            // the previous nodes' TMA stores must be complete before this node
+            // overwrites their staging tile or reads their rows back
+            if (tid == 0) tc::bulk_wait0();
             // child sources; leaf weights and the K chunks they touch
             NodeSrc<2> ns2;
             LeafW lw[2];
-            setup_src<2>(a, ch_sh, nch, Esh, tmem + lane_base, fam, tid, S, ns2, lw, cmask_sh);
+            const int cnt_cur[2] = {cnt_next[0], cnt_next[1]};
+            setup_src<2>(a, nd.c, nch, Esh, tmem + lane_base, fam, tid, S, W, cnt_cur, ns2, lw, cmask);
+            // counts of the next node's leaves, in flight during this node
+            if (ii + 1 < P.n_internal) {
+                const NodeInfo& nx = nodes[ii + 1];
+#pragma unroll
+                for (int c = 0; c < 2; ++c)
+                    cnt_next[c] = (fam >= 0 && c < nx.nch && nx.c[c].leaf_col >= 0) ? __ldg(fam_counts + nx.c[c].leaf_col) : 0;
+            }
             __syncthreads();
 
             // ---------------- one GEMM per child into TMEM ----------------
+            // K chunks of both children form one list (CTA-uniform); thread 0
+            // runs the TMA loads up to NS - 1 chunks ahead of the MMAs. A leaf
+            // chunk's A tile is written by all threads into its stage.
             long long t0 = timing ? clock64() : 0;
-            // the previous nodes' TMA stores must be complete: their staging
-            // tile is about to be overwritten and their rows may be read back
-            if (tid == 0) tc::bulk_wait0();
             {
                 const int kpc = W / KC;             // K chunks per child
-                int ci = 0;                         // chunks issued for this node
-                for (int c = 0; c < nch; ++c) {
-                    const ChildInfo chi = ch_sh[c];
-                    const bool leaf = chi.leaf_col >= 0;
-                    unsigned mask = leaf ? (unsigned)cmask_sh[c] : ((1u << kpc) - 1);
-                    if (!mask) mask = 1;            // all-zero leaf tile: still initialise D
-                    bool first = true;
-                    for (int kc = 0; kc < kpc; ++kc) {
-                        if (!((mask >> kc) & 1u)) continue;
-                        const uint32_t cg = g + (uint32_t)ci;
+                unsigned cm[2];
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    if (c >= nch) {
+                        cm[c] = 0;
+                    } else if (nd.c[c].leaf_col >= 0) {
+                        cm[c] = (unsigned)cmask[c];
+                        if (!cm[c]) cm[c] = 1;      // all-zero leaf tile: still initialise D
+                    } else {
+                        cm[c] = (1u << kpc) - 1;
+                    }
+                }
+                const int n0 = __popc(cm[0]);
+                const int n_chunks = n0 + __popc(cm[1]);
+                for (int i = 0; i < n_chunks + NS - 1; ++i) {
+                    // ---- produce chunk i ----
+                    if (i < n_chunks) {
+                        const int c = i < n0 ? 0 : 1;
+                        const int kc = (int)__fns(cm[c], 0, (c == 0 ? i : i - n0) + 1);
+                        const ChildInfo chi = nd.c[c];
+                        const bool leaf = chi.leaf_col >= 0;
+                        const bool with_lo = !leaf || a.err != nullptr;
+                        const uint32_t cg = g + (uint32_t)i;
                         const int st = (int)(cg % (uint32_t)NS);
                         const uint32_t u = cg / (uint32_t)NS;
                         uint8_t* base = smem + st * sbytes;
@@ -414,15 +486,33 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                         float* Alo = Ahi + TM * KC;
                         float* Bhi = Alo + TM * KC;
                         float* Blo = Bhi + a.Ws * KC;
-                        const bool with_lo = !leaf || a.err != nullptr;
-                        if (leaf) {
-                            // the stage must be free before the threads write its A tile;
-                            // on a time-out every thread still walks the same barriers
-                            if (tid == 0 && !abort_sh && u >= 1 && !tc::mbar_wait(&bar_empty[st], (u - 1) & 1)) {
-                                atomicExch(a.status, 1);
-                                abort_sh = 1;
+                        // the first NS chunks of a node find their stages free: the
+                        // previous node's MMAs completed before its epilogue and its
+                        // staging-tile stores were waited for at the node start
+                        if (tid == 0 && !abort_sh && i >= NS && !tc::mbar_wait(&bar_empty[st], (u - 1) & 1)) {
+                            atomicExch(a.status, 1);
+                            abort_sh = 1;
+                        }
+                        if (leaf && i >= NS) __syncthreads();      // stage free for every writer
+                        if (tid == 0 && !abort_sh) {
+                            tc::mbar_expect_tx(&bar_full[st], (uint32_t)(((leaf ? 0 : 2 * TM) + 2 * W) * KC * sizeof(float)));
+                            if (!leaf) {
+                                const int vrow = (int)(vrow_cta + (int64_t)chi.slot * TM);
+                                for (int r = 0; r < TM / 32; ++r) {
+                                    tc::tma_load_2d(Ahi + r * 32 * KC, &map_vhi, kc * KC, vrow + 32 * r, &bar_full[st]);
+                                    tc::tma_load_2d(Alo + r * 32 * KC, &map_vlo, kc * KC, vrow + 32 * r, &bar_full[st]);
+                                }
                             }
-                            __syncthreads();
+                            const int mrow = chi.mat * Wm;
+                            for (int r = 0; r < W / 32; ++r) {
+                                tc::tma_load_2d(Bhi + r * 32 * KC, &map_mhi, kc * KC, mrow + 32 * r, &bar_full[st]);
+                                tc::tma_load_2d(Blo + r * 32 * KC, &map_mlo, kc * KC, mrow + 32 * r, &bar_full[st]);
+                            }
+                            last_full[st] = 1;
+                            last_full_parity[st] = u & 1;
+                        }
+                        if (leaf) {
+                            // on a time-out every thread still walks the same barriers
                             if (!abort_sh) {
                                 write_leaf_row(Ahi, tid, lw[c], kc, false);
                                 if (with_lo) write_leaf_row(Alo, tid, lw[c], kc, true);
@@ -430,51 +520,43 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                             }
                             __syncthreads();
                         }
-                        if (tid == 0 && !abort_sh) {
-                            bool ok = true;
-                            if (!leaf && u >= 1) ok = tc::mbar_wait(&bar_empty[st], (u - 1) & 1);
-                            if (ok) {
-                                const uint32_t bytes = (uint32_t)((leaf ? 0 : 2 * TM) + 2 * W) * KC * sizeof(float);
-                                tc::mbar_expect_tx(&bar_full[st], bytes);
-                                if (!leaf) {
-                                    const int vrow = (int)(vrow_cta + (int64_t)P.slot[chi.node] * TM);
-                                    for (int r = 0; r < TM / 32; ++r) {
-                                        tc::tma_load_2d(Ahi + r * 32 * KC, &map_vhi, kc * KC, vrow + 32 * r, &bar_full[st]);
-                                        tc::tma_load_2d(Alo + r * 32 * KC, &map_vlo, kc * KC, vrow + 32 * r, &bar_full[st]);
-                                    }
-                                }
-                                const int mrow = chi.mat * Wm;
-                                for (int r = 0; r < W / 32; ++r) {
-                                    tc::tma_load_2d(Bhi + r * 32 * KC, &map_mhi, kc * KC, mrow + 32 * r, &bar_full[st]);
-                                    tc::tma_load_2d(Blo + r * 32 * KC, &map_mlo, kc * KC, mrow + 32 * r, &bar_full[st]);
-                                }
-                                last_full = st;
-                                last_full_parity = u & 1;
-                                ok = tc::mbar_wait(&bar_full[st], u & 1);
-                            }
-                            if (ok) {
-                                tc::fence_after();
-                                const uint32_t d = tmem + (uint32_t)chi.tcol;
+                    }
+                    // ---- consume chunk j = i - (NS - 1) ----
+                    const int j = i - (NS - 1);
+                    if (j >= 0 && tid == 0 && !abort_sh) {
+                        const int c = j < n0 ? 0 : 1;
+                        const bool first = j == 0 || j == n0;
+                        const ChildInfo chi = nd.c[c];
+                        const bool with_lo = chi.leaf_col < 0 || a.err != nullptr;
+                        const uint32_t cg = g + (uint32_t)j;
+                        const int st = (int)(cg % (uint32_t)NS);
+                        const uint32_t u = cg / (uint32_t)NS;
+                        uint8_t* base = smem + st * sbytes;
+                        const float* Ahi = reinterpret_cast<const float*>(base);
+                        const float* Alo = Ahi + TM * KC;
+                        const float* Bhi = Alo + TM * KC;
+                        const float* Blo = Bhi + a.Ws * KC;
+                        if (tc::mbar_wait(&bar_full[st], u & 1)) {
+                            last_full[st] = 0;
+                            tc::fence_after();
+                            const uint32_t d = tmem + (uint32_t)(chi.tcol * W);
 #pragma unroll
-                                for (int ks = 0; ks < KC / 8; ++ks) {
-                                    const uint64_t ah = tc::desc_sw128(Ahi + ks * 8), al = tc::desc_sw128(Alo + ks * 8);
-                                    const uint64_t bh = tc::desc_sw128(Bhi + ks * 8), bl = tc::desc_sw128(Blo + ks * 8);
-                                    tc::mma_tf32(d, ah, bh, idesc, (first && ks == 0) ? 0u : 1u);
-                                    tc::mma_tf32(d, ah, bl, idesc, 1);
-                                    if (with_lo) tc::mma_tf32(d, al, bh, idesc, 1);
-                                }
-                                tc::mma_commit(&bar_empty[st]);
-                            } else {
-                                atomicExch(a.status, 1);
-                                abort_sh = 1;
+                            for (int ks = 0; ks < KC / 8; ++ks) {
+                                const uint64_t ah = desc_k(Ahi + ks * 8), al = desc_k(Alo + ks * 8);
+                                const uint64_t bh = desc_k(Bhi + ks * 8), bl = desc_k(Blo + ks * 8);
+                                tc::mma_tf32(d, ah, bh, idesc, (first && ks == 0) ? 0u : 1u);
+                                tc::mma_tf32(d, ah, bl, idesc, 1);
+                                if (with_lo) tc::mma_tf32(d, al, bh, idesc, 1);
                             }
+                            tc::mma_commit(&bar_empty[st]);
+                        } else {
+                            atomicExch(a.status, 1);
+                            abort_sh = 1;
                         }
-                        first = false;
-                        ++ci;
                     }
                 }
                 if (tid == 0 && !abort_sh) tc::mma_commit(&bar_done);
-                g += (uint32_t)ci;        // every thread tracks the stage sequence
+                g += (uint32_t)n_chunks;        // every thread tracks the stage sequence
                 __syncthreads();
                 if (!abort_sh) {
                     if (!tc::mbar_wait(&bar_done, dn & 1)) {
@@ -487,6 +569,10 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             }
             __syncthreads();
             if (abort_sh) break;
+            if (tid == 0) {
+                cmask_sh[(ii + 1) & 1][0] = 0;
+                cmask_sh[(ii + 1) & 1][1] = 0;
+            }
             long long t1 = timing ? clock64() : 0;
 
             // ---------------- epilogue: product over children ----------------
@@ -531,8 +617,8 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             flag |= nflag;
             if (!is_root) {
                 float* stg_hi = reinterpret_cast<float*>(smem);               // stage 0 as staging tile
-                float* stg_lo = stg_hi + TM * KC;
-                epi_store<2>(ns2, W, scl, stg_hi, stg_lo, tid, &map_vhi, &map_vlo, (int)(vrow_cta + (int64_t)vs * TM));
+                float* stg_lo = stg_hi + TM * SC;
+                epi_store<2>(ns2, W, scl, stg_hi, stg_lo, tid, &map_shi, &map_slo, (int)(vrow_cta + (int64_t)vs * TM));
                 Esh[vs * TM + tid] = E;
             } else if (fam >= 0) {
                 double o = NAN;
@@ -570,7 +656,9 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
     if (tid == 0) tc::bulk_wait0();
     tc::fence_before();
     __syncthreads();
-    if (abort_sh && tid == 0 && last_full >= 0) tc::mbar_wait(&bar_full[last_full], last_full_parity, 1 << 20);
+    if (abort_sh && tid == 0)
+        for (int q = 0; q < MAXST; ++q)
+            if (q < NS && last_full[q]) tc::mbar_wait(&bar_full[q], last_full_parity[q], 1 << 20);
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)a.tmem_cols);
 }
@@ -661,8 +749,10 @@ cudaError_t launch_fallback_plan(const FallbackPlanArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages) {
-    return (size_t)stages * stage_bytes(Ws) + (size_t)n_slots * TM * sizeof(int) + 1024;
+int prune_tc_kchunk() { return KC; }
+
+size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages, int n_internal) {
+    return stages_region(Ws, stages) + (size_t)n_slots * TM * sizeof(int) + (size_t)n_internal * sizeof(NodeInfo) + 1024;
 }
 
 cudaError_t launch_convert_tc(const ConvertJob* d_jobs, int n_jobs, TcBuffers b, cudaStream_t s) {
@@ -675,7 +765,8 @@ cudaError_t launch_prune_tc(const TcMaps& m, const PruneTcArgs& a, int n_ctas, s
     if (a.n_tiles <= 0) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(k_prune_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_prune_tc<<<n_ctas, NTHREADS, smem, s>>>(m.mat_hi, m.mat_lo, m.vec_hi, m.vec_lo, a);
+    if (a.stages < 1 || a.stages > MAXST) return cudaErrorInvalidValue;
+    k_prune_tc<<<n_ctas, NTHREADS, smem, s>>>(m.mat_hi, m.mat_lo, m.vec_hi, m.vec_lo, m.vst_hi, m.vst_lo, a);
     return cudaGetLastError();
 }
 

@@ -108,8 +108,9 @@ struct Workspace {
         const void* ptr = nullptr;
         int64_t rows = 0;
         int cols = 0;
+        int box = 0;
         CUtensorMap map;
-    } map_cache[4];
+    } map_cache[6];
     DevBuf scratch, tiles, mats, cat, fam_lnl, total, nfail, jobs, catp;
     PinnedBuf h_tiles, h_mats, h_jobs, h_out, h_catp;
     // tensor-core path

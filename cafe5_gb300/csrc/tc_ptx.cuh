@@ -66,6 +66,12 @@ CAFE_DEV uint64_t desc_sw128(const void* p) {
     const uint64_t a = (uint64_t)(smem_u32(p) & 0x3FFFF) >> 4;
     return a | (1ull << 16) | (64ull << 32) | (1ull << 46) | (2ull << 61);
 }
+// Shared-memory matrix descriptor: K-major, 64-byte swizzle, 8-row groups
+// 512 bytes apart (stride byte offset), descriptor version 1.
+CAFE_DEV uint64_t desc_sw64(const void* p) {
+    const uint64_t a = (uint64_t)(smem_u32(p) & 0x3FFFF) >> 4;
+    return a | (1ull << 16) | (32ull << 32) | (1ull << 46) | (4ull << 61);
+}
 // Instruction descriptor, kind::tf32: D = F32, A = B = TF32, both K-major.
 CAFE_DEV uint32_t idesc_tf32(int M, int N) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
