@@ -1,21 +1,35 @@
-"""Benchmark of the CAFE5 likelihood hot path on one GB300.
+"""Benchmark of the CAFE5 likelihood hot path on GB300.
 
-Workload: 24-taxon Yule tree (root age 150), 10,000 families, gamma model
-with K = 4 categories (alpha = 0.5): the gamma configuration the headline
-metric is quoted on. Synthetic, seeded (no public dataset exists for this
-path). A "step" is one infer_family_likelihoods evaluation over all
-families at a new lambda (as one optimizer step: matrices are rebuilt for
-the new lambda every step). One family-lnL evaluation is one family's lnL
-with all K categories.
+Workload: 24-taxon Yule tree (root age 150), 10,000 families per GPU, gamma
+model with K = 4 categories (alpha = 0.5): the gamma configuration the
+headline metric is quoted on. Synthetic and seeded (no public dataset exists
+for this path). A "step" is one batched score of B candidate parameter
+vectors (lambda and alpha of B concurrent optimizer steps) over every
+family: the transition matrices of the step's new lambdas are built, every
+family is pruned in every category of every candidate, and each candidate's
+-lnL is reduced. One family-lnL evaluation is one family's lnL for one
+candidate with all K categories, so a step is B x F evaluations.
 
-  value   family-lnL evals/s with inputs resident in HBM (cafe_score_device),
-          CUDA events on the launching stream, L2 flushed between steps
-  e2e     the same through the public API (cafe_families_update from pinned
-          host memory + cafe_score copying per-family lnL back), host clock
+  value        mixed-precision (TF32x3 tensor-core) evals/s with inputs
+               resident in HBM (cafe_score_batch_device), CUDA events on the
+               launching stream, L2 flushed between steps (256 MB write)
+  fp64_paths   the plain FP64 GPU paths on the same steps: FP64_BINNED (same
+               per-family state bins) and FP64_REF (the reference's global
+               bounds); `mixed_over_fp64` is value / FP64_BINNED
+  e2e          the same metric through the public API with host buffers:
+               cafe_families_update from pinned host memory, cafe_score_batch
+               copying every candidate's per-family lnL back; host clock
+  serving      closed-loop clients (one optimizer each) submitting
+               single-candidate requests to the continuous-batching loop
+               (cafe_submit / cafe_poll): throughput, p50 and p99 latency
+  accuracy     max relative |dlnL| per family of the mixed path vs FP64_BINNED
+
+Under torchrun each rank scores its own shard of world x 10,000 families
+(weak scaling; the candidates' totals are combined across ranks).
 
 `--impl reference` times the reference algorithm on the host cores instead
-(the compiled reference when it exists on this machine, else the CPU
-oracle that restates it).
+(the CPU oracle that restates it; the compiled reference does not exist on
+the GPU machine).
 """
 from __future__ import annotations
 
@@ -24,6 +38,7 @@ import json
 import os
 import subprocess
 import sys
+import threading
 import time
 
 import numpy as np
@@ -31,7 +46,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "family-lnL evals/s (gamma K=4, 24 taxa, 10k families; batched, dLnL<=1e-6 vs FP64)"
+METRIC = "family-lnL evals/s, batched mixed-prec vs plain FP64 GPU (dLnL<=1e-6); p99 ms"
 
 
 def parse():
@@ -40,9 +55,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default=os.environ.get("CAFE_BENCH_PRECISION", "auto"))
-    ap.add_argument("--families", type=int, default=10000)
+    ap.add_argument("--precision", default=os.environ.get("CAFE_BENCH_PRECISION", "mixed_tf32x3"))
+    ap.add_argument("--families", type=int, default=10000, help="families per GPU")
+    ap.add_argument("--candidates", type=int, default=16, help="candidate parameter vectors per step")
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--serving-clients", type=int, default=8)
+    ap.add_argument("--serving-requests", type=int, default=12, help="requests per client")
     return ap.parse_args()
 
 
@@ -171,6 +190,35 @@ def cpu_baseline(w, S, R, seconds: float, threads: int):
                       f"{done_fam // len(sample)} evaluations, matrices rebuilt each evaluation"}
 
 
+def candidates(w, B: int, step: int):
+    """B candidate (lambda, alpha) vectors around the simulating values, as B
+    concurrent optimizer steps would propose them; new lambdas every step."""
+    from cafe5_gb300.inputs import discrete_gamma
+    out = []
+    for b in range(B):
+        alpha = w.alpha * (1.0 + 0.02 * b)
+        probs, mult = discrete_gamma(alpha, len(w.multipliers))
+        # every step's lambdas are new (new matrices) but stay within 1 % of
+        # the simulating value: far from the saturation bound lambda*m*t < 1
+        out.append(dict(lambdas=[w.true_lambda * (1.0 + 0.01 * b) * (1.0 + 1e-6 * (step % 10000))],
+                        multipliers=mult, cat_probs=probs))
+    return out
+
+
+def profiled_traffic(kernel: str, workload_name: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary of
+    this workload (profiles/), or None when no capture covers it."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        d = json.load(open(path))
+        e = d.get(kernel, {})
+        if e.get("workload") == workload_name:
+            return e.get("bytes_per_launch"), e.get("source")
+    except Exception:
+        pass
+    return None, None
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -186,7 +234,7 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
             "config": {"workload": w.name, "families": args.families, "taxa": 24, "K": 4, "alpha": 0.5,
-                       "S": S, "R": R},
+                       "S": S, "R": R, "candidates_per_step": 1},
             "cpu_baseline": base,
             "e2e": {"value": base["value"], "unit": "family-lnL evals/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -194,11 +242,60 @@ def run_reference(args):
     return 0
 
 
+def time_steps(ctx, torch, stream, flush, tid, sid, w, B, steps, warmup, d_fam, d_tot, kw, step0=0):
+    """Device time (ms) of `steps` batched scores after `warmup` untimed ones."""
+    for i in range(warmup):
+        ctx.score_batch_device(tid, sid, candidates(w, B, step0 - 1 - i), d_fam.data_ptr(), d_tot.data_ptr(),
+                               stream.cuda_stream, **kw)
+    torch.cuda.synchronize()
+    total = 0.0
+    for i in range(steps):
+        cands = candidates(w, B, step0 + i)
+        flush.fill_(float(i))                      # evict L2 between steps (untimed)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.score_batch_device(tid, sid, cands, d_fam.data_ptr(), d_tot.data_ptr(), stream.cuda_stream, **kw)
+        e1.record(stream)
+        e1.synchronize()
+        total += e0.elapsed_time(e1)
+    return total
+
+
+def serving_phase(ctx, tid, sid, w, clients: int, per_client: int, kw):
+    """Closed-loop optimizer clients on the continuous-batching loop."""
+    lat = []
+    lock = threading.Lock()
+
+    def client(c):
+        for r in range(per_client):
+            cand = candidates(w, 1, 5000 + 100 * c + r)[0]
+            t0 = time.perf_counter()
+            h = ctx.submit(tid, sid, cand["lambdas"], multipliers=cand["multipliers"], cat_probs=cand["cat_probs"],
+                           **kw)
+            ctx.poll(h, -1)
+            with lock:
+                lat.append((time.perf_counter() - t0) * 1e3)
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=client, args=(c,)) for c in range(clients)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    wall = time.perf_counter() - t0
+    lat.sort()
+    pct = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]
+    return {"clients": clients, "requests": len(lat), "evals_per_s": len(lat) * w.families.n_families / wall,
+            "p50_ms": pct(0.5), "p99_ms": pct(0.99), "unit": "family-lnL evals/s",
+            "note": "single-candidate requests from concurrent closed-loop optimizer clients, merged by the continuous-batching loop; latency submit -> done"}
+
+
 def run_ours(args):
     import torch
     from cafe5_gb300.engine import Context
-    from cafe5_gb300.families import bin_families
+    from cafe5_gb300.families import FamilySet, bin_families
     from cafe5_gb300.inputs import RootPrior
+    from cafe5_gb300.shard import allgather_totals, shard_range
 
     rank, world, local = dist_env()
     if world > 1:
@@ -207,102 +304,121 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
 
-    w = workload(args.families)
-    F = w.families.n_families
-    S, R = global_bounds(w.families)
+    # weak scaling: world x F families, this rank's contiguous shard
+    wall_fams = workload(args.families * world)
+    lo, hi = shard_range(wall_fams.families.n_families, rank, world)
+    w = wall_fams
+    fams = FamilySet(w.families.ids[lo:hi], np.ascontiguousarray(w.families.counts[lo:hi]))
+    F = fams.n_families
+    B = max(1, args.candidates)
+    S, R = global_bounds(fams)
     prec = args.precision
-    if prec == "auto":
-        prec = "mixed_tf32x3"
-    Wb, Sb, Rb = bin_families(w.families)
+    Wb, Sb, Rb = bin_families(fams)
     prior = RootPrior.uniform(max(R, int(Wb.max()) + 8)).vector()
 
     ctx = Context(device=local)
     tid = ctx.upload_tree(w.tree)
-    sid = ctx.upload_families(tid, w.families.counts)
+    sid = ctx.upload_families(tid, fams.counts)
     ctx.set_prior(prior)
     ctx.set_error_model(None)
-    kw = dict(model=1, multipliers=w.multipliers, cat_probs=w.cat_probs, precision=prec,
-              S=S if prec == "fp64_ref" else 0, R=R if prec == "fp64_ref" else 0)
+
+    def kw_for(p):
+        return dict(model=1, precision=p, S=S if p == "fp64_ref" else 0, R=R if p == "fp64_ref" else 0)
+
+    kw = kw_for(prec)
     # a dedicated stream: the legacy default stream has handle 0, which the
     # C ABI reads as "the context's own stream"
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
-    d_fam = torch.empty(F, dtype=torch.float64, device=dev)
-    d_tot = torch.empty(1, dtype=torch.float64, device=dev)
+    d_fam = torch.empty(B * F, dtype=torch.float64, device=dev)
+    d_tot = torch.empty(B, dtype=torch.float64, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > 129 MB L2
 
-    def lam_of(step):
-        return [w.true_lambda * (1.0 + 1e-4 * step)]
-
-    # warm-up
-    for i in range(args.warmup):
-        ctx.score_device(tid, sid, lam_of(-1 - i), d_fam.data_ptr(), d_tot.data_ptr(), stream.cuda_stream, **kw)
+    # warm-up, then the timed steps (barrier + synchronize on both sides)
+    time_steps(ctx, torch, stream, flush, tid, sid, w, B, 0, args.warmup, d_fam, d_tot, kw)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-
     clocks = ClockSampler(local)
     clocks.start()
     ctx.profile(True)
     ctx.profile_read()
-    total_ms = 0.0
-    for i in range(args.steps):
-        flush.fill_(float(i))                       # evict L2 between steps (untimed)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        ctx.score_device(tid, sid, lam_of(i), d_fam.data_ptr(), d_tot.data_ptr(), stream.cuda_stream, **kw)
-        e1.record(stream)
-        e1.synchronize()
-        total_ms += e0.elapsed_time(e1)
+    total_ms = time_steps(ctx, torch, stream, flush, tid, sid, w, B, args.steps, 0, d_fam, d_tot, kw)
     torch.cuda.synchronize()
     prof = ctx.profile_read()
     ctx.profile(False)
     clk = clocks.stop()
     if world > 1:
+        torch.distributed.barrier()
         t = torch.tensor([total_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
-    value = F * world * args.steps / (total_ms / 1e3)
+    value = B * F * world * args.steps / (total_ms / 1e3)
+    step_totals = allgather_totals(d_tot.cpu().numpy().tolist()) if world > 1 else d_tot.cpu().numpy().tolist()
+
+    # the plain FP64 GPU paths on the same kind of steps
+    fp64 = {}
+    for p in ("fp64_binned", "fp64_ref"):
+        if p == prec:
+            continue
+        ms = time_steps(ctx, torch, stream, flush, tid, sid, w, B, max(1, args.fp64_steps), 1, d_fam, d_tot,
+                        kw_for(p), step0=20000)
+        fp64[p] = {"value": B * F * world * max(1, args.fp64_steps) / (ms / 1e3), "ms_per_step":
+                   ms / max(1, args.fp64_steps)}
 
     # end to end through the public API, host buffers
-    pinned = torch.empty((F, w.families.counts.shape[1]), dtype=torch.int32, pin_memory=True)
-    pinned.numpy()[:] = w.families.counts
+    pinned = torch.empty((F, fams.counts.shape[1]), dtype=torch.int32, pin_memory=True)
+    pinned.numpy()[:] = fams.counts
     host_counts = pinned.numpy()
     e2e_ms = 0.0
     n_e2e = max(3, min(args.steps, 10))
-    last = None
     for i in range(n_e2e + 1):
         flush.fill_(float(i))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ctx.update_families(sid, host_counts)
-        last = ctx.score(tid, sid, lam_of(1000 + i), **kw)
+        res = ctx.score_batch(tid, sid, candidates(w, B, 1000 + i), **kw)
         dt = (time.perf_counter() - t0) * 1e3
         if i > 0:
             e2e_ms += dt
-    e2e_value = F * world * n_e2e / (e2e_ms / 1e3)
+    e2e_value = B * F * world * n_e2e / (e2e_ms / 1e3)
 
-    # accuracy of this path vs FP64 at the same bins (dLnL per family)
-    ref64 = ctx.score(tid, sid, lam_of(0), **dict(kw, precision="fp64_binned"))
-    cur = ctx.score(tid, sid, lam_of(0), **kw)
-    dl = np.abs(cur.family_lnl - ref64.family_lnl) / np.maximum(np.abs(ref64.family_lnl), 1e-300)
+    # accuracy of this path vs FP64 at the same bins (dLnL per family, per candidate)
+    cands = candidates(w, B, 0)
+    ref64 = ctx.score_batch(tid, sid, cands, **kw_for("fp64_binned"))
+    cur = ctx.score_batch(tid, sid, cands, **kw)
+    dl = max(float(np.max(np.abs(c.family_lnl - r.family_lnl) / np.maximum(np.abs(r.family_lnl), 1e-300)))
+             for c, r in zip(cur, ref64))
+    n_fb = int(max(c.n_fallback for c in cur))
+
+    serving = None
+    if rank == 0 and args.serving_clients > 0:
+        serving = serving_phase(ctx, tid, sid, w, args.serving_clients, args.serving_requests, kw)
 
     peaks = measured_peaks()
     fp64_peak = fp64_peak_tflops(torch, dev)
-    achieved = prof["prune_flops"] / max(prof["prune_launches"], 1) / (prof["prune_ms"] / max(prof["prune_launches"], 1) / 1e3) / 1e12 if prof["prune_ms"] > 0 else 0.0
+    nl = max(prof["prune_launches"], 1)
+    achieved = prof["prune_flops"] / nl / (prof["prune_ms"] / nl / 1e3) / 1e12 if prof["prune_ms"] > 0 else 0.0
     if prec.startswith("mixed"):
         roof = {"bound": "tensor", "achieved": achieved, "peak": peaks.get("bf16_tflops", 1900.0),
-                "unit": "TFLOP/s", "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)"}
+                "unit": "TFLOP/s",
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)" if "bf16_tflops" in peaks
+                else "fallback 1.9 PFLOP/s bf16 (of fallback)"}
     else:
         roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                 "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FP64 pipe)"}
     roof["frac"] = roof["achieved"] / roof["peak"] if roof["peak"] else None
-    roof["traffic"] = None
-    roof["kernel"] = "k_prune64" if not prec.startswith("mixed") else "k_prune_tc"
-    roof["other_ms_per_step"] = prof["other_ms"] / args.steps
+    kernel = "k_prune64" if not prec.startswith("mixed") else "k_prune_tc"
+    traffic, tsrc = profiled_traffic(kernel, w.name + f"_B{B}")
+    roof["traffic"] = traffic
+    roof["traffic_source"] = tsrc
+    roof["kernel"] = kernel
+    roof["achieved_basis"] = ("algorithmic flops of the pruning launches (2 x rows x states per child "
+                              "contraction + child products) / their CUDA-event time")
     roof["prune_ms_per_step"] = prof["prune_ms"] / args.steps
     roof["matrix_ms_per_step"] = prof["matrix_ms"] / args.steps
+    roof["other_ms_per_step"] = prof["other_ms"] / args.steps
     roof["finish_ms_per_step"] = prof["finish_ms"] / args.steps
 
     base = None
@@ -310,21 +426,28 @@ def run_ours(args):
         base = cpu_baseline(w, S, R, args.cpu_seconds, os.cpu_count() or 1)
 
     if rank == 0:
+        fb = fp64.get("fp64_binned", {}).get("value")
         line = {"metric": METRIC, "value": value, "unit": "family-lnL evals/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64" if "fp64" in prec else "tf32x3",
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if "fp64" in prec else "tf32x3",
                 "data": "synthetic",
-                "config": {"workload": w.name, "families": F, "taxa": 24, "K": 4, "alpha": 0.5,
-                           "precision": prec, "bins": sorted(set(int(x) for x in Wb)),
-                           "l2": "flushed between timed steps (256 MB write)", "lambda": "new each step"},
+                "config": {"workload": w.name, "families_per_gpu": F, "taxa": 24, "K": 4, "alpha": 0.5,
+                           "candidates_per_step": B, "precision": prec,
+                           "bins": sorted(set(int(x) for x in Wb)),
+                           "l2": "flushed between timed steps (256 MB write)",
+                           "lambda": "new each step (matrices rebuilt)", "parallelism": f"families sharded x{world}"},
                 "roofline": roof,
+                "fp64_paths": fp64,
+                "mixed_over_fp64": (value / fb) if fb else None,
                 "cpu_baseline": base,
                 "e2e": {"value": e2e_value, "unit": "family-lnL evals/s",
-                        "h2d_bytes_per_step": int(w.families.counts.nbytes), "d2h_bytes_per_step": int(F * 8 + 8)},
+                        "h2d_bytes_per_step": int(fams.counts.nbytes), "d2h_bytes_per_step": int(B * (F * 8 + 8))},
+                "serving": serving,
                 "gpu_launches": int(prof["launches"]),
                 "clocks": clk,
-                "accuracy": {"max_rel_dlnl_vs_fp64": float(np.max(dl)), "n_fallback": int(cur.n_fallback)},
-                "neg_lnl": cur.total}
+                "accuracy": {"max_rel_dlnl_vs_fp64": dl, "n_fallback": n_fb},
+                "neg_lnl": step_totals[0]}
         print(json.dumps(line))
     ctx.close()
     if world > 1:

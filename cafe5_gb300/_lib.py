@@ -26,7 +26,7 @@ EXPORTS = [
     "cafe_matrix_cache_size", "cafe_matrix_cache_clear", "cafe_is_saturated", "cafe_score",
     "cafe_score_device", "cafe_submit", "cafe_poll", "cafe_serving_stats", "cafe_profile_enable",
     "cafe_profile_read", "cafe_prune_fp64_noalloc", "cafe_optimize", "cafe_discrete_gamma",
-    "cafe_nelder_mead", "cafe_score_batch", "cafe_score_batch_device",
+    "cafe_nelder_mead", "cafe_score_batch", "cafe_score_batch_device", "cafe_serving_counters",
 ]
 OPT_LAMBDA, OPT_LAMBDA_ALPHA, OPT_LAMBDA_EPSILON, OPT_ALPHA = 0, 1, 2, 3
 
@@ -67,6 +67,11 @@ OBJECTIVE = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.c_int, C.c_void_p)
 class OptResult(C.Structure):
     _fields_ = [("values", C.c_void_p), ("score", C.c_double), ("iterations", C.c_int),
                 ("evaluations", C.c_int), ("converged", C.c_int)]
+
+
+class ServingInfo(C.Structure):
+    _fields_ = [("batches", C.c_int64), ("merged", C.c_int64), ("retried", C.c_int64), ("enqueue_ms", C.c_double),
+                ("wait_ms", C.c_double), ("device_ms", C.c_double)]
 
 
 _lib = None
@@ -111,6 +116,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
         "cafe_submit": (i, [p, P(Request), P(Result), P(C.c_uint64)]),
         "cafe_poll": (i, [p, C.c_uint64, i]),
         "cafe_serving_stats": (i, [p, P(i64), P(d), P(d), P(i)]),
+        "cafe_serving_counters": (i, [p, P(ServingInfo)]),
         "cafe_profile_enable": (i, [p, i]),
         "cafe_profile_read": (i, [p, P(Timings)]),
         "cafe_prune_fp64_noalloc": (i, [i, p, p, i, p, i64, i, i, i, p, i, i, p, p]),

@@ -27,16 +27,35 @@ namespace cafe {
 const int kDefaultBins[] = {32, 64, 96, 128, 192, 256, 384, 512, 768, 1024};
 const int kNumDefaultBins = sizeof(kDefaultBins) / sizeof(int);
 
+// Stream that device buffers growing on this thread are ordered on (set
+// while a request is enqueued): growth then neither synchronises the device
+// nor waits for other requests' work.
+thread_local cudaStream_t t_alloc_stream = nullptr;
+
+AllocScope::AllocScope(cudaStream_t s) : prev(t_alloc_stream) { t_alloc_stream = s; }
+AllocScope::~AllocScope() { t_alloc_stream = prev; }
+
 DevBuf::~DevBuf() {
     if (p) cudaFree(p);
 }
 cudaError_t DevBuf::reserve(size_t n) {
     if (n <= bytes) return cudaSuccess;
-    if (p) cudaFree(p);
+    const cudaStream_t s = t_alloc_stream;
+    if (p) {
+        if (s) cudaFreeAsync(p, s);
+        else cudaFree(p);
+    }
     p = nullptr;
+    // geometric growth: request sizes that creep up (merged batches) cost
+    // O(log) reallocations
+    size_t want = std::max<size_t>(std::max<size_t>(n, bytes + bytes / 2), 256);
     bytes = 0;
-    size_t want = std::max<size_t>(n, 256);
-    cudaError_t e = cudaMalloc(&p, want);
+    cudaError_t e = s ? cudaMallocAsync(&p, want, s) : cudaMalloc(&p, want);
+    if (e != cudaSuccess && want > n) {
+        cudaGetLastError();
+        want = n;
+        e = s ? cudaMallocAsync(&p, want, s) : cudaMalloc(&p, want);
+    }
     if (e != cudaSuccess) {
         p = nullptr;
         cudaGetLastError();
@@ -376,7 +395,10 @@ int cache_build(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
     if (C->slabs.empty() || C->slabs.back().used + need > C->slabs.back().size) {
         Slab sl;
         sl.size = std::max(need, (size_t)256 << 20);
-        CK(cudaMalloc(&sl.p, sl.size), "matrix cache");
+        // stream-ordered when a request is being enqueued: requests on other
+        // streams reach these matrices only through the build's ready event
+        CK(t_alloc_stream ? cudaMallocAsync(&sl.p, sl.size, t_alloc_stream) : cudaMalloc(&sl.p, sl.size),
+           "matrix cache");
         sl.used = 0;
         C->slabs.push_back(sl);
     }
@@ -737,10 +759,12 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
                     L.smem = sm;
                 }
             }
-            if (best_per < 1) return fail(C, CAFE_ERR_INVALID, "tensor-core tile does not fit shared memory");
+            if (best_per < 1 || L.smem > (size_t)prune_tc_max_smem())
+                return fail(C, CAFE_ERR_INVALID, "tensor-core tile does not fit shared memory");
             L.per_sm = best_per;
             // pad shared memory so no more CTAs of this launch than TMEM allows share an SM
             L.smem = std::max(L.smem, (size_t)((227 * 1024) / L.per_sm) - 2048);
+            L.smem = std::min(L.smem, (size_t)prune_tc_max_smem());
             L.first_tile = (int64_t)i;
             L.n_tiles = (int64_t)(j - i);
             L.n_ctas = (int)std::max<int64_t>(1, std::min<int64_t>(L.n_tiles, (int64_t)C->sm_count * L.per_sm));
@@ -821,6 +845,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
                 CK(cudaStreamWaitEvent(ws.stream, ws.ev_join[q], 0), "join");
             }
         }
+
         if (phase_env) {
             unsigned long long h[6];
             CK(cudaMemcpyAsync(h, ws.phase.p, sizeof(h), cudaMemcpyDeviceToHost, ws.stream), "phase clocks");
@@ -1147,11 +1172,26 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     return finish_batch(C, ws, info, gamma, scaled, dedupe ? S.d_ref.as<int64_t>() : nullptr, nullptr, d_fam, d_total);
 }
 
+// Requests' device timelines run one after another: each waits for the
+// previous request's last launch. Persistent tensor-core CTAs take every
+// register of an SM, so interleaving the launches of concurrent requests
+// would starve their small kernels; ordered, each request runs at full
+// speed while host work and copies of the others overlap. Caller holds C->mu.
+cudaError_t gate_enter(cafe_ctx* C, Workspace& ws) {
+    return C->gate_set ? cudaStreamWaitEvent(ws.stream, C->gate, 0) : cudaSuccess;
+}
+cudaError_t gate_leave(cafe_ctx* C, Workspace& ws) {
+    const cudaError_t e = cudaEventRecord(C->gate, ws.stream);
+    if (e == cudaSuccess) C->gate_set = true;
+    return e;
+}
+
 // Phase 1 of a host-visible score of NB batched candidates: enqueue the
 // evaluation and the copies back into pinned staging (caller holds C->mu).
 // Host staging: totals [NB], fail counts [NB], family lnL [NB][F], then
 // category values [F][NB * K] when any result asks for them.
 int score_enqueue(cafe_ctx* C, Workspace& ws, const cafe_request* R, int NB, cafe_result* res, ScoreInfo* info) {
+    AllocScope scope(ws.stream);
     auto si = C->sets.find(R ? R->set_id : -1);
     if (si == C->sets.end()) return fail(C, CAFE_ERR_NOT_FOUND, "unknown family set");
     if (NB < 1) return fail(C, CAFE_ERR_INVALID, "empty batch");
@@ -1159,8 +1199,10 @@ int score_enqueue(cafe_ctx* C, Workspace& ws, const cafe_request* R, int NB, caf
     CK(ws.fam_lnl.reserve((size_t)std::max<int64_t>(F, 1) * NB * sizeof(double)), "family buffer");
     CK(ws.total.reserve((size_t)NB * sizeof(double)), "total");
     CK(cudaEventRecord(ws.ev_start, ws.stream), "event");
+    CK(gate_enter(C, ws), "gate");
     int rc = enqueue_score(C, ws, R, NB, ws.fam_lnl.as<double>(), ws.total.as<double>(), info);
     if (rc) return rc;
+    CK(gate_leave(C, ws), "gate");
     CK(cudaEventRecord(ws.ev_staged, ws.stream), "event");
     ws.staged = true;
     CK(cudaEventRecord(ws.ev_stop, ws.stream), "event");
@@ -1294,10 +1336,26 @@ int cafe_ctx_create(const cafe_config* cfg, cafe_ctx** out) {
     cudaDeviceProp prop;
     cudaGetDeviceProperties(&prop, dev);
     C->sm_count = prop.multiProcessorCount;
+    if (tc_kernels_init() != cudaSuccess ||
+        cudaEventCreateWithFlags(&C->gate, cudaEventDisableTiming) != cudaSuccess) {
+        delete C;
+        return CAFE_ERR_CUDA;
+    }
     C->n_ctas = prop.multiProcessorCount * 4;
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
     C->cache_cap = (cfg && cfg->matrix_cache_bytes) ? cfg->matrix_cache_bytes : fr / 4;
+    {
+        // stream-ordered buffer growth draws on the device's default pool;
+        // keep what it frees instead of returning it at every synchronisation
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        cudaGetLastError();
+    }
+    C->serve_budget = fr / 4;
     const int n_streams = (cfg && cfg->n_streams > 0) ? cfg->n_streams : 4;
     for (int i = 0; i <= n_streams; ++i) {
         auto w = std::make_unique<Workspace>();
@@ -1319,6 +1377,7 @@ int cafe_ctx_destroy(cafe_ctx* C) {
     cafe_serving_stop(C);
     cudaDeviceSynchronize();
     cache_reset(C);
+    if (C->gate) cudaEventDestroy(C->gate);
     delete C;
     return CAFE_OK;
 }
@@ -1544,6 +1603,7 @@ int cafe_score_batch_device(cafe_ctx* C, const cafe_request* req, int n, double*
     std::lock_guard<std::mutex> lk(C->mu);
     cudaSetDevice(C->device);
     Workspace& ws = *C->ws[0];
+    AllocScope scope(ws.stream);
     cudaStream_t user = static_cast<cudaStream_t>(stream);
     ScoreInfo info;
     auto si = C->sets.find(req ? req->set_id : -1);
@@ -1556,9 +1616,11 @@ int cafe_score_batch_device(cafe_ctx* C, const cafe_request* req, int n, double*
         CK(cudaEventRecord(ws.ev_start, user), "event");
         CK(cudaStreamWaitEvent(ws.stream, ws.ev_start, 0), "event");
     }
+    CK(gate_enter(C, ws), "gate");
     int rc = enqueue_score(C, ws, req, n, d_family_lnl ? d_family_lnl : ws.fam_lnl.as<double>(),
                            d_total ? d_total : ws.total.as<double>(), &info);
     if (rc) return rc;
+    CK(gate_leave(C, ws), "gate");
     CK(cudaEventRecord(ws.ev_staged, ws.stream), "event");
     ws.staged = true;
     if (user) {
@@ -1577,6 +1639,7 @@ struct Request {
     cafe_request req{};
     std::vector<double> lambdas, mult, probs;
     cafe_result* res = nullptr;
+    size_t bytes = 0;          // admission footprint
     int rc = CAFE_OK;
     bool done = false;
     std::chrono::steady_clock::time_point t_submit;
@@ -1587,42 +1650,132 @@ struct Request {
 
 namespace {
 
+// Requests that can share one batched launch: same tree, family set,
+// model, category count, precision and error-model use (and FP64_REF
+// bounds); each keeps its own lambdas, multipliers and probabilities.
+bool batchable(const cafe_request& a, const cafe_request& b) {
+    if (a.tree_id != b.tree_id || a.set_id != b.set_id || a.model != b.model || a.precision != b.precision ||
+        a.use_error_model != b.use_error_model || a.lambda_kind != b.lambda_kind || a.dedupe != b.dedupe ||
+        a.n_lambdas != b.n_lambdas)
+        return false;
+    if (a.model == CAFE_MODEL_GAMMA && a.n_categories != b.n_categories) return false;
+    if (a.precision == CAFE_PREC_FP64_REF &&
+        (a.max_family_size != b.max_family_size || a.max_root_family_size != b.max_root_family_size))
+        return false;
+    return true;
+}
+
+// Device bytes a request holds while admitted: per-family category terms,
+// results and flags (the workspaces' fixed buffers are not counted).
+size_t request_footprint(cafe_ctx* C, const cafe_request& r) {
+    auto it = C->sets.find(r.set_id);
+    const int64_t F = it == C->sets.end() ? 0 : it->second->F;
+    const int K = r.model == CAFE_MODEL_GAMMA ? std::max(r.n_categories, 1) : 1;
+    return (size_t)F * ((size_t)K * 8 + 8 + 4) + 4096;
+}
+
+constexpr int kMaxMerge = 32;           // candidates merged into one batched launch
+constexpr int kMaxBatchesInFlight = 2;  // one on the device, one being enqueued
+
 void server_loop(cafe_ctx* C, int wi) {
     cudaSetDevice(C->device);
     Workspace& ws = *C->ws[wi];
     for (;;) {
-        std::shared_ptr<Request> r;
+        std::vector<std::shared_ptr<Request>> batch;
+        size_t bytes = 0;
         {
             std::unique_lock<std::mutex> lk(C->qmu);
-            C->qcv.wait(lk, [&] { return C->stop || !C->queue.empty(); });
+            // admit when the queue has work and the footprint fits (an idle
+            // loop always admits one request, however large)
+            // (and while at most one other batch is in flight, so requests that
+            // arrive meanwhile queue up and share the next launch)
+            C->qcv.wait(lk, [&] {
+                if (C->stop) return true;
+                if (C->queue.empty() || C->batches_in_flight >= kMaxBatchesInFlight) return false;
+                return C->in_flight == 0 || C->in_flight_bytes + C->queue.front()->bytes <= C->serve_budget;
+            });
             if (C->stop && C->queue.empty()) return;
-            r = C->queue.front();
+            batch.push_back(C->queue.front());
             C->queue.pop_front();
-            C->in_flight++;
+            bytes = batch[0]->bytes;
+            // continuous batching: compatible requests queued behind it join
+            // the same launch
+            for (auto it = C->queue.begin(); it != C->queue.end() && (int)batch.size() < kMaxMerge;) {
+                if (batchable(batch[0]->req, (*it)->req) && C->in_flight_bytes + bytes + (*it)->bytes <= C->serve_budget) {
+                    bytes += (*it)->bytes;
+                    batch.push_back(*it);
+                    it = C->queue.erase(it);
+                } else {
+                    ++it;
+                }
+            }
+            C->in_flight += (int)batch.size();
+            C->in_flight_bytes += bytes;
+            C->batches_in_flight++;
+        }
+        const int n = (int)batch.size();
+        std::vector<cafe_request> reqs(n);
+        std::vector<cafe_result> res(n);
+        for (int i = 0; i < n; ++i) {
+            reqs[i] = batch[i]->req;
+            res[i] = batch[i]->res ? *batch[i]->res : cafe_result{};
         }
         int rc;
         ScoreInfo info;
+        const auto t0 = std::chrono::steady_clock::now();
         {
-            // enqueue under the context lock; the GPU work of this request
-            // then overlaps with requests running on the other streams
+            // enqueue under the context lock; the GPU work of this batch then
+            // overlaps with batches running on the other streams
             std::unique_lock<std::mutex> lk(C->mu);
-            rc = score_enqueue(C, ws, &r->req, 1, r->res, &info);
+            rc = score_enqueue(C, ws, reqs.data(), n, res.data(), &info);
         }
-        if (rc == CAFE_OK) rc = score_complete(C, ws, &r->req, 1, r->res, info);
-        const double ms =
-            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - r->t_submit).count();
+        const auto t1 = std::chrono::steady_clock::now();
+        if (rc == CAFE_OK) rc = score_complete(C, ws, reqs.data(), n, res.data(), info);
+        const auto t2 = std::chrono::steady_clock::now();
+        std::vector<int> rcs(n, rc);
         {
             std::lock_guard<std::mutex> lk(C->qmu);
-            C->in_flight--;
-            C->completed++;
-            C->latencies_ms.push_back(ms);
+            cafe_serving_info& si = C->serving;
+            si.batches++;
+            si.merged += n > 1 ? n : 0;
+            si.retried += (rc != CAFE_OK && n > 1) ? n : 0;
+            si.enqueue_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
+            si.wait_ms += std::chrono::duration<double, std::milli>(t2 - t1).count();
+            if (rc == CAFE_OK) si.device_ms += res[0].device_ms;
         }
+        if (rc != CAFE_OK && n > 1) {
+            // one bad request must not fail the others: run them one by one
+            for (int i = 0; i < n; ++i) {
+                ScoreInfo one;
+                res[i] = batch[i]->res ? *batch[i]->res : cafe_result{};
+                {
+                    std::unique_lock<std::mutex> lk(C->mu);
+                    rcs[i] = score_enqueue(C, ws, &reqs[i], 1, &res[i], &one);
+                }
+                if (rcs[i] == CAFE_OK) rcs[i] = score_complete(C, ws, &reqs[i], 1, &res[i], one);
+            }
+        }
+        const auto now = std::chrono::steady_clock::now();
         {
-            std::lock_guard<std::mutex> lk(r->m);
-            r->rc = rc;
-            r->done = true;
+            std::lock_guard<std::mutex> lk(C->qmu);
+            C->in_flight -= n;
+            C->in_flight_bytes -= bytes;
+            C->batches_in_flight--;
+            C->completed += n;
+            for (auto& r : batch)
+                C->latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
         }
-        r->cv.notify_all();
+        C->qcv.notify_all();     // freed footprint may admit queued requests
+        for (int i = 0; i < n; ++i) {
+            auto& r = batch[i];
+            {
+                std::lock_guard<std::mutex> lk(r->m);
+                if (r->res) *r->res = res[i];
+                r->rc = rcs[i];
+                r->done = true;
+            }
+            r->cv.notify_all();
+        }
     }
 }
 
@@ -1655,6 +1808,10 @@ int cafe_submit(cafe_ctx* C, const cafe_request* req, cafe_result* res, uint64_t
     }
     r->res = res;
     r->t_submit = std::chrono::steady_clock::now();
+    {
+        std::lock_guard<std::mutex> lk(C->mu);
+        r->bytes = request_footprint(C, r->req);
+    }
     std::lock_guard<std::mutex> lk(C->qmu);
     if (C->servers.empty()) {
         C->stop = false;
@@ -1687,6 +1844,13 @@ int cafe_poll(cafe_ctx* C, uint64_t ticket, int wait_ms) {
     std::lock_guard<std::mutex> lk2(C->qmu);
     C->tickets.erase(ticket);
     return rc;
+}
+
+int cafe_serving_counters(cafe_ctx* C, cafe_serving_info* out) {
+    if (!C || !out) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->qmu);
+    *out = C->serving;
+    return CAFE_OK;
 }
 
 int cafe_serving_stats(cafe_ctx* C, int64_t* completed, double* p50, double* p99, int* in_flight) {

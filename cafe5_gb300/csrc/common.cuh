@@ -62,6 +62,9 @@ namespace cafe {
 
 cudaError_t launch_matrix_build(const MatrixJob* d_jobs, int n_jobs, int max_size, cudaStream_t s);
 
+// One-time per-device kernel attributes (shared-memory limits).
+cudaError_t tc_kernels_init();
+
 struct Prune64Args {
     TreePlan plan;
     const PruneTile* tiles;
@@ -166,6 +169,7 @@ struct TcMaps {
 cudaError_t launch_prune_tc(const TcMaps& maps, const PruneTcArgs& a, int n_ctas, size_t smem, cudaStream_t s);
 size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages, int n_internal);
 int prune_tc_kchunk();   // K columns per operand box of k_prune_tc (its load maps' box width)
+int prune_tc_max_smem(); // dynamic shared memory one k_prune_tc CTA may use
 
 // Device-side plan of the FP64 recompute of flagged families: compacts the
 // flagged families of each listed bin (in permutation order) into fb_perm

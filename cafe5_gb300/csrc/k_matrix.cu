@@ -13,8 +13,8 @@
 //    For c < s both coefficients are >= 0, so the forward recurrence only
 //    adds non-negative terms and is stable; it starts at g_0 = a^s.
 //  * The upper triangle follows from c P(s->c) = s P(c->s) (the two
-//    binomial sums differ term by term by the factor s/c), so it is read
-//    from the stably computed lower triangle of row c.
+//    binomial sums differ term by term by the factor s/c): the chain of row
+//    s also writes P(c->s) = (c/s) P(s->c) into rows c < s.
 //  * The running value is kept as mantissa * 2^E so rows whose left end
 //    underflows FP64 (a^s < 1e-308) still reach their diagonal exactly.
 //
@@ -24,6 +24,8 @@
 // matrix_cache.cpp:139-154). Entries are clamped to <= 1 as in
 // probability.cpp:147.
 #include "common.cuh"
+
+#include <algorithm>
 
 namespace cafe {
 namespace {
@@ -36,7 +38,10 @@ __device__ __forceinline__ double out_value(double m, int e) {
     return v < 1.0 ? v : 1.0;
 }
 
-// Lower triangle and diagonal of row s (columns 0..s).
+// Row s of the matrix, columns 0..s, and its mirror: c P(s->c) = s P(c->s)
+// gives the upper-triangle entry P(c->s) = (c/s) P(s->c) of row c < s,
+// written in the same step. Neighbouring threads own neighbouring rows, so
+// the mirror stores of a warp land in one contiguous run of row c.
 __device__ void row_chain(double* __restrict__ M, int W, int s, double alpha, double coeff, double q, double la,
                           const double* __restrict__ inv, const double* __restrict__ bq) {
     double L0 = (double)s * la;  // log(a^s)
@@ -50,9 +55,15 @@ __device__ void row_chain(double* __restrict__ M, int W, int s, double alpha, do
     }
     double mp = 0.0;
     double sm = (double)s, sp = (double)s;  // s - c, s + c
+    const double inv_s = inv[s];
     double* row = M + (size_t)s * W;
     for (int c = 0; c < s; ++c) {
-        row[c] = out_value(m, E);
+        const double v = out_value(m, E);
+        row[c] = v;
+        if (c > 0) {
+            const double u = (double)c * inv_s * v;
+            M[(size_t)c * W + s] = u < 1.0 ? u : 1.0;
+        }
         double a = fma(sm, q, alpha * sp) * inv[c + 1];
         double b = coeff * bq[c];
         double nx = fma(a, m, b * mp);
@@ -69,7 +80,10 @@ __device__ void row_chain(double* __restrict__ M, int W, int s, double alpha, do
     row[s] = out_value(m, E);
 }
 
-__global__ void __launch_bounds__(256) k_matrix_build(const MatrixJob* __restrict__ jobs) {
+// One CTA per matrix; thread p owns rows 1 + p and W - 1 - p (about W
+// recurrence steps each). Row 0 and column 0 of rows >= 1 come from the
+// chains (P(s -> 0) = a^s); M[0][c] = delta(c, 0).
+__global__ void __launch_bounds__(128) k_matrix_build(const MatrixJob* __restrict__ jobs) {
     extern __shared__ double sh[];
     const MatrixJob J = jobs[blockIdx.x];
     const int W = J.size;
@@ -92,23 +106,11 @@ __global__ void __launch_bounds__(256) k_matrix_build(const MatrixJob* __restric
     __syncthreads();
     const double q = coeff / alpha;
     const double la = log(alpha);
-    // rows 1..W-1, paired (1 + p, W - 1 - p) so every thread walks ~W steps
     const int nrows = W - 1;
     for (int p = threadIdx.x; p < (nrows + 1) / 2; p += blockDim.x) {
-        int s1 = 1 + p, s2 = W - 1 - p;
+        const int s1 = 1 + p, s2 = W - 1 - p;
         row_chain(M, W, s1, alpha, coeff, q, la, inv, bq);
         if (s2 != s1) row_chain(M, W, s2, alpha, coeff, q, la, inv, bq);
-    }
-    __syncthreads();
-    // upper triangle: P(s -> c) = (s / c) P(c -> s), 1 <= s < c < W
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int s = 1 + warp; s < W; s += nw) {
-        double ds = (double)s;
-        double* row = M + (size_t)s * W;
-        for (int c = s + 1 + lane; c < W; c += 32) {
-            double v = ds * inv[c] * M[(size_t)c * W + s];
-            row[c] = v < 1.0 ? v : 1.0;
-        }
     }
 }
 
@@ -121,7 +123,10 @@ cudaError_t launch_matrix_build(const MatrixJob* d_jobs, int n_jobs, int max_siz
         cudaError_t e = cudaFuncSetAttribute(k_matrix_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    k_matrix_build<<<n_jobs, 256, smem, s>>>(d_jobs);
+    // one thread per row pair, in whole warps (at most 128)
+    const int pairs = max_size / 2;
+    const int threads = std::min(128, std::max(32, (pairs + 31) / 32 * 32));
+    k_matrix_build<<<n_jobs, threads, smem, s>>>(d_jobs);
     return cudaGetLastError();
 }
 

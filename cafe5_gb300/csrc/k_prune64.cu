@@ -248,6 +248,27 @@ __device__ __forceinline__ void neumaier_add(double& sum, double& comp, double x
 
 constexpr int kFinishThreads = 64;
 
+// Pairwise tree over the block's (sum, compensation, fail, -inf) partials in
+// a fixed order: log2(N) dependent steps instead of N (FP64 latency is long
+// on this part). Deterministic for a given N. Leaves the result in slot 0.
+template <int N>
+__device__ __forceinline__ void block_combine(double* ssum, double* scomp, int* sfail, int* sinf) {
+    __syncthreads();
+#pragma unroll
+    for (int h = N / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+            const int o = threadIdx.x + h;
+            double s = ssum[threadIdx.x], c = scomp[threadIdx.x] + scomp[o];
+            neumaier_add(s, c, ssum[o]);
+            ssum[threadIdx.x] = s;
+            scomp[threadIdx.x] = c;
+            sfail[threadIdx.x] += sfail[o];
+            sinf[threadIdx.x] += sinf[o];
+        }
+        __syncthreads();
+    }
+}
+
 // Candidate b (blockIdx.y here, blockIdx.x in k_finish_total) reads
 // category k of family row r at cat[r * K * n_cand + b * K + k] and writes
 // family_lnl[b * F + f], total[b], n_failed[b].
@@ -299,21 +320,13 @@ __global__ void __launch_bounds__(kFinishThreads) k_finish_fam(FinishArgs a) {
     scomp[threadIdx.x] = comp;
     sfail[threadIdx.x] = fail;
     sinf[threadIdx.x] = ninf;
-    __syncthreads();
+    block_combine<kFinishThreads>(ssum, scomp, sfail, sinf);
     if (threadIdx.x == 0) {
-        double s = 0.0, c = 0.0;
-        int fl = 0, ni = 0;
-        for (int i = 0; i < (int)blockDim.x; ++i) {
-            neumaier_add(s, c, ssum[i]);
-            c += scomp[i];
-            fl += sfail[i];
-            ni += sinf[i];
-        }
         const size_t p = (size_t)b * gridDim.x + blockIdx.x;
-        a.part_sum[2 * p] = s;
-        a.part_sum[2 * p + 1] = c;
-        a.part_cnt[2 * p] = fl;
-        a.part_cnt[2 * p + 1] = ni;
+        a.part_sum[2 * p] = ssum[0];
+        a.part_sum[2 * p + 1] = scomp[0];
+        a.part_cnt[2 * p] = sfail[0];
+        a.part_cnt[2 * p + 1] = sinf[0];
     }
 }
 
@@ -337,18 +350,12 @@ __global__ void __launch_bounds__(256) k_finish_total(FinishArgs a, int n_parts)
     scomp[threadIdx.x] = c;
     sfail[threadIdx.x] = fl;
     sinf[threadIdx.x] = ni;
-    __syncthreads();
+    block_combine<256>(ssum, scomp, sfail, sinf);
     if (threadIdx.x != 0) return;
-    s = 0.0;
-    c = 0.0;
-    fl = 0;
-    ni = 0;
-    for (int i = 0; i < (int)blockDim.x; ++i) {
-        neumaier_add(s, c, ssum[i]);
-        c += scomp[i];
-        fl += sfail[i];
-        ni += sinf[i];
-    }
+    s = ssum[0];
+    c = scomp[0];
+    fl = sfail[0];
+    ni = sinf[0];
     a.n_failed[b] = fl;
     // -sum lnL: +inf on gamma failure or when any family's lnL is -inf;
     // NaN if the tensor-core pass reported a time-out

@@ -57,6 +57,7 @@ static_assert(KC == 32 || KC == 16, "K chunk of 16 or 32 columns");
 constexpr int SC = 32;    // columns per staging tile of the epilogue's TMA stores (128-byte swizzle)
 constexpr int MAXST = 4;  // pipeline stages at most
 constexpr int NTHREADS = 128;
+
 #ifndef CAFE_TC_CW
 #define CAFE_TC_CW 16
 #endif
@@ -744,12 +745,36 @@ __global__ void __launch_bounds__(256) k_fallback_plan(FallbackPlanArgs a) {
 
 }  // namespace
 
+// k_prune_tc's dynamic shared-memory limit is raised once, to the most a
+// CTA may use, so launches of different widths need no per-launch change.
+cudaError_t tc_kernels_init() {
+    return cudaFuncSetAttribute(k_prune_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, prune_tc_max_smem());
+}
+
 cudaError_t launch_fallback_plan(const FallbackPlanArgs& a, cudaStream_t s) {
     k_fallback_plan<<<1, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
 int prune_tc_kchunk() { return KC; }
+
+// Dynamic shared memory one k_prune_tc CTA may use: the device's per-block
+// opt-in limit minus the kernel's static shared memory.
+int prune_tc_max_smem() {
+    static int cached = -1;
+    if (cached < 0) {
+        int dev = 0, optin = 0;
+        cudaFuncAttributes fa{};
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+            cudaFuncGetAttributes(&fa, (const void*)k_prune_tc) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        cached = optin - (int)fa.sharedSizeBytes;
+    }
+    return cached;
+}
 
 size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages, int n_internal) {
     return stages_region(Ws, stages) + (size_t)n_slots * TM * sizeof(int) + (size_t)n_internal * sizeof(NodeInfo) + 1024;
@@ -763,8 +788,7 @@ cudaError_t launch_convert_tc(const ConvertJob* d_jobs, int n_jobs, TcBuffers b,
 
 cudaError_t launch_prune_tc(const TcMaps& m, const PruneTcArgs& a, int n_ctas, size_t smem, cudaStream_t s) {
     if (a.n_tiles <= 0) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_prune_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+    if (smem > (size_t)prune_tc_max_smem()) return cudaErrorInvalidValue;
     if (a.stages < 1 || a.stages > MAXST) return cudaErrorInvalidValue;
     k_prune_tc<<<n_ctas, NTHREADS, smem, s>>>(m.mat_hi, m.mat_lo, m.vec_hi, m.vec_lo, m.vst_hi, m.vst_lo, a);
     return cudaGetLastError();

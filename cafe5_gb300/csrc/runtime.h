@@ -22,6 +22,14 @@ namespace cafe {
 extern const int kDefaultBins[];
 extern const int kNumDefaultBins;
 
+// While alive, device buffers that grow on this thread are freed and
+// allocated stream-ordered on `s`.
+struct AllocScope {
+    cudaStream_t prev;
+    explicit AllocScope(cudaStream_t s);
+    ~AllocScope();
+};
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
@@ -168,7 +176,15 @@ struct cafe_ctx {
     bool stop = false;
     uint64_t next_ticket = 1;
     int in_flight = 0;
+    size_t in_flight_bytes = 0;       // estimated device footprint of admitted requests
+    size_t serve_budget = 0;          // admission limit for that footprint
     std::vector<double> latencies_ms;
+    int batches_in_flight = 0;
+    cafe_serving_info serving{};     // serving counters
+    // last launch of the most recent request: the next request's device work
+    // starts after it
+    cudaEvent_t gate = nullptr;
+    bool gate_set = false;
     int64_t completed = 0;
     cafe::Profiler prof;
 };

@@ -227,7 +227,11 @@ class Context:
         p99 = C.c_double()
         inf = C.c_int()
         self._check(self.lib.cafe_serving_stats(self.h, C.byref(n), C.byref(p50), C.byref(p99), C.byref(inf)))
-        return {"completed": n.value, "p50_ms": p50.value, "p99_ms": p99.value, "in_flight": inf.value}
+        si = _lib.ServingInfo()
+        self._check(self.lib.cafe_serving_counters(self.h, C.byref(si)))
+        return {"completed": n.value, "p50_ms": p50.value, "p99_ms": p99.value, "in_flight": inf.value,
+                "batches": si.batches, "merged": si.merged, "retried": si.retried, "enqueue_ms": si.enqueue_ms,
+                "wait_ms": si.wait_ms, "device_ms": si.device_ms}
 
 
 _default_ctx: Optional[Context] = None

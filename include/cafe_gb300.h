@@ -177,9 +177,12 @@ int cafe_score_batch_device(cafe_ctx* ctx, const cafe_request* reqs, int n, doub
                             void* stream);
 
 /* Continuous-batching request loop for many concurrent optimizers: submit
- * returns at once with a ticket; the request is admitted when a stream and
- * enough device memory are free, runs concurrently with other admitted
- * requests, and fills `res` (host buffers must stay valid until done).
+ * returns at once with a ticket; the request is admitted when a stream is
+ * free and its estimated device footprint fits the loop's budget (a quarter
+ * of the device memory free at context creation). Compatible requests
+ * queued at that moment (the batching rules of cafe_score_batch) are merged
+ * into one batched launch; admitted batches run concurrently on separate
+ * streams. `res` is filled when done (host buffers must stay valid).
  * poll returns CAFE_OK when finished, CAFE_ERR_BUSY while pending;
  * wait_ms < 0 waits without limit, otherwise at most wait_ms. */
 int cafe_submit(cafe_ctx* ctx, const cafe_request* req, cafe_result* res, uint64_t* ticket);
@@ -238,6 +241,16 @@ int cafe_prune_fp64_noalloc(int n_nodes, const int32_t* parent, const double* co
 /* Serving statistics since context creation: completed requests, p50 and
  * p99 latency (ms, submit -> done), current in-flight count. */
 int cafe_serving_stats(cafe_ctx* ctx, int64_t* completed, double* p50_ms, double* p99_ms, int* in_flight);
+/* Serving-loop counters since context creation. */
+typedef struct {
+    int64_t batches;             /* batched launches */
+    int64_t merged;              /* requests that shared a launch with others */
+    int64_t retried;             /* requests rerun alone after their batch failed */
+    double enqueue_ms;           /* host time enqueuing batches (context lock held) */
+    double wait_ms;              /* host time waiting for batches to finish */
+    double device_ms;            /* device time of the batches (events) */
+} cafe_serving_info;
+int cafe_serving_counters(cafe_ctx* ctx, cafe_serving_info* out);
 
 /* ---- parameter search (src/optimizer.cpp, src/optimizer_scorer.cpp) ---- */
 /* Which parameters the search varies (the scorer classes of

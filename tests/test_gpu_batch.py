@@ -156,3 +156,45 @@ def test_batch_rejects_mismatched_requests(ctx):
         res = (_lib.Result * 2)()
         ctx._check(ctx.lib.cafe_score_batch(ctx.h, C.cast(arr, C.c_void_p), 2, C.cast(res, C.c_void_p)))
     ctx.free_families(sid)
+
+
+def test_serving_merges_requests_and_matches_alone(ctx):
+    """Continuous batching: requests from many optimizers queued together on
+    two family sets (mixed precision and FP64) are merged into batched
+    launches where compatible; every result equals the request scored alone
+    (bit for bit in FP64, within 1e-6 relative per family in mixed
+    precision)."""
+    from cafe5_gb300.inputs import RootPrior
+    from cafe5_gb300.synth import workload
+    w = workload(1, n_families=1500, seed=34)
+    w0 = workload(0, n_families=400, seed=35)
+    ctx.set_prior(RootPrior.uniform(400).vector())
+    ctx.set_error_model(None)
+    t1 = ctx.upload_tree(w.tree)
+    s1 = ctx.upload_families(t1, w.families.counts)
+    t0 = ctx.upload_tree(w0.tree)
+    s0 = ctx.upload_families(t0, w0.families.counts)
+    jobs = []
+    for i in range(24):
+        if i % 3 == 2:
+            jobs.append((t0, s0, dict(lambdas=[0.002 * (1 + 0.03 * i)], model=0, precision="fp64_binned")))
+        else:
+            jobs.append((t1, s1, dict(lambdas=[0.002 * (1 + 0.01 * i)], model=1, multipliers=w.multipliers,
+                                      cat_probs=w.cat_probs, precision="mixed_tf32x3")))
+    handles = []
+    for t, s, kw in jobs:
+        kw = dict(kw)
+        lam = kw.pop("lambdas")
+        handles.append(ctx.submit(t, s, lam, **kw))
+    got = [ctx.poll(h, -1) for h in handles]
+    for (t, s, kw), g in zip(jobs, got):
+        kw = dict(kw)
+        lam = kw.pop("lambdas")
+        one = ctx.score(t, s, lam, **kw)
+        if kw["precision"] == "fp64_binned":
+            assert np.array_equal(g.family_lnl, one.family_lnl) and g.total == one.total
+        else:
+            rel = np.abs(g.family_lnl - one.family_lnl) / np.abs(one.family_lnl)
+            assert rel.max() <= 1e-6
+    ctx.free_families(s1)
+    ctx.free_families(s0)
