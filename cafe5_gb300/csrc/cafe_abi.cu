@@ -349,10 +349,11 @@ int prepare_set(cafe_ctx* C, FamSet& S) {
 }
 
 // Matrix cache: look up or schedule (size, lambda, t). Caller holds C->mu.
+// Matrices a request still has to build: their keys and the cache entries
+// already inserted for them (filled by cache_build).
 struct PendingJobs {
     std::vector<MatKey> keys;
-    std::unordered_set<MatKey, MatKeyHash> seen;
-    std::vector<double> lam, t;
+    std::vector<MatEntry*> entries;
 };
 
 void cache_reset(cafe_ctx* C) {
@@ -369,8 +370,21 @@ double* cache_lookup(cafe_ctx* C, const MatKey& k) {
     return it == C->cache.end() ? nullptr : it->second.d;
 }
 
-// Allocate and enqueue K1 for the pending keys on `ws`.
+int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P);
+
+// Allocate and enqueue K1 for the pending keys on `ws`. On failure the
+// keys' placeholder entries leave the cache again.
 int cache_build(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
+    const int rc = cache_build_impl(C, ws, P);
+    if (rc) {
+        for (const MatKey& k : P.keys) C->cache.erase(k);
+        P.keys.clear();
+        P.entries.clear();
+    }
+    return rc;
+}
+
+int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
     const size_t n = P.keys.size();
     if (!n) return CAFE_OK;
     size_t total = 0;
@@ -378,17 +392,6 @@ int cache_build(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
     for (auto& k : P.keys) {
         total += (size_t)k.size * k.size * sizeof(double);
         max_size = std::max(max_size, k.size);
-    }
-    bool idle;
-    {
-        std::lock_guard<std::mutex> lk(C->qmu);
-        idle = C->in_flight == 0 && C->queue.empty();
-    }
-    if (C->cache_cap && C->cache_bytes + total > C->cache_cap && idle) {
-        // over the cap: start a fresh cache (the reference's cache lives for
-        // one evaluation; keeping matrices across calls is only a speed-up)
-        cudaDeviceSynchronize();
-        cache_reset(C);
     }
     // bump allocation from large slabs (no cudaMalloc per evaluation)
     const size_t need = (total + 255) & ~(size_t)255;
@@ -422,10 +425,8 @@ int cache_build(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
         j.dst = reinterpret_cast<double*>(cur);
         j.size = k.size;
         J[i] = j;
-        MatEntry e;
-        e.d = j.dst;
-        e.chunk = batch;
-        C->cache[k] = e;
+        P.entries[i]->d = j.dst;
+        P.entries[i]->chunk = batch;
         cur += (size_t)k.size * k.size * sizeof(double);
     }
     CK(cudaMemcpyAsync(ws.jobs.p, J, n * sizeof(MatrixJob), cudaMemcpyHostToDevice, ws.stream), "jobs");
@@ -440,21 +441,7 @@ int cache_build(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
     // requests on other streams order themselves after this build
     CK(cudaEventRecord(ready, ws.stream), "event");
     P.keys.clear();
-    P.seen.clear();
-    return CAFE_OK;
-}
-
-// Make ws.stream wait for the builds of every matrix it is about to read.
-int cache_wait_ready(cafe_ctx* C, Workspace& ws, const std::vector<MatKey>& keys) {
-    std::vector<int> seen;
-    for (const MatKey& k : keys) {
-        auto it = C->cache.find(k);
-        if (it == C->cache.end()) continue;
-        const int b = it->second.chunk;
-        if (std::find(seen.begin(), seen.end(), b) != seen.end()) continue;
-        seen.push_back(b);
-        CK(cudaStreamWaitEvent(ws.stream, C->batch_events[b], 0), "event");
-    }
+    P.entries.clear();
     return CAFE_OK;
 }
 
@@ -466,10 +453,32 @@ MatKey make_key(int size, double lambda, double t) {
     return k;
 }
 
-void schedule(cafe_ctx* C, PendingJobs& P, const MatKey& k) {
-    if (cache_lookup(C, k)) return;
-    if (!P.seen.insert(k).second) return;
-    P.keys.push_back(k);
+// The cache entry of key k; a key seen for the first time gets an entry
+// now and is queued for the next cache_build.
+MatEntry* schedule(cafe_ctx* C, PendingJobs& P, const MatKey& k) {
+    auto ins = C->cache.try_emplace(k);
+    MatEntry* e = &ins.first->second;
+    if (ins.second) {
+        P.keys.push_back(k);
+        P.entries.push_back(e);
+    }
+    return e;
+}
+
+// Over the cap with nothing else in flight: start a fresh cache before a
+// request inserts its keys (the reference's cache lives for one evaluation;
+// keeping matrices across calls is only a speed-up). `bytes` bounds what the
+// request may add.
+void cache_make_room(cafe_ctx* C, size_t bytes) {
+    if (!C->cache_cap || C->cache_bytes + bytes <= C->cache_cap) return;
+    bool idle;
+    {
+        std::lock_guard<std::mutex> lk(C->qmu);
+        idle = C->in_flight == 0 && C->queue.empty();
+    }
+    if (!idle) return;
+    cudaDeviceSynchronize();
+    cache_reset(C);
 }
 
 struct ScoreInfo {
@@ -532,6 +541,10 @@ int cached_map(cafe_ctx* C, Workspace& ws, int slot, CUtensorMap* out, const flo
     }
     *out = mc.map;
     return CAFE_OK;
+}
+
+double host_ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
 // Category probabilities of every (candidate, category) index, and the list
@@ -627,18 +640,35 @@ int launch_fp64_tiles(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHos
     return CAFE_OK;
 }
 
-double tile_flops(const TreeHost& T, const PruneTile& t, bool err) {
+// Algorithmic flops of one family of a tile (the roofline basis), by the
+// tile's (S, R) and error-model use.
+double family_flops(const TreeHost& T, int S, int R, bool err) {
     double per = 0;
     for (size_t ii = 0; ii < T.internal.size(); ++ii) {
         const int v = T.internal[ii];
-        const int rows = (v == T.root) ? t.R : t.S + 1;
+        const int rows = (v == T.root) ? R : S + 1;
         const int nch = T.cstart[ii + 1] - T.cstart[ii];
         for (int ci = T.cstart[ii]; ci < T.cstart[ii + 1]; ++ci)
-            if (!T.children[T.child[ci]].empty()) per += 2.0 * rows * (t.S + 1);
+            if (!T.children[T.child[ci]].empty()) per += 2.0 * rows * (S + 1);
             else if (err) per += 6.0 * rows;
         per += (double)(nch - 1) * rows;
     }
-    return per * t.count;
+    return per;
+}
+
+double tiles_flops(const TreeHost& T, const std::vector<PruneTile>& tiles, bool err) {
+    double fl = 0;
+    int last_S = -1, last_R = -1;
+    double per = 0;
+    for (const PruneTile& t : tiles) {
+        if (t.S != last_S || t.R != last_R) {
+            per = family_flops(T, t.S, t.R, err);
+            last_S = t.S;
+            last_R = t.R;
+        }
+        fl += per * t.count;
+    }
+    return fl;
 }
 
 // MIXED_TF32X3: tensor-core tiles for bins <= 256 states, FP64 tiles for
@@ -657,24 +687,21 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         if (w <= 256) Wm = std::max(Wm, w);
     info->scaled = true;
 
-    // request-local matrix list and conversion to TF32 operands
+    // request-local matrix list and conversion to TF32 operands (a cache
+    // entry stamped with this request already has its conversion slot)
     std::vector<int32_t> mat_index((size_t)K * T.n_nodes, -1);
     std::vector<ConvertJob> jobs;
-    std::unordered_map<const double*, int> seen;
+    const uint64_t stamp = ++C->request_stamp;
     for (int k = 0; k < K; ++k)
         for (int v = 0; v < T.n_nodes; ++v) {
-            const double* m = hm[(size_t)k * T.n_nodes + v];
-            if (!m) continue;
-            auto it = seen.find(m);
-            int idx;
-            if (it == seen.end()) {
-                idx = (int)jobs.size();
-                seen[m] = idx;
-                jobs.push_back(ConvertJob{m, msize, idx});
-            } else {
-                idx = it->second;
+            MatEntry* e = ws.entry_vec[(size_t)k * T.n_nodes + v];
+            if (!e) continue;
+            if (e->stamp != stamp) {
+                e->stamp = stamp;
+                e->conv = (int)jobs.size();
+                jobs.push_back(ConvertJob{e->d, msize, e->conv});
             }
-            mat_index[(size_t)k * T.n_nodes + v] = idx;
+            mat_index[(size_t)k * T.n_nodes + v] = e->conv;
         }
     const int n_mat = (int)jobs.size();
 
@@ -691,9 +718,10 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
     CK(cudaMemsetAsync(ws.flags.p, 0, (size_t)std::max<int64_t>(F, 1) * sizeof(int32_t) + 64, ws.stream), "flags");
 
     // tiles: 128 families (tensor cores) or 32 families (FP64, wide bins)
+    // grouped by bin (bins ascend in width), so each bin's tiles are contiguous
     std::vector<PruneTile> tc_tiles, wide_tiles;
-    for (int k : active)
-        for (size_t b = 0; b < B.widths.size(); ++b) {
+    for (size_t b = 0; b < B.widths.size(); ++b)
+        for (int k : active) {
             const int w = B.widths[b];
             const int step = w <= 256 ? 128 : 32;
             for (int64_t i = 0; i < B.bin_count[b]; i += step) {
@@ -736,8 +764,6 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             int64_t first_tile, n_tiles, vrow_base;
         };
         std::vector<BinLaunch> launches;
-        std::stable_sort(tc_tiles.begin(), tc_tiles.end(),
-                         [](const PruneTile& x, const PruneTile& y) { return x.S < y.S; });
         int64_t vrows = 0;
         for (size_t i = 0; i < tc_tiles.size();) {
             size_t j = i;
@@ -819,7 +845,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         }
         if (prof) {
             C->prof.begin(1, ws.stream, &ev);
-            for (const PruneTile& t : tc_tiles) C->prof.acc.prune_flops += tile_flops(T, t, R->use_error_model);
+            C->prof.acc.prune_flops += tiles_flops(T, tc_tiles, R->use_error_model);
         }
         // fork: bins run on the auxiliary streams after everything queued so far
         const bool fork = launches.size() > 1;
@@ -1033,9 +1059,12 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     }
 
     // matrices for every (candidate, category, non-root node)
+    const auto t_keys = std::chrono::steady_clock::now();
+    cache_make_room(C, active.size() * (size_t)T.n_nodes * msize * msize * sizeof(double));
     PendingJobs P;
-    std::vector<MatKey> node_key((size_t)CT * T.n_nodes);
-    std::vector<MatKey> wait_keys;
+    std::vector<MatEntry*>& node_entry = ws.entry_vec;
+    node_entry.assign((size_t)CT * T.n_nodes, nullptr);
+    bool any_saturated = false;   // a key with 1 - 2a outside (0, 1): zero rows
     for (int c : active) {
         const cafe_request& Q = Rs[c / K];
         const double m = gamma ? Q.multipliers[c % K] : 1.0;
@@ -1043,36 +1072,35 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
             if (T.parent[v] < 0) continue;
             const double lam = Q.lambdas[T.lambda_index[v]] * m;
             const MatKey key = make_key(msize, lam, T.branch_length[v]);
-            node_key[(size_t)c * T.n_nodes + v] = key;
-            wait_keys.push_back(key);
-            schedule(C, P, key);
+            node_entry[(size_t)c * T.n_nodes + v] = schedule(C, P, key);
+            const double lq = (double)key.lq / 1000000000.0, tq = (double)key.tq / 1000.0;
+            const double al = lq * tq / (1 + lq * tq), co = 1 - 2 * al;
+            if (!(co > 0 && co != 1)) any_saturated = true;
         }
     }
     int rc = cache_build(C, ws, P);
     if (rc) return rc;
-    rc = cache_wait_ready(C, ws, wait_keys);
-    if (rc) return rc;
+    // one pass over the entries: matrix pointers, and the builds to wait for
     CK(ws.h_mats.reserve((size_t)CT * T.n_nodes * sizeof(double*)), "mats");
     CK(ws.mats.reserve((size_t)CT * T.n_nodes * sizeof(double*)), "mats");
     double** hm = ws.h_mats.as<double*>();
     std::fill(hm, hm + (size_t)CT * T.n_nodes, nullptr);
+    std::vector<int> wait_chunks;
     for (int c : active)
-        for (int v = 0; v < T.n_nodes; ++v)
-            if (T.parent[v] >= 0) hm[(size_t)c * T.n_nodes + v] = cache_lookup(C, node_key[(size_t)c * T.n_nodes + v]);
+        for (int v = 0; v < T.n_nodes; ++v) {
+            const MatEntry* e = node_entry[(size_t)c * T.n_nodes + v];
+            if (!e) continue;
+            if (!e->d) return fail(C, CAFE_ERR_MISSING_MATRIX, "matrix not built");
+            hm[(size_t)c * T.n_nodes + v] = e->d;
+            if (std::find(wait_chunks.begin(), wait_chunks.end(), e->chunk) == wait_chunks.end())
+                wait_chunks.push_back(e->chunk);
+        }
+    for (int b : wait_chunks) CK(cudaStreamWaitEvent(ws.stream, C->batch_events[b], 0), "event");
+    if (C->prof.on) C->prof.acc.host_keys_ms += host_ms_since(t_keys);
     CK(ws.cat.reserve((size_t)std::max<int64_t>(F, 1) * CT * sizeof(double)), "category buffer");
     if (R->precision == CAFE_PREC_MIXED_TF32X3) {
         // saturated keys (1 - 2a < 0) and polytomies stay on the FP64 path
-        bool to_fp64 = T.max_children > 2;
-        for (int c : active) {
-            if (to_fp64) break;
-            for (int v = 0; v < T.n_nodes; ++v)
-                if (T.parent[v] >= 0) {
-                    const MatKey& key = node_key[(size_t)c * T.n_nodes + v];
-                    const double lq = (double)key.lq / 1000000000.0, tq = (double)key.tq / 1000.0;
-                    const double al = lq * tq / (1 + lq * tq), co = 1 - 2 * al;
-                    if (!(co > 0 && co != 1)) to_fp64 = true;
-                }
-        }
+        const bool to_fp64 = T.max_children > 2 || any_saturated;
         if (!to_fp64) {
             CK(ws.catids.reserve(active.size() * sizeof(int32_t)), "categories");
             CK(ws.h_catids.reserve(active.size() * sizeof(int32_t)), "categories");
@@ -1080,7 +1108,10 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
             CK(cudaMemcpyAsync(ws.catids.p, ws.h_catids.p, active.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
                                ws.stream),
                "categories");
-            return enqueue_mixed(C, ws, Rs, T, S, K, CT, active, hm, d_fam, d_total, info);
+            const auto t_plan = std::chrono::steady_clock::now();
+            const int rcm = enqueue_mixed(C, ws, Rs, T, S, K, CT, active, hm, d_fam, d_total, info);
+            if (C->prof.on) C->prof.acc.host_plan_ms += host_ms_since(t_plan);
+            return rcm;
         }
         info->n_fallback = F;
     }
@@ -1165,7 +1196,7 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     cudaEvent_t ev;
     if (prof) {
         C->prof.begin(1, ws.stream, &ev);
-        for (const PruneTile& t : tiles) C->prof.acc.prune_flops += tile_flops(T, t, R->use_error_model);
+        C->prof.acc.prune_flops += tiles_flops(T, tiles, R->use_error_model);
     }
     CK(launch_prune64(a, n_ctas, ws.stream), "prune");
     if (prof) C->prof.end(1, ws.stream, ev);
@@ -1200,8 +1231,10 @@ int score_enqueue(cafe_ctx* C, Workspace& ws, const cafe_request* R, int NB, caf
     CK(ws.total.reserve((size_t)NB * sizeof(double)), "total");
     CK(cudaEventRecord(ws.ev_start, ws.stream), "event");
     CK(gate_enter(C, ws), "gate");
+    const auto t_host = std::chrono::steady_clock::now();
     int rc = enqueue_score(C, ws, R, NB, ws.fam_lnl.as<double>(), ws.total.as<double>(), info);
     if (rc) return rc;
+    if (C->prof.on && &ws == C->ws[0].get()) C->prof.acc.host_total_ms += host_ms_since(t_host);
     CK(gate_leave(C, ws), "gate");
     CK(cudaEventRecord(ws.ev_staged, ws.stream), "event");
     ws.staged = true;
@@ -1525,6 +1558,7 @@ int cafe_matrices_build(cafe_ctx* C, const double* lambdas, int n_lambdas, const
         return fail(C, CAFE_ERR_INVALID, "bad matrix build arguments");
     std::lock_guard<std::mutex> lk(C->mu);
     cudaSetDevice(C->device);
+    cache_make_room(C, (size_t)n_lambdas * n_t * matrix_size * matrix_size * sizeof(double));
     PendingJobs P;
     for (int i = 0; i < n_lambdas; ++i)
         for (int j = 0; j < n_t; ++j) schedule(C, P, make_key(matrix_size, lambdas[i], branch_lengths[j]));
@@ -1617,9 +1651,11 @@ int cafe_score_batch_device(cafe_ctx* C, const cafe_request* req, int n, double*
         CK(cudaStreamWaitEvent(ws.stream, ws.ev_start, 0), "event");
     }
     CK(gate_enter(C, ws), "gate");
+    const auto t_host = std::chrono::steady_clock::now();
     int rc = enqueue_score(C, ws, req, n, d_family_lnl ? d_family_lnl : ws.fam_lnl.as<double>(),
                            d_total ? d_total : ws.total.as<double>(), &info);
     if (rc) return rc;
+    if (C->prof.on) C->prof.acc.host_total_ms += host_ms_since(t_host);
     CK(gate_leave(C, ws), "gate");
     CK(cudaEventRecord(ws.ev_staged, ws.stream), "event");
     ws.staged = true;

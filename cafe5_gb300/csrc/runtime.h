@@ -93,8 +93,10 @@ struct MatKeyHash {
 };
 
 struct MatEntry {
-    double* d = nullptr;       // FP64 row-major size x size
+    double* d = nullptr;       // FP64 row-major size x size (null until its build is enqueued)
     int chunk = -1;            // build batch (index of its ready event)
+    uint64_t stamp = 0;        // request that last gave it a conversion slot
+    int conv = -1;             // that request's converted-matrix index
 };
 
 struct Slab {
@@ -126,6 +128,7 @@ struct Workspace {
         catids;
     PinnedBuf h_conv, h_mi, h_flags, h_tiles64, h_tiles_fb, h_tail, h_catids;
     std::vector<PruneTile> tile_vec;
+    std::vector<MatEntry*> entry_vec;   // cache entry of every (combined category, node)
     ~Workspace();
     int init(int device);
 };
@@ -163,6 +166,7 @@ struct cafe_ctx {
     std::vector<cafe::Slab> slabs;
     std::vector<cudaEvent_t> batch_events;
     size_t cache_bytes = 0, cache_cap = 0;
+    uint64_t request_stamp = 0;
     // workspaces: [0] for synchronous calls, [1..] for the serving loop
     std::vector<std::unique_ptr<cafe::Workspace>> ws;
     int n_ctas = 0;

@@ -204,6 +204,9 @@ typedef struct {
     int64_t launches;            /* kernels launched */
     int64_t prune_launches;
     int64_t matrices_built;
+    double host_keys_ms;         /* host: matrix keys, cache builds, pointer tables */
+    double host_plan_ms;         /* host: conversion jobs, tiles, launch plans */
+    double host_total_ms;        /* host: whole enqueue of the profiled calls */
 } cafe_timings;
 int cafe_profile_enable(cafe_ctx* ctx, int enable);
 int cafe_profile_read(cafe_ctx* ctx, cafe_timings* out);
