@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--serving-clients", type=int, default=8)
     ap.add_argument("--serving-requests", type=int, default=12, help="requests per client")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default tensor-core launch shapes (no cafe_autotune before the warm-up)")
     ap.add_argument("--profile-only", action="store_true",
                     help="two batched scores of the workload and nothing else (a small case for ncu captures)")
     return ap.parse_args()
@@ -345,6 +347,10 @@ def run_ours(args):
         return 0
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > 129 MB L2
 
+    # launch shapes tuned once per workload (untimed), as a deployment would
+    tuned = None
+    if prec.startswith("mixed") and not args.no_autotune:
+        tuned = ctx.autotune(tid, sid, candidates(w, B, 9000), reps=2, **kw)
     # warm-up, then the timed steps (barrier + synchronize on both sides)
     time_steps(ctx, torch, stream, flush, tid, sid, w, B, 0, args.warmup, d_fam, d_tot, kw)
     torch.cuda.synchronize()
@@ -447,7 +453,8 @@ def run_ours(args):
                            "candidates_per_step": B, "precision": prec,
                            "bins": sorted(set(int(x) for x in Wb)),
                            "l2": "flushed between timed steps (256 MB write)",
-                           "lambda": "new each step (matrices rebuilt)", "parallelism": f"families sharded x{world}"},
+                           "lambda": "new each step (matrices rebuilt)", "parallelism": f"families sharded x{world}",
+                           "tc_shapes": tuned},
                 "roofline": roof,
                 "fp64_paths": fp64,
                 "mixed_over_fp64": (value / fb) if fb else None,

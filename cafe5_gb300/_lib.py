@@ -26,7 +26,7 @@ EXPORTS = [
     "cafe_matrix_cache_size", "cafe_matrix_cache_clear", "cafe_is_saturated", "cafe_score",
     "cafe_score_device", "cafe_submit", "cafe_poll", "cafe_serving_stats", "cafe_profile_enable",
     "cafe_profile_read", "cafe_prune_fp64_noalloc", "cafe_optimize", "cafe_discrete_gamma",
-    "cafe_nelder_mead", "cafe_score_batch", "cafe_score_batch_device", "cafe_serving_counters",
+    "cafe_nelder_mead", "cafe_score_batch", "cafe_score_batch_device", "cafe_serving_counters", "cafe_autotune",
 ]
 OPT_LAMBDA, OPT_LAMBDA_ALPHA, OPT_LAMBDA_EPSILON, OPT_ALPHA = 0, 1, 2, 3
 
@@ -68,6 +68,10 @@ OBJECTIVE = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.c_int, C.c_void_p)
 class OptResult(C.Structure):
     _fields_ = [("values", C.c_void_p), ("score", C.c_double), ("iterations", C.c_int),
                 ("evaluations", C.c_int), ("converged", C.c_int)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("width", C.c_int), ("ctas_per_sm", C.c_int), ("stages", C.c_int), ("ms", C.c_double)]
 
 
 class ServingInfo(C.Structure):
@@ -113,6 +117,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
         "cafe_score": (i, [p, P(Request), P(Result)]),
         "cafe_score_batch": (i, [p, p, i, p]),
         "cafe_score_batch_device": (i, [p, p, i, p, p, p]),
+        "cafe_autotune": (i, [p, p, i, i, p, i, P(i)]),
         "cafe_score_device": (i, [p, P(Request), p, p, p]),
         "cafe_submit": (i, [p, P(Request), P(Result), P(C.c_uint64)]),
         "cafe_poll": (i, [p, C.c_uint64, i]),

@@ -671,6 +671,49 @@ double tiles_flops(const TreeHost& T, const std::vector<PruneTile>& tiles, bool 
     return fl;
 }
 
+// Launch shape of the tensor-core kernel for bin width W: TMEM columns per
+// CTA, CTAs per SM and pipeline stages. By default the most CTAs per SM that
+// TMEM and shared memory allow, then the deepest pipeline that keeps them;
+// cafe_autotune may have measured a better pair for this width.
+struct TcShape {
+    int tmem_cols = 0, per_sm = 0, stages = 0;
+    size_t smem = 0;
+};
+
+int tc_by_smem(const TreeHost& T, int W, int stages, size_t* smem) {
+    *smem = prune_tc_smem_bytes(W, T.n_slots, stages, (int)T.internal.size());
+    if (*smem > (size_t)prune_tc_max_smem()) return 0;
+    return (int)((227 * 1024) / (*smem + 1024));
+}
+
+TcShape tc_shape(cafe_ctx* C, const TreeHost& T, int W) {
+    TcShape sh;
+    sh.tmem_cols = 32;
+    while (sh.tmem_cols < 2 * W) sh.tmem_cols *= 2;
+    const int by_tmem = 512 / sh.tmem_cols;
+    auto it = C->tuned.find(W);
+    if (it != C->tuned.end()) {
+        size_t sm;
+        const int per = it->second.first, st = it->second.second;
+        if (per >= 1 && per <= by_tmem && st >= 1 && st <= 4 && tc_by_smem(T, W, st, &sm) >= per) {
+            sh.per_sm = per;
+            sh.stages = st;
+            sh.smem = sm;
+            return sh;
+        }
+    }
+    for (int st = 4; st >= 1; --st) {
+        size_t sm;
+        const int per = std::min(by_tmem, tc_by_smem(T, W, st, &sm));
+        if (per > sh.per_sm) {
+            sh.per_sm = per;
+            sh.stages = st;
+            sh.smem = sm;
+        }
+    }
+    return sh;
+}
+
 // MIXED_TF32X3: tensor-core tiles for bins <= 256 states, FP64 tiles for
 // wider bins and for families the tensor-core pass flags. Caller holds C->mu;
 // hm holds the FP64 matrix of every (category, node).
@@ -770,24 +813,12 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             while (j < tc_tiles.size() && tc_tiles[j].S == tc_tiles[i].S) ++j;
             BinLaunch L{};
             L.W = tc_tiles[i].S + 1;
-            L.tmem_cols = 32;
-            while (L.tmem_cols < 2 * L.W) L.tmem_cols *= 2;
-            const int by_tmem = 512 / L.tmem_cols;
-            // most CTAs per SM first, then the deepest pipeline that keeps them
-            int best_per = 0;
-            for (int st = 4; st >= 1; --st) {
-                const size_t sm = prune_tc_smem_bytes(L.W, T.n_slots, st, (int)T.internal.size());
-                const int by_smem = (int)((227 * 1024) / (sm + 1024));
-                const int per = std::min(by_tmem, by_smem);
-                if (per > best_per) {
-                    best_per = per;
-                    L.stages = st;
-                    L.smem = sm;
-                }
-            }
-            if (best_per < 1 || L.smem > (size_t)prune_tc_max_smem())
-                return fail(C, CAFE_ERR_INVALID, "tensor-core tile does not fit shared memory");
-            L.per_sm = best_per;
+            const TcShape shape = tc_shape(C, T, L.W);
+            if (shape.per_sm < 1) return fail(C, CAFE_ERR_INVALID, "tensor-core tile does not fit shared memory");
+            L.tmem_cols = shape.tmem_cols;
+            L.stages = shape.stages;
+            L.smem = shape.smem;
+            L.per_sm = shape.per_sm;
             // pad shared memory so no more CTAs of this launch than TMEM allows share an SM
             L.smem = std::max(L.smem, (size_t)((227 * 1024) / L.per_sm) - 2048);
             L.smem = std::min(L.smem, (size_t)prune_tc_max_smem());
@@ -1601,6 +1632,67 @@ int cafe_score(cafe_ctx* C, const cafe_request* req, cafe_result* res) {
     std::lock_guard<std::mutex> lk(C->mu);
     cudaSetDevice(C->device);
     return score_sync(C, *C->ws[0], req, 1, res);
+}
+
+int cafe_autotune(cafe_ctx* C, const cafe_request* reqs, int n, int reps, cafe_tune_result* out, int max_out,
+                  int* n_out) {
+    if (!C || !reqs || n < 1 || (max_out > 0 && !out)) return CAFE_ERR_INVALID;
+    if (reqs[0].precision != CAFE_PREC_MIXED_TF32X3) return fail(C, CAFE_ERR_INVALID, "autotune needs MIXED_TF32X3");
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    auto si = C->sets.find(reqs[0].set_id);
+    auto ti = C->trees.find(reqs[0].tree_id);
+    if (si == C->sets.end() || ti == C->trees.end()) return fail(C, CAFE_ERR_NOT_FOUND, "unknown tree or family set");
+    const TreeHost& T = *ti->second;
+    reps = std::max(1, reps);
+    std::vector<cafe_result> res(n);
+    // mean device time of the request with the current shapes (one untimed run first)
+    auto timed = [&](double* ms) -> int {
+        *ms = 0;
+        for (int r = 0; r <= reps; ++r) {
+            for (auto& x : res) x = cafe_result{};
+            const int rc = score_sync(C, *C->ws[0], reqs, n, res.data());
+            if (rc) return rc;
+            if (r > 0) *ms += res[0].device_ms / reps;
+        }
+        return CAFE_OK;
+    };
+    std::vector<int> widths;
+    const BinPlan& B = si->second->bins;
+    for (size_t b = 0; b < B.widths.size(); ++b)
+        if (B.widths[b] <= 256 && B.bin_count[b] > 0) widths.push_back(B.widths[b]);
+    int k = 0;
+    for (int W : widths) {
+        // candidates: the three largest feasible CTA counts per SM, each with every stage count that fits
+        C->tuned.erase(W);
+        const TcShape def = tc_shape(C, T, W);
+        double best_ms;
+        int rc = timed(&best_ms);
+        if (rc) return rc;
+        std::pair<int, int> best{def.per_sm, def.stages};
+        const int by_tmem = 512 / def.tmem_cols;
+        for (int per = by_tmem; per >= 1 && per > by_tmem - 3; --per)
+            for (int st = 1; st <= 4; ++st) {
+                size_t sm;
+                if (tc_by_smem(T, W, st, &sm) < per || (per == def.per_sm && st == def.stages)) continue;
+                C->tuned[W] = {per, st};
+                double ms;
+                rc = timed(&ms);
+                if (rc) {
+                    C->tuned.erase(W);
+                    return rc;
+                }
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = {per, st};
+                }
+            }
+        C->tuned[W] = best;
+        if (k < max_out) out[k] = cafe_tune_result{W, best.first, best.second, best_ms};
+        ++k;
+    }
+    if (n_out) *n_out = k;
+    return CAFE_OK;
 }
 
 int cafe_score_batch(cafe_ctx* C, const cafe_request* reqs, int n, cafe_result* results) {

@@ -15,6 +15,8 @@
 //  * The upper triangle follows from c P(s->c) = s P(c->s) (the two
 //    binomial sums differ term by term by the factor s/c): the chain of row
 //    s also writes P(c->s) = (c/s) P(s->c) into rows c < s.
+//  * Both kinds of store leave each warp as contiguous row segments (the
+//    lower triangle through a shared-memory staging tile).
 //  * The running value is kept as mantissa * 2^E so rows whose left end
 //    underflows FP64 (a^s < 1e-308) still reach their diagonal exactly.
 //
@@ -38,35 +40,34 @@ __device__ __forceinline__ double out_value(double m, int e) {
     return v < 1.0 ? v : 1.0;
 }
 
-// Row s of the matrix, columns 0..s, and its mirror: c P(s->c) = s P(c->s)
-// gives the upper-triangle entry P(c->s) = (c/s) P(s->c) of row c < s,
-// written in the same step. Neighbouring threads own neighbouring rows, so
-// the mirror stores of a warp land in one contiguous run of row c.
-__device__ void row_chain(double* __restrict__ M, int W, int s, double alpha, double coeff, double q, double la,
-                          const double* __restrict__ inv, const double* __restrict__ bq) {
-    double L0 = (double)s * la;  // log(a^s)
-    int E = 0;
-    double m;
-    if (L0 > -700.0) {
-        m = exp(L0);
-    } else {
-        E = (int)floor(L0 * 1.4426950408889634) + 1;
-        m = exp((L0 - (double)E * kLn2Hi) - (double)E * kLn2Lo);
-    }
-    double mp = 0.0;
-    double sm = (double)s, sp = (double)s;  // s - c, s + c
-    const double inv_s = inv[s];
-    double* row = M + (size_t)s * W;
-    for (int c = 0; c < s; ++c) {
-        const double v = out_value(m, E);
-        row[c] = v;
-        if (c > 0) {
-            const double u = (double)c * inv_s * v;
-            M[(size_t)c * W + s] = u < 1.0 ? u : 1.0;
+// One row chain: the coefficients g_c of row s, c = 0..s, as a running
+// mantissa m (and the previous one mp) times 2^E.
+struct RowChain {
+    int s, E;
+    double m, mp, sm, sp, inv_s;
+
+    __device__ void init(int s_, double la, const double* inv) {
+        s = s_;
+        const double L0 = (double)s * la;  // log(a^s)
+        E = 0;
+        if (L0 > -700.0) {
+            m = exp(L0);
+        } else {
+            E = (int)floor(L0 * 1.4426950408889634) + 1;
+            m = exp((L0 - (double)E * kLn2Hi) - (double)E * kLn2Lo);
         }
-        double a = fma(sm, q, alpha * sp) * inv[c + 1];
-        double b = coeff * bq[c];
-        double nx = fma(a, m, b * mp);
+        mp = 0.0;
+        sm = (double)s;  // s - c
+        sp = (double)s;  // s + c
+        inv_s = inv[s];
+    }
+    __device__ __forceinline__ double value() const { return out_value(m, E); }
+    // g_c -> g_{c+1}
+    __device__ __forceinline__ void advance(int c, double alpha, double coeff, double q, const double* inv,
+                                            const double* bq) {
+        const double a = fma(sm, q, alpha * sp) * inv[c + 1];
+        const double b = coeff * bq[c];
+        const double nx = fma(a, m, b * mp);
         mp = m;
         m = nx;
         sm -= 1.0;
@@ -77,18 +78,28 @@ __device__ void row_chain(double* __restrict__ M, int W, int s, double alpha, do
             E += 600;
         }
     }
-    row[s] = out_value(m, E);
-}
+};
 
-// One CTA per matrix; thread p owns rows 1 + p and W - 1 - p (about W
-// recurrence steps each). Row 0 and column 0 of rows >= 1 come from the
-// chains (P(s -> 0) = a^s); M[0][c] = delta(c, 0).
+constexpr int kStageCols = 16;   // columns of a warp's staging tile
+constexpr int kStagePitch = 33;  // padded row pitch (doubles) of the staging tile
+
+// One CTA per matrix. Lane l of warp w owns the row pair p = 32 w + l: the
+// short row 1 + p and the long row W - 1 - p, one after the other. Each
+// step c writes two entries of row s's chain: the mirror P(c->s) =
+// (c/s) P(s->c) of row c < s, contiguous across the warp (neighbouring lanes
+// own neighbouring rows), and P(s->c) itself, which is strided across the
+// warp and so goes through a 16-column staging tile in shared memory and
+// leaves as contiguous row segments. Row 0 is delta(c, 0).
 __global__ void __launch_bounds__(128) k_matrix_build(const MatrixJob* __restrict__ jobs) {
     extern __shared__ double sh[];
     const MatrixJob J = jobs[blockIdx.x];
     const int W = J.size;
     double* inv = sh;          // inv[k] = 1/k, k = 0..W
     double* bq = sh + W + 1;   // bq[c] = (c - 1)/(c + 1), c = 0..W
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* stage = sh + 2 * (W + 1) + (size_t)warp * kStageCols * kStagePitch;
+    int* srow = reinterpret_cast<int*>(sh + 2 * (W + 1) + (size_t)(blockDim.x >> 5) * kStageCols * kStagePitch) +
+                warp * 32;
     for (int k = threadIdx.x; k <= W; k += blockDim.x) {
         inv[k] = k ? 1.0 / (double)k : 0.0;
         bq[k] = (double)(k - 1) / (double)(k + 1);
@@ -106,11 +117,43 @@ __global__ void __launch_bounds__(128) k_matrix_build(const MatrixJob* __restric
     __syncthreads();
     const double q = coeff / alpha;
     const double la = log(alpha);
-    const int nrows = W - 1;
-    for (int p = threadIdx.x; p < (nrows + 1) / 2; p += blockDim.x) {
-        const int s1 = 1 + p, s2 = W - 1 - p;
-        row_chain(M, W, s1, alpha, coeff, q, la, inv, bq);
-        if (s2 != s1) row_chain(M, W, s2, alpha, coeff, q, la, inv, bq);
+    const int npairs = W / 2;   // rows 1..W-1 in pairs (the middle row once when W is even)
+    for (int p0 = warp * 32; p0 < npairs; p0 += blockDim.x) {
+        const int p = p0 + lane;
+        for (int set = 0; set < 2; ++set) {
+            const int s = set == 0 ? 1 + p : W - 1 - p;
+            const bool act = p < npairs && (set == 0 || s != 1 + p);
+            srow[lane] = act ? s : 0;
+            __syncwarp();
+            int maxlen = act ? s : 0;
+            for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
+            RowChain ch;
+            if (act) ch.init(s, la, inv);
+            for (int c0 = 0; c0 < maxlen; c0 += kStageCols) {
+                for (int cc = 0; cc < kStageCols; ++cc) {
+                    const int c = c0 + cc;
+                    if (act && c < s) {
+                        const double v = ch.value();
+                        stage[cc * kStagePitch + lane] = v;
+                        if (c > 0) {
+                            const double u = (double)c * ch.inv_s * v;
+                            M[(size_t)c * W + s] = u < 1.0 ? u : 1.0;
+                        }
+                        ch.advance(c, alpha, coeff, q, inv, bq);
+                    }
+                }
+                __syncwarp();
+                // the tile's rows, 16 columns each: two rows per warp instruction
+                for (int idx = lane; idx < 32 * kStageCols; idx += 32) {
+                    const int r = idx / kStageCols, col = idx % kStageCols;
+                    const int sr = srow[r];
+                    if (c0 + col < sr) M[(size_t)sr * W + c0 + col] = stage[col * kStagePitch + r];
+                }
+                __syncwarp();
+            }
+            if (act) M[(size_t)s * W + s] = ch.value();   // the diagonal, g_s
+            __syncwarp();
+        }
     }
 }
 
@@ -118,14 +161,15 @@ __global__ void __launch_bounds__(128) k_matrix_build(const MatrixJob* __restric
 
 cudaError_t launch_matrix_build(const MatrixJob* d_jobs, int n_jobs, int max_size, cudaStream_t s) {
     if (n_jobs <= 0) return cudaSuccess;
-    size_t smem = sizeof(double) * 2 * (size_t)(max_size + 2);
+    // one thread per row pair, in whole warps (at most 128)
+    const int pairs = max_size / 2;
+    const int threads = std::min(128, std::max(32, (pairs + 31) / 32 * 32));
+    size_t smem = sizeof(double) * (2 * (size_t)(max_size + 1) + (size_t)(threads / 32) * kStageCols * kStagePitch) +
+                  sizeof(int) * (size_t)threads;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_matrix_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    // one thread per row pair, in whole warps (at most 128)
-    const int pairs = max_size / 2;
-    const int threads = std::min(128, std::max(32, (pairs + 31) / 32 * 32));
     k_matrix_build<<<n_jobs, threads, smem, s>>>(d_jobs);
     return cudaGetLastError();
 }

@@ -167,6 +167,7 @@ struct cafe_ctx {
     std::vector<cudaEvent_t> batch_events;
     size_t cache_bytes = 0, cache_cap = 0;
     uint64_t request_stamp = 0;
+    std::map<int, std::pair<int, int>> tuned;   // bin width -> (CTAs per SM, stages) chosen by cafe_autotune
     // workspaces: [0] for synchronous calls, [1..] for the serving loop
     std::vector<std::unique_ptr<cafe::Workspace>> ws;
     int n_ctas = 0;

@@ -181,6 +181,18 @@ class Context:
             keep.append(k)
         return (_lib.Request * len(reqs))(*reqs), keep
 
+    def autotune(self, tree_id, set_id, candidates, reps: int = 3, **kw) -> List[dict]:
+        """cafe_autotune: pick the tensor-core launch shape of every S-bin by
+        timing this batch (precision mixed_tf32x3)."""
+        kw.setdefault("precision", "mixed_tf32x3")
+        arr, keep = self._batch_requests(tree_id, set_id, candidates, kw)
+        out = (_lib.TuneResult * 16)()
+        n = C.c_int()
+        self._check(self.lib.cafe_autotune(self.h, C.cast(arr, C.c_void_p), len(arr), reps, C.cast(out, C.c_void_p),
+                                           16, C.byref(n)))
+        return [{"width": out[i].width, "ctas_per_sm": out[i].ctas_per_sm, "stages": out[i].stages, "ms": out[i].ms}
+                for i in range(n.value)]
+
     def score_batch_device(self, tree_id, set_id, candidates, d_family_lnl=0, d_total=0, stream=0, **kw):
         """cafe_score_batch_device: d_family_lnl [n][F], d_total [n] (device pointers)."""
         arr, keep = self._batch_requests(tree_id, set_id, candidates, kw)

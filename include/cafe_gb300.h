@@ -164,6 +164,23 @@ int cafe_score(cafe_ctx* ctx, const cafe_request* req, cafe_result* res);
  * others. */
 int cafe_score_batch(cafe_ctx* ctx, const cafe_request* reqs, int n, cafe_result* results);
 
+/* Autotuner for the tensor-core launch shapes: for every S-bin width of the
+ * requests' family set (<= 256 states), times the batch (cafe_score_batch
+ * semantics, MIXED_TF32X3) with the default shape and with the candidate
+ * shapes (the three largest feasible CTA counts per SM x 1-4 pipeline
+ * stages), one bin at a time, and keeps the fastest per width for every
+ * later call on this context. `reps` timed runs per candidate (after one
+ * untimed run). Results do not depend on the shape. Writes up to max_out
+ * (width, CTAs per SM, stages, ms) entries. */
+typedef struct {
+    int width;
+    int ctas_per_sm;
+    int stages;
+    double ms;                   /* mean device time of the batch with this shape */
+} cafe_tune_result;
+int cafe_autotune(cafe_ctx* ctx, const cafe_request* reqs, int n, int reps, cafe_tune_result* out, int max_out,
+                  int* n_out);
+
 /* Device-resident variant: enqueues the whole evaluation on `stream`
  * (a cudaStream_t; NULL = the context's stream) and writes per-family lnL
  * to d_family_lnl (device, n_families doubles, may be NULL) and the total

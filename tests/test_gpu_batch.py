@@ -198,3 +198,26 @@ def test_serving_merges_requests_and_matches_alone(ctx):
             assert rel.max() <= 1e-6
     ctx.free_families(s1)
     ctx.free_families(s0)
+
+
+def test_autotune_picks_shapes_and_keeps_results(ctx):
+    """cafe_autotune times the candidate launch shapes of every tensor-core
+    S-bin and keeps the fastest; the scores do not depend on the shape (bit
+    for bit)."""
+    from cafe5_gb300.inputs import RootPrior
+    from cafe5_gb300.families import bin_families
+    from cafe5_gb300.synth import workload
+    w = workload(1, n_families=3000, seed=36)
+    tid, sid = _setup(ctx, w.tree, w.families.counts, prior=RootPrior.uniform(400).vector())
+    cands = [dict(lambdas=[0.002], multipliers=w.multipliers, cat_probs=w.cat_probs),
+             dict(lambdas=[0.0021], multipliers=w.multipliers, cat_probs=w.cat_probs)]
+    before = ctx.score_batch(tid, sid, cands, model=1, precision="mixed_tf32x3")
+    tuned = ctx.autotune(tid, sid, cands, reps=2, model=1)
+    Wb, _, _ = bin_families(w.families)
+    assert sorted(t["width"] for t in tuned) == sorted(set(int(x) for x in Wb if x <= 256))
+    for t in tuned:
+        assert 1 <= t["ctas_per_sm"] <= 16 and 1 <= t["stages"] <= 4 and t["ms"] > 0
+    after = ctx.score_batch(tid, sid, cands, model=1, precision="mixed_tf32x3")
+    for a, b in zip(before, after):
+        assert np.array_equal(a.family_lnl, b.family_lnl) and a.total == b.total
+    ctx.free_families(sid)
