@@ -83,6 +83,8 @@ cudaError_t PinnedBuf::reserve(size_t n) {
     return cudaSuccess;
 }
 Workspace::~Workspace() {
+    for (auto& g : graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     if (stream) cudaStreamDestroy(stream);
     if (ev_start) cudaEventDestroy(ev_start);
     if (ev_stop) cudaEventDestroy(ev_stop);
@@ -547,6 +549,39 @@ double host_ms_since(std::chrono::steady_clock::time_point t0) {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
+// ---- op log: the stream operations of the pruning phase. In the dry mode
+// they are only recorded (their parameters form the CUDA-graph signature),
+// in the run and capture modes they are also issued.
+template <class T>
+void oplog(Workspace& ws, const T& v) {
+    const uint8_t* p = reinterpret_cast<const uint8_t*>(&v);
+    ws.oplog.insert(ws.oplog.end(), p, p + sizeof(T));
+}
+bool op_issue(const Workspace& ws) { return ws.op_mode != Workspace::kOpDry; }
+cudaError_t op_h2d(Workspace& ws, void* dst, const void* src, size_t n, cudaStream_t s) {
+    oplog(ws, 1); oplog(ws, dst); oplog(ws, src); oplog(ws, n); oplog(ws, s);
+    return op_issue(ws) ? cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, s) : cudaSuccess;
+}
+cudaError_t op_memset(Workspace& ws, void* dst, int v, size_t n, cudaStream_t s) {
+    oplog(ws, 2); oplog(ws, dst); oplog(ws, v); oplog(ws, n); oplog(ws, s);
+    return op_issue(ws) ? cudaMemsetAsync(dst, v, n, s) : cudaSuccess;
+}
+cudaError_t op_record(Workspace& ws, cudaEvent_t e, cudaStream_t s) {
+    oplog(ws, 3); oplog(ws, e); oplog(ws, s);
+    return op_issue(ws) ? cudaEventRecord(e, s) : cudaSuccess;
+}
+cudaError_t op_wait(Workspace& ws, cudaStream_t s, cudaEvent_t e) {
+    oplog(ws, 4); oplog(ws, s); oplog(ws, e);
+    return op_issue(ws) ? cudaStreamWaitEvent(s, e, 0) : cudaSuccess;
+}
+// A kernel launch: `sig` are the launch's argument values (all of them).
+template <class F, class... A>
+cudaError_t op_launch(Workspace& ws, int tag, F&& launch, const A&... sig) {
+    oplog(ws, 100 + tag);
+    (oplog(ws, sig), ...);
+    return op_issue(ws) ? launch() : cudaSuccess;
+}
+
 // Category probabilities of every (candidate, category) index, and the list
 // of indices that are pruned (candidates not rejected), staged to the device.
 int stage_cat_probs(cafe_ctx* C, Workspace& ws, const cafe_request* R, int K, int NB) {
@@ -556,7 +591,7 @@ int stage_cat_probs(cafe_ctx* C, Workspace& ws, const cafe_request* R, int K, in
     double* h = ws.h_catp.as<double>();
     for (int b = 0; b < NB; ++b)
         for (int k = 0; k < K; ++k) h[b * K + k] = R[b].model == CAFE_MODEL_GAMMA ? R[b].cat_probs[k] : 1.0;
-    CK(cudaMemcpyAsync(ws.catp.p, h, (size_t)CT * sizeof(double), cudaMemcpyHostToDevice, ws.stream), "cat probs");
+    CK(op_h2d(ws, ws.catp.p, h, (size_t)CT * sizeof(double), ws.stream), "cat probs");
     return CAFE_OK;
 }
 
@@ -566,7 +601,8 @@ int finish_batch(cafe_ctx* C, Workspace& ws, const ScoreInfo* info, bool gamma, 
                  const int32_t* d_status, double* d_fam, double* d_total) {
     const int64_t F = info->F;
     const int NB = info->B;
-    FinishArgs fa{};
+    FinishArgs fa;
+    std::memset(&fa, 0, sizeof fa);
     fa.F = F;
     fa.K = info->K;
     fa.n_cand = NB;
@@ -585,13 +621,21 @@ int finish_batch(cafe_ctx* C, Workspace& ws, const ScoreInfo* info, bool gamma, 
     const bool prof = (&ws == C->ws[0].get());
     cudaEvent_t ev;
     if (prof) C->prof.begin(2, ws.stream, &ev);
-    CK(launch_finish(fa, ws.stream), "finish");
+    CK(op_launch(ws, 1, [&] { return launch_finish(fa, ws.stream); }, fa, ws.stream), "finish");
     if (prof) C->prof.end(2, ws.stream, ev);
     for (int b = 0; b < NB; ++b) {
         if (!info->cand_rejected[b]) continue;
-        if (d_total) CK(launch_fill(d_total + b, 1, INFINITY, ws.stream), "fill");
-        if (d_fam && F) CK(launch_fill(d_fam + (size_t)b * F, F, NAN, ws.stream), "fill");
-        CK(launch_fill_i32(ws.nfail.as<int32_t>() + b, 1, 0, ws.stream), "fill");
+        double* pt = d_total ? d_total + b : nullptr;
+        double* pf = (d_fam && F) ? d_fam + (size_t)b * F : nullptr;
+        int32_t* pn = ws.nfail.as<int32_t>() + b;
+        CK(op_launch(ws, 2, [&] {
+               cudaError_t e = cudaSuccess;
+               if (pt) e = launch_fill(pt, 1, INFINITY, ws.stream);
+               if (e == cudaSuccess && pf) e = launch_fill(pf, F, NAN, ws.stream);
+               if (e == cudaSuccess) e = launch_fill_i32(pn, 1, 0, ws.stream);
+               return e;
+           }, pt, pf, pn, F, ws.stream),
+           "fill");
     }
     return CAFE_OK;
 }
@@ -605,11 +649,12 @@ int launch_fp64_tiles(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHos
     CK(h_tiles.reserve(n * sizeof(PruneTile)), "tiles");
     CK(d_tiles.reserve(n * sizeof(PruneTile)), "tiles");
     std::memcpy(h_tiles.p, tiles.data(), n * sizeof(PruneTile));
-    CK(cudaMemcpyAsync(d_tiles.p, h_tiles.p, n * sizeof(PruneTile), cudaMemcpyHostToDevice, ws.stream), "tiles");
+    CK(op_h2d(ws, d_tiles.p, h_tiles.p, n * sizeof(PruneTile), ws.stream), "tiles");
     const int n_ctas = std::max(1, std::min(n, C->n_ctas));
     const int64_t per_cta = (int64_t)T.n_slots * W * 32;
     CK(ws.scratch.reserve((size_t)n_ctas * per_cta * sizeof(double)), "scratch");
-    Prune64Args a{};
+    Prune64Args a;
+    std::memset(&a, 0, sizeof a);
     a.plan = T.plan;
     a.tiles = d_tiles.as<PruneTile>();
     a.n_tiles = n;
@@ -635,7 +680,7 @@ int launch_fp64_tiles(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHos
     const bool prof = (&ws == C->ws[0].get());
     cudaEvent_t ev;
     if (prof) C->prof.begin(prof_kind, ws.stream, &ev);
-    CK(launch_prune64(a, n_ctas, ws.stream), "prune fp64");
+    CK(op_launch(ws, 3, [&] { return launch_prune64(a, n_ctas, ws.stream); }, a, n_ctas, ws.stream), "prune fp64");
     if (prof) C->prof.end(prof_kind, ws.stream, ev);
     return CAFE_OK;
 }
@@ -752,13 +797,13 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
     int rc0 = stage_cat_probs(C, ws, R, KC, CT / KC);
     if (rc0) return rc0;
     CK(ws.mats.reserve((size_t)K * T.n_nodes * sizeof(double*)), "mats");
-    CK(cudaMemcpyAsync(ws.mats.p, hm, (size_t)K * T.n_nodes * sizeof(double*), cudaMemcpyHostToDevice, ws.stream), "mats");
+    CK(op_h2d(ws, ws.mats.p, hm, (size_t)K * T.n_nodes * sizeof(double*), ws.stream), "mats");
     CK(ws.cat.reserve((size_t)std::max<int64_t>(F, 1) * K * sizeof(double)), "category buffer");
     CK(ws.nfail.reserve(sizeof(int32_t)), "fail counter");
     CK(ws.flags.reserve((size_t)std::max<int64_t>(F, 1) * sizeof(int32_t) + 64), "flags");
     int32_t* d_flags = ws.flags.as<int32_t>();
     int32_t* d_status = d_flags + std::max<int64_t>(F, 1);
-    CK(cudaMemsetAsync(ws.flags.p, 0, (size_t)std::max<int64_t>(F, 1) * sizeof(int32_t) + 64, ws.stream), "flags");
+    CK(op_memset(ws, ws.flags.p, 0, (size_t)std::max<int64_t>(F, 1) * sizeof(int32_t) + 64, ws.stream), "flags");
 
     // tiles: 128 families (tensor cores) or 32 families (FP64, wide bins)
     // grouped by bin (bins ascend in width), so each bin's tiles are contiguous
@@ -786,16 +831,20 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         CK(ws.h_conv.reserve(jobs.size() * sizeof(ConvertJob)), "convert jobs");
         CK(ws.conv.reserve(jobs.size() * sizeof(ConvertJob)), "convert jobs");
         std::memcpy(ws.h_conv.p, jobs.data(), jobs.size() * sizeof(ConvertJob));
-        CK(cudaMemcpyAsync(ws.conv.p, ws.h_conv.p, jobs.size() * sizeof(ConvertJob), cudaMemcpyHostToDevice, ws.stream),
-           "convert jobs");
+        CK(op_h2d(ws, ws.conv.p, ws.h_conv.p, jobs.size() * sizeof(ConvertJob), ws.stream), "convert jobs");
         CK(ws.tc_mi.reserve(mat_index.size() * sizeof(int32_t)), "mat index");
         CK(ws.h_mi.reserve(mat_index.size() * sizeof(int32_t)), "mat index");
         std::memcpy(ws.h_mi.p, mat_index.data(), mat_index.size() * sizeof(int32_t));
-        CK(cudaMemcpyAsync(ws.tc_mi.p, ws.h_mi.p, mat_index.size() * sizeof(int32_t), cudaMemcpyHostToDevice, ws.stream),
-           "mat index");
-        TcBuffers tb{ws.tc_hi.as<float>(), ws.tc_lo.as<float>(), Wm};
+        CK(op_h2d(ws, ws.tc_mi.p, ws.h_mi.p, mat_index.size() * sizeof(int32_t), ws.stream), "mat index");
+        TcBuffers tb;
+        std::memset(&tb, 0, sizeof tb);
+        tb.hi = ws.tc_hi.as<float>();
+        tb.lo = ws.tc_lo.as<float>();
+        tb.Wm = Wm;
         if (prof) C->prof.begin(3, ws.stream, &ev);
-        CK(launch_convert_tc(ws.conv.as<ConvertJob>(), n_mat, tb, ws.stream), "convert");
+        const ConvertJob* cj = ws.conv.as<ConvertJob>();
+        CK(op_launch(ws, 4, [&] { return launch_convert_tc(cj, n_mat, tb, ws.stream); }, cj, n_mat, tb, ws.stream),
+           "convert");
         if (prof) C->prof.end(3, ws.stream, ev);
 
         // one launch per S-bin, each sized for its own width, run
@@ -845,9 +894,9 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         CK(ws.tiles.reserve(n_tc * sizeof(PruneTile)), "tiles");
         CK(ws.h_tiles.reserve(n_tc * sizeof(PruneTile)), "tiles");
         std::memcpy(ws.h_tiles.p, tc_tiles.data(), n_tc * sizeof(PruneTile));
-        CK(cudaMemcpyAsync(ws.tiles.p, ws.h_tiles.p, n_tc * sizeof(PruneTile), cudaMemcpyHostToDevice, ws.stream),
-           "tiles");
-        PruneTcArgs a{};
+        CK(op_h2d(ws, ws.tiles.p, ws.h_tiles.p, n_tc * sizeof(PruneTile), ws.stream), "tiles");
+        PruneTcArgs a;
+        std::memset(&a, 0, sizeof a);
         a.plan = T.plan;
         a.counts = S.d_counts.as<int32_t>();
         a.perm = B.d_perm.as<int64_t>();
@@ -881,12 +930,13 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         // fork: bins run on the auxiliary streams after everything queued so far
         const bool fork = launches.size() > 1;
         if (fork) {
-            CK(cudaEventRecord(ws.ev_fork, ws.stream), "fork");
-            for (int q = 0; q < Workspace::kAux; ++q) CK(cudaStreamWaitEvent(ws.aux[q], ws.ev_fork, 0), "fork");
+            CK(op_record(ws, ws.ev_fork, ws.stream), "fork");
+            for (int q = 0; q < Workspace::kAux; ++q) CK(op_wait(ws, ws.aux[q], ws.ev_fork), "fork");
         }
         for (size_t li = 0; li < launches.size(); ++li) {
             const BinLaunch& L = launches[li];
-            PruneTcArgs b = a;
+            PruneTcArgs b;
+            std::memcpy(&b, &a, sizeof b);     // padding included: the bytes are a graph signature
             b.tiles = ws.tiles.as<PruneTile>() + L.first_tile;
             b.n_tiles = (int)L.n_tiles;
             b.tmem_cols = L.tmem_cols;
@@ -894,12 +944,14 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             b.stages = L.stages;
             b.vrow_base = L.vrow_base;
             cudaStream_t st = fork ? ws.aux[li % Workspace::kAux] : ws.stream;
-            CK(launch_prune_tc(maps, b, L.n_ctas, L.smem, st), "prune tc");
+            CK(op_launch(ws, 5, [&] { return launch_prune_tc(maps, b, L.n_ctas, L.smem, st); }, maps, b, L.n_ctas, L.smem,
+                         st),
+               "prune tc");
         }
         if (fork) {
             for (int q = 0; q < Workspace::kAux; ++q) {
-                CK(cudaEventRecord(ws.ev_join[q], ws.aux[q]), "join");
-                CK(cudaStreamWaitEvent(ws.stream, ws.ev_join[q], 0), "join");
+                CK(op_record(ws, ws.ev_join[q], ws.aux[q]), "join");
+                CK(op_wait(ws, ws.stream, ws.ev_join[q]), "join");
             }
         }
 
@@ -921,7 +973,8 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
     // families the tensor-core pass could not represent: planned on the
     // device and recomputed in FP64 without a host round trip
     if (!tc_tiles.empty()) {
-        FallbackPlanArgs fp{};
+        FallbackPlanArgs fp;
+        std::memset(&fp, 0, sizeof fp);
         fp.flags = d_flags;
         fp.perm = B.d_perm.as<int64_t>();
         fp.n_bins = 0;
@@ -942,12 +995,13 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         fp.out_counts = d_status + 1;     // [families, tiles]
         fp.any_flag = d_status + 3;
         if (prof) C->prof.begin(3, ws.stream, &ev);
-        CK(launch_fallback_plan(fp, ws.stream), "fallback plan");
+        CK(op_launch(ws, 6, [&] { return launch_fallback_plan(fp, ws.stream); }, fp, ws.stream), "fallback plan");
         if (prof) C->prof.end(3, ws.stream, ev);
         const int n_ctas = C->sm_count;
         const int64_t per_cta = (int64_t)T.n_slots * msize * 32;
         CK(ws.scratch.reserve((size_t)n_ctas * per_cta * sizeof(double)), "scratch");
-        Prune64Args a{};
+        Prune64Args a;
+        std::memset(&a, 0, sizeof a);
         a.plan = T.plan;
         a.tiles = fp.fb_tiles;
         a.n_tiles = 0;
@@ -972,12 +1026,71 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         a.tile_families = 32;
         a.W = msize;
         if (prof) C->prof.begin(3, ws.stream, &ev);
-        CK(launch_prune64(a, n_ctas, ws.stream), "fallback prune");
+        CK(op_launch(ws, 7, [&] { return launch_prune64(a, n_ctas, ws.stream); }, a, n_ctas, ws.stream),
+           "fallback prune");
         if (prof) C->prof.end(3, ws.stream, ev);
         info->d_tail = d_status;     // [status, fallback families, fallback tiles]
     }
 
     return finish_batch(C, ws, info, gamma, true, nullptr, tc_tiles.empty() ? nullptr : d_status, d_fam, d_total);
+}
+
+// The pruning phase of a mixed-precision request as a CUDA graph. A dry
+// pass runs the host planning (it fills the pinned tables the graph's copy
+// nodes read) and records every stream op; if the record matches a graph
+// this workspace captured before, that graph is launched; otherwise the
+// phase is captured (thread-local stream capture, the auxiliary streams
+// joined by events) and instantiated. Profiled calls issue directly.
+int enqueue_mixed_graph(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T, FamSet& S, int K, int CT,
+                        const std::vector<int32_t>& active, double** hm, double* d_fam, double* d_total,
+                        ScoreInfo* info) {
+    static const bool phase_env = getenv("CAFE_TC_PHASES") != nullptr;
+    ws.oplog.clear();
+    if (C->prof.on || phase_env) {
+        ws.op_mode = Workspace::kOpRun;
+        return enqueue_mixed(C, ws, R, T, S, K, CT, active, hm, d_fam, d_total, info);
+    }
+    ws.op_mode = Workspace::kOpDry;
+    int rc = enqueue_mixed(C, ws, R, T, S, K, CT, active, hm, d_fam, d_total, info);
+    ws.op_mode = Workspace::kOpRun;
+    if (rc) return rc;
+    for (auto& g : ws.graphs)
+        if (g.exec && g.sig == ws.oplog) {
+            g.used = ++ws.graph_clock;
+            CK(cudaGraphLaunch(g.exec, ws.stream), "graph launch");
+            return CAFE_OK;
+        }
+    std::vector<uint8_t> sig;
+    sig.swap(ws.oplog);
+    auto issue_directly = [&]() {
+        cudaGetLastError();
+        ws.oplog.clear();
+        ws.op_mode = Workspace::kOpRun;
+        return enqueue_mixed(C, ws, R, T, S, K, CT, active, hm, d_fam, d_total, info);
+    };
+    if (cudaStreamBeginCapture(ws.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return issue_directly();
+    ws.op_mode = Workspace::kOpCapture;
+    rc = enqueue_mixed(C, ws, R, T, S, K, CT, active, hm, d_fam, d_total, info);
+    ws.op_mode = Workspace::kOpRun;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(ws.stream, &graph);
+    cudaGraphExec_t exec = nullptr;
+    const bool same = ws.oplog == sig;
+    if (rc || ec != cudaSuccess || !graph || !same || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        if (rc) return rc;
+        return issue_directly();
+    }
+    cudaGraphDestroy(graph);
+    Workspace::GraphEntry* slot = &ws.graphs[0];
+    for (auto& g : ws.graphs)
+        if (!g.exec || g.used < slot->used) slot = &g;
+    if (slot->exec) cudaGraphExecDestroy(slot->exec);
+    slot->sig.swap(sig);
+    slot->exec = exec;
+    slot->used = ++ws.graph_clock;
+    CK(cudaGraphLaunch(exec, ws.stream), "graph launch");
+    return CAFE_OK;
 }
 
 // Enqueue the evaluation of NB candidate requests (same tree, family set,
@@ -1140,7 +1253,7 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
                                ws.stream),
                "categories");
             const auto t_plan = std::chrono::steady_clock::now();
-            const int rcm = enqueue_mixed(C, ws, Rs, T, S, K, CT, active, hm, d_fam, d_total, info);
+            const int rcm = enqueue_mixed_graph(C, ws, Rs, T, S, K, CT, active, hm, d_fam, d_total, info);
             if (C->prof.on) C->prof.acc.host_plan_ms += host_ms_since(t_plan);
             return rcm;
         }

@@ -129,6 +129,17 @@ struct Workspace {
     PinnedBuf h_conv, h_mi, h_flags, h_tiles64, h_tiles_fb, h_tail, h_catids;
     std::vector<PruneTile> tile_vec;
     std::vector<MatEntry*> entry_vec;   // cache entry of every (combined category, node)
+    // CUDA graphs of the pruning phase: stream ops go through an op log;
+    // a dry pass records their parameters as the graph's signature
+    enum OpMode { kOpRun = 0, kOpDry = 1, kOpCapture = 2 };
+    int op_mode = kOpRun;
+    std::vector<uint8_t> oplog;
+    struct GraphEntry {
+        std::vector<uint8_t> sig;
+        cudaGraphExec_t exec = nullptr;
+        uint64_t used = 0;
+    } graphs[4];
+    uint64_t graph_clock = 0;
     ~Workspace();
     int init(int device);
 };

@@ -221,3 +221,25 @@ def test_autotune_picks_shapes_and_keeps_results(ctx):
     for a, b in zip(before, after):
         assert np.array_equal(a.family_lnl, b.family_lnl) and a.total == b.total
     ctx.free_families(sid)
+
+
+def test_graph_replay_matches_direct_launches(ctx):
+    """The pruning phase replayed from a captured CUDA graph gives the same
+    bits as direct launches (profiling forces direct launches), across many
+    steps at new lambdas that reuse the graph."""
+    from cafe5_gb300.inputs import RootPrior
+    from cafe5_gb300.synth import workload
+    w = workload(1, n_families=2500, seed=37)
+    tid, sid = _setup(ctx, w.tree, w.families.counts, prior=RootPrior.uniform(400).vector())
+    kw = dict(model=1, precision="mixed_tf32x3")
+    for i in range(5):
+        cands = [dict(lambdas=[0.002 * (1 + 1e-4 * i + 0.01 * b)], multipliers=w.multipliers, cat_probs=w.cat_probs)
+                 for b in range(3)]
+        graph = ctx.score_batch(tid, sid, cands, **kw)        # graph path (captured once, then replayed)
+        ctx.profile(True)
+        direct = ctx.score_batch(tid, sid, cands, **kw)       # direct launches
+        ctx.profile_read()
+        ctx.profile(False)
+        for g, d in zip(graph, direct):
+            assert np.array_equal(g.family_lnl, d.family_lnl) and g.total == d.total
+    ctx.free_families(sid)
