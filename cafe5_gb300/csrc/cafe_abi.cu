@@ -35,6 +35,82 @@ thread_local cudaStream_t t_alloc_stream = nullptr;
 AllocScope::AllocScope(cudaStream_t s) : prev(t_alloc_stream) { t_alloc_stream = s; }
 AllocScope::~AllocScope() { t_alloc_stream = prev; }
 
+// ---- MatCache
+size_t MatCache::home(const MatKey& k) const {
+    uint64_t h = (uint64_t)k.size * 0x9E3779B97F4A7C15ull ^ (uint64_t)k.lq * 0xC2B2AE3D27D4EB4Full ^
+                 (uint64_t)k.tq * 0x165667B19E3779F9ull;
+    h ^= h >> 33;   // 64-bit finaliser (xor-shift-multiply)
+    h *= 0xFF51AFD7ED558CCDull;
+    h ^= h >> 33;
+    return (size_t)h & mask_;
+}
+void MatCache::grow(size_t cap) {
+    std::vector<Slot> old_s;
+    std::vector<MatEntry> old_v;
+    old_s.swap(slots_);
+    old_v.swap(vals_);
+    slots_.assign(cap, Slot());
+    vals_.assign(cap, MatEntry());
+    mask_ = cap - 1;
+    n_ = 0;
+    for (size_t i = 0; i < old_s.size(); ++i)
+        if (old_s[i].used) {
+            auto r = try_emplace(old_s[i].key);
+            *r.first = old_v[i];
+        }
+}
+void MatCache::reserve(size_t n_entries) {
+    size_t cap = slots_.empty() ? 1024 : slots_.size();
+    while (cap < 2 * n_entries) cap *= 2;
+    if (cap != slots_.size()) grow(cap);
+}
+MatEntry* MatCache::find(const MatKey& k) {
+    if (slots_.empty()) return nullptr;
+    for (size_t i = home(k);; i = (i + 1) & mask_) {
+        if (!slots_[i].used) return nullptr;
+        if (slots_[i].key == k) return &vals_[i];
+    }
+}
+std::pair<MatEntry*, bool> MatCache::try_emplace(const MatKey& k) {
+    if (2 * (n_ + 1) > slots_.size()) reserve(n_ + 1);
+    for (size_t i = home(k);; i = (i + 1) & mask_) {
+        if (!slots_[i].used) {
+            slots_[i].used = true;
+            slots_[i].key = k;
+            vals_[i] = MatEntry();
+            ++n_;
+            return {&vals_[i], true};
+        }
+        if (slots_[i].key == k) return {&vals_[i], false};
+    }
+}
+void MatCache::erase(const MatKey& k) {
+    if (slots_.empty()) return;
+    size_t i = home(k);
+    for (;; i = (i + 1) & mask_) {
+        if (!slots_[i].used) return;
+        if (slots_[i].key == k) break;
+    }
+    // backward shift: pull later members of the probe run into the hole
+    for (size_t j = (i + 1) & mask_; slots_[j].used; j = (j + 1) & mask_) {
+        const size_t h = home(slots_[j].key);
+        const bool movable = (i <= j) ? (h <= i || h > j) : (h <= i && h > j);
+        if (movable) {
+            slots_[i] = slots_[j];
+            vals_[i] = vals_[j];
+            i = j;
+        }
+    }
+    slots_[i].used = false;
+    --n_;
+}
+void MatCache::clear() {
+    slots_.clear();
+    vals_.clear();
+    n_ = 0;
+    mask_ = 0;
+}
+
 DevBuf::~DevBuf() {
     if (p) cudaFree(p);
 }
@@ -368,8 +444,8 @@ void cache_reset(cafe_ctx* C) {
 }
 
 double* cache_lookup(cafe_ctx* C, const MatKey& k) {
-    auto it = C->cache.find(k);
-    return it == C->cache.end() ? nullptr : it->second.d;
+    const MatEntry* e = C->cache.find(k);
+    return e ? e->d : nullptr;
 }
 
 int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P);
@@ -459,7 +535,7 @@ MatKey make_key(int size, double lambda, double t) {
 // now and is queued for the next cache_build.
 MatEntry* schedule(cafe_ctx* C, PendingJobs& P, const MatKey& k) {
     auto ins = C->cache.try_emplace(k);
-    MatEntry* e = &ins.first->second;
+    MatEntry* e = ins.first;
     if (ins.second) {
         P.keys.push_back(k);
         P.entries.push_back(e);
@@ -1205,6 +1281,7 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     // matrices for every (candidate, category, non-root node)
     const auto t_keys = std::chrono::steady_clock::now();
     cache_make_room(C, active.size() * (size_t)T.n_nodes * msize * msize * sizeof(double));
+    C->cache.reserve(C->cache.size() + active.size() * (size_t)T.n_nodes);   // entry pointers stay valid
     PendingJobs P;
     std::vector<MatEntry*>& node_entry = ws.entry_vec;
     node_entry.assign((size_t)CT * T.n_nodes, nullptr);
@@ -1703,6 +1780,7 @@ int cafe_matrices_build(cafe_ctx* C, const double* lambdas, int n_lambdas, const
     std::lock_guard<std::mutex> lk(C->mu);
     cudaSetDevice(C->device);
     cache_make_room(C, (size_t)n_lambdas * n_t * matrix_size * matrix_size * sizeof(double));
+    C->cache.reserve(C->cache.size() + (size_t)n_lambdas * n_t);
     PendingJobs P;
     for (int i = 0; i < n_lambdas; ++i)
         for (int j = 0; j < n_t; ++j) schedule(C, P, make_key(matrix_size, lambdas[i], branch_lengths[j]));

@@ -99,6 +99,32 @@ struct MatEntry {
     int conv = -1;             // that request's converted-matrix index
 };
 
+// Open-addressing hash table of the matrix cache: keys and entries inline
+// (one cache line per probe instead of a node chase), linear probing,
+// backward-shift deletion. Entry pointers stay valid until the table grows;
+// callers reserve() for a request's keys before taking pointers.
+class MatCache {
+   public:
+    MatEntry* find(const MatKey& k);
+    // (entry, inserted)
+    std::pair<MatEntry*, bool> try_emplace(const MatKey& k);
+    void erase(const MatKey& k);
+    void reserve(size_t n_entries);
+    void clear();
+    size_t size() const { return n_; }
+
+   private:
+    struct Slot {
+        MatKey key;
+        bool used = false;
+    };
+    std::vector<Slot> slots_;
+    std::vector<MatEntry> vals_;
+    size_t n_ = 0, mask_ = 0;
+    size_t home(const MatKey& k) const;
+    void grow(size_t cap);
+};
+
 struct Slab {
     void* p = nullptr;
     size_t size = 0, used = 0;
@@ -173,7 +199,7 @@ struct cafe_ctx {
     int err_rows = 0, err_ndev = 0;
     cafe::DevBuf d_err;
     // matrix cache
-    std::unordered_map<cafe::MatKey, cafe::MatEntry, cafe::MatKeyHash> cache;
+    cafe::MatCache cache;
     std::vector<cafe::Slab> slabs;
     std::vector<cudaEvent_t> batch_events;
     size_t cache_bytes = 0, cache_cap = 0;
