@@ -467,3 +467,214 @@ int oracle_score(const oracle_tree* tree, const int32_t* counts, int64_t F, int 
     free(bl);
     return fail < 0 ? -1 : 0;
 }
+
+/* ---- Pupko joint reconstruction (src/gene_family_reconstructor.cpp) ---- */
+
+/* Matrices of every (lambda_i * m_k, t) key a tree needs, computed at the
+ * quantised key values; nm[k * n + v] is the matrix of the branch above v
+ * in category k (NULL at the root). */
+typedef struct {
+    cache_entry* e;
+    int n;
+    const double** nm;
+} node_mats;
+
+static void node_mats_build(const oracle_tree* tree, const double* lambdas, int K, const double* mult,
+                            int size, node_mats* out) {
+    int n = tree->n_nodes;
+    out->e = calloc((size_t)K * n + 1, sizeof(cache_entry));
+    out->n = 0;
+    out->nm = calloc((size_t)K * n, sizeof(double*));
+    for (int k = 0; k < K; k++)
+        for (int v = 0; v < n; v++) {
+            if (tree->parent[v] < 0) continue;
+            double lam = lambdas[tree->lambda_index[v]] * mult[k];
+            long lq = (long)(lam * 1000000000), tq = (long)(tree->branch_length[v] * 1000);
+            int idx = find_key(out->e, out->n, lq, tq);
+            if (idx < 0) {
+                idx = out->n++;
+                out->e[idx].lq = lq;
+                out->e[idx].tq = tq;
+                out->e[idx].m = malloc(sizeof(double) * (size_t)size * size);
+                oracle_fill_matrix((double)lq / 1000000000.0, (double)tq / 1000.0, size, out->e[idx].m);
+            }
+            out->nm[(size_t)k * n + v] = out->e[idx].m;
+        }
+}
+
+static void node_mats_free(node_mats* m) {
+    for (int i = 0; i < m->n; i++) free(m->e[i].m);
+    free(m->e);
+    free(m->nm);
+}
+
+/* reconstruct_gene_family (src/gene_family_reconstructor.cpp:161-190) for
+ * one family and one category: leaf (:30-45), root (:47-78) and internal
+ * (:80-116) steps in reverse-level order, then the backtrack from the
+ * root's single state. L / C hold n_nodes * (S + 1) entries. */
+static void pupko_one(const oracle_tree* tree, const int* order, const int* cstart, const int* children,
+                      const int32_t* counts_row, const double* const* nm, int size, const double* prior,
+                      int n_prior, int S, int R, double* L, int* C, int32_t* state, double* root_max) {
+    int n = tree->n_nodes;
+    int len = S + 1;
+    int root_len = (S < R ? S : R) + 1;
+    memset(L, 0, sizeof(double) * (size_t)n * len);
+    memset(C, 0, sizeof(int) * (size_t)n * len);
+    int root = order[n - 1];
+    for (int oi = 0; oi < n; oi++) {
+        int v = order[oi];
+        double* Lv = L + (size_t)v * len;
+        int* Cv = C + (size_t)v * len;
+        if (cstart[v] == cstart[v + 1]) {
+            int cnt = counts_row[tree->leaf_col[v]];
+            const double* m = nm[v];
+            for (int i = 0; i < len; i++) {
+                Cv[i] = cnt;
+                Lv[i] = m[(size_t)i * size + cnt];
+            }
+        } else if (v == root) {
+            for (int i = 1; i < root_len; i++) {
+                double max_val = -1;
+                for (int j = 1; j < root_len; j++) {
+                    double value = 1.0;
+                    for (int k = cstart[v]; k < cstart[v + 1]; k++) value *= L[(size_t)children[k] * len + j];
+                    double eq = j < n_prior ? prior[j] : 0.0;
+                    double val = value * eq;
+                    if (val > max_val) {
+                        max_val = val;
+                        Cv[0] = j;
+                    }
+                }
+                Lv[i] = max_val;
+            }
+        } else {
+            const double* m = nm[v];
+            for (int i = 0; i < len; i++) {
+                int max_j = 0;
+                double max_val = -1;
+                for (int j = 0; j < len; j++) {
+                    double value = 1.0;
+                    for (int k = cstart[v]; k < cstart[v + 1]; k++) value *= L[(size_t)children[k] * len + j];
+                    double val = value * m[(size_t)i * size + j];
+                    if (val > max_val) {
+                        max_j = j;
+                        max_val = val;
+                    }
+                }
+                Lv[i] = max_val;
+                Cv[i] = max_j;
+            }
+        }
+    }
+    /* backtracker: internal nodes take C[parent state]; leaves keep their
+     * observed count (get_node_count, src/base_model.cpp:190-199) */
+    double mx = L[(size_t)root * len];
+    for (int i = 1; i < root_len; i++)
+        if (L[(size_t)root * len + i] > mx) mx = L[(size_t)root * len + i];
+    *root_max = mx;
+    for (int oi = n - 1; oi >= 0; oi--) {
+        int v = order[oi];
+        if (v == root) state[v] = C[(size_t)root * len];
+        else if (cstart[v] == cstart[v + 1]) state[v] = counts_row[tree->leaf_col[v]];
+        else state[v] = C[(size_t)v * len + state[tree->parent[v]]];
+    }
+}
+
+int oracle_reconstruct(const oracle_tree* tree, const int32_t* counts, int64_t F, int n_leaves,
+                       const double* lambdas, int n_lambdas, int K, const double* multipliers,
+                       const double* cat_probs, const double* prior, int n_prior, int S, int R,
+                       int n_threads, int32_t* state, double* mean, int32_t* node_count, double* root_max) {
+    int n = tree->n_nodes;
+    if (n <= 0 || F < 0 || n_lambdas <= 0 || S < 1 || R < 1) return -1;
+    double one = 1.0;
+    int gamma = K > 0;
+    if (!gamma) {
+        K = 1;
+        multipliers = &one;
+    }
+    for (int64_t f = 0; f < F * n_leaves; f++)
+        if (counts[f] < 0 || counts[f] > S) return -1;
+    int size = (S > R ? S : R) + 1;
+    node_mats nm;
+    node_mats_build(tree, lambdas, K, multipliers, size, &nm);
+    int *cstart, *children;
+    int* order = reverse_level_order(tree, &cstart, &children);
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+#pragma omp parallel
+    {
+        double* L = malloc(sizeof(double) * (size_t)n * (S + 1));
+        int* C = malloc(sizeof(int) * (size_t)n * (S + 1));
+#pragma omp for schedule(dynamic, 4) collapse(2)
+        for (int k = 0; k < K; k++)
+            for (int64_t f = 0; f < F; f++)
+                pupko_one(tree, order, cstart, children, counts + (size_t)f * n_leaves, nm.nm + (size_t)k * n, size,
+                          prior, n_prior, S, R, L, C, state + ((size_t)k * F + f) * n, root_max + (size_t)k * F + f);
+        free(L);
+        free(C);
+    }
+    /* gamma: get_weighted_averages (src/gamma_core.cpp:268-287) over the
+     * categories in order, rounded by get_node_count (:396-402); the
+     * reference's category maps hold internal nodes and the root only */
+    for (int64_t f = 0; f < F; f++)
+        for (int v = 0; v < n; v++) {
+            const int leaf = cstart[v] == cstart[v + 1];
+            double val;
+            if (leaf) {
+                val = (double)counts[(size_t)f * n_leaves + tree->leaf_col[v]];
+            } else if (gamma) {
+                val = 0.0;
+                for (int k = 0; k < K; k++) val += cat_probs[k] * (double)state[((size_t)k * F + f) * n + v];
+            } else {
+                val = (double)state[(size_t)f * n + v];
+            }
+            if (mean) mean[(size_t)f * n + v] = val;
+            if (node_count) node_count[(size_t)f * n + v] = (int32_t)round(val);
+        }
+    free(order);
+    free(cstart);
+    free(children);
+    node_mats_free(&nm);
+    return 0;
+}
+
+/* compute_viterbi_sum (src/gene_family_reconstructor.cpp:390-430): for the
+ * branch above each non-root node, the probability mass of child sizes
+ * m < S that are less likely than the reconstructed one (ties count half),
+ * under the model's own lambdas. NaN at the root (invalid). */
+int oracle_branch_probabilities(const oracle_tree* tree, const double* lambdas, int n_lambdas,
+                                const int32_t* node_count, int64_t F, int S, int R, double* out) {
+    int n = tree->n_nodes;
+    if (n <= 0 || F < 0 || n_lambdas <= 0 || S < 1) return -1;
+    int size = (S > R ? S : R) + 1;
+    double one = 1.0;
+    node_mats nm;
+    node_mats_build(tree, lambdas, 1, &one, size, &nm);
+    int rc = 0;
+    for (int64_t f = 0; f < F; f++)
+        for (int v = 0; v < n; v++) {
+            double* o = out + (size_t)f * n + v;
+            int p = tree->parent[v];
+            if (p < 0) {
+                *o = NAN;
+                continue;
+            }
+            int ps = node_count[(size_t)f * n + p], cs = node_count[(size_t)f * n + v];
+            if (ps < 0 || cs < 0 || ps >= size || cs >= size || S > size) {
+                rc = -1;
+                *o = NAN;
+                continue;
+            }
+            const double* row = nm.nm[v] + (size_t)ps * size;
+            double calc = row[cs], result = 0;
+            for (int m = 0; m < S; m++) {
+                double pm = row[m];
+                if (pm == calc) result += pm / 2.0;
+                else if (pm < calc) result += pm;
+            }
+            *o = result;
+        }
+    node_mats_free(&nm);
+    return rc;
+}

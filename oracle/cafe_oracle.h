@@ -73,6 +73,28 @@ int oracle_score(const oracle_tree* tree, const int32_t* counts, int64_t F, int 
                  int model, int dedupe, int scaled, int n_threads,
                  double* fam_lnl, double* cat_lh, double* total);
 
+/* Pupko joint ancestral reconstruction (model::reconstruct_ancestral_states,
+ * src/base_model.cpp:133-170 and src/gamma_core.cpp:290-339, over
+ * reconstruct_gene_family, src/gene_family_reconstructor.cpp:161-190).
+ *   K = 0        base model (one pass at the lambdas themselves)
+ *   K >= 1       gamma model: one pass per category at lambda * m_k
+ *   S, R         max_family_size / max_root_family_size
+ * Outputs state[K'][F][n_nodes] (K' = max(K, 1); leaves hold their observed
+ * count), mean[F][n_nodes] (gamma: sum_k p_k * state_k; base: the state),
+ * node_count[F][n_nodes] (mean rounded half away from zero) and
+ * root_max[K'][F] (largest root L; the reference calls a family
+ * reconstructed iff > 0). mean / node_count may be NULL. */
+int oracle_reconstruct(const oracle_tree* tree, const int32_t* counts, int64_t F, int n_leaves,
+                       const double* lambdas, int n_lambdas, int K, const double* multipliers,
+                       const double* cat_probs, const double* prior, int n_prior, int S, int R,
+                       int n_threads, int32_t* state, double* mean, int32_t* node_count, double* root_max);
+
+/* compute_viterbi_sum (src/gene_family_reconstructor.cpp:390-430) for every
+ * family and node from reconstructed node counts [F][n_nodes]; NaN at the
+ * root. */
+int oracle_branch_probabilities(const oracle_tree* tree, const double* lambdas, int n_lambdas,
+                                const int32_t* node_count, int64_t F, int S, int R, double* out);
+
 #ifdef __cplusplus
 }
 #endif

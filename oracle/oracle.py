@@ -53,6 +53,11 @@ def lib():
         _lib.oracle_score.restype = i
         _lib.oracle_score.argtypes = [C.POINTER(_Tree), p, C.c_int64, i, p, i, i, i, p, p, p, i, p, i, i,
                                       i, i, p, p, i, i, i, i, p, p, p]
+        _lib.oracle_reconstruct.restype = i
+        _lib.oracle_reconstruct.argtypes = [C.POINTER(_Tree), p, C.c_int64, i, p, i, i, p, p, p, i, i, i, i,
+                                            p, p, p, p]
+        _lib.oracle_branch_probabilities.restype = i
+        _lib.oracle_branch_probabilities.argtypes = [C.POINTER(_Tree), p, i, p, C.c_int64, i, i, p]
     return _lib
 
 
@@ -141,3 +146,42 @@ def score(tree: TreeArrays, counts: np.ndarray, lambdas: Sequence[float], *, lam
     if rc:
         raise RuntimeError(f"oracle_score failed: {rc}")
     return float(tot[0]), fam, cat
+
+
+def reconstruct(tree: TreeArrays, counts: np.ndarray, lambdas: Sequence[float], *, prior: np.ndarray,
+                S: int, R: int, multipliers: Optional[Sequence[float]] = None,
+                cat_probs: Optional[Sequence[float]] = None, n_threads: int = 0):
+    """Pupko reconstruction: (state[K][F][n], mean[F][n], node_count[F][n],
+    root_max[K][F]); K = 1 for the base model (multipliers None)."""
+    counts = np.ascontiguousarray(counts, dtype=np.int32)
+    F, n_leaves = counts.shape
+    n = len(tree.parent)
+    lam = np.ascontiguousarray(lambdas, dtype=np.float64)
+    gamma = multipliers is not None
+    mult = np.ascontiguousarray(multipliers if gamma else [1.0], dtype=np.float64)
+    cp = np.ascontiguousarray(cat_probs if gamma else [1.0], dtype=np.float64)
+    K = len(mult)
+    pr = np.ascontiguousarray(prior, dtype=np.float64)
+    state = np.zeros((K, F, n), np.int32)
+    mean = np.zeros((F, n))
+    cnt = np.zeros((F, n), np.int32)
+    rmax = np.zeros((K, F))
+    rc = lib().oracle_reconstruct(C.byref(tree.c), counts.ctypes.data, F, n_leaves, lam.ctypes.data, len(lam),
+                                  K if gamma else 0, mult.ctypes.data, cp.ctypes.data, pr.ctypes.data, len(pr),
+                                  S, R, n_threads, state.ctypes.data, mean.ctypes.data, cnt.ctypes.data,
+                                  rmax.ctypes.data)
+    if rc:
+        raise RuntimeError(f"oracle_reconstruct failed: {rc}")
+    return state, mean, cnt, rmax
+
+
+def branch_probabilities(tree: TreeArrays, lambdas: Sequence[float], node_count: np.ndarray, S: int, R: int):
+    """compute_viterbi_sum for every family and node: [F][n], NaN at the root."""
+    nc = np.ascontiguousarray(node_count, dtype=np.int32)
+    lam = np.ascontiguousarray(lambdas, dtype=np.float64)
+    out = np.zeros(nc.shape)
+    rc = lib().oracle_branch_probabilities(C.byref(tree.c), lam.ctypes.data, len(lam), nc.ctypes.data,
+                                           nc.shape[0], S, R, out.ctypes.data)
+    if rc:
+        raise RuntimeError(f"oracle_branch_probabilities failed: {rc}")
+    return out

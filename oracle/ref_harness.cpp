@@ -9,6 +9,9 @@
 //   inference_prune                        (src/core.cpp:134-145)
 //   fminsearch_min over the optimizer scorers (src/optimizer.cpp:281-322,
 //                                           src/optimizer_scorer.cpp:22-180)
+//   model::reconstruct_ancestral_states     (src/base_model.cpp:133-170,
+//                                           src/gamma_core.cpp:290-339)
+//   compute_viterbi_sum                     (src/gene_family_reconstructor.cpp:390-430)
 //
 // It reads the reference's own file formats (Newick tree, CAFE family
 // table, error-model file) through the reference's own readers
@@ -42,6 +45,7 @@
 #include "gamma.h"
 #include "gamma_core.h"
 #include "gene_family.h"
+#include "gene_family_reconstructor.h"
 #include "io.h"
 #include "lambda.h"
 #include "matrix_cache.h"
@@ -49,6 +53,7 @@
 #include "optimizer_scorer.h"
 #include "probability.h"
 #include "root_equilibrium_distribution.h"
+#include "user_data.h"
 
 INITIALIZE_EASYLOGGINGPP
 
@@ -148,6 +153,7 @@ void usage() {
         "   [--max-family S --max-root R] [--prior uniform|uniform:N|poisson:X|rootdist:s=n,..]\n"
         "   [--repeat N] [--quiet]\n"
         "   [--optimize lambda|alpha|lambda_alpha|lambda_epsilon --initial x1,..]\n"
+        "   [--reconstruct]\n"
         "cafe_ref_harness nm rosen|wall|bowl|product <maxiters> x1,..\n");
 }
 
@@ -214,7 +220,7 @@ int main(int argc, char** argv) {
     std::vector<double> lambdas, gmult, gprob;
     double alpha = -1;
     int gk = 0, S = -1, R = -1, repeat = 1;
-    bool quiet = false;
+    bool quiet = false, recon = false;
     for (int i = 1; i < argc; ++i) {
         std::string a = argv[i];
         auto next = [&]() -> std::string {
@@ -237,6 +243,7 @@ int main(int argc, char** argv) {
         else if (a == "--quiet") quiet = true;
         else if (a == "--optimize") opt_kind = next();
         else if (a == "--initial") opt_initial = parse_list(next());
+        else if (a == "--reconstruct") recon = true;
         else { usage(); return 2; }
     }
     if (tree_path.empty() || fam_path.empty() || lambdas.empty()) { usage(); return 2; }
@@ -363,6 +370,58 @@ int main(int argc, char** argv) {
                 for (auto& s : pg->stash())
                     std::printf("cat %s %a %a %a\n", s.family_id.c_str(), s.lambda_multiplier,
                                 s.category_likelihood, s.family_likelihood);
+            }
+        }
+        if (recon) {
+            // model::reconstruct_ancestral_states as the estimate action runs
+            // it (src/execute.cpp:161-185): a cache of side
+            // max(max family, max root) + 100, then compute_viterbi_sum for
+            // every node of every family. Nodes are printed in prefix
+            // (Newick) order.
+            std::vector<const clade*> nodes;
+            tree->apply_prefix_order([&](const clade* c) { nodes.push_back(c); });
+            user_data ud;
+            ud.max_family_size = max_fam;
+            ud.max_root_family_size = max_root;
+            ud.p_tree = tree.get();
+            ud.gene_families.swap(families);   // gene_family is not copy-assignable
+            ud.prior = std::move(*prior);
+            input_parameters ui;
+            matrix_cache cache(std::max(max_fam, max_root) + 100);
+            cache.precalculate_matrices(get_lambda_values(lam.get()), tree->get_branch_lengths());
+            std::unique_ptr<reconstruction> rec(m->reconstruct_ancestral_states(ud, ui, &cache));
+            for (auto& gf : ud.gene_families) {
+                std::printf("rec %s", gf.id().c_str());
+                for (auto* c : nodes) std::printf(" %d", rec->get_node_count(gf, c));
+                std::printf("\n");
+                std::printf("bp %s", gf.id().c_str());
+                for (auto* c : nodes) {
+                    auto bp = compute_viterbi_sum(c, gf, rec.get(), max_fam, cache, lam.get());
+                    if (bp._is_valid) std::printf(" %a", bp._value);
+                    else std::printf(" NA");
+                }
+                std::printf("\n");
+            }
+            if (pg) {
+                auto* gr = dynamic_cast<gamma_model_reconstruction*>(rec.get());
+                for (auto& gf : ud.gene_families) {
+                    auto& r = gr->_reconstructions.at(gf.id());
+                    for (size_t k = 0; k < r.category_reconstruction.size(); ++k) {
+                        std::printf("rcat %s %zu", gf.id().c_str(), k);
+                        for (auto* c : nodes) {
+                            auto it = r.category_reconstruction[k].find(c);
+                            std::printf(" %d", it == r.category_reconstruction[k].end() ? -1 : it->second);
+                        }
+                        std::printf("\n");
+                    }
+                    std::printf("rmean %s", gf.id().c_str());
+                    for (auto* c : nodes) {
+                        auto it = r.reconstruction.find(c);
+                        if (it == r.reconstruction.end()) std::printf(" NA");
+                        else std::printf(" %a", it->second);
+                    }
+                    std::printf("\n");
+                }
             }
         }
     } catch (std::exception& e) {

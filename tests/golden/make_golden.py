@@ -5,7 +5,10 @@ oracle/Makefile into oracle/_ref/cafe_ref_harness -- on small seeded
 synthetic cases and on the inputs of the reference's own known-answer
 tests, and stores inputs plus hex-float outputs:
 
-  ref_cases.json     end-to-end infer_family_likelihoods cases
+  ref_cases.json     end-to-end infer_family_likelihoods cases, with the
+                     Pupko reconstruction and branch probabilities of each
+                     valid case (reconstruct_ancestral_states,
+                     compute_viterbi_sum)
   ref_matrices.json  transition matrices from matrix_cache
   ref_optimizer.json Nelder-Mead searches (fminsearch_min) over analytic
                      objectives and over the likelihood scorers
@@ -78,9 +81,32 @@ def parse_search(out: str):
     return res
 
 
+def parse_recon(out: str, ids, n_nodes):
+    """`rec` / `bp` / `rcat` / `rmean` lines of the harness's --reconstruct."""
+    rec, bp, rcat, rmean = {}, {}, {}, {}
+    for ln in out.splitlines():
+        tok = ln.split()
+        if tok[0] == "rec":
+            rec[tok[1]] = [int(x) for x in tok[2:]]
+        elif tok[0] == "bp":
+            bp[tok[1]] = [None if x == "NA" else x for x in tok[2:]]
+        elif tok[0] == "rcat":
+            rcat.setdefault(tok[1], []).append([int(x) for x in tok[3:]])
+        elif tok[0] == "rmean":
+            rmean[tok[1]] = [None if x == "NA" else x for x in tok[2:]]
+    for d in (rec, bp):
+        assert all(len(d[i]) == n_nodes for i in ids)
+    # one space-separated string per family (per category for cat_state)
+    # keeps the fixture small
+    j = lambda v: " ".join("NA" if x is None else str(x) for x in v)
+    return {"node_count": [j(rec[i]) for i in ids], "bp_hex": [j(bp[i]) for i in ids],
+            "cat_state": [[j(r) for r in rcat[i]] for i in ids] if rcat else None,
+            "mean_hex": [j(rmean[i]) for i in ids] if rmean else None}
+
+
 def make_case(name, tree, fams, lambdas, *, lam_idx=None, model="base", mult=None, probs=None,
               err=None, S=None, R=None, prior="uniform", note="", alpha=None, K=None, optimize=None,
-              initial=None):
+              initial=None, recon=False):
     with tempfile.TemporaryDirectory() as d:
         tp, fp = os.path.join(d, "t.nwk"), os.path.join(d, "f.tab")
         nwk = tree.to_newick()
@@ -110,6 +136,7 @@ def make_case(name, tree, fams, lambdas, *, lam_idx=None, model="base", mult=Non
             search = parse_search(run(args + ["--optimize", optimize, "--initial",
                                               ",".join(repr(x) for x in initial)]))
         out = parse_output(run(args))
+        rec = parse_recon(run(args + ["--reconstruct", "--quiet"]), fams.ids, tree.n_nodes) if recon else None
     case = {
         "name": name, "note": note, "newick": nwk, "lambda_newick": lnwk, "taxa": tree.leaf_names,
         "ids": fams.ids, "counts": fams.counts.tolist(), "lambdas": [float(x).hex() for x in lambdas],
@@ -120,11 +147,18 @@ def make_case(name, tree, fams, lambdas, *, lam_idx=None, model="base", mult=Non
         "expected": {"total_hex": out["total_hex"], "fam_lnl_hex": [out["fam"].get(i) for i in fams.ids],
                      "cat": [out["cat"].get(i) for i in fams.ids] if model == "gamma" else None},
     }
+    if rec is not None:
+        case["recon"] = rec
     if optimize is not None:
         case["optimize"] = optimize
         case["initial"] = [float(x).hex() for x in initial]
         case["search"] = search
     return case
+
+
+def make_case_r(*a, **kw):
+    kw.setdefault("recon", True)
+    return make_case(*a, **kw)
 
 
 def main():
@@ -134,48 +168,50 @@ def main():
     # -- the reference's own known-answer inputs (test.cpp) --------------
     t = parse_newick("(A:1,B:1);")
     fams = FamilySet(["f1", "f2", "f3", "f4"], np.array([[1, 2], [2, 1], [3, 6], [6, 3]], np.int32))
-    cases.append(make_case("kat_infer_processes", t, fams, [0.01], S=56, R=8, prior="uniform:100",
+    cases.append(make_case_r("kat_infer_processes", t, fams, [0.01], S=56, R=8, prior="uniform:100",
                            note="test.cpp:461-488, expected -lnL 46.56632"))
     t = parse_newick("(A:1,B:3):7;")
     fams = FamilySet(["f1"], np.array([[3, 6]], np.int32))
-    cases.append(make_case("kat_gamma_prune", t, fams, [0.005], model="gamma", mult=[0.1, 0.5], probs=[0.01, 0.05],
+    cases.append(make_case_r("kat_gamma_prune", t, fams, [0.005], model="gamma", mult=[0.1, 0.5], probs=[0.01, 0.05],
                            S=10, R=8, prior="rootdist:1=2,2=2,3=2,4=2,5=1",
                            note="test.cpp:1269-1294, log category likelihoods -23.04433, -16.68005"))
     t = parse_newick("(A:1,B:3):7;")
-    cases.append(make_case("kat_gamma_saturated", t, fams, [0.9], model="gamma", mult=[0.1, 0.5], probs=[1.0, 1.0],
-                           S=10, R=8, prior="uniform:100", note="test.cpp:1296-1311: saturated -> +inf"))
+    cases.append(make_case_r("kat_gamma_saturated", t, fams, [0.9], model="gamma", mult=[0.1, 0.5], probs=[1.0, 1.0],
+                           S=10, R=8, prior="uniform:100", note="test.cpp:1296-1311: saturated -> +inf",
+                           recon=False))
     # -- seeded synthetic cases ---------------------------------------------
     w0 = workload(0, n_families=150, seed=3)
-    cases.append(make_case("syn_base_12taxa", w0.tree, w0.families, [0.0025],
+    cases.append(make_case_r("syn_base_12taxa", w0.tree, w0.families, [0.0025],
                            note="config-0 shape, global S/R, uniform prior"))
-    cases.append(make_case("syn_base_12taxa_poisson", w0.tree, w0.families, [0.004], prior="poisson:5.5",
+    cases.append(make_case_r("syn_base_12taxa_poisson", w0.tree, w0.families, [0.004], prior="poisson:5.5",
                            note="Poisson root prior (float-rounded)"))
     zero = FamilySet(w0.families.ids[:20] + ["zero"], np.vstack([w0.families.counts[:20],
                                                                   np.zeros((1, 12), np.int32)]))
-    cases.append(make_case("syn_base_zero_family", w0.tree, zero, [0.003], note="an all-zero family row"))
-    cases.append(make_case("syn_base_invalid_lambda", w0.tree, zero, [0.0], note="lambda <= 0 -> +inf"))
+    cases.append(make_case_r("syn_base_zero_family", w0.tree, zero, [0.003], note="an all-zero family row"))
+    cases.append(make_case_r("syn_base_invalid_lambda", w0.tree, zero, [0.0], note="lambda <= 0 -> +inf",
+                           recon=False))
     w1 = workload(1, n_families=120, seed=4)
-    cases.append(make_case("syn_gamma_24taxa_k4", w1.tree, w1.families, [0.002], model="gamma",
+    cases.append(make_case_r("syn_gamma_24taxa_k4", w1.tree, w1.families, [0.002], model="gamma",
                            mult=w1.multipliers, probs=w1.cat_probs, note="config-1 shape, K=4 alpha=0.5"))
     probs8, mult8 = discrete_gamma(0.5, 8)
-    cases.append(make_case("syn_gamma_24taxa_k8_small_cat", w1.tree, FamilySet(w1.families.ids[:40],
+    cases.append(make_case_r("syn_gamma_24taxa_k8_small_cat", w1.tree, FamilySet(w1.families.ids[:40],
                                                                               w1.families.counts[:40]),
                            [0.003], model="gamma", mult=mult8, probs=probs8, note="K=8"))
     w2 = workload(2, n_families=400, seed=5)
     keep = w2.families.max_counts() <= 30
     f2 = FamilySet([i for i, k in zip(w2.families.ids, keep) if k][:80], w2.families.counts[keep][:80])
     err = "maxcnt: 200\ncntdiff: -1 0 1\n0 0 0.95 0.05\n1 0.05 0.9 0.05\n"
-    cases.append(make_case("syn_multilambda_error_32taxa", w2.tree, f2, [0.0015, 0.006], lam_idx=w2.lambda_of_node,
+    cases.append(make_case_r("syn_multilambda_error_32taxa", w2.tree, f2, [0.0015, 0.006], lam_idx=w2.lambda_of_node,
                            err=err, note="config-2 shape (counts<=30), two lambdas + error model"))
     # a family whose likelihood underflows FP64 (alternating 0 / 50 counts)
     uf = FamilySet(["alt", "flat"], np.array([[0 if i % 2 else 50 for i in range(24)], [1] * 24], np.int32))
-    cases.append(make_case("syn_base_underflow", w1.tree, uf, [0.001], S=110, R=75,
+    cases.append(make_case_r("syn_base_underflow", w1.tree, uf, [0.001], S=110, R=75,
                            note="first family underflows to L = 0 in FP64 -> -lnL = +inf"))
     # non-binary tree (a polytomy)
     tp = parse_newick("((A:2,B:2,C:2):3,(D:4,E:4):1);")
     rng = np.random.default_rng(7)
     cnt = simulate_families(tp, 30, np.full(30, 0.01), rng.integers(1, 6, 30), seed=8)
-    cases.append(make_case("syn_polytomy", tp, FamilySet([f"p{i}" for i in range(30)], cnt), [0.01],
+    cases.append(make_case_r("syn_polytomy", tp, FamilySet([f"p{i}" for i in range(30)], cnt), [0.01],
                            note="three children at one node"))
     json.dump({"generator": "tests/golden/make_golden.py", "cases": cases},
               open(os.path.join(HERE, "ref_cases.json"), "w"), indent=1)

@@ -42,6 +42,29 @@ class Case:
     total: float
     fam_lnl: List[Optional[float]]
     cat: Optional[list]
+    recon: Optional[dict] = None
+
+
+def _ints(rows):
+    return np.array([[int(x) for x in r.split()] for r in rows], dtype=np.int32)
+
+
+def _hexes(rows):
+    return np.array([[np.nan if x == "NA" else float.fromhex(x) for x in r.split()] for r in rows])
+
+
+def recon_from_json(r) -> Optional[dict]:
+    """The reference's reconstruction of a case: node_count[F][n],
+    branch_prob[F][n] (NaN at the root), and for the gamma model
+    cat_state[K][F][n] (-1 at leaves) and mean[F][n] (NaN at leaves)."""
+    if r is None:
+        return None
+    out = {"node_count": _ints(r["node_count"]), "branch_prob": _hexes(r["bp_hex"]),
+           "cat_state": None, "mean": None}
+    if r["cat_state"] is not None:
+        out["cat_state"] = np.stack([_ints(per_fam) for per_fam in r["cat_state"]]).transpose(1, 0, 2).copy()
+        out["mean"] = _hexes(r["mean_hex"])
+    return out
 
 
 def prior_from_spec(spec: str, R: int) -> RootPrior:
@@ -86,7 +109,7 @@ def case_from_json(c) -> Case:
         total=float.fromhex(c["expected"]["total_hex"]) if "x" in c["expected"]["total_hex"]
         else float(c["expected"]["total_hex"]),
         fam_lnl=[hexf(x) if x is not None else None for x in c["expected"]["fam_lnl_hex"]],
-        cat=cat)
+        cat=cat, recon=recon_from_json(c.get("recon")))
 
 
 def load_cases() -> List[Case]:

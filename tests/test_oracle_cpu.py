@@ -215,3 +215,40 @@ def test_saturated_category_is_rejected_by_both():
     tot, _, _ = oracle.score(ta, case.counts, case.lambdas, model=1, multipliers=case.multipliers,
                              cat_probs=case.cat_probs, prior=case.prior, S=case.S, R=case.R, scaled=True)
     assert tot == math.inf
+
+
+RECON = [c for c in CASES if c.recon is not None]
+
+
+@pytest.mark.parametrize("case", RECON, ids=[c.name for c in RECON])
+def test_oracle_reconstruction_matches_reference(case):
+    """Pupko joint reconstruction and branch probabilities, bit for bit
+    against model::reconstruct_ancestral_states and compute_viterbi_sum of
+    the compiled reference: node counts, per-category states and weighted
+    means (gamma), and every branch probability."""
+    ta = oracle.TreeArrays.from_tree(case.tree, case.lambda_of_node)
+    gamma = case.model == 1
+    state, mean, cnt, rmax = oracle.reconstruct(ta, case.counts, case.lambdas, prior=case.prior, S=case.S,
+                                                R=case.R, multipliers=case.multipliers if gamma else None,
+                                                cat_probs=case.cat_probs if gamma else None)
+    ref = case.recon
+    assert np.array_equal(cnt, ref["node_count"])
+    if gamma:
+        internal = ref["cat_state"][0, 0] >= 0
+        assert np.array_equal(state[:, :, internal], ref["cat_state"][:, :, internal])
+        assert np.array_equal(mean[:, internal], ref["mean"][:, internal])
+    bp = oracle.branch_probabilities(ta, case.lambdas, ref["node_count"], case.S, case.R)
+    assert np.array_equal(bp, ref["branch_prob"], equal_nan=True)
+
+
+def test_reconstruction_edge_cases_present():
+    """The fixtures cover a family whose likelihood underflows (root L = 0
+    -> the reference's failed reconstruction), a polytomy, two lambdas and
+    gamma categories whose root L underflows."""
+    names = {c.name for c in RECON}
+    assert {"syn_base_underflow", "syn_polytomy", "syn_multilambda_error_32taxa",
+            "syn_gamma_24taxa_k8_small_cat"} <= names
+    case = [c for c in RECON if c.name == "syn_base_underflow"][0]
+    ta = oracle.TreeArrays.from_tree(case.tree, case.lambda_of_node)
+    _, _, _, rmax = oracle.reconstruct(ta, case.counts, case.lambdas, prior=case.prior, S=case.S, R=case.R)
+    assert rmax[0, 0] == 0 and rmax[0, 1] > 0
