@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--serving-clients", type=int, default=8)
     ap.add_argument("--serving-requests", type=int, default=12, help="requests per client")
+    ap.add_argument("--no-reconstruct", dest="reconstruct", action="store_false",
+                    help="skip the ancestral-reconstruction measurement")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default tensor-core launch shapes (no cafe_autotune before the warm-up)")
     ap.add_argument("--profile-only", action="store_true",
@@ -294,6 +296,51 @@ def serving_phase(ctx, tid, sid, w, clients: int, per_client: int, kw):
             "note": "single-candidate requests from concurrent closed-loop optimizer clients, merged by the continuous-batching loop; latency submit -> done"}
 
 
+def reconstruction_phase(ctx, tid, sid, w, fams, S, R, cpu_seconds: float, reps: int = 3):
+    """Pupko joint reconstruction of every family x gamma category at the
+    reference's global bounds (cafe_reconstruct): the log2-filtered kernel,
+    the exhaustive FP64 scan, and the CPU oracle on a bounded sample."""
+    from cafe5_gb300.inputs import RootPrior
+    prior = RootPrior.uniform(R).vector(R + 8)
+    ctx.set_prior(prior)
+    kw = dict(S=S, R=R, model=1, multipliers=w.multipliers, cat_probs=w.cat_probs)
+    lam = [w.true_lambda]
+    ctx.reconstruct(tid, sid, lam, **kw)                     # matrices built, buffers sized
+    ms = min(ctx.reconstruct(tid, sid, lam, **kw).device_ms for _ in range(reps))
+    ex = ctx.reconstruct(tid, sid, lam, exhaustive=True, **kw)
+    rec = ctx.reconstruct(tid, sid, lam, **kw)
+    F, K = fams.n_families, len(w.multipliers)
+    out = {"unit": "family-category reconstructions/s", "value": F * K / (ms / 1e3), "device_ms": ms,
+           "exhaustive_fp64_device_ms": ex.device_ms, "filter_speedup": ex.device_ms / ms,
+           "identical_to_exhaustive": bool(np.array_equal(ex.category_state, rec.category_state)),
+           "families": F, "K": K, "S": S, "R": R, "n_failed": int(rec.n_failed),
+           "note": "device time of cafe_reconstruct (matrices cached); states 0..S per node"}
+    if cpu_seconds > 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        ta = oracle.TreeArrays.from_tree(w.tree)
+
+        def timed(n):
+            t0 = time.perf_counter()
+            oracle.reconstruct(ta, fams.counts[:n], lam, prior=prior, S=S, R=R, multipliers=w.multipliers,
+                               cat_probs=w.cat_probs, n_threads=os.cpu_count() or 1)
+            return time.perf_counter() - t0
+
+        # the oracle builds its matrices inside each call: the difference of
+        # two sample sizes leaves the per-family work
+        t0 = timed(16)
+        n = 64
+        while True:
+            dt = timed(n)
+            if dt - t0 >= cpu_seconds / 2 or n >= F:
+                break
+            n = min(F, n * 4)
+        out["cpu_port"] = {"value": (n - 16) * K / max(dt - t0, 1e-9), "cores": os.cpu_count() or 1,
+                           "kind": "port",
+                           "sample": f"{n} minus 16 of {F} families x K={K} (matrix build cancelled out)"}
+    return out
+
+
 def run_ours(args):
     import torch
     from cafe5_gb300.engine import Context
@@ -418,6 +465,10 @@ def run_ours(args):
     if rank == 0 and args.serving_clients > 0:
         serving = serving_phase(ctx, tid, sid, w, args.serving_clients, args.serving_requests, kw)
 
+    recon = None
+    if rank == 0 and args.reconstruct:
+        recon = reconstruction_phase(ctx, tid, sid, w, fams, S, R, args.cpu_seconds / 2)
+
     peaks = measured_peaks()
     fp64_peak = fp64_peak_tflops(torch, dev)
     nl = max(prof["prune_launches"], 1)
@@ -469,6 +520,7 @@ def run_ours(args):
                 "e2e": {"value": e2e_value, "unit": "family-lnL evals/s",
                         "h2d_bytes_per_step": int(fams.counts.nbytes), "d2h_bytes_per_step": int(B * (F * 8 + 8))},
                 "serving": serving,
+                "reconstruction": recon,
                 "gpu_launches": int(round(prof["launches"] / prof_steps * args.steps)),
                 "cuda_graphs": "pruning phase (conversion, tensor-core bins, fallback, finish) replayed as a CUDA "
                                "graph per launch signature; matrix builds launched directly",

@@ -27,6 +27,7 @@ EXPORTS = [
     "cafe_score_device", "cafe_submit", "cafe_poll", "cafe_serving_stats", "cafe_profile_enable",
     "cafe_profile_read", "cafe_prune_fp64_noalloc", "cafe_optimize", "cafe_discrete_gamma",
     "cafe_nelder_mead", "cafe_score_batch", "cafe_score_batch_device", "cafe_serving_counters", "cafe_autotune",
+    "cafe_reconstruct", "cafe_branch_probabilities",
 ]
 OPT_LAMBDA, OPT_LAMBDA_ALPHA, OPT_LAMBDA_EPSILON, OPT_ALPHA = 0, 1, 2, 3
 
@@ -79,6 +80,12 @@ class ServingInfo(C.Structure):
                 ("wait_ms", C.c_double), ("device_ms", C.c_double)]
 
 
+class Reconstruction(C.Structure):
+    _fields_ = [("node_count", C.c_void_p), ("node_mean", C.c_void_p), ("category_state", C.c_void_p),
+                ("root_max", C.c_void_p), ("exhaustive", C.c_int), ("n_failed", C.c_int64),
+                ("device_ms", C.c_double)]
+
+
 _lib = None
 
 
@@ -129,6 +136,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
         "cafe_optimize": (i, [p, P(Request), P(OptConfig), P(OptResult)]),
         "cafe_discrete_gamma": (i, [i, d, p, p]),
         "cafe_nelder_mead": (i, [P(OptConfig), OBJECTIVE, p, P(OptResult)]),
+        "cafe_reconstruct": (i, [p, P(Request), P(Reconstruction)]),
+        "cafe_branch_probabilities": (i, [p, P(Request), p, p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

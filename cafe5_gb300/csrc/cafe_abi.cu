@@ -1543,6 +1543,226 @@ int score_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, int NB, cafe_r
     return score_complete(C, ws, R, NB, res, info);
 }
 
+// ---- ancestral reconstruction
+
+// Shared checks of cafe_reconstruct / cafe_branch_probabilities: tree, set,
+// lambdas, bounds; the FP64 matrix of every (category, non-root node) at
+// side max(S, R) + 1 (the reference's cache side plus 100 holds the same
+// entries), pointers staged into ws.mats with the builds waited for.
+struct ReconSetup {
+    TreeHost* T = nullptr;
+    FamSet* S = nullptr;
+    int K = 1, Smax = 0, Rmax = 0, msize = 0;
+    bool gamma = false;
+};
+
+int recon_setup(cafe_ctx* C, Workspace& ws, const cafe_request* R, bool categories, ReconSetup* o) {
+    if (!R) return fail(C, CAFE_ERR_INVALID, "null request");
+    auto ti = C->trees.find(R->tree_id);
+    if (ti == C->trees.end()) return fail(C, CAFE_ERR_NOT_FOUND, "unknown tree id %d", R->tree_id);
+    auto si = C->sets.find(R->set_id);
+    if (si == C->sets.end()) return fail(C, CAFE_ERR_NOT_FOUND, "unknown family set id %d", R->set_id);
+    TreeHost& T = *ti->second;
+    FamSet& S = *si->second;
+    if (S.tree_id != R->tree_id) return fail(C, CAFE_ERR_INVALID, "family set %d belongs to tree %d", R->set_id, S.tree_id);
+    const bool gamma = categories && R->model == CAFE_MODEL_GAMMA;
+    if (R->model != CAFE_MODEL_BASE && R->model != CAFE_MODEL_GAMMA) return fail(C, CAFE_ERR_INVALID, "bad model %d", R->model);
+    const int K = gamma ? R->n_categories : 1;
+    if (gamma && (K < 1 || !R->multipliers || !R->cat_probs))
+        return fail(C, CAFE_ERR_INVALID, "gamma needs K >= 1 with multipliers and probabilities");
+    if (R->n_lambdas < 1 || !R->lambdas) return fail(C, CAFE_ERR_INVALID, "no lambdas");
+    for (int v = 0; v < T.n_nodes; ++v)
+        if (T.parent[v] >= 0 && (T.lambda_index[v] < 0 || T.lambda_index[v] >= R->n_lambdas))
+            return fail(C, CAFE_ERR_INVALID, "lambda index %d out of range at node %d", T.lambda_index[v], v);
+    const int Sg = R->max_family_size, Rg = R->max_root_family_size;
+    if (Sg < 1 || Rg < 1) return fail(C, CAFE_ERR_INVALID, "reconstruction needs max_family_size and max_root_family_size");
+    int maxc = 0;
+    for (int64_t f = 0; f < S.F; ++f) maxc = std::max(maxc, S.max_count[f]);
+    if (maxc > Sg) return fail(C, CAFE_ERR_INVALID, "a count (%d) exceeds max_family_size (%d)", maxc, Sg);
+    const int msize = std::max(Sg, Rg) + 1;
+    cache_make_room(C, (size_t)K * T.n_nodes * msize * msize * sizeof(double));
+    C->cache.reserve(C->cache.size() + (size_t)K * T.n_nodes);
+    PendingJobs P;
+    std::vector<MatEntry*>& ent = ws.entry_vec;
+    ent.assign((size_t)K * T.n_nodes, nullptr);
+    for (int k = 0; k < K; ++k) {
+        const double m = gamma ? R->multipliers[k] : 1.0;
+        for (int v = 0; v < T.n_nodes; ++v) {
+            if (T.parent[v] < 0) continue;
+            const double lam = R->lambdas[T.lambda_index[v]] * m;   // lambda::multiply, then get_value_for_clade
+            ent[(size_t)k * T.n_nodes + v] = schedule(C, P, make_key(msize, lam, T.branch_length[v]));
+        }
+    }
+    int rc = cache_build(C, ws, P);
+    if (rc) return rc;
+    CK(ws.h_mats.reserve((size_t)K * T.n_nodes * sizeof(double*)), "mats");
+    CK(ws.mats.reserve((size_t)K * T.n_nodes * sizeof(double*)), "mats");
+    double** hm = ws.h_mats.as<double*>();
+    std::vector<int> wait_chunks;
+    for (size_t i = 0; i < (size_t)K * T.n_nodes; ++i) {
+        const MatEntry* e = ent[i];
+        hm[i] = e ? e->d : nullptr;
+        if (!e) continue;
+        if (!e->d) return fail(C, CAFE_ERR_MISSING_MATRIX, "matrix not built");
+        if (std::find(wait_chunks.begin(), wait_chunks.end(), e->chunk) == wait_chunks.end())
+            wait_chunks.push_back(e->chunk);
+    }
+    for (int b : wait_chunks) CK(cudaStreamWaitEvent(ws.stream, C->batch_events[b], 0), "event");
+    CK(cudaMemcpyAsync(ws.mats.p, hm, (size_t)K * T.n_nodes * sizeof(double*), cudaMemcpyHostToDevice, ws.stream),
+       "mats");
+    o->T = &T;
+    o->S = &S;
+    o->K = K;
+    o->Smax = Sg;
+    o->Rmax = Rg;
+    o->msize = msize;
+    o->gamma = gamma;
+    return CAFE_OK;
+}
+
+int reconstruct_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_reconstruction* out) {
+    AllocScope scope(ws.stream);
+    if (ws.staged) {   // the previous request's copies out of the pinned staging buffers
+        CK(cudaEventSynchronize(ws.ev_staged), "staging");
+        ws.staged = false;
+    }
+    if (!out) return fail(C, CAFE_ERR_INVALID, "null output");
+    if (C->prior.empty()) return fail(C, CAFE_ERR_INVALID, "no prior set (cafe_prior_set)");
+    CK(cudaEventRecord(ws.ev_start, ws.stream), "event");
+    ReconSetup Z;
+    int rc = recon_setup(C, ws, R, true, &Z);
+    if (rc) return rc;
+    TreeHost& T = *Z.T;
+    const int64_t F = Z.S->F;
+    const int K = Z.K, n = T.n_nodes;
+    std::vector<PruneTile>& tiles = ws.tile_vec;
+    tiles.clear();
+    for (int k = 0; k < K; ++k)
+        for (int64_t f = 0; f < F; f += 32) {
+            PruneTile t{};
+            t.first = (int)f;
+            t.count = (int)std::min<int64_t>(32, F - f);
+            t.k = k;
+            tiles.push_back(t);
+        }
+    const int n_tiles = (int)tiles.size();
+    const int n_ctas = std::max(1, std::min(n_tiles, C->n_ctas));
+    const size_t per_cta = pupko_scratch_doubles(T.plan, Z.Smax);
+    const size_t c_per_cta = pupko_c_entries(T.plan, Z.Smax);
+    CK(ws.h_tiles.reserve(std::max(n_tiles, 1) * sizeof(PruneTile)), "tiles");
+    CK(ws.tiles.reserve(std::max(n_tiles, 1) * sizeof(PruneTile)), "tiles");
+    CK(ws.scratch.reserve((size_t)n_ctas * per_cta * sizeof(double)), "scratch");
+    CK(ws.rc_c.reserve(std::max<size_t>((size_t)n_ctas * c_per_cta, 1) * sizeof(int32_t)), "argmax tables");
+    const size_t n_state = (size_t)K * F * n, n_fam = (size_t)F * n;
+    CK(ws.rc_state.reserve(std::max<size_t>(n_state, 1) * sizeof(int32_t)), "states");
+    CK(ws.rc_rmax.reserve(std::max<size_t>((size_t)K * F, 1) * sizeof(double)), "root max");
+    CK(ws.rc_mean.reserve(std::max<size_t>(n_fam, 1) * sizeof(double)), "means");
+    CK(ws.rc_count.reserve(std::max<size_t>(n_fam, 1) * sizeof(int32_t)), "counts");
+    CK(ws.rc_nfail.reserve(sizeof(int32_t)), "failed");
+    std::memcpy(ws.h_tiles.p, tiles.data(), n_tiles * sizeof(PruneTile));
+    CK(cudaMemcpyAsync(ws.tiles.p, ws.h_tiles.p, n_tiles * sizeof(PruneTile), cudaMemcpyHostToDevice, ws.stream),
+       "tiles");
+    CK(cudaMemsetAsync(ws.rc_nfail.p, 0, sizeof(int32_t), ws.stream), "failed");
+    if (Z.gamma) {
+        rc = stage_cat_probs(C, ws, R, K, 1);
+        if (rc) return rc;
+    }
+    PupkoArgs a{};
+    a.plan = T.plan;
+    a.tiles = ws.tiles.as<PruneTile>();
+    a.n_tiles = n_tiles;
+    a.counts = Z.S->d_counts.as<int32_t>();
+    a.F = F;
+    a.mats = ws.mats.as<const double*>();
+    a.ld_mat = Z.msize;
+    a.prior = C->d_prior.as<double>();
+    a.n_prior = (int)C->prior.size();
+    a.S = Z.Smax;
+    a.root_len = std::min(Z.Smax, Z.Rmax) + 1;
+    a.scratch = ws.scratch.as<double>();
+    a.scratch_per_cta = (int64_t)per_cta;
+    a.cscratch = ws.rc_c.as<int32_t>();
+    a.c_per_cta = (int64_t)c_per_cta;
+    a.state = ws.rc_state.as<int32_t>();
+    a.root_max = ws.rc_rmax.as<double>();
+    a.n_failed = ws.rc_nfail.as<int32_t>();
+    a.exhaustive = out->exhaustive ? 1 : 0;
+    if (F > 0) {
+        CK(launch_pupko(a, n_ctas, ws.stream), "reconstruct");
+        CK(launch_recon_counts(ws.rc_state.as<int32_t>(), F, n, K, Z.gamma ? ws.catp.as<double>() : nullptr,
+                               Z.gamma ? 1 : 0, T.plan.leaf_col, ws.rc_mean.as<double>(), ws.rc_count.as<int32_t>(),
+                               ws.stream),
+           "node counts");
+    }
+    CK(cudaEventRecord(ws.ev_stop, ws.stream), "event");
+    int32_t nf = 0;
+    CK(cudaMemcpyAsync(&nf, ws.rc_nfail.p, sizeof(int32_t), cudaMemcpyDeviceToHost, ws.stream), "d2h");
+    if (F > 0) {
+        if (out->node_count)
+            CK(cudaMemcpyAsync(out->node_count, ws.rc_count.p, n_fam * sizeof(int32_t), cudaMemcpyDeviceToHost, ws.stream),
+               "d2h");
+        if (out->node_mean)
+            CK(cudaMemcpyAsync(out->node_mean, ws.rc_mean.p, n_fam * sizeof(double), cudaMemcpyDeviceToHost, ws.stream),
+               "d2h");
+        if (out->category_state)
+            CK(cudaMemcpyAsync(out->category_state, ws.rc_state.p, n_state * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                               ws.stream),
+               "d2h");
+        if (out->root_max)
+            CK(cudaMemcpyAsync(out->root_max, ws.rc_rmax.p, (size_t)K * F * sizeof(double), cudaMemcpyDeviceToHost,
+                               ws.stream),
+               "d2h");
+    }
+    CK(cudaStreamSynchronize(ws.stream), "reconstruct");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ws.ev_start, ws.ev_stop);
+    out->device_ms = ms;
+    out->n_failed = nf;
+    return CAFE_OK;
+}
+
+int branch_prob_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, const int32_t* node_count, double* out) {
+    AllocScope scope(ws.stream);
+    if (ws.staged) {   // the previous request's copies out of the pinned staging buffers
+        CK(cudaEventSynchronize(ws.ev_staged), "staging");
+        ws.staged = false;
+    }
+    if (!node_count || !out) return fail(C, CAFE_ERR_INVALID, "null buffers");
+    ReconSetup Z;
+    int rc = recon_setup(C, ws, R, false, &Z);
+    if (rc) return rc;
+    TreeHost& T = *Z.T;
+    const int64_t F = Z.S->F;
+    const size_t n_fam = (size_t)F * T.n_nodes;
+    if (!n_fam) return CAFE_OK;
+    CK(ws.rc_count.reserve(n_fam * sizeof(int32_t)), "counts");
+    CK(ws.rc_bp.reserve(n_fam * sizeof(double)), "branch probabilities");
+    CK(ws.rc_parent.reserve((size_t)T.n_nodes * sizeof(int32_t)), "parents");
+    CK(ws.rc_nfail.reserve(sizeof(int32_t)), "bad");
+    CK(cudaMemcpyAsync(ws.rc_count.p, node_count, n_fam * sizeof(int32_t), cudaMemcpyHostToDevice, ws.stream), "h2d");
+    CK(cudaMemcpyAsync(ws.rc_parent.p, T.parent.data(), (size_t)T.n_nodes * sizeof(int32_t), cudaMemcpyHostToDevice,
+                       ws.stream),
+       "h2d");
+    CK(cudaMemsetAsync(ws.rc_nfail.p, 0, sizeof(int32_t), ws.stream), "bad");
+    BranchProbArgs a{};
+    a.parent = ws.rc_parent.as<int32_t>();
+    a.n_nodes = T.n_nodes;
+    a.F = F;
+    a.node_count = ws.rc_count.as<int32_t>();
+    a.mats = ws.mats.as<const double*>();
+    a.ld_mat = Z.msize;
+    a.S = Z.Smax;
+    a.out = ws.rc_bp.as<double>();
+    a.n_bad = ws.rc_nfail.as<int32_t>();
+    CK(launch_branch_prob(a, ws.stream), "branch probabilities");
+    int32_t bad = 0;
+    CK(cudaMemcpyAsync(out, ws.rc_bp.p, n_fam * sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");
+    CK(cudaMemcpyAsync(&bad, ws.rc_nfail.p, sizeof(int32_t), cudaMemcpyDeviceToHost, ws.stream), "d2h");
+    CK(cudaStreamSynchronize(ws.stream), "branch probabilities");
+    if (bad) return fail(C, CAFE_ERR_INVALID, "%d node counts lie outside the transition matrices", bad);
+    return CAFE_OK;
+}
+
 }  // namespace
 
 // ===================================================================== ABI
@@ -1823,6 +2043,20 @@ int cafe_score(cafe_ctx* C, const cafe_request* req, cafe_result* res) {
     std::lock_guard<std::mutex> lk(C->mu);
     cudaSetDevice(C->device);
     return score_sync(C, *C->ws[0], req, 1, res);
+}
+
+int cafe_reconstruct(cafe_ctx* C, const cafe_request* req, cafe_reconstruction* out) {
+    if (!C) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    return reconstruct_sync(C, *C->ws[0], req, out);
+}
+
+int cafe_branch_probabilities(cafe_ctx* C, const cafe_request* req, const int32_t* node_count, double* out) {
+    if (!C) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    return branch_prob_sync(C, *C->ws[0], req, node_count, out);
 }
 
 int cafe_autotune(cafe_ctx* C, const cafe_request* reqs, int n, int reps, cafe_tune_result* out, int max_out,

@@ -191,4 +191,49 @@ struct FallbackPlanArgs {
 };
 cudaError_t launch_fallback_plan(const FallbackPlanArgs& a, cudaStream_t s);
 
+// ---- Pupko joint reconstruction (k_reconstruct.cu) ----
+// One CTA walks 32-family tiles of one category up the tree; node L
+// vectors (S + 1 states) live in per-CTA scratch, the argmax tables C in
+// per-CTA int32 scratch; the backtrack writes every node's state.
+struct PupkoArgs {
+    TreePlan plan;
+    const PruneTile* tiles;      // first family, count (<= 32), category k
+    int n_tiles;
+    const int32_t* counts;       // [F][n_leaves]
+    int64_t F;
+    const double* const* mats;   // [K][n_nodes] FP64 matrix per (category, node)
+    int ld_mat;                  // matrix side (>= S + 1)
+    const double* prior;         // prior[j] = P(root size j)
+    int n_prior;
+    int S;                       // max_family_size: states 0..S
+    int root_len;                // min(S, R) + 1: root sizes 1..root_len - 1
+    double* scratch;             // n_ctas * scratch_per_cta doubles
+    int64_t scratch_per_cta;     // pupko_scratch_doubles()
+    int32_t* cscratch;           // n_ctas * c_per_cta
+    int64_t c_per_cta;           // pupko_c_entries()
+    int32_t* state;              // [K][F][n_nodes] out
+    double* root_max;            // [K][F] out
+    int32_t* n_failed;           // [1] out: (category, family) pairs with root max 0
+    int exhaustive;              // 1: exact FP64 scan of every child state
+};
+cudaError_t launch_pupko(const PupkoArgs& a, int n_ctas, cudaStream_t s);
+size_t pupko_scratch_doubles(const TreePlan& P, int S);
+size_t pupko_c_entries(const TreePlan& P, int S);
+cudaError_t launch_recon_counts(const int32_t* state, int64_t F, int n_nodes, int K, const double* cat_probs,
+                                int gamma, const int32_t* leaf_col, double* mean, int32_t* node_count,
+                                cudaStream_t s);
+
+struct BranchProbArgs {
+    const int32_t* parent;       // [n_nodes], -1 at the root
+    int n_nodes;
+    int64_t F;
+    const int32_t* node_count;   // [F][n_nodes]
+    const double* const* mats;   // [n_nodes] matrix of the branch above each node
+    int ld_mat;
+    int S;                       // child sizes 0..S-1 are summed
+    double* out;                 // [F][n_nodes], NaN at the root
+    int32_t* n_bad;              // [1] counts outside the matrices
+};
+cudaError_t launch_branch_prob(const BranchProbArgs& a, cudaStream_t s);
+
 }  // namespace cafe

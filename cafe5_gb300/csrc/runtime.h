@@ -153,6 +153,8 @@ struct Workspace {
     DevBuf tc_hi, tc_lo, tc_mi, tc_vhi, tc_vlo, conv, flags, fb_perm, tiles64, tiles_fb, parts, fb_count, phase,
         catids;
     PinnedBuf h_conv, h_mi, h_flags, h_tiles64, h_tiles_fb, h_tail, h_catids;
+    // reconstruction
+    DevBuf rc_c, rc_state, rc_rmax, rc_mean, rc_count, rc_nfail, rc_parent, rc_bp;
     std::vector<PruneTile> tile_vec;
     std::vector<MatEntry*> entry_vec;   // cache entry of every (combined category, node)
     // CUDA graphs of the pruning phase: stream ops go through an op log;

@@ -36,6 +36,20 @@ def _p(a: Optional[np.ndarray]):
 
 
 @dataclass
+class Reconstruction:
+    """cafe_reconstruct output. node_count[F][n] is what
+    reconstruction::get_node_count reports (leaves: observed counts);
+    category_state[K][F][n] the Pupko state of each category; root_max[K][F]
+    the largest root likelihood (0 = the reference's failed reconstruction)."""
+    node_count: np.ndarray
+    node_mean: np.ndarray
+    category_state: np.ndarray
+    root_max: np.ndarray
+    n_failed: int
+    device_ms: float
+
+
+@dataclass
 class ScoreResult:
     total: float
     family_lnl: np.ndarray
@@ -59,6 +73,7 @@ class Context:
             raise _lib.CafeError(rc, "cafe_ctx_create failed (is a CUDA GPU visible?)")
         self.h = h
         self._tree_leaves = {}
+        self._tree_nodes = {}
         self._set_shape = {}
 
     def close(self):
@@ -83,6 +98,7 @@ class Context:
         self._check(self.lib.cafe_tree_upload(self.h, tree.n_nodes, _p(a["parent"]), _p(a["branch_length"]),
                                               _p(a["lambda_index"]), C.byref(tid)))
         self._tree_leaves[tid.value] = len(tree.leaves)
+        self._tree_nodes[tid.value] = tree.n_nodes
         return tid.value
 
     def upload_families(self, tree_id: int, counts: np.ndarray) -> int:
@@ -225,6 +241,35 @@ class Context:
         return ScoreResult(r.total_neg_lnl, handle["fam"], handle["cat"], r.status, r.n_failed, r.n_fallback,
                            r.device_ms)
 
+    # ---- ancestral reconstruction -------------------------------------------
+    def reconstruct(self, tree_id, set_id, lambdas, *, S: int, R: int, model=0, lambda_kind=0,
+                    multipliers=(1.0,), cat_probs=(1.0,), exhaustive: bool = False) -> Reconstruction:
+        """cafe_reconstruct: Pupko joint reconstruction of every family
+        (one pass per gamma category) with states 0..S and root sizes
+        1..min(S, R)."""
+        req, keep = self.make_request(tree_id, set_id, lambdas, model=model, lambda_kind=lambda_kind,
+                                      multipliers=multipliers, cat_probs=cat_probs, S=S, R=R)
+        F, _ = self._set_shape.get(set_id, (0, 0))
+        n = self._tree_nodes.get(tree_id, 0)
+        K = req.n_categories
+        cnt = np.zeros((F, n), np.int32)
+        mean = np.zeros((F, n))
+        st = np.zeros((K, F, n), np.int32)
+        rmax = np.zeros((K, F))
+        out = _lib.Reconstruction(_p(cnt), _p(mean), _p(st), _p(rmax), 1 if exhaustive else 0, 0, 0.0)
+        self._check(self.lib.cafe_reconstruct(self.h, C.byref(req), C.byref(out)))
+        return Reconstruction(cnt, mean, st, rmax, out.n_failed, out.device_ms)
+
+    def branch_probabilities(self, tree_id, set_id, lambdas, node_count: np.ndarray, *, S: int, R: int,
+                             lambda_kind=0) -> np.ndarray:
+        """cafe_branch_probabilities: compute_viterbi_sum of every family and
+        node ([F][n], NaN at the root)."""
+        req, keep = self.make_request(tree_id, set_id, lambdas, lambda_kind=lambda_kind, S=S, R=R)
+        nc = np.ascontiguousarray(node_count, dtype=np.int32)
+        out = np.zeros(nc.shape)
+        self._check(self.lib.cafe_branch_probabilities(self.h, C.byref(req), _p(nc), _p(out)))
+        return out
+
     def profile(self, enable: bool = True):
         self._check(self.lib.cafe_profile_enable(self.h, 1 if enable else 0))
 
@@ -360,6 +405,25 @@ class BaseModel:
     def _score_kw(self, lam):
         return dict(model=_lib.MODEL_BASE, lambda_kind=lam.kind, dedupe=self.dedupe, **self._kw())
 
+    def reconstruct_ancestral_states(self, prior: RootPrior, lam=None, exhaustive: bool = False) -> Reconstruction:
+        """base_model::reconstruct_ancestral_states (src/base_model.cpp:133-170)."""
+        lam = lam or self.lam
+        self._common(prior)
+        return self.ctx.reconstruct(self.tree_id, self.set_id, lam.values, S=self.max_family_size,
+                                    R=self.max_root_family_size, lambda_kind=lam.kind, **self._recon_kw())
+
+    def _recon_kw(self):
+        return dict(model=_lib.MODEL_BASE)
+
+    def branch_probabilities(self, rec: Reconstruction, lam=None) -> np.ndarray:
+        """compute_viterbi_sum for every family and node (the estimate action
+        applies it to families below the p-value threshold,
+        src/execute.cpp:177-185); uses the model's own lambdas."""
+        lam = lam or self.lam
+        return self.ctx.branch_probabilities(self.tree_id, self.set_id, lam.values, rec.node_count,
+                                             S=self.max_family_size, R=self.max_root_family_size,
+                                             lambda_kind=lam.kind)
+
     def infer_family_likelihoods(self, prior: RootPrior, lam=None) -> float:
         lam = lam or self.lam
         self._common(prior)
@@ -394,6 +458,12 @@ class GammaModel(BaseModel):
     def _score_kw(self, lam):
         return dict(model=_lib.MODEL_GAMMA, lambda_kind=lam.kind, multipliers=self.multipliers,
                     cat_probs=self.cat_probs, **self._kw())
+
+    def _recon_kw(self):
+        """gamma_model::reconstruct_ancestral_states (src/gamma_core.cpp:290-339):
+        one pass per category at lambda * m_k, node counts from the
+        probability-weighted category states."""
+        return dict(model=_lib.MODEL_GAMMA, multipliers=self.multipliers, cat_probs=self.cat_probs)
 
     def infer_family_likelihoods(self, prior: RootPrior, lam=None) -> float:
         lam = lam or self.lam

@@ -334,6 +334,40 @@ int cafe_nelder_mead(const cafe_opt_config* cfg, double (*objective)(const doubl
  * by its median, rescaled so the multipliers average 1. */
 int cafe_discrete_gamma(int K, double alpha, double* probs, double* multipliers);
 
+/* ---- ancestral reconstruction ------------------------------------------ */
+
+typedef struct {
+    int32_t* node_count;         /* host [F][n_nodes] or NULL: reconstructed family size per node
+                                    (reconstruction::get_node_count); leaves hold the observed count */
+    double* node_mean;           /* host [F][n_nodes] or NULL: gamma sum_k p_k * state_k
+                                    (get_weighted_averages); base: the state */
+    int32_t* category_state;     /* host [K][F][n_nodes] or NULL: Pupko state per category (K = 1 for base) */
+    double* root_max;            /* host [K][F] or NULL: largest root L (reconstructed iff > 0) */
+    int exhaustive;              /* in: 1 = exact FP64 scan of every child state (no log2 filter) */
+    int64_t n_failed;            /* out: (category, family) pairs whose root L is all 0 */
+    double device_ms;            /* out: device time (CUDA events) */
+} cafe_reconstruction;
+
+/* Pupko joint ancestral reconstruction of every family of the set
+ * (model::reconstruct_ancestral_states, src/base_model.cpp:133-170 and
+ * src/gamma_core.cpp:290-339, over pupko_reconstructor::reconstruct_gene_family,
+ * src/gene_family_reconstructor.cpp:161-190): one max-product pass per
+ * gamma category at lambda * m_k, states 0..max_family_size, root sizes
+ * 1..min(max_family_size, max_root_family_size). Uses the request's tree,
+ * family set, model, lambdas, gamma categories and both bounds; precision,
+ * dedupe and the error model are ignored (the reference reconstructs in
+ * plain FP64 from the observed counts). Counts above max_family_size are
+ * CAFE_ERR_INVALID. */
+int cafe_reconstruct(cafe_ctx* ctx, const cafe_request* req, cafe_reconstruction* out);
+
+/* compute_viterbi_sum (src/gene_family_reconstructor.cpp:390-430) for every
+ * family and node: node_count[F][n_nodes] (host, e.g. from cafe_reconstruct)
+ * in, out[F][n_nodes] (host) = the probability mass of child sizes below
+ * max_family_size that are less likely than the reconstructed one given the
+ * parent's (ties count half), under the request's own lambdas; NaN at the
+ * root. */
+int cafe_branch_probabilities(cafe_ctx* ctx, const cafe_request* req, const int32_t* node_count, double* out);
+
 #ifdef __cplusplus
 }
 #endif
