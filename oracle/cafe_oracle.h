@@ -95,6 +95,16 @@ int oracle_reconstruct(const oracle_tree* tree, const int32_t* counts, int64_t F
 int oracle_branch_probabilities(const oracle_tree* tree, const double* lambdas, int n_lambdas,
                                 const int32_t* node_count, int64_t F, int S, int R, double* out);
 
+/* compute_pvalues (src/probability.cpp:376-570): n_sim families simulated
+ * per root size 1..R from a std::mt19937 seeded with `seed` (the
+ * reference's randomizer_engine draws, in its order), pruned with the root
+ * fixed; observed families pruned with states 0..S and root sizes 1..R.
+ * Outputs pvalues[F], and optionally the sorted conditional distributions
+ * conditional[R][n_sim] and the observed root vectors root_vectors[F][R]. */
+int oracle_pvalues(const oracle_tree* tree, const int32_t* counts, int64_t F, int n_leaves,
+                   const double* lambdas, int n_lambdas, int S, int R, int n_sim, uint32_t seed,
+                   double* pvalues, double* conditional, double* root_vectors);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,8 @@ def lib():
                                             p, p, p, p]
         _lib.oracle_branch_probabilities.restype = i
         _lib.oracle_branch_probabilities.argtypes = [C.POINTER(_Tree), p, i, p, C.c_int64, i, i, p]
+        _lib.oracle_pvalues.restype = i
+        _lib.oracle_pvalues.argtypes = [C.POINTER(_Tree), p, C.c_int64, i, p, i, i, i, i, C.c_uint32, p, p, p]
     return _lib
 
 
@@ -185,3 +187,19 @@ def branch_probabilities(tree: TreeArrays, lambdas: Sequence[float], node_count:
     if rc:
         raise RuntimeError(f"oracle_branch_probabilities failed: {rc}")
     return out
+
+
+def pvalues(tree: TreeArrays, counts: np.ndarray, lambdas: Sequence[float], *, S: int, R: int, n_sim: int,
+            seed: int):
+    """compute_pvalues: (pvalues[F], conditional[R][n_sim], root_vectors[F][R])."""
+    counts = np.ascontiguousarray(counts, dtype=np.int32)
+    F, n_leaves = counts.shape
+    lam = np.ascontiguousarray(lambdas, dtype=np.float64)
+    pv = np.zeros(F)
+    cd = np.zeros((R, n_sim))
+    rv = np.zeros((F, R))
+    rc = lib().oracle_pvalues(C.byref(tree.c), counts.ctypes.data, F, n_leaves, lam.ctypes.data, len(lam), S, R,
+                              n_sim, seed, pv.ctypes.data, cd.ctypes.data, rv.ctypes.data)
+    if rc:
+        raise RuntimeError(f"oracle_pvalues failed: {rc}")
+    return pv, cd, rv

@@ -153,7 +153,7 @@ void usage() {
         "   [--max-family S --max-root R] [--prior uniform|uniform:N|poisson:X|rootdist:s=n,..]\n"
         "   [--repeat N] [--quiet]\n"
         "   [--optimize lambda|alpha|lambda_alpha|lambda_epsilon --initial x1,..]\n"
-        "   [--reconstruct]\n"
+        "   [--reconstruct] [--pvalues N_SIMULATIONS --seed S]\n"
         "cafe_ref_harness nm rosen|wall|bowl|product <maxiters> x1,..\n");
 }
 
@@ -221,6 +221,8 @@ int main(int argc, char** argv) {
     double alpha = -1;
     int gk = 0, S = -1, R = -1, repeat = 1;
     bool quiet = false, recon = false;
+    int n_sim = 0;
+    unsigned long seed = 10;
     for (int i = 1; i < argc; ++i) {
         std::string a = argv[i];
         auto next = [&]() -> std::string {
@@ -244,6 +246,8 @@ int main(int argc, char** argv) {
         else if (a == "--optimize") opt_kind = next();
         else if (a == "--initial") opt_initial = parse_list(next());
         else if (a == "--reconstruct") recon = true;
+        else if (a == "--pvalues") n_sim = std::stoi(next());
+        else if (a == "--seed") seed = std::stoul(next());
         else { usage(); return 2; }
     }
     if (tree_path.empty() || fam_path.empty() || lambdas.empty()) { usage(); return 2; }
@@ -371,6 +375,27 @@ int main(int argc, char** argv) {
                     std::printf("cat %s %a %a %a\n", s.family_id.c_str(), s.lambda_multiplier,
                                 s.category_likelihood, s.family_likelihood);
             }
+        }
+        if (n_sim > 0) {
+            // compute_pvalues as the estimate action runs it
+            // (src/execute.cpp:166-171): a cache of side
+            // max(max family, max root) + 100 at the model's own lambdas,
+            // the simulation stream seeded first. Prints the conditional
+            // distribution of every root size and each family's p-value.
+            matrix_cache cache(std::max(max_fam, max_root) + 100);
+            cache.precalculate_matrices(get_lambda_values(lam.get()), tree->get_branch_lengths());
+            randomizer_engine.seed(seed);
+            pvalue_parameters pp = {tree.get(), lam.get(), max_fam, max_root, cache};
+            std::vector<std::vector<double>> cd(max_root);
+            for (int i = 0; i < max_root; ++i) cd[i] = get_random_probabilities(pp, n_sim, i + 1);
+            randomizer_engine.seed(seed);
+            std::vector<double> pv = compute_pvalues(pp, families, n_sim);
+            for (int i = 0; i < max_root; ++i) {
+                std::printf("cd %d", i + 1);
+                for (double x : cd[i]) std::printf(" %a", x);
+                std::printf("\n");
+            }
+            for (size_t i = 0; i < families.size(); ++i) std::printf("pv %s %a\n", families[i].id().c_str(), pv[i]);
         }
         if (recon) {
             // model::reconstruct_ancestral_states as the estimate action runs

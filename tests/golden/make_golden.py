@@ -12,6 +12,8 @@ tests, and stores inputs plus hex-float outputs:
   ref_matrices.json  transition matrices from matrix_cache
   ref_optimizer.json Nelder-Mead searches (fminsearch_min) over analytic
                      objectives and over the likelihood scorers
+  ref_pvalues.json   compute_pvalues with the random engine seeded:
+                     conditional distributions and per-family p-values
 
 Only this script reads the reference (it needs /root/reference and the
 built harness); the tests read the committed JSON. Usage:
@@ -156,6 +158,35 @@ def make_case(name, tree, fams, lambdas, *, lam_idx=None, model="base", mult=Non
     return case
 
 
+def make_pvalue_case(name, tree, fams, lambdas, *, n_sim, seed, lam_idx=None, S=None, R=None, note=""):
+    """compute_pvalues of the compiled reference with its random engine
+    seeded: the sorted conditional distribution of every root size and the
+    p-value of every family."""
+    with tempfile.TemporaryDirectory() as d:
+        tp, fp = os.path.join(d, "t.nwk"), os.path.join(d, "f.tab")
+        nwk = tree.to_newick()
+        open(tp, "w").write(nwk)
+        write_families(fp, fams, tree)
+        args = ["--tree", tp, "--families", fp, "--lambdas", ",".join(repr(x) for x in lambdas),
+                "--pvalues", str(n_sim), "--seed", str(seed), "--quiet"]
+        lnwk = None
+        if lam_idx is not None:
+            lp = os.path.join(d, "l.nwk")
+            lnwk = lambda_tree_newick(tree, lam_idx)
+            open(lp, "w").write(lnwk)
+            args += ["--lambda-tree", lp]
+        if S is not None:
+            args += ["--max-family", str(S), "--max-root", str(R)]
+        out = run(args).splitlines()
+    bounds = [ln for ln in out if ln.startswith("bounds")][0].split()
+    cd = [" ".join(ln.split()[2:]) for ln in out if ln.startswith("cd ")]
+    pv = {ln.split()[1]: ln.split()[2] for ln in out if ln.startswith("pv ")}
+    return {"name": name, "note": note, "newick": nwk, "lambda_newick": lnwk, "taxa": tree.leaf_names,
+            "ids": fams.ids, "counts": fams.counts.tolist(), "lambdas": [float(x).hex() for x in lambdas],
+            "S": int(bounds[1]), "R": int(bounds[2]), "n_sim": n_sim, "seed": seed,
+            "conditional_hex": cd, "pvalue_hex": [pv[i] for i in fams.ids]}
+
+
 def make_case_r(*a, **kw):
     kw.setdefault("recon", True)
     return make_case(*a, **kw)
@@ -227,6 +258,22 @@ def main():
         gam.append({"K": k, "alpha": a, "probs": [r[0] for r in rows], "multipliers": [r[1] for r in rows]})
     json.dump({"generator": "tests/golden/make_golden.py", "matrices": mats, "gamma": gam},
               open(os.path.join(HERE, "ref_matrices.json"), "w"))
+
+    # -- p-values (compute_pvalues, seeded) -----------------------------------
+    pvs = []
+    w0p = workload(0, n_families=30, seed=3)
+    pvs.append(make_pvalue_case("pv_base_12taxa", w0p.tree, w0p.families, [0.0025], n_sim=50, seed=7,
+                                note="config-0 shape, global bounds, 50 simulations per root size"))
+    pvs.append(make_pvalue_case("pv_two_lambdas_32taxa", w2.tree, FamilySet(f2.ids[:25], f2.counts[:25]),
+                                [0.0015, 0.006], lam_idx=w2.lambda_of_node, n_sim=30, seed=11,
+                                note="two lambdas (lambda tree), 30 simulations"))
+    pvs.append(make_pvalue_case("pv_polytomy", tp, FamilySet([f"p{i}" for i in range(30)], cnt), [0.01],
+                                n_sim=40, seed=5, note="a three-child node"))
+    pvs.append(make_pvalue_case("pv_kat_small_bounds", parse_newick("(A:1,B:3):7;"),
+                                FamilySet(["f1", "f2"], np.array([[3, 6], [1, 2]], np.int32)), [0.005],
+                                n_sim=25, seed=3, S=10, R=8, note="explicit small bounds"))
+    json.dump({"generator": "tests/golden/make_golden.py", "cases": pvs},
+              open(os.path.join(HERE, "ref_pvalues.json"), "w"))
 
     # -- Nelder-Mead: analytic objectives and likelihood searches ------------
     analytic = []

@@ -119,3 +119,35 @@ def load_cases() -> List[Case]:
 def load_searches():
     """(raw json, Case) per likelihood search of ref_optimizer.json."""
     return [(c, case_from_json(c)) for c in load_json("ref_optimizer.json")["searches"]]
+
+
+@dataclass
+class PvalueCase:
+    name: str
+    tree: Tree
+    lambda_of_node: List[int]
+    lambda_kind: int
+    counts: np.ndarray
+    lambdas: List[float]
+    S: int
+    R: int
+    n_sim: int
+    seed: int
+    conditional: np.ndarray    # [R][n_sim], sorted
+    pvalues: np.ndarray        # [F]
+
+
+def load_pvalue_cases() -> List[PvalueCase]:
+    out = []
+    for c in load_json("ref_pvalues.json")["cases"]:
+        tree = parse_newick(c["newick"])
+        lam_idx, kind = [0] * tree.n_nodes, 0
+        if c["lambda_newick"]:
+            lam_idx = lambda_index_of_nodes(tree, parse_newick(c["lambda_newick"], lambda_tree=True))
+            kind = 1
+        out.append(PvalueCase(
+            name=c["name"], tree=tree, lambda_of_node=lam_idx, lambda_kind=kind,
+            counts=np.asarray(c["counts"], dtype=np.int32).reshape(len(c["ids"]), len(c["taxa"])),
+            lambdas=[hexf(x) for x in c["lambdas"]], S=c["S"], R=c["R"], n_sim=c["n_sim"], seed=c["seed"],
+            conditional=_hexes(c["conditional_hex"]), pvalues=np.array([hexf(x) for x in c["pvalue_hex"]])))
+    return out

@@ -252,3 +252,18 @@ def test_reconstruction_edge_cases_present():
     ta = oracle.TreeArrays.from_tree(case.tree, case.lambda_of_node)
     _, _, _, rmax = oracle.reconstruct(ta, case.counts, case.lambdas, prior=case.prior, S=case.S, R=case.R)
     assert rmax[0, 0] == 0 and rmax[0, 1] > 0
+
+
+PVALUE_CASES = __import__("golden_cases").load_pvalue_cases()
+
+
+@pytest.mark.parametrize("case", PVALUE_CASES, ids=[c.name for c in PVALUE_CASES])
+def test_oracle_pvalues_match_reference(case):
+    """compute_pvalues with the same seed: every conditional distribution
+    (sorted simulated likelihoods per root size) and every p-value equal
+    the compiled reference's bit for bit."""
+    ta = oracle.TreeArrays.from_tree(case.tree, case.lambda_of_node)
+    pv, cd, _ = oracle.pvalues(ta, case.counts, case.lambdas, S=case.S, R=case.R, n_sim=case.n_sim,
+                               seed=case.seed)
+    assert np.array_equal(cd, case.conditional)
+    assert np.array_equal(pv, case.pvalues)
