@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--serving-requests", type=int, default=12, help="requests per client")
     ap.add_argument("--no-reconstruct", dest="reconstruct", action="store_false",
                     help="skip the ancestral-reconstruction measurement")
+    ap.add_argument("--no-pvalues", dest="pvalues", action="store_false",
+                    help="skip the p-value measurement")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default tensor-core launch shapes (no cafe_autotune before the warm-up)")
     ap.add_argument("--profile-only", action="store_true",
@@ -341,6 +343,49 @@ def reconstruction_phase(ctx, tid, sid, w, fams, S, R, cpu_seconds: float, reps:
     return out
 
 
+def pvalue_phase(ctx, tid, sid, w, fams, S, R, cpu_seconds: float, n_sim: int = 1000):
+    """compute_pvalues at the reference's defaults (1,000 simulated families
+    per root size 1..R, global bounds): wall time of cafe_pvalues, split into
+    host (simulation with the reference's random stream, sorting, ranks) and
+    device (pruning every simulated and observed family)."""
+    lam = [w.true_lambda]
+    ctx.pvalues(tid, sid, lam, S=S, R=R, n_simulations=50, seed=1)      # buffers, matrices
+    t0 = time.perf_counter()
+    r = ctx.pvalues(tid, sid, lam, S=S, R=R, n_simulations=n_sim, seed=10)
+    wall = (time.perf_counter() - t0) * 1e3
+    F = fams.n_families
+    pruned = R * n_sim + F
+    out = {"unit": "families pruned/s (simulated + observed)", "value": pruned / (wall / 1e3), "wall_ms": wall,
+           "device_ms": r["device_ms"], "host_ms": r["host_ms"], "n_simulations": n_sim, "root_sizes": R,
+           "simulated_families": R * n_sim, "observed_families": F, "S": S,
+           "note": "whole cafe_pvalues call; the simulation is sequential on the host (the reference's "
+                   "mt19937 stream), both prunings on the GPU"}
+    if cpu_seconds > 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        ta = oracle.TreeArrays.from_tree(w.tree)
+
+        def timed(ns, nf):
+            t = time.perf_counter()
+            oracle.pvalues(ta, fams.counts[:nf], lam, S=S, R=R, n_sim=ns, seed=10)
+            return time.perf_counter() - t
+
+        # the oracle builds its matrices inside each call: the difference of
+        # two sample sizes leaves the per-family work
+        base = timed(10, 50)
+        ns, nf = 40, 200
+        while True:
+            dt = timed(ns, nf)
+            if dt - base >= cpu_seconds / 2 or ns >= n_sim:
+                break
+            ns, nf = ns * 2, min(F, nf * 2)
+        fam = (ns * R + nf) - (10 * R + 50)
+        out["cpu_port"] = {"value": fam / max(dt - base, 1e-9), "cores": os.cpu_count() or 1, "kind": "port",
+                           "sample": f"{ns} simulations x {R} root sizes + {nf} observed families, minus a "
+                                     f"10 x {R} + 50 run (matrix build cancelled out)"}
+    return out
+
+
 def run_ours(args):
     import torch
     from cafe5_gb300.engine import Context
@@ -468,6 +513,9 @@ def run_ours(args):
     recon = None
     if rank == 0 and args.reconstruct:
         recon = reconstruction_phase(ctx, tid, sid, w, fams, S, R, args.cpu_seconds / 2)
+    pvals = None
+    if rank == 0 and args.pvalues:
+        pvals = pvalue_phase(ctx, tid, sid, w, fams, S, R, args.cpu_seconds / 2)
 
     peaks = measured_peaks()
     fp64_peak = fp64_peak_tflops(torch, dev)
@@ -521,6 +569,7 @@ def run_ours(args):
                         "h2d_bytes_per_step": int(fams.counts.nbytes), "d2h_bytes_per_step": int(B * (F * 8 + 8))},
                 "serving": serving,
                 "reconstruction": recon,
+                "pvalues": pvals,
                 "gpu_launches": int(round(prof["launches"] / prof_steps * args.steps)),
                 "cuda_graphs": "pruning phase (conversion, tensor-core bins, fallback, finish) replayed as a CUDA "
                                "graph per launch signature; matrix builds launched directly",

@@ -27,7 +27,7 @@ EXPORTS = [
     "cafe_score_device", "cafe_submit", "cafe_poll", "cafe_serving_stats", "cafe_profile_enable",
     "cafe_profile_read", "cafe_prune_fp64_noalloc", "cafe_optimize", "cafe_discrete_gamma",
     "cafe_nelder_mead", "cafe_score_batch", "cafe_score_batch_device", "cafe_serving_counters", "cafe_autotune",
-    "cafe_reconstruct", "cafe_branch_probabilities",
+    "cafe_reconstruct", "cafe_branch_probabilities", "cafe_pvalues",
 ]
 OPT_LAMBDA, OPT_LAMBDA_ALPHA, OPT_LAMBDA_EPSILON, OPT_ALPHA = 0, 1, 2, 3
 
@@ -86,6 +86,12 @@ class Reconstruction(C.Structure):
                 ("device_ms", C.c_double)]
 
 
+class PvaluesOut(C.Structure):
+    _fields_ = [("n_simulations", C.c_int), ("seed", C.c_uint32), ("pvalues", C.c_void_p),
+                ("conditional", C.c_void_p), ("root_likelihood", C.c_void_p), ("device_ms", C.c_double),
+                ("host_ms", C.c_double)]
+
+
 _lib = None
 
 
@@ -138,6 +144,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
         "cafe_nelder_mead": (i, [P(OptConfig), OBJECTIVE, p, P(OptResult)]),
         "cafe_reconstruct": (i, [p, P(Request), P(Reconstruction)]),
         "cafe_branch_probabilities": (i, [p, P(Request), p, p]),
+        "cafe_pvalues": (i, [p, P(Request), P(PvaluesOut)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

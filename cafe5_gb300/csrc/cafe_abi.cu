@@ -16,6 +16,7 @@
 #include <cstring>
 #include <functional>
 #include <numeric>
+#include <random>
 #include <unordered_set>
 
 #include "runtime.h"
@@ -1721,6 +1722,233 @@ int reconstruct_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_rec
     return CAFE_OK;
 }
 
+// ---- p-values
+
+// FP64 pruning of `fams` (rows of `counts`) through k_prune64 with the root
+// vectors as output: families grouped into 32-family tiles of equal state
+// bound S_f and root range root_lo..root_lo + nroot - 1, unscaled FP64 (the
+// reference's arithmetic), out[f * root_ld + j].
+int prune_root_vectors(cafe_ctx* C, Workspace& ws, TreeHost& T, const int32_t* d_counts, const int64_t* d_perm,
+                       const std::vector<PruneTile>& tiles, int msize, int W, double* d_out, int root_ld) {
+    const int n_tiles = (int)tiles.size();
+    if (!n_tiles) return CAFE_OK;
+    CK(ws.h_tiles.reserve(n_tiles * sizeof(PruneTile)), "tiles");
+    CK(ws.tiles.reserve(n_tiles * sizeof(PruneTile)), "tiles");
+    std::memcpy(ws.h_tiles.p, tiles.data(), n_tiles * sizeof(PruneTile));
+    CK(cudaMemcpyAsync(ws.tiles.p, ws.h_tiles.p, n_tiles * sizeof(PruneTile), cudaMemcpyHostToDevice, ws.stream),
+       "tiles");
+    const int n_ctas = std::max(1, std::min(n_tiles, C->n_ctas));
+    const int64_t per_cta = (int64_t)T.n_slots * W * 32;
+    CK(ws.scratch.reserve((size_t)n_ctas * per_cta * sizeof(double)), "scratch");
+    Prune64Args a{};
+    a.plan = T.plan;
+    a.tiles = ws.tiles.as<PruneTile>();
+    a.n_tiles = n_tiles;
+    a.counts = d_counts;
+    a.perm = d_perm;
+    a.mats = ws.mats.as<const double*>();
+    a.ld_mat = msize;
+    a.prior = C->d_prior.p ? C->d_prior.as<double>() : nullptr;
+    a.n_prior = 0;
+    a.scratch = ws.scratch.as<double>();
+    a.scratch_per_cta = per_cta;
+    a.scaled = 0;
+    a.model = 0;
+    a.K = 1;
+    a.tile_families = 32;
+    a.W = W;
+    a.root_out = d_out;
+    a.root_ld = root_ld;
+    CK(launch_prune64(a, n_ctas, ws.stream), "prune root vectors");
+    // the tile staging buffers are rewritten by the next call
+    CK(cudaStreamSynchronize(ws.stream), "prune root vectors");
+    return CAFE_OK;
+}
+
+// compute_pvalues (src/probability.cpp:376-570). The simulation runs on the
+// host because its random stream is the reference's: one std::mt19937
+// seeded by the caller, drawing in the reference's order (create_family,
+// :351-373, set_weighted_random_family_size, :449-476) through
+// std::discrete_distribution over the parent's matrix row
+// (matrix::select_random_y, src/matrix_cache.cpp:60-66) -- identical draws
+// for identical rows. The distributions are built once per (matrix, row)
+// instead of once per draw. Both prunings (R x n_sim simulated families
+// with the root fixed, and the observed families) run on the GPU.
+int pvalues_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_pvalues_out* out) {
+    AllocScope scope(ws.stream);
+    if (ws.staged) {
+        CK(cudaEventSynchronize(ws.ev_staged), "staging");
+        ws.staged = false;
+    }
+    if (!out || !out->pvalues || out->n_simulations < 1) return fail(C, CAFE_ERR_INVALID, "bad p-value arguments");
+    const auto t_host0 = std::chrono::steady_clock::now();
+    double host_ms = 0.0;
+    ReconSetup Z;
+    int rc = recon_setup(C, ws, R, false, &Z);
+    if (rc) return rc;
+    TreeHost& T = *Z.T;
+    FamSet& FS = *Z.S;
+    const int S = Z.Smax, RR = Z.Rmax, msize = Z.msize, nsim = out->n_simulations, n = T.n_nodes;
+    const int64_t F = FS.F;
+    // matrices of the non-root nodes on the host (rows are sampled there)
+    const double* const* hm = ws.h_mats.as<const double*>();
+    std::map<const double*, std::vector<double>> host_mats;
+    for (int v = 0; v < n; ++v) {
+        if (T.parent[v] < 0 || host_mats.count(hm[v])) continue;
+        std::vector<double>& m = host_mats[hm[v]];
+        m.resize((size_t)msize * msize);
+        CK(cudaMemcpyAsync(m.data(), hm[v], m.size() * sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");
+    }
+    CK(cudaStreamSynchronize(ws.stream), "matrices");
+    host_ms += host_ms_since(t_host0);
+    const auto t_sim = std::chrono::steady_clock::now();
+    // prefix order (clade::apply_prefix_order, src/clade.cpp:275-291)
+    std::vector<int> prefix;
+    {
+        std::vector<int> st{T.root};
+        while (!st.empty()) {
+            const int v = st.back();
+            st.pop_back();
+            prefix.push_back(v);
+            for (auto it = T.children[v].rbegin(); it != T.children[v].rend(); ++it) st.push_back(*it);
+        }
+    }
+    std::vector<char> saturated(n, 0);
+    std::vector<const double*> node_mat(n, nullptr);
+    for (int v = 0; v < n; ++v) {
+        if (T.parent[v] < 0) continue;
+        node_mat[v] = host_mats[hm[v]].data();
+        const double lam = R->lambdas[T.lambda_index[v]], t = T.branch_length[v];
+        saturated[v] = (1 - 2 * (lam * t / (1 + lam * t))) < 0;   // matrix_cache::is_saturated
+    }
+    std::map<std::pair<const double*, int>, std::discrete_distribution<int>> dists;
+    std::mt19937 engine(out->seed);
+    const int64_t NS = (int64_t)RR * nsim;
+    const int L = T.n_leaves;
+    std::vector<int32_t> sim_counts((size_t)NS * L);
+    std::vector<int32_t> sim_m(NS);
+    std::vector<int> sizes(n);
+    for (int i = 0; i < RR; ++i)
+        for (int k = 0; k < nsim; ++k) {
+            const int64_t fi = (int64_t)i * nsim + k;
+            sizes[T.root] = i + 1;
+            int mx = i + 1;
+            for (int v : prefix) {
+                if (v == T.root) continue;
+                const int ps = sizes[T.parent[v]];
+                int c = 0;
+                if (ps > 0) {
+                    if (saturated[v]) {
+                        std::uniform_int_distribution<int> d(0, S - 1);
+                        c = d(engine);   // drawn and discarded, as the reference does
+                    }
+                    auto key = std::make_pair(node_mat[v], ps);
+                    auto it = dists.find(key);
+                    if (it == dists.end()) {
+                        const double* row = node_mat[v] + (size_t)ps * msize;
+                        it = dists.emplace(key, std::discrete_distribution<int>(row, row + S)).first;
+                    }
+                    c = it->second(engine);
+                }
+                sizes[v] = c;
+                mx = std::max(mx, c);
+            }
+            for (int v = 0; v < n; ++v)
+                if (T.leaf_col[v] >= 0) sim_counts[(size_t)fi * L + T.leaf_col[v]] = sizes[v];
+            sim_m[fi] = std::min(S, mx + std::max(50, mx / 5));   // compute_family_probabilities bound
+        }
+    // tiles: simulated families grouped by (root size, bound)
+    std::vector<int64_t> perm(NS);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::stable_sort(perm.begin(), perm.end(), [&](int64_t a, int64_t b) {
+        const int ra = (int)(a / nsim), rb = (int)(b / nsim);
+        return ra != rb ? ra < rb : sim_m[a] < sim_m[b];
+    });
+    std::vector<PruneTile> tiles;
+    int Wsim = 1;
+    for (int64_t i = 0; i < NS;) {
+        const int64_t f0 = perm[i];
+        const int r = (int)(f0 / nsim), m = sim_m[f0];
+        int64_t j = i;
+        while (j < NS && j - i < 32 && perm[j] / nsim == r && sim_m[perm[j]] == m) ++j;
+        PruneTile t{};
+        t.first = (int)i;
+        t.count = (int)(j - i);
+        t.k = 0;
+        t.S = m;
+        t.R = 1;
+        t.root_lo = r + 1;
+        tiles.push_back(t);
+        Wsim = std::max(Wsim, m + 1);
+        i = j;
+    }
+    host_ms += host_ms_since(t_sim);
+    CK(cudaEventRecord(ws.ev_start, ws.stream), "event");
+    // device buffers: simulated counts, their order, the root values
+    DevBuf d_sim, d_perm, d_simL, d_obsL, d_obs_perm;
+    CK(d_sim.reserve(std::max<size_t>(sim_counts.size(), 1) * sizeof(int32_t)), "simulated families");
+    CK(d_perm.reserve(std::max<size_t>(perm.size(), 1) * sizeof(int64_t)), "simulated families");
+    CK(d_simL.reserve(std::max<int64_t>(NS, 1) * sizeof(double)), "simulated likelihoods");
+    CK(d_obsL.reserve(std::max<int64_t>(F * RR, 1) * sizeof(double)), "root vectors");
+    CK(cudaMemcpyAsync(d_sim.p, sim_counts.data(), sim_counts.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                       ws.stream),
+       "h2d");
+    CK(cudaMemcpyAsync(d_perm.p, perm.data(), perm.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ws.stream),
+       "h2d");
+    rc = prune_root_vectors(C, ws, T, d_sim.as<int32_t>(), d_perm.as<int64_t>(), tiles, msize, Wsim,
+                            d_simL.as<double>(), 1);
+    if (rc) return rc;
+    // observed families: states 0..S, root sizes 1..R
+    tiles.clear();
+    for (int64_t f = 0; f < F; f += 32) {
+        PruneTile t{};
+        t.first = (int)f;
+        t.count = (int)std::min<int64_t>(32, F - f);
+        t.S = S;
+        t.R = RR;
+        t.root_lo = 1;
+        tiles.push_back(t);
+    }
+    rc = prune_root_vectors(C, ws, T, FS.d_counts.as<int32_t>(), FS.d_identity.as<int64_t>(), tiles, msize,
+                            std::max(S + 1, RR), d_obsL.as<double>(), RR);
+    if (rc) return rc;
+    CK(cudaEventRecord(ws.ev_stop, ws.stream), "event");
+    std::vector<double> simL(NS), obsL((size_t)F * RR);
+    CK(cudaMemcpyAsync(simL.data(), d_simL.p, NS * sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");
+    if (F) CK(cudaMemcpyAsync(obsL.data(), d_obsL.p, obsL.size() * sizeof(double), cudaMemcpyDeviceToHost, ws.stream),
+              "d2h");
+    CK(cudaStreamSynchronize(ws.stream), "p-values");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ws.ev_start, ws.ev_stop);
+    const auto t_pv = std::chrono::steady_clock::now();
+    // sorted conditional distributions (get_random_probabilities)
+    for (int i = 0; i < RR; ++i) std::sort(simL.begin() + (size_t)i * nsim, simL.begin() + (size_t)(i + 1) * nsim);
+    if (out->conditional) std::memcpy(out->conditional, simL.data(), NS * sizeof(double));
+    if (out->root_likelihood && F) std::memcpy(out->root_likelihood, obsL.data(), obsL.size() * sizeof(double));
+    // find_best_pvalue / pvalue (:503-528)
+    const std::vector<int32_t>& hc = FS.h_counts;
+    std::vector<double> pv(RR);
+    for (int64_t f = 0; f < F; ++f) {
+        int fmax = 0;
+        for (int c = 0; c < L; ++c) fmax = std::max(fmax, hc[(size_t)f * L + c]);
+        std::fill(pv.begin(), pv.end(), 0.0);
+        const int check = std::min(RR, (int)std::rint(fmax * 1.25));
+        for (int j = 0; j < check; ++j) {
+            const double* d = simL.data() + (size_t)j * nsim;
+            const double v = obsL[(size_t)f * RR + j];
+            int idx = nsim - 1;
+            const double* b = std::upper_bound(d, d + nsim, v);
+            if (b != d + nsim) idx = (int)(b - d);
+            pv[j] = idx / (double)nsim;
+        }
+        out->pvalues[f] = *std::max_element(pv.begin(), pv.end());
+    }
+    host_ms += host_ms_since(t_pv);
+    out->device_ms = ms;
+    out->host_ms = host_ms;
+    return CAFE_OK;
+}
+
 int branch_prob_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, const int32_t* node_count, double* out) {
     AllocScope scope(ws.stream);
     if (ws.staged) {   // the previous request's copies out of the pinned staging buffers
@@ -2050,6 +2278,13 @@ int cafe_reconstruct(cafe_ctx* C, const cafe_request* req, cafe_reconstruction* 
     std::lock_guard<std::mutex> lk(C->mu);
     cudaSetDevice(C->device);
     return reconstruct_sync(C, *C->ws[0], req, out);
+}
+
+int cafe_pvalues(cafe_ctx* C, const cafe_request* req, cafe_pvalues_out* out) {
+    if (!C) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    return pvalues_sync(C, *C->ws[0], req, out);
 }
 
 int cafe_branch_probabilities(cafe_ctx* C, const cafe_request* req, const int32_t* node_count, double* out) {

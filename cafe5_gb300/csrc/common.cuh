@@ -23,14 +23,16 @@ struct MatrixJob {
 
 // Work tile of the pruning kernels: `count` families (indices into the
 // request's family permutation starting at `first`) scored in category `k`
-// with state bound S (vectors of S + 1 states) and root rows 1..R.
+// with state bound S (vectors of S + 1 states) and R root rows starting at
+// root size `root_lo` (0 means 1: root sizes 1..R).
 struct PruneTile {
     int first;
     int count;
     int k;
     int S;
     int R;
-    int pad[3];
+    int root_lo;
+    int pad[2];
 };
 
 // Flattened tree for the kernels, in one device allocation.
@@ -89,6 +91,9 @@ struct Prune64Args {
     int tile_families;           // families per tile (<= 32)
     int W;                       // max vector length over tiles (S + 1 or R)
     const int32_t* n_tiles_dev;  // optional: tile count read from device memory
+    double* root_out;            // optional (unscaled runs): root vector of every family,
+                                 // root_out[f * root_ld + j] = L(root size root_lo + j); no reduction
+    int root_ld;
 };
 
 cudaError_t launch_prune64(const Prune64Args& a, int n_ctas, cudaStream_t s);

@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(NT) k_prune64(Prune64Args a) {
             const int v = P.internal[ii];
             const bool is_root = (v == P.root);
             const int rows = is_root ? R : S + 1;
-            const int row0 = is_root ? 1 : 0;
+            const int row0 = is_root ? (tile.root_lo > 0 ? tile.root_lo : 1) : 0;
             const int vs = P.slot[v];
             double* dst = slot_ptr(base, vs, W);
             if (tid < TF) s_exp[vs * TF + tid] = 0;
@@ -179,6 +179,16 @@ __global__ void __launch_bounds__(NT) k_prune64(Prune64Args a) {
         // ---- root weighting (K4) ----
         const int rs = P.slot[P.root];
         const double* root = slot_ptr(base, rs, W);
+        if (a.root_out) {
+            // the root vectors themselves (p-values: compute_family_probabilities
+            // and the observed families of compute_pvalues)
+            for (int idx = tid; idx < R * TF; idx += NT) {
+                const int j = idx / TF, ii = idx % TF;
+                if (ii < cnt) a.root_out[(size_t)fam[ii] * a.root_ld + j] = root[(size_t)j * TF + ii];
+            }
+            __syncthreads();
+            continue;
+        }
         const int i = lane;
         const int64_t f = i < cnt ? fam[i] : -1;
         const int Rf = (f >= 0 && a.fam_R) ? a.fam_R[f] : R;

@@ -731,7 +731,7 @@ __global__ void __launch_bounds__(256) k_fallback_plan(FallbackPlanArgs a) {
                     t.k = k;
                     t.S = a.bin_width[b] - 1;
                     t.R = a.bin_width[b] - 1;
-                    t.pad[0] = t.pad[1] = t.pad[2] = 0;
+                    t.root_lo = t.pad[0] = t.pad[1] = 0;
                     a.fb_tiles[n_tiles_sh++] = t;
                 }
         }

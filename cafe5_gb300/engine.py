@@ -270,6 +270,21 @@ class Context:
         self._check(self.lib.cafe_branch_probabilities(self.h, C.byref(req), _p(nc), _p(out)))
         return out
 
+    def pvalues(self, tree_id, set_id, lambdas, *, S: int, R: int, n_simulations: int = 1000, seed: int = 10,
+                lambda_kind=0) -> dict:
+        """cafe_pvalues (compute_pvalues): per-family p-values, the sorted
+        conditional distributions [R][n_simulations] and the observed root
+        vectors [F][R]."""
+        req, keep = self.make_request(tree_id, set_id, lambdas, lambda_kind=lambda_kind, S=S, R=R)
+        F, _ = self._set_shape.get(set_id, (0, 0))
+        pv = np.zeros(F)
+        cd = np.zeros((R, n_simulations))
+        rl = np.zeros((F, R))
+        out = _lib.PvaluesOut(n_simulations, seed & 0xFFFFFFFF, _p(pv), _p(cd), _p(rl), 0.0, 0.0)
+        self._check(self.lib.cafe_pvalues(self.h, C.byref(req), C.byref(out)))
+        return {"pvalues": pv, "conditional": cd, "root_likelihood": rl, "device_ms": out.device_ms,
+                "host_ms": out.host_ms}
+
     def profile(self, enable: bool = True):
         self._check(self.lib.cafe_profile_enable(self.h, 1 if enable else 0))
 
@@ -423,6 +438,15 @@ class BaseModel:
         return self.ctx.branch_probabilities(self.tree_id, self.set_id, lam.values, rec.node_count,
                                              S=self.max_family_size, R=self.max_root_family_size,
                                              lambda_kind=lam.kind)
+
+    def compute_pvalues(self, n_simulations: int = 1000, seed: int = 10, lam=None) -> np.ndarray:
+        """compute_pvalues (src/probability.cpp:530-570) at the model's own
+        lambdas, as the estimate action calls it (src/execute.cpp:166-171);
+        `seed` seeds the simulation stream (the reference's randomizer_engine)."""
+        lam = lam or self.lam
+        return self.ctx.pvalues(self.tree_id, self.set_id, lam.values, S=self.max_family_size,
+                                R=self.max_root_family_size, n_simulations=n_simulations, seed=seed,
+                                lambda_kind=lam.kind)["pvalues"]
 
     def infer_family_likelihoods(self, prior: RootPrior, lam=None) -> float:
         lam = lam or self.lam

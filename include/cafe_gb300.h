@@ -368,6 +368,32 @@ int cafe_reconstruct(cafe_ctx* ctx, const cafe_request* req, cafe_reconstruction
  * root. */
 int cafe_branch_probabilities(cafe_ctx* ctx, const cafe_request* req, const int32_t* node_count, double* out);
 
+/* ---- p-values ------------------------------------------------------------ */
+
+typedef struct {
+    int n_simulations;           /* in: simulated families per root size (the reference uses 1000) */
+    uint32_t seed;               /* in: seed of the std::mt19937 simulation stream (randomizer_engine) */
+    double* pvalues;             /* host [F] out */
+    double* conditional;         /* host [R][n_simulations] out, or NULL: sorted simulated likelihoods
+                                    of root sizes 1..R */
+    double* root_likelihood;     /* host [F][R] out, or NULL: observed root vectors (root sizes 1..R) */
+    double device_ms;            /* out: device time of both prunings */
+    double host_ms;              /* out: host time (simulation, sorting, p-values) */
+} cafe_pvalues_out;
+
+/* compute_pvalues (src/probability.cpp:376-570) at the request's own
+ * lambdas (its multipliers are not used, as the estimate action passes the
+ * model's base lambda, src/execute.cpp:166-171): for every root size
+ * r = 1..max_root_family_size, n_simulations families are simulated down
+ * the tree by sampling each child size from the parent's matrix row
+ * (std::mt19937 + std::discrete_distribution, the reference's draws in its
+ * order), pruned on the GPU with the root fixed at r and states 0..min(S,
+ * largest size + max(50, largest / 5)); the observed families are pruned
+ * with states 0..S and root sizes 1..R; each family's p-value is the
+ * largest, over root sizes up to 1.25 x its largest count, of the share of
+ * simulated likelihoods that do not exceed its own. */
+int cafe_pvalues(cafe_ctx* ctx, const cafe_request* req, cafe_pvalues_out* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -139,6 +139,7 @@ extern "C" int oracle_pvalues(const oracle_tree* tree, const int32_t* counts, in
         // compute_family_probabilities: each family pruned with the root fixed at r
         std::vector<double>& out = cd[i];
         out.resize(n_sim);
+#pragma omp parallel for schedule(dynamic, 4)
         for (int k = 0; k < n_sim; ++k) {
             const std::vector<int>& z = fams[k];
             const int mx = *std::max_element(z.begin(), z.end());
@@ -151,6 +152,7 @@ extern "C" int oracle_pvalues(const oracle_tree* tree, const int32_t* counts, in
     }
 
     // observed families: global bounds, root sizes 1..R; find_best_pvalue
+#pragma omp parallel for schedule(dynamic, 4)
     for (int64_t f = 0; f < F; ++f) {
         std::vector<int> z(T.n, 0);
         int fmax = 0;
