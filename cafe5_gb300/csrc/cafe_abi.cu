@@ -509,7 +509,7 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
         cur += (size_t)k.size * k.size * sizeof(double);
     }
     CK(cudaMemcpyAsync(ws.jobs.p, J, n * sizeof(MatrixJob), cudaMemcpyHostToDevice, ws.stream), "jobs");
-    const bool prof = (&ws == C->ws[0].get());
+    const bool prof = ws.sync;
     cudaEvent_t ev;
     if (prof) C->prof.begin(0, ws.stream, &ev);
     CK(launch_matrix_build(ws.jobs.as<MatrixJob>(), (int)n, max_size, ws.stream), "matrix build");
@@ -695,7 +695,7 @@ int finish_batch(cafe_ctx* C, Workspace& ws, const ScoreInfo* info, bool gamma, 
     fa.part_sum = ws.parts.as<double>();
     fa.part_cnt = reinterpret_cast<int32_t*>(fa.part_sum + 2 * parts);
     fa.status = d_status;
-    const bool prof = (&ws == C->ws[0].get());
+    const bool prof = ws.sync;
     cudaEvent_t ev;
     if (prof) C->prof.begin(2, ws.stream, &ev);
     CK(op_launch(ws, 1, [&] { return launch_finish(fa, ws.stream); }, fa, ws.stream), "finish");
@@ -754,7 +754,7 @@ int launch_fp64_tiles(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHos
     a.cat_probs = ws.catp.as<double>();
     a.tile_families = 32;
     a.W = W;
-    const bool prof = (&ws == C->ws[0].get());
+    const bool prof = ws.sync;
     cudaEvent_t ev;
     if (prof) C->prof.begin(prof_kind, ws.stream, &ev);
     CK(op_launch(ws, 3, [&] { return launch_prune64(a, n_ctas, ws.stream); }, a, n_ctas, ws.stream), "prune fp64");
@@ -899,7 +899,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
                 (w <= 256 ? tc_tiles : wide_tiles).push_back(t);
             }
         }
-    const bool prof = (&ws == C->ws[0].get());
+    const bool prof = ws.sync;
     cudaEvent_t ev;
     if (!tc_tiles.empty()) {
         const size_t fl = (size_t)n_mat * Wm * Wm;
@@ -1414,7 +1414,7 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     a.cat_probs = ws.catp.as<double>();
     a.tile_families = TFm;
     a.W = W;
-    const bool prof = (&ws == C->ws[0].get());
+    const bool prof = ws.sync;
     cudaEvent_t ev;
     if (prof) {
         C->prof.begin(1, ws.stream, &ev);
@@ -1456,7 +1456,7 @@ int score_enqueue(cafe_ctx* C, Workspace& ws, const cafe_request* R, int NB, caf
     const auto t_host = std::chrono::steady_clock::now();
     int rc = enqueue_score(C, ws, R, NB, ws.fam_lnl.as<double>(), ws.total.as<double>(), info);
     if (rc) return rc;
-    if (C->prof.on && &ws == C->ws[0].get()) C->prof.acc.host_total_ms += host_ms_since(t_host);
+    if (C->prof.on && ws.sync) C->prof.acc.host_total_ms += host_ms_since(t_host);
     CK(gate_leave(C, ws), "gate");
     CK(cudaEventRecord(ws.ev_staged, ws.stream), "event");
     ws.staged = true;
@@ -1668,7 +1668,37 @@ int reconstruct_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_rec
         rc = stage_cat_probs(C, ws, R, K, 1);
         if (rc) return rc;
     }
+    // transposed log2 of every internal non-root node's matrix (pass 1 of k_pupko)
+    const int nstate = Z.Smax + 1;
+    std::vector<const void*> lsrc, ldst;
+    std::vector<const float*> lmats((size_t)K * n, nullptr);
+    {
+        int n_int = 0;
+        for (int v = 0; v < n; ++v) n_int += (T.parent[v] >= 0 && T.leaf_col[v] < 0);
+        const size_t per = (size_t)nstate * nstate;
+        CK(ws.rc_lm.reserve(std::max<size_t>((size_t)K * n_int * per, 1) * sizeof(float)), "log2 matrices");
+        const double* const* hmats = ws.h_mats.as<const double*>();
+        size_t slot = 0;
+        for (int k = 0; k < K; ++k)
+            for (int v = 0; v < n; ++v) {
+                if (T.parent[v] < 0 || T.leaf_col[v] >= 0) continue;
+                float* d = ws.rc_lm.as<float>() + slot++ * per;
+                lmats[(size_t)k * n + v] = d;
+                lsrc.push_back(hmats[(size_t)k * n + v]);
+                ldst.push_back(d);
+            }
+        const size_t np = lmats.size() + 2 * lsrc.size();
+        CK(ws.rc_lptr.reserve(std::max<size_t>(np, 1) * sizeof(void*)), "log2 matrices");
+        std::vector<const void*> all;
+        all.reserve(np);
+        for (const float* p : lmats) all.push_back(p);
+        all.insert(all.end(), lsrc.begin(), lsrc.end());
+        all.insert(all.end(), ldst.begin(), ldst.end());
+        CK(cudaMemcpyAsync(ws.rc_lptr.p, all.data(), np * sizeof(void*), cudaMemcpyHostToDevice, ws.stream), "h2d");
+    }
+    const void* const* dptr = ws.rc_lptr.as<const void*>();
     PupkoArgs a{};
+    a.lmats = reinterpret_cast<const float* const*>(dptr);
     a.plan = T.plan;
     a.tiles = ws.tiles.as<PruneTile>();
     a.n_tiles = n_tiles;
@@ -1689,6 +1719,10 @@ int reconstruct_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_rec
     a.n_failed = ws.rc_nfail.as<int32_t>();
     a.exhaustive = out->exhaustive ? 1 : 0;
     if (F > 0) {
+        CK(launch_log2_matrices(reinterpret_cast<const double* const*>(dptr + lmats.size()),
+                                reinterpret_cast<float* const*>(const_cast<void**>(dptr + lmats.size() + lsrc.size())),
+                                (int)lsrc.size(), nstate, Z.msize, ws.stream),
+           "log2 matrices");
         CK(launch_pupko(a, n_ctas, ws.stream), "reconstruct");
         CK(launch_recon_counts(ws.rc_state.as<int32_t>(), F, n, K, Z.gamma ? ws.catp.as<double>() : nullptr,
                                Z.gamma ? 1 : 0, T.plan.leaf_col, ws.rc_mean.as<double>(), ws.rc_count.as<int32_t>(),
@@ -1815,13 +1849,19 @@ int pvalues_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_pvalues
     }
     std::vector<char> saturated(n, 0);
     std::vector<const double*> node_mat(n, nullptr);
+    std::vector<int> node_mi(n, -1);   // distinct matrix of each non-root node
+    std::map<const double*, int> mat_ids;
     for (int v = 0; v < n; ++v) {
         if (T.parent[v] < 0) continue;
         node_mat[v] = host_mats[hm[v]].data();
+        node_mi[v] = mat_ids.emplace(hm[v], (int)mat_ids.size()).first->second;
         const double lam = R->lambdas[T.lambda_index[v]], t = T.branch_length[v];
         saturated[v] = (1 - 2 * (lam * t / (1 + lam * t))) < 0;   // matrix_cache::is_saturated
     }
-    std::map<std::pair<const double*, int>, std::discrete_distribution<int>> dists;
+    // one distribution per (matrix, parent size), built on first use; parent
+    // sizes are root sizes <= R or sampled sizes < S
+    const int n_ps = std::max(RR, S) + 1;
+    std::vector<std::unique_ptr<std::discrete_distribution<int>>> dists((size_t)mat_ids.size() * n_ps);
     std::mt19937 engine(out->seed);
     const int64_t NS = (int64_t)RR * nsim;
     const int L = T.n_leaves;
@@ -1842,13 +1882,12 @@ int pvalues_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_pvalues
                         std::uniform_int_distribution<int> d(0, S - 1);
                         c = d(engine);   // drawn and discarded, as the reference does
                     }
-                    auto key = std::make_pair(node_mat[v], ps);
-                    auto it = dists.find(key);
-                    if (it == dists.end()) {
+                    std::unique_ptr<std::discrete_distribution<int>>& d = dists[(size_t)node_mi[v] * n_ps + ps];
+                    if (!d) {
                         const double* row = node_mat[v] + (size_t)ps * msize;
-                        it = dists.emplace(key, std::discrete_distribution<int>(row, row + S)).first;
+                        d.reset(new std::discrete_distribution<int>(row, row + S));
                     }
-                    c = it->second(engine);
+                    c = (*d)(engine);
                 }
                 sizes[v] = c;
                 mx = std::max(mx, c);
@@ -2065,8 +2104,15 @@ int cafe_ctx_create(const cafe_config* cfg, cafe_ctx** out) {
             delete C;
             return CAFE_ERR_CUDA;
         }
+        w->sync = (i == 0);
         C->ws.push_back(std::move(w));
     }
+    C->ws_alt = std::make_unique<Workspace>();
+    if (C->ws_alt->init(dev) != CAFE_OK) {
+        delete C;
+        return CAFE_ERR_CUDA;
+    }
+    C->ws_alt->sync = true;
     *out = C;
     return CAFE_OK;
 }
@@ -2388,7 +2434,11 @@ int cafe_score_batch_device(cafe_ctx* C, const cafe_request* req, int n, double*
     if (!C || n < 1) return CAFE_ERR_INVALID;
     std::lock_guard<std::mutex> lk(C->mu);
     cudaSetDevice(C->device);
-    Workspace& ws = *C->ws[0];
+    // consecutive calls alternate between two workspaces: the host prepares
+    // a call (refilling that workspace's pinned staging buffers) while the
+    // device still runs the previous one
+    C->dev_flip ^= 1;
+    Workspace& ws = C->dev_flip ? *C->ws_alt : *C->ws[0];
     AllocScope scope(ws.stream);
     cudaStream_t user = static_cast<cudaStream_t>(stream);
     ScoreInfo info;

@@ -207,6 +207,8 @@ struct PupkoArgs {
     const int32_t* counts;       // [F][n_leaves]
     int64_t F;
     const double* const* mats;   // [K][n_nodes] FP64 matrix per (category, node)
+    const float* const* lmats;   // [K][n_nodes] transposed log2 of the internal non-root nodes' matrices,
+                                 // (S + 1) x (S + 1) (launch_log2_matrices), null elsewhere
     int ld_mat;                  // matrix side (>= S + 1)
     const double* prior;         // prior[j] = P(root size j)
     int n_prior;
@@ -222,6 +224,8 @@ struct PupkoArgs {
     int exhaustive;              // 1: exact FP64 scan of every child state
 };
 cudaError_t launch_pupko(const PupkoArgs& a, int n_ctas, cudaStream_t s);
+cudaError_t launch_log2_matrices(const double* const* src, float* const* dst, int n_mats, int n, int ld,
+                                 cudaStream_t s);
 size_t pupko_scratch_doubles(const TreePlan& P, int S);
 size_t pupko_c_entries(const TreePlan& P, int S);
 cudaError_t launch_recon_counts(const int32_t* state, int64_t F, int n_nodes, int K, const double* cat_probs,

@@ -13,21 +13,26 @@
 //     u[j]    = prod over children c (descendant order) of L_c[j]
 //     L_v[i]  = max_j u[j] * M_v[i][j],   C_v[i] = first j attaining it
 // in FP64: (S+1)^2 products per node and family. GB300's FP64 pipe issues
-// about two such products per clock and SM, so k_pupko finds the argmax in
-// two passes instead:
-//   pass 1  p_j = log2 u[j] + log2 M[i][j] in FP32 (FP32 pipes, ~60x the
-//           FP64 rate); best = max_j p_j
-//   pass 2  the exact FP64 product u[j] * M[i][j] only for the j with
-//           p_j >= best - delta, scanned in ascending j with the
-//           reference's strict '>' rule
+// about two such products per clock and SM (and a divergent one costs a
+// whole warp's issue), so k_pupko ranks the products in FP32 logarithms:
+//   p_j = log2 u[j] + log2 M[i][j]   (FP32; log2 M precomputed once per
+//                                     request, transposed, by k_log2_matrices)
+// One pass keeps the largest p (b1, at j1) and the second largest (b2).
 // Every log2 carries an absolute error <= 6.3e-5 (FP32 rounding of a value
 // of magnitude <= 1075 plus log2f's 1 ulp) and the sum <= 1.3e-4 more, so a
-// j whose exact product equals the FP64 maximum has p_j >= best - 5e-4;
-// delta = 2^-8 leaves an 8x margin. When the maximum cannot be a normal
-// FP64 number the filter is not used: best below -1075 - delta means every
-// product rounds to 0 (the reference then returns L = 0, C = 0), and best
-// within delta of the subnormal range makes the row scan every j exactly.
-// `exhaustive` turns the filter off everywhere (the plain FP64 scan).
+// j whose exact product equals the FP64 row maximum has p_j >= b1 - 5e-4.
+// With delta = 2^-8 (8x margin):
+//   b1 < -1075 - delta          every product rounds to 0 in FP64: L = 0,
+//                               C = 0 (the reference's result for such rows)
+//   b1 >= -1022 + delta and     only j1 can reach the FP64 maximum: C = j1,
+//   b2 < b1 - delta             L = u[j1] * M[i][j1] in FP64 (one product)
+//   otherwise                   the (row, family) joins a per-block list
+//                               that all threads then scan in FP64 over the
+//                               j with p_j >= b1 - delta (every j when b1 is
+//                               near the subnormal range), ascending, with
+//                               the reference's strict '>'
+// `exhaustive` sends every (row, family) through the FP64 scan of every j:
+// the plain reference arithmetic, used to check the ranking.
 #include "common.cuh"
 
 #include <math.h>
@@ -44,21 +49,30 @@ constexpr int RB = 8 * RW;   // parent states per block
 constexpr int JC = 32;       // child states per staged chunk
 constexpr float kDelta = 0.00390625f;   // 2^-8, in log2 units
 
-// log2 of x >= 0 in FP32 (-inf for 0): exponent exact, mantissa through
-// log2f; absolute error <= 2^-14 + 1 ulp of log2f for |result| < 2048.
+// log2 of x >= 0 in FP32 (-inf for 0) from the bits of x, without FP64
+// arithmetic on normal numbers: exponent exact, the top 23 mantissa bits
+// (truncation: relative error < 2^-23, i.e. < 1.8e-7 in log2) through
+// log2f (1 ulp), then the FP32 sum (<= 2^-14 for |result| < 2048).
 __device__ __forceinline__ float flog2(double x) {
-    if (!(x > 0.0)) return -INFINITY;
-    int e = 0;
-    const double m = frexp(x, &e);   // x = m * 2^e, m in [0.5, 1), exact
-    return (float)(e - 1) + log2f((float)(m * 2.0));
+    long long b = __double_as_longlong(x);
+    if (b <= 0) return -INFINITY;   // +0 (and negative values, which never occur)
+    int e = (int)((b >> 52) & 0x7ff);
+    int bias = 1023;
+    if (e == 0) {                   // subnormal: scale into the normal range
+        b = __double_as_longlong(x * 0x1p64);
+        e = (int)((b >> 52) & 0x7ff);
+        bias += 64;
+    }
+    const float m = __int_as_float(0x3f800000 | (int)((b >> 29) & 0x7fffff));
+    return (float)(e - bias) + log2f(m);
 }
 
 struct Staging {
-    double m[RB][JC + 1];   // M tile: parent states i0.., child states j0..
-    double u[JC][TF];       // u chunk
-    float lm[JC][RB];       // log2 of the M tile, child-state major
-    float lu[JC][TF];
+    float lm[JC][RB];       // log2 M tile, child-state major
+    float lu[JC][TF];       // log2 u chunk
 };
+
+constexpr int kSlowCap = RB * TF;   // (row, family) pairs of one block of rows
 
 // Factor of child `ci` at child state j for family `fam` (tile lane f): a
 // column of the leaf's matrix at the observed count, or the child's L.
@@ -74,32 +88,29 @@ __device__ __forceinline__ double child_value(const PupkoArgs& a, const double* 
     return Lbase[((size_t)P.slot[ch] * n + j) * TF + f];
 }
 
-// Stage the M tile (rows i0.., columns j0..) and the u / log2 u chunk.
-__device__ __forceinline__ void stage(Staging& s, const double* M, int ld, int n, int i0, int j0, const double* U,
-                                      const float* LU, bool with_u) {
+// Stage the log2 tile (parent states i0.., child states j0..) from the
+// transposed log2 matrix LMt[j][i] (pitch n) and the log2 u chunk.
+__device__ __forceinline__ void stage(Staging& s, const float* LMt, int n, int i0, int j0, const float* LU) {
     const int tid = threadIdx.x;
     for (int e = tid; e < RB * JC; e += NT) {
-        const int r = e / JC, jj = e % JC;
+        const int jj = e / RB, r = e % RB;
         const int i = i0 + r, j = j0 + jj;
-        s.m[r][jj] = (i < n && j < n) ? M[(size_t)i * ld + j] : 0.0;
+        s.lm[jj][r] = (i < n && j < n) ? LMt[(size_t)j * n + i] : -INFINITY;
     }
     for (int e = tid; e < JC * TF; e += NT) {
         const int jj = e / TF, f = e % TF;
         const int j = j0 + jj;
         s.lu[jj][f] = j < n ? LU[(size_t)j * TF + f] : -INFINITY;
-        if (with_u) s.u[jj][f] = j < n ? U[(size_t)j * TF + f] : 0.0;
-    }
-    __syncthreads();
-    for (int e = tid; e < RB * JC; e += NT) {
-        const int r = e % RB, jj = e / RB;
-        s.lm[jj][r] = flog2(s.m[r][jj]);
     }
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(NT) k_pupko(PupkoArgs a) {
+__global__ void __launch_bounds__(NT, 4) k_pupko(PupkoArgs a) {
     __shared__ __align__(16) Staging s;
     __shared__ int node_ii[kMaxNodes];
+    __shared__ int slow_pair[kSlowCap];      // (row - i0) * TF + family
+    __shared__ float slow_best[kSlowCap];    // b1 of the pair (-inf: scan every j)
+    __shared__ int n_slow;
     __shared__ int root_arg[TF];
     __shared__ double root_val[TF];
 
@@ -164,43 +175,20 @@ __global__ void __launch_bounds__(NT) k_pupko(PupkoArgs a) {
             double* Lv = Lbase + (size_t)P.slot[v] * n * TF;
             int32_t* Cv = Cbase + (size_t)ii * n * TF;
             const double* M = mats[v];
+            const float* LMt = a.lmats[(size_t)k * P.n_nodes + v];
             for (int i0 = 0; i0 < n; i0 += RB) {
-                float best[RW];
-#pragma unroll
-                for (int r = 0; r < RW; ++r) best[r] = -INFINITY;
-                if (!a.exhaustive) {
-                    for (int j0 = 0; j0 < n; j0 += JC) {
-                        stage(s, M, a.ld_mat, n, i0, j0, U, LU, false);
-                        const int jn = min(JC, n - j0);
-                        for (int jj = 0; jj < jn; ++jj) {
-                            const float lu = s.lu[jj][lane];
-                            const float4 lm = *reinterpret_cast<const float4*>(&s.lm[jj][warp * RW]);
-                            best[0] = fmaxf(best[0], lu + lm.x);
-                            best[1] = fmaxf(best[1], lu + lm.y);
-                            best[2] = fmaxf(best[2], lu + lm.z);
-                            best[3] = fmaxf(best[3], lu + lm.w);
-                        }
-                        __syncthreads();
-                    }
-                }
-                bool zero[RW], exh[RW];
-                float thr[RW];
-                double mx[RW];
-                int arg[RW];
-                bool need = false;
+                float b1[RW], b2[RW];
+                int j1[RW];
 #pragma unroll
                 for (int r = 0; r < RW; ++r) {
-                    const int i = i0 + warp * RW + r;
-                    zero[r] = !a.exhaustive && !(best[r] >= -1075.0f - kDelta);
-                    exh[r] = a.exhaustive || best[r] < -1022.0f + kDelta;
-                    thr[r] = best[r] - kDelta;
-                    mx[r] = -1.0;
-                    arg[r] = 0;
-                    need |= (i < n && lane < cnt && !zero[r]);
+                    b1[r] = -INFINITY;
+                    b2[r] = -INFINITY;
+                    j1[r] = 0;
                 }
-                if (__syncthreads_or(need)) {
+                if (tid == 0) n_slow = 0;
+                if (!a.exhaustive) {
                     for (int j0 = 0; j0 < n; j0 += JC) {
-                        stage(s, M, a.ld_mat, n, i0, j0, U, LU, true);
+                        stage(s, LMt, n, i0, j0, LU);
                         const int jn = min(JC, n - j0);
                         for (int jj = 0; jj < jn; ++jj) {
                             const float lu = s.lu[jj][lane];
@@ -208,26 +196,63 @@ __global__ void __launch_bounds__(NT) k_pupko(PupkoArgs a) {
                             const float lm[RW] = {lm4.x, lm4.y, lm4.z, lm4.w};
 #pragma unroll
                             for (int r = 0; r < RW; ++r) {
-                                if (!zero[r] && (exh[r] || lu + lm[r] >= thr[r])) {
-                                    const double val = s.u[jj][lane] * s.m[warp * RW + r][jj];
-                                    if (val > mx[r]) {
-                                        mx[r] = val;
-                                        arg[r] = j0 + jj;
-                                    }
-                                }
+                                const float p = lu + lm[r];
+                                j1[r] = p > b1[r] ? j0 + jj : j1[r];
+                                b2[r] = fmaxf(b2[r], fminf(b1[r], p));
+                                b1[r] = fmaxf(b1[r], p);
                             }
                         }
                         __syncthreads();
                     }
+                } else {
+                    __syncthreads();
                 }
 #pragma unroll
                 for (int r = 0; r < RW; ++r) {
                     const int i = i0 + warp * RW + r;
-                    if (i < n) {
-                        Lv[(size_t)i * TF + lane] = zero[r] ? 0.0 : mx[r];
-                        Cv[(size_t)i * TF + lane] = zero[r] ? 0 : arg[r];
+                    const bool valid = i < n && lane < cnt;
+                    const bool zero = !a.exhaustive && !(b1[r] >= -1075.0f - kDelta);
+                    const bool near_sub = b1[r] < -1022.0f + kDelta;
+                    const bool fast = !a.exhaustive && !near_sub && b2[r] < b1[r] - kDelta;
+                    if (valid && (zero || fast)) {
+                        double L = 0.0;
+                        int Cj = 0;
+                        if (fast) {
+                            L = U[(size_t)j1[r] * TF + lane] * M[(size_t)i * a.ld_mat + j1[r]];
+                            Cj = j1[r];
+                        }
+                        Lv[(size_t)i * TF + lane] = L;
+                        Cv[(size_t)i * TF + lane] = Cj;
+                    } else if (valid) {
+                        const int q = atomicAdd(&n_slow, 1);
+                        slow_pair[q] = (i - i0) * TF + lane;
+                        slow_best[q] = (a.exhaustive || near_sub) ? -INFINITY : b1[r];
                     }
                 }
+                __syncthreads();
+                // near-ties and rows near the subnormal range: FP64 over the
+                // candidate child states, one (row, family) per thread
+                for (int q = tid; q < n_slow; q += NT) {
+                    const int i = i0 + slow_pair[q] / TF, f = slow_pair[q] % TF;
+                    const float best = slow_best[q];
+                    const bool all = !(best > -INFINITY);
+                    const float thr = best - kDelta;
+                    const double* Mi = M + (size_t)i * a.ld_mat;
+                    double mx = -1.0;
+                    int arg = 0;
+                    for (int j = 0; j < n; ++j) {
+                        if (all || LU[(size_t)j * TF + f] + LMt[(size_t)j * n + i] >= thr) {
+                            const double val = U[(size_t)j * TF + f] * Mi[j];
+                            if (val > mx) {
+                                mx = val;
+                                arg = j;
+                            }
+                        }
+                    }
+                    Lv[(size_t)i * TF + f] = mx;
+                    Cv[(size_t)i * TF + f] = arg;
+                }
+                __syncthreads();
             }
             __syncthreads();   // L_v complete; U / LU free for the next node
         }
@@ -308,7 +333,29 @@ __global__ void k_branch_prob(BranchProbArgs a) {
     }
 }
 
+// Transposed log2 of the first n x n block of each matrix:
+// out[j * n + i] = log2 M[i][j] (one conversion per entry and request
+// instead of one per entry, tile and pass).
+__global__ void k_log2_matrices(const double* const* __restrict__ src, float* const* __restrict__ dst, int n,
+                                int ld) {
+    const double* M = src[blockIdx.y];
+    float* out = dst[blockIdx.y];
+    const int64_t total = (int64_t)n * n;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(e / n), i = (int)(e % n);
+        out[e] = flog2(M[(size_t)i * ld + j]);
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_log2_matrices(const double* const* src, float* const* dst, int n_mats, int n, int ld,
+                                 cudaStream_t s) {
+    if (n_mats <= 0 || n <= 0) return cudaSuccess;
+    const int bx = (int)std::min<int64_t>(((int64_t)n * n + 255) / 256, 64);
+    k_log2_matrices<<<dim3(bx, n_mats), 256, 0, s>>>(src, dst, n, ld);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_pupko(const PupkoArgs& a, int n_ctas, cudaStream_t s) {
     if (a.n_tiles <= 0) return cudaSuccess;

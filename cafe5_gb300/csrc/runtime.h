@@ -133,6 +133,7 @@ struct Slab {
 // Per-request device workspace (one per stream).
 struct Workspace {
     cudaStream_t stream = nullptr;
+    bool sync = false;                 // a synchronous-call workspace (profiled when profiling is on)
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     cudaEvent_t ev_staged = nullptr;   // after the last request's host->device staging copies
     bool staged = false;
@@ -154,7 +155,7 @@ struct Workspace {
         catids;
     PinnedBuf h_conv, h_mi, h_flags, h_tiles64, h_tiles_fb, h_tail, h_catids;
     // reconstruction
-    DevBuf rc_c, rc_state, rc_rmax, rc_mean, rc_count, rc_nfail, rc_parent, rc_bp;
+    DevBuf rc_c, rc_state, rc_rmax, rc_mean, rc_count, rc_nfail, rc_parent, rc_bp, rc_lm, rc_lptr;
     std::vector<PruneTile> tile_vec;
     std::vector<MatEntry*> entry_vec;   // cache entry of every (combined category, node)
     // CUDA graphs of the pruning phase: stream ops go through an op log;
@@ -209,6 +210,8 @@ struct cafe_ctx {
     std::map<int, std::pair<int, int>> tuned;   // bin width -> (CTAs per SM, stages) chosen by cafe_autotune
     // workspaces: [0] for synchronous calls, [1..] for the serving loop
     std::vector<std::unique_ptr<cafe::Workspace>> ws;
+    std::unique_ptr<cafe::Workspace> ws_alt;   // second workspace of the device-pointer calls
+    int dev_flip = 0;
     int n_ctas = 0;
     int sm_count = 0;
     // serving loop
