@@ -35,16 +35,28 @@ namespace {
 constexpr double kLn2Hi = 6.93147180369123816490e-01;  // Cody-Waite split of ln 2
 constexpr double kLn2Lo = 1.90821492927058770002e-10;
 
-__device__ __forceinline__ double out_value(double m, int e) {
-    double v = (e == 0) ? m : scalbn(m, e);
-    return v < 1.0 ? v : 1.0;
-}
+// min(v, 1) for v >= 0 without an FP64 instruction: v >= 1 exactly when
+// the high word of its bits is >= that of 1.0.
+__device__ __forceinline__ double clamp1(double v) { return __double2hiint(v) >= 0x3ff00000 ? 1.0 : v; }
+
+__device__ __forceinline__ double out_value(double m, int e) { return clamp1(e == 0 ? m : scalbn(m, e)); }
+
+// Per-matrix coefficient tables in shared memory (k = 0..W):
+//   p1[c] = (q + alpha) / (c + 1), p2[c] = c (alpha - q) / (c + 1)
+//     so that ((s - c) q + alpha (s + c)) / (c + 1) = s p1[c] + p2[c]
+//   bb[c] = (1 - 2 alpha) (c - 1) / (c + 1)
+struct Coeffs {
+    const double* p1;
+    const double* p2;
+    const double* bb;
+};
 
 // One row chain: the coefficients g_c of row s, c = 0..s, as a running
-// mantissa m (and the previous one mp) times 2^E.
+// mantissa m (and the previous one mp) times 2^E; cs = c / s for the
+// mirrored entry of row c.
 struct RowChain {
     int s, E;
-    double m, mp, sm, sp, inv_s;
+    double m, mp, sd, inv_s, cs;
 
     __device__ void init(int s_, double la, const double* inv) {
         s = s_;
@@ -57,22 +69,19 @@ struct RowChain {
             m = exp((L0 - (double)E * kLn2Hi) - (double)E * kLn2Lo);
         }
         mp = 0.0;
-        sm = (double)s;  // s - c
-        sp = (double)s;  // s + c
+        sd = (double)s;
         inv_s = inv[s];
+        cs = 0.0;
     }
     __device__ __forceinline__ double value() const { return out_value(m, E); }
-    // g_c -> g_{c+1}
-    __device__ __forceinline__ void advance(int c, double alpha, double coeff, double q, const double* inv,
-                                            const double* bq) {
-        const double a = fma(sm, q, alpha * sp) * inv[c + 1];
-        const double b = coeff * bq[c];
-        const double nx = fma(a, m, b * mp);
+    // g_c -> g_{c+1}: two FMAs and a product per step
+    __device__ __forceinline__ void advance(int c, const Coeffs& k) {
+        const double a = fma(sd, k.p1[c], k.p2[c]);
+        const double nx = fma(a, m, k.bb[c] * mp);
         mp = m;
         m = nx;
-        sm -= 1.0;
-        sp += 1.0;
-        if (m > 0x1p+600) {
+        cs += inv_s;
+        if (__double2hiint(m) >= 0x65800000) {   // m >= 2^601
             m *= 0x1p-600;
             mp *= 0x1p-600;
             E += 600;
@@ -94,28 +103,34 @@ __global__ void __launch_bounds__(128) k_matrix_build(const MatrixJob* __restric
     extern __shared__ double sh[];
     const MatrixJob J = jobs[blockIdx.x];
     const int W = J.size;
-    double* inv = sh;          // inv[k] = 1/k, k = 0..W
-    double* bq = sh + W + 1;   // bq[c] = (c - 1)/(c + 1), c = 0..W
+    double* inv = sh;                  // inv[k] = 1/k, k = 0..W
+    double* p1 = sh + (W + 1);         // coefficient tables (Coeffs), k = 0..W
+    double* p2 = sh + 2 * (W + 1);
+    double* bb = sh + 3 * (W + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double* stage = sh + 2 * (W + 1) + (size_t)warp * kStageCols * kStagePitch;
-    int* srow = reinterpret_cast<int*>(sh + 2 * (W + 1) + (size_t)(blockDim.x >> 5) * kStageCols * kStagePitch) +
+    double* stage = sh + 4 * (W + 1) + (size_t)warp * kStageCols * kStagePitch;
+    int* srow = reinterpret_cast<int*>(sh + 4 * (W + 1) + (size_t)(blockDim.x >> 5) * kStageCols * kStagePitch) +
                 warp * 32;
-    for (int k = threadIdx.x; k <= W; k += blockDim.x) {
-        inv[k] = k ? 1.0 / (double)k : 0.0;
-        bq[k] = (double)(k - 1) / (double)(k + 1);
-    }
     double* M = J.dst;
     const double lt = J.lambda * J.t;
     const double alpha = lt / (1 + lt);
     const double coeff = 1 - 2 * alpha;
     const bool live = (coeff > 0 && coeff != 1);
+    const double q = live ? coeff / alpha : 0.0;
+    for (int k = threadIdx.x; k <= W; k += blockDim.x) {
+        const double ik = 1.0 / (double)(k + 1);
+        inv[k] = k ? 1.0 / (double)k : 0.0;
+        p1[k] = (q + alpha) * ik;
+        p2[k] = (double)k * (alpha - q) * ik;
+        bb[k] = coeff * ((double)(k - 1) * ik);
+    }
+    const Coeffs cf{p1, p2, bb};
     for (int c = threadIdx.x; c < W; c += blockDim.x) M[c] = (c == 0) ? 1.0 : 0.0;
     if (!live) {
         for (size_t i = (size_t)W + threadIdx.x; i < (size_t)W * W; i += blockDim.x) M[i] = 0.0;
         return;
     }
     __syncthreads();
-    const double q = coeff / alpha;
     const double la = log(alpha);
     const int npairs = W / 2;   // rows 1..W-1 in pairs (the middle row once when W is even)
     for (int p0 = warp * 32; p0 < npairs; p0 += blockDim.x) {
@@ -135,11 +150,8 @@ __global__ void __launch_bounds__(128) k_matrix_build(const MatrixJob* __restric
                     if (act && c < s) {
                         const double v = ch.value();
                         stage[cc * kStagePitch + lane] = v;
-                        if (c > 0) {
-                            const double u = (double)c * ch.inv_s * v;
-                            M[(size_t)c * W + s] = u < 1.0 ? u : 1.0;
-                        }
-                        ch.advance(c, alpha, coeff, q, inv, bq);
+                        if (c > 0) M[(size_t)c * W + s] = clamp1(ch.cs * v);
+                        ch.advance(c, cf);
                     }
                 }
                 __syncwarp();
@@ -164,7 +176,7 @@ cudaError_t launch_matrix_build(const MatrixJob* d_jobs, int n_jobs, int max_siz
     // one thread per row pair, in whole warps (at most 128)
     const int pairs = max_size / 2;
     const int threads = std::min(128, std::max(32, (pairs + 31) / 32 * 32));
-    size_t smem = sizeof(double) * (2 * (size_t)(max_size + 1) + (size_t)(threads / 32) * kStageCols * kStagePitch) +
+    size_t smem = sizeof(double) * (4 * (size_t)(max_size + 1) + (size_t)(threads / 32) * kStageCols * kStagePitch) +
                   sizeof(int) * (size_t)threads;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_matrix_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
