@@ -105,6 +105,18 @@ int oracle_pvalues(const oracle_tree* tree, const int32_t* counts, int64_t F, in
                    const double* lambdas, int n_lambdas, int S, int R, int n_sim, uint32_t seed,
                    double* pvalues, double* conditional, double* root_vectors);
 
+/* The simulator action (src/simulator.cpp:29-91) from a std::mt19937 seeded
+ * with `seed`: K = 0 base model, K >= 1 gamma (a category drawn per family);
+ * root_sizes[n_fam] are the prior's sizes (select_root_size); err_rows
+ * [err_nrows][3] or NULL, err_max_count the error model's largest count.
+ * Outputs sizes_out[n_fam][n_nodes] and lambda_out[n_fam] (the family's
+ * first lambda). Returns 0, -1 on bad input, -2 where the reference throws
+ * (a simulated leaf size outside the error model). */
+int oracle_simulate(const oracle_tree* tree, const double* lambdas, int n_lambdas, int K,
+                    const double* multipliers, const double* cat_probs, const double* err_rows,
+                    int err_nrows, int err_ndev, int err_max_count, int S, int R, int n_fam,
+                    const int32_t* root_sizes, uint32_t seed, int32_t* sizes_out, double* lambda_out);
+
 #ifdef __cplusplus
 }
 #endif

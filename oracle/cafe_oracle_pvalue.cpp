@@ -176,3 +176,86 @@ extern "C" int oracle_pvalues(const oracle_tree* tree, const int32_t* counts, in
     }
     return 0;
 }
+
+// The simulator action (src/simulator.cpp:29-91): per family, the gamma
+// model first picks a rate category (gamma_model::get_simulation_lambda,
+// src/gamma_core.cpp:91-95, a std::discrete_distribution over the category
+// probabilities); then up to 50 attempts (create_trial) set the root to
+// root_sizes[f] and every other node, in prefix order, from its parent's
+// matrix row (set_weighted_random_family_size, src/probability.cpp:449-476),
+// leaves passed through the error model (adjust_for_error_model, :478-500),
+// until the family exists at the root (gene_family::exists_at_root,
+// src/gene_family.cpp:62-91).
+extern "C" int oracle_simulate(const oracle_tree* tree, const double* lambdas, int n_lambdas, int K,
+                               const double* multipliers, const double* cat_probs, const double* err_rows,
+                               int err_nrows, int err_ndev, int err_max_count, int S, int R, int n_fam,
+                               const int32_t* root_sizes, uint32_t seed, int32_t* sizes_out, double* lambda_out) {
+    if (!tree || tree->n_nodes < 2 || n_lambdas < 1 || S < 1 || R < 1 || n_fam < 0) return -1;
+    if (err_rows && err_ndev != 3) return -1;
+    Tree T = make_tree(tree);
+    const int size = std::max(S, R) + 1;
+    const bool gamma = K > 0;
+    const int KK = gamma ? K : 1;
+    std::map<std::pair<long, long>, std::vector<double>> cache;
+    std::vector<const double*> mats((size_t)KK * T.n, nullptr);
+    std::vector<int> saturated((size_t)KK * T.n, 0);
+    for (int k = 0; k < KK; ++k)
+        for (int v = 0; v < T.n; ++v) {
+            if (T.parent[v] < 0) continue;
+            const double lam = lambdas[T.lam[v]] * (gamma ? multipliers[k] : 1.0);
+            const long lq = (long)(lam * 1000000000), tq = (long)(T.t[v] * 1000);
+            auto& m = cache[{lq, tq}];
+            if (m.empty()) {
+                m.resize((size_t)size * size);
+                oracle_fill_matrix((double)lq / 1000000000.0, (double)tq / 1000.0, size, m.data());
+            }
+            mats[(size_t)k * T.n + v] = m.data();
+            saturated[(size_t)k * T.n + v] = oracle_is_saturated(T.t[v], lam);
+        }
+    std::mt19937 engine(seed);
+    std::vector<int> z(T.n);
+    std::vector<char> reg(T.n);
+    for (int f = 0; f < n_fam; ++f) {
+        int k = 0;
+        if (gamma) {
+            std::discrete_distribution<int> pick(cat_probs, cat_probs + K);
+            k = pick(engine);
+        }
+        lambda_out[f] = lambdas[0] * (gamma ? multipliers[k] : 1.0);
+        for (int attempt = 0; attempt < 50; ++attempt) {
+            z[T.root] = root_sizes[f];
+            for (int v : T.prefix) {
+                if (v == T.root) continue;
+                const int ps = z[T.parent[v]];
+                int c = 0;
+                if (ps > 0) {
+                    if (saturated[(size_t)k * T.n + v]) {
+                        std::uniform_int_distribution<int> d(0, S - 1);
+                        c = d(engine);
+                    }
+                    const double* row = mats[(size_t)k * T.n + v] + (size_t)ps * size;
+                    std::discrete_distribution<int> d(row, row + S);
+                    c = d(engine);
+                }
+                if (T.kids[v].empty() && err_rows) {
+                    if (c >= err_max_count) return -2;
+                    const double* p = err_rows + (size_t)std::min(c, err_nrows - 1) * 3;
+                    std::uniform_real_distribution<double> u(0.0, 1.0);
+                    const double rnd = u(engine);
+                    if (rnd < p[0]) c--;
+                    else if (rnd > (1 - p[2])) c++;
+                }
+                z[v] = c;
+            }
+            std::fill(reg.begin(), reg.end(), 0);
+            for (int v : T.post)
+                if (T.kids[v].empty() && z[v] > 0)
+                    for (int p = v; p >= 0 && !reg[p]; p = T.parent[p]) reg[p] = 1;
+            bool all = true;
+            for (int ch : T.kids[T.root]) all &= reg[ch] != 0;
+            if (all) break;
+        }
+        std::memcpy(sizes_out + (size_t)f * T.n, z.data(), sizeof(int32_t) * T.n);
+    }
+    return 0;
+}

@@ -60,6 +60,8 @@ def lib():
         _lib.oracle_branch_probabilities.argtypes = [C.POINTER(_Tree), p, i, p, C.c_int64, i, i, p]
         _lib.oracle_pvalues.restype = i
         _lib.oracle_pvalues.argtypes = [C.POINTER(_Tree), p, C.c_int64, i, p, i, i, i, i, C.c_uint32, p, p, p]
+        _lib.oracle_simulate.restype = i
+        _lib.oracle_simulate.argtypes = [C.POINTER(_Tree), p, i, i, p, p, p, i, i, i, i, i, i, p, C.c_uint32, p, p]
     return _lib
 
 
@@ -203,3 +205,25 @@ def pvalues(tree: TreeArrays, counts: np.ndarray, lambdas: Sequence[float], *, S
     if rc:
         raise RuntimeError(f"oracle_pvalues failed: {rc}")
     return pv, cd, rv
+
+
+def simulate(tree: TreeArrays, lambdas: Sequence[float], root_sizes: Sequence[int], *, S: int, R: int, seed: int,
+             multipliers: Optional[Sequence[float]] = None, cat_probs: Optional[Sequence[float]] = None,
+             err_rows: Optional[np.ndarray] = None, err_max_count: int = 0):
+    """The simulator action: (sizes[n][n_nodes], lambda[n])."""
+    lam = np.ascontiguousarray(lambdas, dtype=np.float64)
+    roots = np.ascontiguousarray(root_sizes, dtype=np.int32)
+    gamma = multipliers is not None
+    mult = np.ascontiguousarray(multipliers if gamma else [1.0], dtype=np.float64)
+    cp = np.ascontiguousarray(cat_probs if gamma else [1.0], dtype=np.float64)
+    er = None if err_rows is None else np.ascontiguousarray(err_rows, dtype=np.float64)
+    n = len(tree.parent)
+    sizes = np.zeros((len(roots), n), np.int32)
+    lout = np.zeros(len(roots))
+    rc = lib().oracle_simulate(C.byref(tree.c), lam.ctypes.data, len(lam), len(mult) if gamma else 0,
+                               mult.ctypes.data, cp.ctypes.data, _ptr(er), 0 if er is None else er.shape[0],
+                               0 if er is None else er.shape[1], err_max_count, S, R, len(roots),
+                               roots.ctypes.data, seed, sizes.ctypes.data, lout.ctypes.data)
+    if rc:
+        raise RuntimeError(f"oracle_simulate failed: {rc}")
+    return sizes, lout

@@ -53,6 +53,7 @@
 #include "optimizer_scorer.h"
 #include "probability.h"
 #include "root_equilibrium_distribution.h"
+#include "simulator.h"
 #include "user_data.h"
 
 INITIALIZE_EASYLOGGINGPP
@@ -153,7 +154,7 @@ void usage() {
         "   [--max-family S --max-root R] [--prior uniform|uniform:N|poisson:X|rootdist:s=n,..]\n"
         "   [--repeat N] [--quiet]\n"
         "   [--optimize lambda|alpha|lambda_alpha|lambda_epsilon --initial x1,..]\n"
-        "   [--reconstruct] [--pvalues N_SIMULATIONS --seed S]\n"
+        "   [--reconstruct] [--pvalues N_SIMULATIONS --seed S] [--simulate N --seed S]\n"
         "cafe_ref_harness nm rosen|wall|bowl|product <maxiters> x1,..\n");
 }
 
@@ -221,7 +222,7 @@ int main(int argc, char** argv) {
     double alpha = -1;
     int gk = 0, S = -1, R = -1, repeat = 1;
     bool quiet = false, recon = false;
-    int n_sim = 0;
+    int n_sim = 0, n_simulate = 0;
     unsigned long seed = 10;
     for (int i = 1; i < argc; ++i) {
         std::string a = argv[i];
@@ -248,6 +249,7 @@ int main(int argc, char** argv) {
         else if (a == "--reconstruct") recon = true;
         else if (a == "--pvalues") n_sim = std::stoi(next());
         else if (a == "--seed") seed = std::stoul(next());
+        else if (a == "--simulate") n_simulate = std::stoi(next());
         else { usage(); return 2; }
     }
     if (tree_path.empty() || fam_path.empty() || lambdas.empty()) { usage(); return 2; }
@@ -375,6 +377,39 @@ int main(int argc, char** argv) {
                     std::printf("cat %s %a %a %a\n", s.family_id.c_str(), s.lambda_multiplier,
                                 s.category_likelihood, s.family_likelihood);
             }
+        }
+        if (n_simulate > 0) {
+            // the simulator action (src/simulator.cpp:61-91): the prior is
+            // resized to N families first (user_data::create_prior,
+            // src/user_data.cpp:204-205, drawing from the engine seeded
+            // with seed + 1), then the engine is seeded with `seed` and
+            // simulate_processes runs. Prints the root size of every family
+            // and every family's simulated sizes in prefix order.
+            std::vector<const clade*> nodes;
+            tree->apply_prefix_order([&](const clade* c) { nodes.push_back(c); });
+            randomizer_engine.seed(seed + 1);
+            prior->resize(n_simulate);
+            std::printf("roots");
+            for (int i = 0; i < n_simulate; ++i) std::printf(" %d", prior->select_root_size(i));
+            std::printf("\n");
+            user_data ud;
+            ud.max_family_size = max_fam;
+            ud.max_root_family_size = max_root;
+            ud.p_tree = tree.get();
+            ud.p_error_model = em.get();
+            ud.prior = std::move(*prior);
+            input_parameters ui;
+            ui.nsims = n_simulate;
+            simulator sim(ud, ui);
+            randomizer_engine.seed(seed);
+            std::vector<simulated_family> results;
+            sim.simulate_processes(m.get(), results);
+            for (auto& r : results) {
+                std::printf("sim %a", r.lambda);
+                for (auto* c : nodes) std::printf(" %d", r.values.at(c));
+                std::printf("\n");
+            }
+            return 0;
         }
         if (n_sim > 0) {
             // compute_pvalues as the estimate action runs it

@@ -14,6 +14,8 @@ tests, and stores inputs plus hex-float outputs:
                      objectives and over the likelihood scorers
   ref_pvalues.json   compute_pvalues with the random engine seeded:
                      conditional distributions and per-family p-values
+  ref_simulations.json  the simulator action with the engine seeded: root
+                     sizes and every simulated node size
 
 Only this script reads the reference (it needs /root/reference and the
 built harness); the tests read the committed JSON. Usage:
@@ -187,6 +189,41 @@ def make_pvalue_case(name, tree, fams, lambdas, *, n_sim, seed, lam_idx=None, S=
             "conditional_hex": cd, "pvalue_hex": [pv[i] for i in fams.ids]}
 
 
+def make_sim_case(name, tree, fams, lambdas, *, n, seed, prior, lam_idx=None, err=None, alpha=None, K=None,
+                  note=""):
+    """The simulator action of the compiled reference: the prior resized to
+    n families (engine seeded with seed + 1), then simulate_processes with
+    the engine seeded with `seed`."""
+    with tempfile.TemporaryDirectory() as d:
+        tp, fp = os.path.join(d, "t.nwk"), os.path.join(d, "f.tab")
+        nwk = tree.to_newick()
+        open(tp, "w").write(nwk)
+        write_families(fp, fams, tree)
+        args = ["--tree", tp, "--families", fp, "--lambdas", ",".join(repr(x) for x in lambdas),
+                "--prior", prior, "--simulate", str(n), "--seed", str(seed), "--quiet"]
+        lnwk = None
+        if lam_idx is not None:
+            lp = os.path.join(d, "l.nwk")
+            lnwk = lambda_tree_newick(tree, lam_idx)
+            open(lp, "w").write(lnwk)
+            args += ["--lambda-tree", lp]
+        if err is not None:
+            ep = os.path.join(d, "e.txt")
+            open(ep, "w").write(err)
+            args += ["--error", ep]
+        if alpha is not None:
+            args += ["--gamma-alpha", repr(alpha), "--gamma-k", str(K)]
+        out = run(args).splitlines()
+    bounds = [ln for ln in out if ln.startswith("bounds")][0].split()
+    roots = [int(x) for x in [ln for ln in out if ln.startswith("roots")][0].split()[1:]]
+    sims = [ln.split()[1:] for ln in out if ln.startswith("sim ")]
+    return {"name": name, "note": note, "newick": nwk, "lambda_newick": lnwk, "taxa": tree.leaf_names,
+            "ids": fams.ids, "counts": fams.counts.tolist(), "lambdas": [float(x).hex() for x in lambdas],
+            "S": int(bounds[1]), "R": int(bounds[2]), "n": n, "seed": seed, "prior": prior, "error_model": err,
+            "alpha": alpha, "K": K, "roots": roots, "lambda_hex": [r[0] for r in sims],
+            "sizes": [" ".join(r[1:]) for r in sims]}
+
+
 def make_case_r(*a, **kw):
     kw.setdefault("recon", True)
     return make_case(*a, **kw)
@@ -274,6 +311,25 @@ def main():
                                 n_sim=25, seed=3, S=10, R=8, note="explicit small bounds"))
     json.dump({"generator": "tests/golden/make_golden.py", "cases": pvs},
               open(os.path.join(HERE, "ref_pvalues.json"), "w"))
+
+    # -- the simulator action (seeded) ------------------------------------------
+    sims = []
+    sims.append(make_sim_case("sim_base_12taxa_rootdist", w0p.tree, w0p.families, [0.0025], n=40, seed=5,
+                              prior="rootdist:1=3,2=5,4=4,7=2", note="base model, root sizes from a rootdist"))
+    sims.append(make_sim_case("sim_base_12taxa_uniform", w0p.tree, w0p.families, [0.004], n=20, seed=2,
+                              prior="uniform:10", note="uniform prior: root size 0 included (50 failed attempts)"))
+    sims.append(make_sim_case("sim_gamma_24taxa_k4", w1.tree, FamilySet(w1.families.ids[:30], w1.families.counts[:30]),
+                              [0.002], n=30, seed=9, prior="rootdist:2=10,5=10,9=10", alpha=0.5, K=4,
+                              note="gamma: one category drawn per family"))
+    # the simulator refuses leaf sizes beyond the error model's rows
+    # (error_model::get_max_family_size is the row count), so give it 61
+    err_sim = "maxcnt: 60\ncntdiff: -1 0 1\n0 0 0.95 0.05\n" + "".join(
+        f"{i} 0.05 0.9 0.05\n" for i in range(1, 61))
+    sims.append(make_sim_case("sim_two_lambdas_error_32taxa", w2.tree, f2, [0.0015, 0.006], lam_idx=w2.lambda_of_node,
+                              n=30, seed=13, prior="rootdist:1=10,3=10,6=10", err=err_sim,
+                              note="two lambdas, error model at the leaves"))
+    json.dump({"generator": "tests/golden/make_golden.py", "cases": sims},
+              open(os.path.join(HERE, "ref_simulations.json"), "w"))
 
     # -- Nelder-Mead: analytic objectives and likelihood searches ------------
     analytic = []

@@ -151,3 +151,38 @@ def load_pvalue_cases() -> List[PvalueCase]:
             lambdas=[hexf(x) for x in c["lambdas"]], S=c["S"], R=c["R"], n_sim=c["n_sim"], seed=c["seed"],
             conditional=_hexes(c["conditional_hex"]), pvalues=np.array([hexf(x) for x in c["pvalue_hex"]])))
     return out
+
+
+@dataclass
+class SimulationCase:
+    name: str
+    tree: Tree
+    lambda_of_node: List[int]
+    lambda_kind: int
+    lambdas: List[float]
+    S: int
+    R: int
+    seed: int
+    roots: np.ndarray          # [n]
+    err: Optional["ErrorModel"]
+    alpha: Optional[float]
+    K: Optional[int]
+    lambda_used: np.ndarray    # [n]
+    sizes: np.ndarray          # [n][n_nodes], prefix order
+
+
+def load_simulation_cases() -> List[SimulationCase]:
+    out = []
+    for c in load_json("ref_simulations.json")["cases"]:
+        tree = parse_newick(c["newick"])
+        lam_idx, kind = [0] * tree.n_nodes, 0
+        if c["lambda_newick"]:
+            lam_idx = lambda_index_of_nodes(tree, parse_newick(c["lambda_newick"], lambda_tree=True))
+            kind = 1
+        out.append(SimulationCase(
+            name=c["name"], tree=tree, lambda_of_node=lam_idx, lambda_kind=kind,
+            lambdas=[hexf(x) for x in c["lambdas"]], S=c["S"], R=c["R"], seed=c["seed"],
+            roots=np.asarray(c["roots"], dtype=np.int32),
+            err=ErrorModel.parse(c["error_model"]) if c["error_model"] else None, alpha=c["alpha"], K=c["K"],
+            lambda_used=np.array([hexf(x) for x in c["lambda_hex"]]), sizes=_ints(c["sizes"])))
+    return out

@@ -267,3 +267,23 @@ def test_oracle_pvalues_match_reference(case):
                                seed=case.seed)
     assert np.array_equal(cd, case.conditional)
     assert np.array_equal(pv, case.pvalues)
+
+
+SIM_CASES = __import__("golden_cases").load_simulation_cases()
+
+
+@pytest.mark.parametrize("case", SIM_CASES, ids=[c.name for c in SIM_CASES])
+def test_oracle_simulation_matches_reference(case):
+    """The simulator action with the same seed and root sizes: every
+    simulated node size and the lambda of every family equal the compiled
+    reference's (simulator::simulate_processes)."""
+    ta = oracle.TreeArrays.from_tree(case.tree, case.lambda_of_node)
+    kw = {}
+    if case.K:
+        probs, mult = discrete_gamma(case.alpha, case.K)
+        kw = dict(multipliers=mult, cat_probs=probs)
+    if case.err is not None:
+        kw.update(err_rows=case.err.table(), err_max_count=len(case.err.rows))
+    sizes, lam = oracle.simulate(ta, case.lambdas, case.roots, S=case.S, R=case.R, seed=case.seed, **kw)
+    assert np.array_equal(sizes, case.sizes)
+    assert np.array_equal(lam, case.lambda_used)
