@@ -27,7 +27,7 @@ EXPORTS = [
     "cafe_score_device", "cafe_submit", "cafe_poll", "cafe_serving_stats", "cafe_profile_enable",
     "cafe_profile_read", "cafe_prune_fp64_noalloc", "cafe_optimize", "cafe_discrete_gamma",
     "cafe_nelder_mead", "cafe_score_batch", "cafe_score_batch_device", "cafe_serving_counters", "cafe_autotune",
-    "cafe_reconstruct", "cafe_branch_probabilities", "cafe_pvalues",
+    "cafe_reconstruct", "cafe_branch_probabilities", "cafe_pvalues", "cafe_simulate",
 ]
 OPT_LAMBDA, OPT_LAMBDA_ALPHA, OPT_LAMBDA_EPSILON, OPT_ALPHA = 0, 1, 2, 3
 
@@ -92,6 +92,11 @@ class PvaluesOut(C.Structure):
                 ("host_ms", C.c_double)]
 
 
+class Simulation(C.Structure):
+    _fields_ = [("n_families", C.c_int), ("root_sizes", C.c_void_p), ("seed", C.c_uint32), ("sizes", C.c_void_p),
+                ("lambdas", C.c_void_p)]
+
+
 _lib = None
 
 
@@ -145,6 +150,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
         "cafe_reconstruct": (i, [p, P(Request), P(Reconstruction)]),
         "cafe_branch_probabilities": (i, [p, P(Request), p, p]),
         "cafe_pvalues": (i, [p, P(Request), P(PvaluesOut)]),
+        "cafe_simulate": (i, [p, P(Request), P(Simulation)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -1756,6 +1756,86 @@ int reconstruct_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_rec
     return CAFE_OK;
 }
 
+// ---- host row sampling (p-values, simulation)
+
+// Prefix order (clade::apply_prefix_order, src/clade.cpp:275-291): a node,
+// then its children's subtrees in descendant order.
+std::vector<int> prefix_order(const TreeHost& T) {
+    std::vector<int> prefix, st{T.root};
+    while (!st.empty()) {
+        const int v = st.back();
+        st.pop_back();
+        prefix.push_back(v);
+        for (auto it = T.children[v].rbegin(); it != T.children[v].rend(); ++it) st.push_back(*it);
+    }
+    return prefix;
+}
+
+// Samples a child size from the parent's matrix row with the reference's
+// draws (matrix::select_random_y, src/matrix_cache.cpp:60-66:
+// std::discrete_distribution over the first S entries of the row; on a
+// saturated branch set_weighted_random_family_size, src/probability.cpp:
+// 458-468, first draws and discards a uniform size). The matrices are the
+// context cache's (built on the GPU), copied to the host; distributions are
+// built once per (matrix, parent size) instead of once per draw.
+struct HostSampler {
+    int msize = 0, S = 0, n = 0, n_ps = 0;
+    std::vector<std::vector<double>> mats;   // distinct matrices
+    std::vector<int> node_mi;                // [K][n] matrix of (category, node), -1 at the root
+    std::vector<char> saturated;             // [K][n]
+    std::vector<std::unique_ptr<std::discrete_distribution<int>>> dists;   // [matrix][parent size]
+
+    int draw(int k, int v, int ps, std::mt19937& eng) {
+        const size_t kv = (size_t)k * n + v;
+        if (saturated[kv]) {
+            std::uniform_int_distribution<int> d(0, S - 1);
+            d(eng);
+        }
+        std::unique_ptr<std::discrete_distribution<int>>& d = dists[(size_t)node_mi[kv] * n_ps + ps];
+        if (!d) {
+            const double* row = mats[node_mi[kv]].data() + (size_t)ps * msize;
+            d.reset(new std::discrete_distribution<int>(row, row + S));
+        }
+        return (*d)(eng);
+    }
+};
+
+// ws.h_mats holds the K x n matrix pointers recon_setup staged; parent sizes
+// reach max(R, S).
+int host_sampler_init(cafe_ctx* C, Workspace& ws, const cafe_request* R, const TreeHost& T, const ReconSetup& Z,
+                      int K, const double* multipliers, HostSampler* hs) {
+    const int n = T.n_nodes;
+    hs->msize = Z.msize;
+    hs->S = Z.Smax;
+    hs->n = n;
+    hs->n_ps = std::max(Z.Rmax, Z.Smax) + 1;
+    hs->node_mi.assign((size_t)K * n, -1);
+    hs->saturated.assign((size_t)K * n, 0);
+    const double* const* hm = ws.h_mats.as<const double*>();
+    std::map<const double*, int> ids;
+    for (int k = 0; k < K; ++k) {
+        const double mult = multipliers ? multipliers[k] : 1.0;
+        for (int v = 0; v < n; ++v) {
+            if (T.parent[v] < 0) continue;
+            const double* d = hm[(size_t)k * n + v];
+            auto ins = ids.emplace(d, (int)hs->mats.size());
+            if (ins.second) {
+                hs->mats.emplace_back((size_t)Z.msize * Z.msize);
+                CK(cudaMemcpyAsync(hs->mats.back().data(), d, hs->mats.back().size() * sizeof(double),
+                                   cudaMemcpyDeviceToHost, ws.stream),
+                   "d2h");
+            }
+            hs->node_mi[(size_t)k * n + v] = ins.first->second;
+            const double lam = R->lambdas[T.lambda_index[v]] * mult, t = T.branch_length[v];
+            hs->saturated[(size_t)k * n + v] = (1 - 2 * (lam * t / (1 + lam * t))) < 0;   // matrix_cache::is_saturated
+        }
+    }
+    CK(cudaStreamSynchronize(ws.stream), "matrices");
+    hs->dists.clear();
+    hs->dists.resize(hs->mats.size() * (size_t)hs->n_ps);
+    return CAFE_OK;
+}
+
 // ---- p-values
 
 // FP64 pruning of `fams` (rows of `counts`) through k_prune64 with the root
@@ -1824,44 +1904,12 @@ int pvalues_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_pvalues
     FamSet& FS = *Z.S;
     const int S = Z.Smax, RR = Z.Rmax, msize = Z.msize, nsim = out->n_simulations, n = T.n_nodes;
     const int64_t F = FS.F;
-    // matrices of the non-root nodes on the host (rows are sampled there)
-    const double* const* hm = ws.h_mats.as<const double*>();
-    std::map<const double*, std::vector<double>> host_mats;
-    for (int v = 0; v < n; ++v) {
-        if (T.parent[v] < 0 || host_mats.count(hm[v])) continue;
-        std::vector<double>& m = host_mats[hm[v]];
-        m.resize((size_t)msize * msize);
-        CK(cudaMemcpyAsync(m.data(), hm[v], m.size() * sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");
-    }
-    CK(cudaStreamSynchronize(ws.stream), "matrices");
+    HostSampler hs;
+    rc = host_sampler_init(C, ws, R, T, Z, 1, nullptr, &hs);
+    if (rc) return rc;
     host_ms += host_ms_since(t_host0);
     const auto t_sim = std::chrono::steady_clock::now();
-    // prefix order (clade::apply_prefix_order, src/clade.cpp:275-291)
-    std::vector<int> prefix;
-    {
-        std::vector<int> st{T.root};
-        while (!st.empty()) {
-            const int v = st.back();
-            st.pop_back();
-            prefix.push_back(v);
-            for (auto it = T.children[v].rbegin(); it != T.children[v].rend(); ++it) st.push_back(*it);
-        }
-    }
-    std::vector<char> saturated(n, 0);
-    std::vector<const double*> node_mat(n, nullptr);
-    std::vector<int> node_mi(n, -1);   // distinct matrix of each non-root node
-    std::map<const double*, int> mat_ids;
-    for (int v = 0; v < n; ++v) {
-        if (T.parent[v] < 0) continue;
-        node_mat[v] = host_mats[hm[v]].data();
-        node_mi[v] = mat_ids.emplace(hm[v], (int)mat_ids.size()).first->second;
-        const double lam = R->lambdas[T.lambda_index[v]], t = T.branch_length[v];
-        saturated[v] = (1 - 2 * (lam * t / (1 + lam * t))) < 0;   // matrix_cache::is_saturated
-    }
-    // one distribution per (matrix, parent size), built on first use; parent
-    // sizes are root sizes <= R or sampled sizes < S
-    const int n_ps = std::max(RR, S) + 1;
-    std::vector<std::unique_ptr<std::discrete_distribution<int>>> dists((size_t)mat_ids.size() * n_ps);
+    const std::vector<int> prefix = prefix_order(T);
     std::mt19937 engine(out->seed);
     const int64_t NS = (int64_t)RR * nsim;
     const int L = T.n_leaves;
@@ -1877,18 +1925,7 @@ int pvalues_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_pvalues
                 if (v == T.root) continue;
                 const int ps = sizes[T.parent[v]];
                 int c = 0;
-                if (ps > 0) {
-                    if (saturated[v]) {
-                        std::uniform_int_distribution<int> d(0, S - 1);
-                        c = d(engine);   // drawn and discarded, as the reference does
-                    }
-                    std::unique_ptr<std::discrete_distribution<int>>& d = dists[(size_t)node_mi[v] * n_ps + ps];
-                    if (!d) {
-                        const double* row = node_mat[v] + (size_t)ps * msize;
-                        d.reset(new std::discrete_distribution<int>(row, row + S));
-                    }
-                    c = (*d)(engine);
-                }
+                if (ps > 0) c = hs.draw(0, v, ps, engine);
                 sizes[v] = c;
                 mx = std::max(mx, c);
             }
@@ -1985,6 +2022,77 @@ int pvalues_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_pvalues
     host_ms += host_ms_since(t_pv);
     out->device_ms = ms;
     out->host_ms = host_ms;
+    return CAFE_OK;
+}
+
+// The simulator action (src/simulator.cpp:29-91) on the host sampler: per
+// family the gamma model draws its rate category
+// (gamma_model::get_simulation_lambda, src/gamma_core.cpp:91-95), then up
+// to 50 attempts (simulator::create_trial) fill the tree in prefix order
+// from the family's root size, leaves through the error model
+// (adjust_for_error_model, src/probability.cpp:478-500), until the family
+// exists at the root (gene_family::exists_at_root, src/gene_family.cpp:62-91).
+int simulate_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_simulation* io) {
+    AllocScope scope(ws.stream);
+    if (ws.staged) {
+        CK(cudaEventSynchronize(ws.ev_staged), "staging");
+        ws.staged = false;
+    }
+    if (!io || io->n_families < 0 || (io->n_families && (!io->root_sizes || !io->sizes)))
+        return fail(C, CAFE_ERR_INVALID, "bad simulation arguments");
+    if (R && R->use_error_model && (C->err_rows == 0 || C->err_ndev != 3))
+        return fail(C, CAFE_ERR_INVALID, "the simulation's error model needs deviations -1, 0, +1");
+    ReconSetup Z;
+    int rc = recon_setup(C, ws, R, true, &Z);
+    if (rc) return rc;
+    TreeHost& T = *Z.T;
+    const int n = T.n_nodes, K = Z.K;
+    HostSampler hs;
+    rc = host_sampler_init(C, ws, R, T, Z, K, Z.gamma ? R->multipliers : nullptr, &hs);
+    if (rc) return rc;
+    const std::vector<int> prefix = prefix_order(T);
+    std::vector<int> post(prefix.rbegin(), prefix.rend());
+    std::mt19937 engine(io->seed);
+    std::vector<int> z(n);
+    std::vector<char> reg(n);
+    const double* err = R->use_error_model ? C->err.data() : nullptr;
+    for (int f = 0; f < io->n_families; ++f) {
+        const int root = io->root_sizes[f];
+        if (root < 0 || root >= hs.n_ps) return fail(C, CAFE_ERR_INVALID, "root size %d outside 0..%d", root, hs.n_ps - 1);
+        int k = 0;
+        if (Z.gamma) {
+            std::discrete_distribution<int> pick(R->cat_probs, R->cat_probs + K);
+            k = pick(engine);
+        }
+        if (io->lambdas) io->lambdas[f] = R->lambdas[0] * (Z.gamma ? R->multipliers[k] : 1.0);
+        for (int attempt = 0; attempt < 50; ++attempt) {
+            z[T.root] = root;
+            for (int v : prefix) {
+                if (v == T.root) continue;
+                const int ps = z[T.parent[v]];
+                int c = ps > 0 ? hs.draw(k, v, ps, engine) : 0;
+                if (err && T.leaf_col[v] >= 0) {
+                    if (c >= C->err_rows)
+                        return fail(C, CAFE_ERR_INVALID,
+                                    "Trying to simulate leaf family size that was not included in error model");
+                    const double* p = err + (size_t)c * 3;
+                    std::uniform_real_distribution<double> u(0.0, 1.0);
+                    const double rnd = u(engine);
+                    if (rnd < p[0]) c--;
+                    else if (rnd > (1 - p[2])) c++;
+                }
+                z[v] = c;
+            }
+            std::fill(reg.begin(), reg.end(), 0);
+            for (int v : post)
+                if (T.leaf_col[v] >= 0 && z[v] > 0)
+                    for (int p = v; p >= 0 && !reg[p]; p = T.parent[p]) reg[p] = 1;
+            bool all = true;
+            for (int ch : T.children[T.root]) all &= reg[ch] != 0;
+            if (all) break;
+        }
+        std::memcpy(io->sizes + (size_t)f * n, z.data(), sizeof(int32_t) * n);
+    }
     return CAFE_OK;
 }
 
@@ -2331,6 +2439,13 @@ int cafe_pvalues(cafe_ctx* C, const cafe_request* req, cafe_pvalues_out* out) {
     std::lock_guard<std::mutex> lk(C->mu);
     cudaSetDevice(C->device);
     return pvalues_sync(C, *C->ws[0], req, out);
+}
+
+int cafe_simulate(cafe_ctx* C, const cafe_request* req, cafe_simulation* io) {
+    if (!C) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->mu);
+    cudaSetDevice(C->device);
+    return simulate_sync(C, *C->ws[0], req, io);
 }
 
 int cafe_branch_probabilities(cafe_ctx* C, const cafe_request* req, const int32_t* node_count, double* out) {

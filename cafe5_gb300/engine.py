@@ -285,6 +285,20 @@ class Context:
         return {"pvalues": pv, "conditional": cd, "root_likelihood": rl, "device_ms": out.device_ms,
                 "host_ms": out.host_ms}
 
+    def simulate(self, tree_id, set_id, lambdas, root_sizes, *, S: int, R: int, seed: int = 10, model=0,
+                 lambda_kind=0, multipliers=(1.0,), cat_probs=(1.0,), use_error_model=False):
+        """cafe_simulate (the simulator action): (sizes[n][n_nodes], lambda[n])."""
+        req, keep = self.make_request(tree_id, set_id, lambdas, model=model, lambda_kind=lambda_kind,
+                                      multipliers=multipliers, cat_probs=cat_probs, use_error_model=use_error_model,
+                                      S=S, R=R)
+        roots = np.ascontiguousarray(root_sizes, dtype=np.int32)
+        n_nodes = self._tree_nodes.get(tree_id, 0)
+        sizes = np.zeros((len(roots), n_nodes), np.int32)
+        lam = np.zeros(len(roots))
+        io = _lib.Simulation(len(roots), _p(roots), seed & 0xFFFFFFFF, _p(sizes), _p(lam))
+        self._check(self.lib.cafe_simulate(self.h, C.byref(req), C.byref(io)))
+        return sizes, lam
+
     def profile(self, enable: bool = True):
         self._check(self.lib.cafe_profile_enable(self.h, 1 if enable else 0))
 

@@ -394,6 +394,30 @@ typedef struct {
  * simulated likelihoods that do not exceed its own. */
 int cafe_pvalues(cafe_ctx* ctx, const cafe_request* req, cafe_pvalues_out* out);
 
+/* ---- simulation ------------------------------------------------------------ */
+
+typedef struct {
+    int n_families;              /* in */
+    const int32_t* root_sizes;   /* in [n_families]: root size of each family
+                                    (root_equilibrium_distribution::select_root_size) */
+    uint32_t seed;               /* in: seed of the std::mt19937 stream (randomizer_engine) */
+    int32_t* sizes;              /* host [n_families][n_nodes] out: every node's simulated size */
+    double* lambdas;             /* host [n_families] out, or NULL: the family's (first) lambda */
+} cafe_simulation;
+
+/* The simulator action (simulator::simulate_processes / create_trial,
+ * src/simulator.cpp:29-91) with LAMBDA_PERTURBATION_STEP_SIZE = 1: per
+ * family the gamma model draws a rate category from the category
+ * probabilities, then up to 50 attempts fill the tree in prefix order, each
+ * child size drawn from its parent's row of the transition matrix (states
+ * below max_family_size), leaves passed through the error model when
+ * use_error_model is set (deviations -1, 0, +1; a leaf size past the
+ * model's rows is CAFE_ERR_INVALID, where the reference throws), until every
+ * child of the root has a descendant leaf with a nonzero size. Matrices come
+ * from the context cache (built on the GPU); the draws run on the host in
+ * the reference's order, so a seed reproduces the reference's families. */
+int cafe_simulate(cafe_ctx* ctx, const cafe_request* req, cafe_simulation* io);
+
 #ifdef __cplusplus
 }
 #endif
