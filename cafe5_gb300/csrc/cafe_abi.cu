@@ -2330,13 +2330,18 @@ int cafe_families_update(cafe_ctx* C, int set_id, const int32_t* counts) {
     if (si == C->sets.end()) return fail(C, CAFE_ERR_NOT_FOUND, "unknown family set id %d", set_id);
     FamSet& S = *si->second;
     const size_t n = (size_t)S.F * S.n_leaves;
-    for (size_t i = 0; i < n; ++i)
-        if (counts[i] < 0) return fail(C, CAFE_ERR_INVALID, "negative count");
-    S.h_counts.assign(counts, counts + n);
+    if (!counts && n) return fail(C, CAFE_ERR_INVALID, "null counts");
+    // unchanged counts keep their derived tables (maxima, duplicates, bins)
+    const bool same = S.h_counts.size() == n && (n == 0 || std::memcmp(S.h_counts.data(), counts, n * sizeof(int32_t)) == 0);
+    if (!same) {
+        for (size_t i = 0; i < n; ++i)
+            if (counts[i] < 0) return fail(C, CAFE_ERR_INVALID, "negative count");
+        S.h_counts.assign(counts, counts + n);
+    }
     Workspace& ws = *C->ws[0];
     CK(cudaMemcpyAsync(S.d_counts.p, counts, n * sizeof(int32_t), cudaMemcpyHostToDevice, ws.stream), "counts");
     CK(cudaStreamSynchronize(ws.stream), "counts");
-    return prepare_set(C, S);
+    return same ? CAFE_OK : prepare_set(C, S);
 }
 
 int cafe_families_free(cafe_ctx* C, int set_id) {

@@ -116,7 +116,9 @@ int cafe_tree_upload(cafe_ctx* ctx, int n_nodes, const int32_t* parent, const do
  * counts[n_families][n_leaves], kept resident on the device. */
 int cafe_families_upload(cafe_ctx* ctx, int tree_id, const int32_t* counts, int64_t n_families, int n_leaves,
                          int* set_id);
-/* Replace the counts of an existing set in place (same shape). */
+/* Replace the counts of an existing set in place (same shape): always
+ * copied to the device; the derived tables (per-family maxima, duplicate
+ * rows, S-bins) are rebuilt only when the counts differ from the set's. */
 int cafe_families_update(cafe_ctx* ctx, int set_id, const int32_t* counts);
 int cafe_families_free(cafe_ctx* ctx, int set_id);
 

@@ -243,3 +243,38 @@ def test_graph_replay_matches_direct_launches(ctx):
         for g, d in zip(graph, direct):
             assert np.array_equal(g.family_lnl, d.family_lnl) and g.total == d.total
     ctx.free_families(sid)
+
+
+def test_families_update_rebuilds_derived_tables(ctx):
+    """cafe_families_update: new counts (a larger maximum moves families
+    into wider S-bins) score like a fresh upload; re-sending unchanged
+    counts leaves the results unchanged."""
+    from cafe5_gb300.families import global_bounds
+    from cafe5_gb300.inputs import RootPrior
+    from cafe5_gb300.synth import workload
+    w = workload(1, n_families=500, seed=31)
+    counts = w.families.counts.copy()
+    tid = ctx.upload_tree(w.tree)
+    sid = ctx.upload_families(tid, counts)
+    ctx.set_prior(RootPrior.uniform(400).vector())
+    ctx.set_error_model(None)
+    kw = dict(model=1, multipliers=w.multipliers, cat_probs=w.cat_probs, precision="fp64_binned")
+    a = ctx.score(tid, sid, [0.002], **kw)
+    ctx.update_families(sid, counts)                 # unchanged
+    b = ctx.score(tid, sid, [0.002], **kw)
+    assert np.array_equal(a.family_lnl, b.family_lnl)
+    bigger = counts.copy()
+    bigger[::7, 0] += 60                             # wider bins for every 7th family
+    ctx.update_families(sid, bigger)
+    c = ctx.score(tid, sid, [0.002], **kw)
+    sid2 = ctx.upload_families(tid, bigger)
+    d = ctx.score(tid, sid2, [0.002], **kw)
+    assert np.array_equal(c.family_lnl, d.family_lnl)
+    assert not np.array_equal(c.family_lnl, a.family_lnl)
+    for pr in ("fp64_ref",):
+        S, R = global_bounds(type(w.families)(w.families.ids, bigger))
+        e = ctx.score(tid, sid, [0.002], model=1, multipliers=w.multipliers, cat_probs=w.cat_probs,
+                      precision=pr, S=S, R=R)
+        f = ctx.score(tid, sid2, [0.002], model=1, multipliers=w.multipliers, cat_probs=w.cat_probs,
+                      precision=pr, S=S, R=R)
+        assert np.array_equal(e.family_lnl, f.family_lnl)
