@@ -46,7 +46,7 @@ constexpr int TF = 32;       // families per tile (one per lane)
 constexpr int NT = 256;      // threads: 8 warps
 constexpr int RW = 4;        // parent states per warp and block
 constexpr int RB = 8 * RW;   // parent states per block
-constexpr int JC = 32;       // child states per staged chunk
+constexpr int JC = 64;       // child states per staged chunk
 constexpr float kDelta = 0.00390625f;   // 2^-8, in log2 units
 
 // log2 of x >= 0 in FP32 (-inf for 0) from the bits of x, without FP64

@@ -3,7 +3,10 @@
  * Drop-in boundary for CAFE5's likelihood hot path: transition-matrix
  * construction (matrix_cache / probability.cpp) and Felsenstein pruning of
  * every gene family (inference_prune) as called by the base and gamma
- * models and, through them, by optimizer_scorer. Plain C types only.
+ * models and, through them, by optimizer_scorer and the Nelder-Mead search;
+ * and for the analyses built on the same matrices and walk: Pupko ancestral
+ * reconstruction and branch probabilities, p-values, and the simulator.
+ * Plain C types only.
  *
  * Every entry point returns a cafe_status. No call throws, and no pointer
  * handed back to the host aliases device memory. A context owns all
