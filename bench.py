@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--serving-clients", type=int, default=8)
     ap.add_argument("--serving-requests", type=int, default=12, help="requests per client")
+    ap.add_argument("--serving-optimizers", type=int, default=256,
+                    help="clients of the config-4 request stream (0: skip)")
     ap.add_argument("--no-reconstruct", dest="reconstruct", action="store_false",
                     help="skip the ancestral-reconstruction measurement")
     ap.add_argument("--no-pvalues", dest="pvalues", action="store_false",
@@ -303,6 +305,87 @@ def serving_phase(ctx, tid, sid, w, clients: int, per_client: int, kw):
             "note": "single-candidate requests from concurrent closed-loop optimizer clients, merged by the continuous-batching loop; latency submit -> done"}
 
 
+def serving_stream(ctx, n_optimizers: int = 256, requests_each: int = 4, think_ms: float = 1.0, seed: int = 4):
+    """The served request stream of the config-4 shape: n_optimizers
+    independent Nelder-Mead clients, each on its own data set (Yule tree of
+    8/16/32/64 taxa, root age 50-250; 100-100,000 families, log-uniform,
+    simulated as in config 0; lambda log-uniform in [5e-4, 1e-2]; K in
+    {1, 4, 8}), each submitting its next request an exponential think time
+    after its previous result (Poisson arrivals). Mixed precision; one event
+    loop drives every client through cafe_submit / cafe_poll. Reports
+    throughput, p50/p99 latency and dlnL against FP64 on a sample."""
+    from cafe5_gb300.families import FamilySet
+    from cafe5_gb300.inputs import RootPrior, discrete_gamma
+    from cafe5_gb300.synth import _keep_nonzero, _poisson_ge1, simulate_families, yule_tree
+    rng = np.random.default_rng(seed)
+    sizes = [100, 316, 1000, 3162, 10000, 31623, 100000]
+    trees = {}
+    for taxa in (8, 16, 32, 64):
+        tree = yule_tree(taxa, float(rng.uniform(50, 250)), seed + taxa)
+        root = _poisson_ge1(rng, 5.0, 130000)
+        c = _keep_nonzero(simulate_families(tree, len(root), np.full(len(root), 0.0025), root, seed + 7 * taxa))
+        tid = ctx.upload_tree(tree)
+        sets = {n: ctx.upload_families(tid, np.ascontiguousarray(c[:n])) for n in sizes}
+        trees[taxa] = (tid, sets, tree)
+    ctx.set_prior(RootPrior.uniform(1100).vector())
+    ctx.set_error_model(None)
+    opts = []
+    for i in range(n_optimizers):
+        taxa = int(rng.choice([8, 16, 32, 64]))
+        F = int(np.exp(rng.uniform(np.log(100), np.log(100000))))
+        n = min(sizes, key=lambda x: abs(np.log(x) - np.log(F)))
+        K = int(rng.choice([1, 4, 8]))
+        lam = float(np.exp(rng.uniform(np.log(5e-4), np.log(1e-2))))
+        kw = dict(precision="mixed_tf32x3")
+        if K > 1:
+            probs, mult = discrete_gamma(0.5, K)
+            kw.update(model=1, multipliers=mult, cat_probs=probs)
+        opts.append({"tid": trees[taxa][0], "sid": trees[taxa][1][n], "F": n, "lam": lam, "kw": kw, "left": requests_each,
+                     "step": 0, "h": None, "t_sub": 0.0, "next": 0.0})
+    lat, done_fam = [], 0
+    t0 = time.perf_counter()
+    for o in opts:
+        o["next"] = t0 + rng.exponential(think_ms) / 1e3
+    active = len(opts)
+    while active:
+        now = time.perf_counter()
+        for o in opts:
+            if o["h"] is None:
+                if o["left"] and now >= o["next"]:
+                    lam = o["lam"] * (1.0 + 1e-3 * o["step"])   # the optimizer's next candidate
+                    o["h"] = ctx.submit(o["tid"], o["sid"], [lam], **o["kw"])
+                    o["t_sub"] = now
+            else:
+                r = ctx.poll(o["h"], 0)
+                if r is not None:
+                    t = time.perf_counter()
+                    lat.append((t - o["t_sub"]) * 1e3)
+                    done_fam += o["F"]
+                    o["h"] = None
+                    o["left"] -= 1
+                    o["step"] += 1
+                    o["next"] = t + rng.exponential(think_ms) / 1e3
+                    if not o["left"]:
+                        active -= 1
+    wall = time.perf_counter() - t0
+    lat.sort()
+    pct = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]
+    # accuracy on a sample of the clients' data sets: mixed vs FP64 at the same bins
+    dl = 0.0
+    for o in opts[:: max(1, len(opts) // 16)]:
+        kw64 = dict(o["kw"], precision="fp64_binned")
+        a = ctx.score(o["tid"], o["sid"], [o["lam"]], **kw64)
+        b = ctx.score(o["tid"], o["sid"], [o["lam"]], **o["kw"])
+        fin = np.isfinite(a.family_lnl)
+        if fin.any():
+            dl = max(dl, float(np.max(np.abs(b.family_lnl[fin] - a.family_lnl[fin]) / np.abs(a.family_lnl[fin]))))
+    return {"optimizers": n_optimizers, "requests": len(lat), "evals_per_s": done_fam / wall,
+            "p50_ms": pct(0.5), "p99_ms": pct(0.99), "unit": "family-lnL evals/s", "max_rel_dlnl_vs_fp64": dl,
+            "note": "config-4 shape: trees of 8/16/32/64 taxa, 100-100,000 families per request (log-uniform), "
+                    "lambda log-uniform [5e-4, 1e-2], K in {1, 4, 8}; exponential think time "
+                    f"{think_ms} ms per client; latency submit -> result"}
+
+
 def reconstruction_phase(ctx, tid, sid, w, fams, S, R, cpu_seconds: float, reps: int = 3):
     """Pupko joint reconstruction of every family x gamma category at the
     reference's global bounds (cafe_reconstruct): the log2-filtered kernel,
@@ -515,6 +598,11 @@ def run_ours(args):
     if rank == 0 and args.serving_clients > 0:
         serving = serving_phase(ctx, tid, sid, w, args.serving_clients, args.serving_requests, kw)
 
+    stream4 = None
+    if rank == 0 and args.serving_optimizers > 0:
+        stream4 = serving_stream(ctx, args.serving_optimizers)
+        ctx.set_prior(prior)
+
     recon = None
     if rank == 0 and args.reconstruct:
         recon = reconstruction_phase(ctx, tid, sid, w, fams, S, R, args.cpu_seconds / 2)
@@ -574,6 +662,7 @@ def run_ours(args):
                 "e2e": {"value": e2e_value, "unit": "family-lnL evals/s",
                         "h2d_bytes_per_step": int(fams.counts.nbytes), "d2h_bytes_per_step": int(B * (F * 8 + 8))},
                 "serving": serving,
+                "serving_stream": stream4,
                 "reconstruction": recon,
                 "pvalues": pvals,
                 "gpu_launches": int(round(prof["launches"] / prof_steps * args.steps)),

@@ -1838,47 +1838,6 @@ int host_sampler_init(cafe_ctx* C, Workspace& ws, const cafe_request* R, const T
 
 // ---- p-values
 
-// FP64 pruning of `fams` (rows of `counts`) through k_prune64 with the root
-// vectors as output: families grouped into 32-family tiles of equal state
-// bound S_f and root range root_lo..root_lo + nroot - 1, unscaled FP64 (the
-// reference's arithmetic), out[f * root_ld + j].
-int prune_root_vectors(cafe_ctx* C, Workspace& ws, TreeHost& T, const int32_t* d_counts, const int64_t* d_perm,
-                       const std::vector<PruneTile>& tiles, int msize, int W, double* d_out, int root_ld) {
-    const int n_tiles = (int)tiles.size();
-    if (!n_tiles) return CAFE_OK;
-    CK(ws.h_tiles.reserve(n_tiles * sizeof(PruneTile)), "tiles");
-    CK(ws.tiles.reserve(n_tiles * sizeof(PruneTile)), "tiles");
-    std::memcpy(ws.h_tiles.p, tiles.data(), n_tiles * sizeof(PruneTile));
-    CK(cudaMemcpyAsync(ws.tiles.p, ws.h_tiles.p, n_tiles * sizeof(PruneTile), cudaMemcpyHostToDevice, ws.stream),
-       "tiles");
-    const int n_ctas = std::max(1, std::min(n_tiles, C->n_ctas));
-    const int64_t per_cta = (int64_t)T.n_slots * W * 32;
-    CK(ws.scratch.reserve((size_t)n_ctas * per_cta * sizeof(double)), "scratch");
-    Prune64Args a{};
-    a.plan = T.plan;
-    a.tiles = ws.tiles.as<PruneTile>();
-    a.n_tiles = n_tiles;
-    a.counts = d_counts;
-    a.perm = d_perm;
-    a.mats = ws.mats.as<const double*>();
-    a.ld_mat = msize;
-    a.prior = C->d_prior.p ? C->d_prior.as<double>() : nullptr;
-    a.n_prior = 0;
-    a.scratch = ws.scratch.as<double>();
-    a.scratch_per_cta = per_cta;
-    a.scaled = 0;
-    a.model = 0;
-    a.K = 1;
-    a.tile_families = 32;
-    a.W = W;
-    a.root_out = d_out;
-    a.root_ld = root_ld;
-    CK(launch_prune64(a, n_ctas, ws.stream), "prune root vectors");
-    // the tile staging buffers are rewritten by the next call
-    CK(cudaStreamSynchronize(ws.stream), "prune root vectors");
-    return CAFE_OK;
-}
-
 // compute_pvalues (src/probability.cpp:376-570). The simulation runs on the
 // host because its random stream is the reference's: one std::mt19937
 // seeded by the caller, drawing in the reference's order (create_family,
@@ -1913,69 +1872,54 @@ int pvalues_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_pvalues
     std::mt19937 engine(out->seed);
     const int64_t NS = (int64_t)RR * nsim;
     const int L = T.n_leaves;
-    std::vector<int32_t> sim_counts((size_t)NS * L);
-    std::vector<int32_t> sim_m(NS);
-    std::vector<int> sizes(n);
-    for (int i = 0; i < RR; ++i)
-        for (int k = 0; k < nsim; ++k) {
-            const int64_t fi = (int64_t)i * nsim + k;
-            sizes[T.root] = i + 1;
-            int mx = i + 1;
-            for (int v : prefix) {
-                if (v == T.root) continue;
-                const int ps = sizes[T.parent[v]];
-                int c = 0;
-                if (ps > 0) c = hs.draw(0, v, ps, engine);
-                sizes[v] = c;
-                mx = std::max(mx, c);
-            }
-            for (int v = 0; v < n; ++v)
-                if (T.leaf_col[v] >= 0) sim_counts[(size_t)fi * L + T.leaf_col[v]] = sizes[v];
-            sim_m[fi] = std::min(S, mx + std::max(50, mx / 5));   // compute_family_probabilities bound
-        }
-    // tiles: simulated families grouped by (root size, bound)
-    std::vector<int64_t> perm(NS);
-    std::iota(perm.begin(), perm.end(), 0);
-    std::stable_sort(perm.begin(), perm.end(), [&](int64_t a, int64_t b) {
-        const int ra = (int)(a / nsim), rb = (int)(b / nsim);
-        return ra != rb ? ra < rb : sim_m[a] < sim_m[b];
-    });
-    std::vector<PruneTile> tiles;
-    int Wsim = 1;
-    for (int64_t i = 0; i < NS;) {
-        const int64_t f0 = perm[i];
-        const int r = (int)(f0 / nsim), m = sim_m[f0];
-        int64_t j = i;
-        while (j < NS && j - i < 32 && perm[j] / nsim == r && sim_m[perm[j]] == m) ++j;
-        PruneTile t{};
-        t.first = (int)i;
-        t.count = (int)(j - i);
-        t.k = 0;
-        t.S = m;
-        t.R = 1;
-        t.root_lo = r + 1;
-        tiles.push_back(t);
-        Wsim = std::max(Wsim, m + 1);
-        i = j;
-    }
-    host_ms += host_ms_since(t_sim);
-    CK(cudaEventRecord(ws.ev_start, ws.stream), "event");
-    // device buffers: simulated counts, their order, the root values
-    DevBuf d_sim, d_perm, d_simL, d_obsL, d_obs_perm;
-    CK(d_sim.reserve(std::max<size_t>(sim_counts.size(), 1) * sizeof(int32_t)), "simulated families");
-    CK(d_perm.reserve(std::max<size_t>(perm.size(), 1) * sizeof(int64_t)), "simulated families");
+    // device buffers: simulated counts, their order, tiles, the root values
+    const int Wmax = std::max(S + 1, RR);
+    const int64_t max_tiles = NS / 32 + (int64_t)RR * (S + 2) + F / 32 + 2;
+    DevBuf d_sim, d_perm, d_simL, d_obsL, d_tiles;
+    CK(d_sim.reserve(std::max<size_t>((size_t)NS * L, 1) * sizeof(int32_t)), "simulated families");
+    CK(d_perm.reserve(std::max<int64_t>(NS, 1) * sizeof(int64_t)), "simulated families");
     CK(d_simL.reserve(std::max<int64_t>(NS, 1) * sizeof(double)), "simulated likelihoods");
     CK(d_obsL.reserve(std::max<int64_t>(F * RR, 1) * sizeof(double)), "root vectors");
-    CK(cudaMemcpyAsync(d_sim.p, sim_counts.data(), sim_counts.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
-                       ws.stream),
-       "h2d");
-    CK(cudaMemcpyAsync(d_perm.p, perm.data(), perm.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ws.stream),
-       "h2d");
-    rc = prune_root_vectors(C, ws, T, d_sim.as<int32_t>(), d_perm.as<int64_t>(), tiles, msize, Wsim,
-                            d_simL.as<double>(), 1);
-    if (rc) return rc;
-    // observed families: states 0..S, root sizes 1..R
-    tiles.clear();
+    CK(d_tiles.reserve((size_t)max_tiles * sizeof(PruneTile)), "tiles");
+    const int n_ctas_max = C->n_ctas;
+    const int64_t per_cta = (int64_t)T.n_slots * Wmax * 32;
+    CK(ws.scratch.reserve((size_t)n_ctas_max * per_cta * sizeof(double)), "scratch");
+    // host staging in pinned memory, so the copies stay asynchronous
+    CK(ws.h_tiles.reserve((size_t)max_tiles * sizeof(PruneTile)), "tiles");
+    CK(ws.h_sim.reserve(std::max<size_t>((size_t)NS * L, 1) * sizeof(int32_t)), "simulated families");
+    CK(ws.h_simperm.reserve(std::max<int64_t>(NS, 1) * sizeof(int64_t)), "simulated families");
+    PruneTile* tiles = ws.h_tiles.as<PruneTile>();
+    size_t n_tiles = 0;
+    // k_prune64 with the root vectors as output over tiles[t0, t1), on the
+    // stream (the host goes on simulating meanwhile)
+    auto launch_tiles = [&](size_t t0, size_t t1, const int32_t* counts, const int64_t* perm, int W, double* d_out,
+                            int root_ld) -> int {
+        const int n_t = (int)(t1 - t0);
+        if (n_t <= 0) return CAFE_OK;
+        CK(cudaMemcpyAsync(d_tiles.as<PruneTile>() + t0, tiles + t0, n_t * sizeof(PruneTile),
+                           cudaMemcpyHostToDevice, ws.stream),
+           "tiles");
+        Prune64Args a{};
+        a.plan = T.plan;
+        a.tiles = d_tiles.as<PruneTile>() + t0;
+        a.n_tiles = n_t;
+        a.counts = counts;
+        a.perm = perm;
+        a.mats = ws.mats.as<const double*>();
+        a.ld_mat = msize;
+        a.scratch = ws.scratch.as<double>();
+        a.scratch_per_cta = (int64_t)T.n_slots * W * 32;
+        a.K = 1;
+        a.tile_families = 32;
+        a.W = W;
+        a.root_out = d_out;
+        a.root_ld = root_ld;
+        CK(launch_prune64(a, std::max(1, std::min(n_t, n_ctas_max)), ws.stream), "prune root vectors");
+        return CAFE_OK;
+    };
+    host_ms += host_ms_since(t_sim);
+    CK(cudaEventRecord(ws.ev_start, ws.stream), "event");
+    // observed families first: states 0..S, root sizes 1..R
     for (int64_t f = 0; f < F; f += 32) {
         PruneTile t{};
         t.first = (int)f;
@@ -1983,11 +1927,72 @@ int pvalues_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_pvalues
         t.S = S;
         t.R = RR;
         t.root_lo = 1;
-        tiles.push_back(t);
+        tiles[n_tiles++] = t;
     }
-    rc = prune_root_vectors(C, ws, T, FS.d_counts.as<int32_t>(), FS.d_identity.as<int64_t>(), tiles, msize,
-                            std::max(S + 1, RR), d_obsL.as<double>(), RR);
+    rc = launch_tiles(0, n_tiles, FS.d_counts.as<int32_t>(), FS.d_identity.as<int64_t>(), Wmax,
+                      d_obsL.as<double>(), RR);
     if (rc) return rc;
+    // simulated families, a group of root sizes at a time: the device prunes
+    // a group while the host draws the next
+    const auto t_sim2 = std::chrono::steady_clock::now();
+    int32_t* sim_counts = ws.h_sim.as<int32_t>();
+    int64_t* perm = ws.h_simperm.as<int64_t>();
+    std::vector<int32_t> sim_m(NS);
+    std::vector<int> sizes(n);
+    const int group = std::max(1, (RR + 7) / 8);
+    for (int g0 = 0; g0 < RR; g0 += group) {
+        const int g1 = std::min(RR, g0 + group);
+        for (int i = g0; i < g1; ++i)
+            for (int k = 0; k < nsim; ++k) {
+                const int64_t fi = (int64_t)i * nsim + k;
+                sizes[T.root] = i + 1;
+                int mx = i + 1;
+                for (int v : prefix) {
+                    if (v == T.root) continue;
+                    const int ps = sizes[T.parent[v]];
+                    int c = 0;
+                    if (ps > 0) c = hs.draw(0, v, ps, engine);
+                    sizes[v] = c;
+                    mx = std::max(mx, c);
+                }
+                for (int v = 0; v < n; ++v)
+                    if (T.leaf_col[v] >= 0) sim_counts[(size_t)fi * L + T.leaf_col[v]] = sizes[v];
+                sim_m[fi] = std::min(S, mx + std::max(50, mx / 5));   // compute_family_probabilities bound
+            }
+        // tiles of the group: families grouped by (root size, bound)
+        const int64_t a0 = (int64_t)g0 * nsim, a1 = (int64_t)g1 * nsim;
+        std::iota(perm + a0, perm + a1, a0);
+        std::stable_sort(perm + a0, perm + a1, [&](int64_t a, int64_t b) {
+            const int ra = (int)(a / nsim), rb = (int)(b / nsim);
+            return ra != rb ? ra < rb : sim_m[a] < sim_m[b];
+        });
+        const size_t t0 = n_tiles;
+        int Wg = 1;
+        for (int64_t i = a0; i < a1;) {
+            const int64_t f0 = perm[i];
+            const int r = (int)(f0 / nsim), m = sim_m[f0];
+            int64_t j = i;
+            while (j < a1 && j - i < 32 && perm[j] / nsim == r && sim_m[perm[j]] == m) ++j;
+            PruneTile t{};
+            t.first = (int)i;
+            t.count = (int)(j - i);
+            t.S = m;
+            t.R = 1;
+            t.root_lo = r + 1;
+            tiles[n_tiles++] = t;
+            Wg = std::max(Wg, m + 1);
+            i = j;
+        }
+        CK(cudaMemcpyAsync(d_sim.as<int32_t>() + (size_t)a0 * L, sim_counts + (size_t)a0 * L,
+                           (size_t)(a1 - a0) * L * sizeof(int32_t), cudaMemcpyHostToDevice, ws.stream),
+           "h2d");
+        CK(cudaMemcpyAsync(d_perm.as<int64_t>() + a0, perm + a0, (size_t)(a1 - a0) * sizeof(int64_t),
+                           cudaMemcpyHostToDevice, ws.stream),
+           "h2d");
+        rc = launch_tiles(t0, n_tiles, d_sim.as<int32_t>(), d_perm.as<int64_t>(), Wg, d_simL.as<double>(), 1);
+        if (rc) return rc;
+    }
+    host_ms += host_ms_since(t_sim2);
     CK(cudaEventRecord(ws.ev_stop, ws.stream), "event");
     std::vector<double> simL(NS), obsL((size_t)F * RR);
     CK(cudaMemcpyAsync(simL.data(), d_simL.p, NS * sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");

@@ -192,8 +192,15 @@ __global__ void __launch_bounds__(NT, 4) k_pupko(PupkoArgs a) {
                         const int jn = min(JC, n - j0);
                         for (int jj = 0; jj < jn; ++jj) {
                             const float lu = s.lu[jj][lane];
-                            const float4 lm4 = *reinterpret_cast<const float4*>(&s.lm[jj][warp * RW]);
-                            const float lm[RW] = {lm4.x, lm4.y, lm4.z, lm4.w};
+                            float lm[RW];
+#pragma unroll
+                            for (int q = 0; q < RW / 4; ++q) {
+                                const float4 lm4 = *reinterpret_cast<const float4*>(&s.lm[jj][warp * RW + 4 * q]);
+                                lm[4 * q + 0] = lm4.x;
+                                lm[4 * q + 1] = lm4.y;
+                                lm[4 * q + 2] = lm4.z;
+                                lm[4 * q + 3] = lm4.w;
+                            }
 #pragma unroll
                             for (int r = 0; r < RW; ++r) {
                                 const float p = lu + lm[r];

@@ -156,6 +156,7 @@ struct Workspace {
     PinnedBuf h_conv, h_mi, h_flags, h_tiles64, h_tiles_fb, h_tail, h_catids;
     // reconstruction
     DevBuf rc_c, rc_state, rc_rmax, rc_mean, rc_count, rc_nfail, rc_parent, rc_bp, rc_lm, rc_lptr;
+    PinnedBuf h_sim, h_simperm;        // p-values: simulated families staged for the device
     std::vector<PruneTile> tile_vec;
     std::vector<MatEntry*> entry_vec;   // cache entry of every (combined category, node)
     // CUDA graphs of the pruning phase: stream ops go through an op log;
