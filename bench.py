@@ -369,7 +369,30 @@ def serving_stream(ctx, n_optimizers: int = 256, requests_each: int = 4, think_m
                         active -= 1
     wall = time.perf_counter() - t0
     lat.sort()
-    pct = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]
+    pct = lambda q, v=lat: v[min(len(v) - 1, int(round(q * (len(v) - 1))))]
+    # open loop: requests of the same clients arriving as a Poisson process
+    # at 60 % of the closed loop's request rate; latency under that load
+    rate = 0.6 * len(lat) / wall
+    n_open = min(600, 4 * len(opts))
+    gaps = rng.exponential(1.0 / rate, n_open)
+    pend, lat_open = [], []
+    t1 = time.perf_counter()
+    due = t1 + np.cumsum(gaps)
+    i = 0
+    while i < n_open or pend:
+        now = time.perf_counter()
+        while i < n_open and now >= due[i]:
+            o = opts[int(rng.integers(len(opts)))]
+            pend.append((ctx.submit(o["tid"], o["sid"], [o["lam"] * (1.0 + 1e-3 * (100 + i))], **o["kw"]), now))
+            i += 1
+        keep = []
+        for h, ts in pend:
+            if ctx.poll(h, 0) is not None:
+                lat_open.append((time.perf_counter() - ts) * 1e3)
+            else:
+                keep.append((h, ts))
+        pend = keep
+    lat_open.sort()
     # accuracy on a sample of the clients' data sets: mixed vs FP64 at the same bins
     dl = 0.0
     for o in opts[:: max(1, len(opts) // 16)]:
@@ -381,9 +404,13 @@ def serving_stream(ctx, n_optimizers: int = 256, requests_each: int = 4, think_m
             dl = max(dl, float(np.max(np.abs(b.family_lnl[fin] - a.family_lnl[fin]) / np.abs(a.family_lnl[fin]))))
     return {"optimizers": n_optimizers, "requests": len(lat), "evals_per_s": done_fam / wall,
             "p50_ms": pct(0.5), "p99_ms": pct(0.99), "unit": "family-lnL evals/s", "max_rel_dlnl_vs_fp64": dl,
+            "open_loop": {"requests": len(lat_open), "arrivals_per_s": rate, "p50_ms": pct(0.5, lat_open),
+                          "p99_ms": pct(0.99, lat_open)},
             "note": "config-4 shape: trees of 8/16/32/64 taxa, 100-100,000 families per request (log-uniform), "
-                    "lambda log-uniform [5e-4, 1e-2], K in {1, 4, 8}; exponential think time "
-                    f"{think_ms} ms per client; latency submit -> result"}
+                    "lambda log-uniform [5e-4, 1e-2], K in {1, 4, 8}. Closed loop: every client waits for its "
+                    f"result, then an exponential think time ({think_ms} ms), so latency includes the queue of "
+                    "all clients; open loop: Poisson arrivals at 60 % of the closed loop's rate. Latency "
+                    "submit -> result"}
 
 
 def reconstruction_phase(ctx, tid, sid, w, fams, S, R, cpu_seconds: float, reps: int = 3):

@@ -866,7 +866,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
                 e->conv = (int)jobs.size();
                 jobs.push_back(ConvertJob{e->d, msize, e->conv});
             }
-            mat_index[(size_t)k * T.n_nodes + v] = e->conv;
+            mat_index[(size_t)k * T.n_nodes + v] = e->conv | (ws.sat_vec[(size_t)k * T.n_nodes + v] ? (1 << 30) : 0);
         }
     const int n_mat = (int)jobs.size();
 
@@ -990,6 +990,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         a.fam_R = B.d_famR.as<int32_t>();
         a.out = ws.cat.as<double>();
         a.K = K;
+        a.model = gamma ? 1 : 0;
         a.cat_probs = ws.catp.as<double>();
         a.flags = d_flags;
         a.status = d_status;
@@ -1145,6 +1146,20 @@ int enqueue_mixed_graph(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeH
         ws.op_mode = Workspace::kOpRun;
         return enqueue_mixed(C, ws, R, T, S, K, CT, active, hm, d_fam, d_total, info);
     };
+    // capture into a free slot at once; evict a cached graph only for a
+    // signature seen before (FNV-1a over the op record), so a stream of
+    // one-off requests does not pay a capture each
+    uint64_t h = 1469598103934665603ull;
+    for (uint8_t b : sig) h = (h ^ b) * 1099511628211ull;
+    h |= 1;
+    bool seen = false, free_slot = false;
+    for (uint64_t x : ws.seen) seen |= (x == h);
+    for (const auto& g : ws.graphs) free_slot |= g.exec == nullptr;
+    if (!seen && !free_slot) {
+        ws.seen[ws.seen_next] = h;
+        ws.seen_next = (ws.seen_next + 1) % (int)(sizeof(ws.seen) / sizeof(ws.seen[0]));
+        return issue_directly();
+    }
     if (cudaStreamBeginCapture(ws.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return issue_directly();
     ws.op_mode = Workspace::kOpCapture;
     rc = enqueue_mixed(C, ws, R, T, S, K, CT, active, hm, d_fam, d_total, info);
@@ -1287,6 +1302,7 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     std::vector<MatEntry*>& node_entry = ws.entry_vec;
     node_entry.assign((size_t)CT * T.n_nodes, nullptr);
     bool any_saturated = false;   // a key with 1 - 2a outside (0, 1): zero rows
+    ws.sat_vec.assign((size_t)CT * T.n_nodes, 0);
     for (int c : active) {
         const cafe_request& Q = Rs[c / K];
         const double m = gamma ? Q.multipliers[c % K] : 1.0;
@@ -1297,7 +1313,10 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
             node_entry[(size_t)c * T.n_nodes + v] = schedule(C, P, key);
             const double lq = (double)key.lq / 1000000000.0, tq = (double)key.tq / 1000.0;
             const double al = lq * tq / (1 + lq * tq), co = 1 - 2 * al;
-            if (!(co > 0 && co != 1)) any_saturated = true;
+            if (!(co > 0 && co != 1)) {
+                any_saturated = true;
+                ws.sat_vec[(size_t)c * T.n_nodes + v] = 1;
+            }
         }
     }
     int rc = cache_build(C, ws, P);
@@ -1322,7 +1341,10 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     CK(ws.cat.reserve((size_t)std::max<int64_t>(F, 1) * CT * sizeof(double)), "category buffer");
     if (R->precision == CAFE_PREC_MIXED_TF32X3) {
         // saturated keys (1 - 2a < 0) and polytomies stay on the FP64 path
-        const bool to_fp64 = T.max_children > 2 || any_saturated;
+        // polytomies stay on the FP64 path; saturated keys run on the tensor
+        // cores (a family that is exactly zero through one ends there)
+        const bool to_fp64 = T.max_children > 2;
+        (void)any_saturated;
         if (!to_fp64) {
             CK(ws.catids.reserve(active.size() * sizeof(int32_t)), "categories");
             CK(ws.h_catids.reserve(active.size() * sizeof(int32_t)), "categories");

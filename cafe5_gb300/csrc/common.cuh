@@ -139,7 +139,8 @@ struct PruneTcArgs {
     int n_tiles;
     const int32_t* counts;
     const int64_t* perm;
-    const int32_t* mat_index;    // [K][n_nodes] converted-matrix index (-1 for the root)
+    const int32_t* mat_index;    // [K][n_nodes] converted-matrix index (-1 for the root); bit 30 set
+                                 // when the key is saturated
     int Wm;                      // pitch of matrices and node vectors (elements)
     float* vec_hi;               // node vectors, rows = CTA x slot x 128 families
     float* vec_lo;
@@ -152,6 +153,7 @@ struct PruneTcArgs {
     const int32_t* fam_R;
     double* out;                 // [F][K] natural log of each category term
     int K;
+    int model;                   // 0 base (a zero family is -inf), 1 gamma (a zero family is NaN: failed)
     const double* cat_probs;
     int32_t* flags;              // [F] set when a family must be recomputed in FP64
     int32_t* status;             // [1] nonzero when a bounded wait gave up

@@ -101,9 +101,13 @@ struct NodeInfo {
     int slot;
     int nch;
     int is_root;
-    int pad;
+    int sat;        // a child's matrix is saturated (rows s >= 1 all zero)
     ChildInfo c[2];
 };
+
+// Matrix indices carry this bit when the key is saturated (1 - 2a outside
+// (0, 1)): such a matrix is delta(s, 0) in row 0 and zero elsewhere.
+constexpr int32_t kSatBit = 1 << 30;
 
 // Per-child source of the factor: TMEM columns, or the unit factor of an
 // absent second child.
@@ -247,6 +251,7 @@ __device__ __forceinline__ void epi_scan(const NodeSrc<NC>& ns, int W, bool is_r
             for (int j = 0; j < CW; ++j) {
                 const int s = col0 + j;
                 if (s >= 1 && s <= Rf) {
+                    maxp = fmaxf(maxp, p[j]);
                     const float q = prior_f[s - 1];
                     const float v = p[j] * q;
                     if (v > best_f) {
@@ -393,6 +398,7 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
         const int32_t* mi = a.mat_index + (size_t)k * P.n_nodes;
         const uint32_t idesc = tc::idesc_tf32(TM, W);
         bool flag = false;
+        bool dead = false;   // an exact zero vector through a saturated branch: the family's term is 0
 
         // the tile's walk: children, matrices and slots of every internal node
         for (int ii = tid; ii < P.n_internal; ii += NTHREADS) {
@@ -401,14 +407,15 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             e.slot = P.slot[v];
             e.is_root = v == P.root;
             e.nch = P.cstart[ii + 1] - P.cstart[ii];
-            e.pad = 0;
+            e.sat = 0;
             for (int c = 0; c < 2; ++c) {
                 ChildInfo ci{0, -1, 0, c};
                 if (c < e.nch) {
                     const int ch = P.child[P.cstart[ii] + c];
                     ci.slot = P.slot[ch];
                     ci.leaf_col = P.leaf_col[ch];
-                    ci.mat = mi[ch];
+                    ci.mat = mi[ch] & ~kSatBit;
+                    e.sat |= (mi[ch] & kSatBit) != 0;
                 }
                 e.c[c] = ci;
             }
@@ -582,6 +589,13 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             bool nflag = ns2.flag;
             float maxp, bf, bp, bq;
             epi_scan<2>(ns2, W, is_root, Rf, prior_f, scl, maxp, bf, bp, bq);
+            // Without an error model, every state-0 entry is exact: row 0 of
+            // every matrix is delta(s, 0), so L[0] is 1 (scaled by a power of
+            // two) when all leaves below are 0, else 0, and it is then the
+            // vector's largest entry. A saturated child's factor is zero at
+            // every state s >= 1, so a product that is zero everywhere here
+            // is exactly zero in FP64 as well: the family's term is 0.
+            if (nd.sat && !a.err && !(maxp > 0.0f)) dead = true;
             const bool need = is_root ? !(bf > 0.0f) : !(maxp >= 0x1p-120f);
             if (!is_root && !need && maxp < 0x1p-32f) {
                 // bring this row's maximum back to [0.5, 1)
@@ -615,7 +629,7 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                 }
             }
             long long t2 = timing ? clock64() : 0;
-            flag |= nflag;
+            flag |= nflag && !dead;
             if (!is_root) {
                 float* stg_hi = reinterpret_cast<float*>(smem);               // stage 0 as staging tile
                 float* stg_lo = stg_hi + TM * SC;
@@ -624,7 +638,8 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             } else if (fam >= 0) {
                 double o = NAN;
                 const double best = (double)bp * (double)bq;
-                if (best > 0.0 && !flag)
+                if (dead) o = a.model == 0 ? -INFINITY : NAN;   // log 0 (base) / a failed family (gamma)
+                else if (best > 0.0 && !flag)
                     o = log(best * a.cat_probs[k]) + (double)E * 0.69314718055994530942;
                 else flag = true;
                 a.out[(size_t)fam * a.K + k] = o;

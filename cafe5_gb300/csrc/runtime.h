@@ -159,6 +159,7 @@ struct Workspace {
     PinnedBuf h_sim, h_simperm;        // p-values: simulated families staged for the device
     std::vector<PruneTile> tile_vec;
     std::vector<MatEntry*> entry_vec;   // cache entry of every (combined category, node)
+    std::vector<uint8_t> sat_vec;       // its key is saturated (1 - 2a outside (0, 1))
     // CUDA graphs of the pruning phase: stream ops go through an op log;
     // a dry pass records their parameters as the graph's signature
     enum OpMode { kOpRun = 0, kOpDry = 1, kOpCapture = 2 };
@@ -168,8 +169,12 @@ struct Workspace {
         std::vector<uint8_t> sig;
         cudaGraphExec_t exec = nullptr;
         uint64_t used = 0;
-    } graphs[4];
+    } graphs[16];
     uint64_t graph_clock = 0;
+    // hashes of recently issued signatures: once every slot holds a graph,
+    // a phase is captured only when its signature comes back
+    uint64_t seen[64] = {};
+    int seen_next = 0;
     ~Workspace();
     int init(int device);
 };

@@ -261,12 +261,60 @@ def test_mixed_polytomy_and_underflow_cases(ctx):
         _check_mixed(a, b)
 
 
+def _check_saturated(a, b):
+    """Saturated keys: the same families end (-inf / NaN) on both paths,
+    the rest agree to MIXED_REL."""
+    fa, fb = a.family_lnl, b.family_lnl
+    assert np.array_equal(np.isnan(fa), np.isnan(fb))
+    assert np.array_equal(np.isneginf(fa), np.isneginf(fb))
+    fin = np.isfinite(fa)
+    assert np.array_equal(fin, np.isfinite(fb))
+    if fin.any():
+        assert np.max(np.abs(fb[fin] - fa[fin]) / np.abs(fa[fin])) <= MIXED_REL
+    assert (a.total == b.total) if not math.isfinite(a.total) else abs(b.total - a.total) <= MIXED_REL * abs(a.total)
+
+
 def test_mixed_saturated_category_matches_fp64(ctx):
-    """The largest K=8 category saturates: the request runs on the FP64 path
-    and both agree on +inf."""
+    """The largest K=8 category saturates (can_infer tests the raw lambda
+    only, so the reference scores it): on the tensor cores a family that is
+    exactly zero through a saturated branch ends there; both paths agree on
+    every family and on +inf."""
     case = [c for c in CASES if c.name == "syn_gamma_24taxa_k8_small_cat"][0]
     a, b = _both(ctx, case.tree, case.counts, case.lambdas, model=1, mult=case.multipliers, probs=case.cat_probs)
     assert a.total == b.total == math.inf
+    _check_saturated(a, b)
+
+
+@pytest.mark.parametrize("lam,err", [(0.01, False), (0.004, False), (0.01, True)])
+def test_mixed_saturated_branches_base_model(ctx, lam, err):
+    """Base model with lambda * t > 1 on the long branches of a 8-taxon tree
+    (root age 224): families with a nonzero count under a saturated branch
+    have lnL = -inf, the others stay finite; with the error model the zero
+    test does not apply and the tensor-core pass sends such families to
+    FP64."""
+    from cafe5_gb300.inputs import ErrorModel
+    from cafe5_gb300.synth import _keep_nonzero, _poisson_ge1, simulate_families, yule_tree
+    rng = np.random.default_rng(4)
+    tree = yule_tree(8, 224.4, 12)
+    root = _poisson_ge1(rng, 5.0, 3000)
+    c = _keep_nonzero(simulate_families(tree, len(root), np.full(len(root), 0.0025), root, 40))[:2000]
+    em = ErrorModel.symmetric(0.05, 200).table() if err else None
+    a, b = _both(ctx, tree, c, [lam], err=em)
+    _check_saturated(a, b)
+    if lam == 0.01 and not err:
+        assert np.isneginf(a.family_lnl).any()
+
+
+def test_mixed_saturated_gamma_many_families_stays_on_tensor_cores(ctx):
+    """A saturated category on 20,000 families: the per-family FP64
+    recompute covers only families that are not exactly zero."""
+    from cafe5_gb300.synth import workload
+    w = workload(1, n_families=20000, seed=9)
+    from cafe5_gb300.inputs import discrete_gamma
+    probs, mult = discrete_gamma(0.5, 8)
+    a, b = _both(ctx, w.tree, w.families.counts, [0.006], model=1, mult=mult, probs=probs)
+    _check_saturated(a, b)
+    assert b.n_fallback < w.families.n_families // 2
 
 
 def test_mixed_wide_bins_hybrid(ctx):
