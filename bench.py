@@ -68,6 +68,8 @@ def parse():
                     help="skip the ancestral-reconstruction measurement")
     ap.add_argument("--no-pvalues", dest="pvalues", action="store_false",
                     help="skip the p-value measurement")
+    ap.add_argument("--no-config3", dest="config3", action="store_false",
+                    help="skip the config-3 batched-candidates measurement")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default tensor-core launch shapes (no cafe_autotune before the warm-up)")
     ap.add_argument("--profile-only", action="store_true",
@@ -85,6 +87,11 @@ def dist_env():
 def workload(n_families: int):
     from cafe5_gb300.synth import workload as wl
     return wl(1, n_families=n_families, seed=0)
+
+
+def workload_cfg(config: int, n_families=None):
+    from cafe5_gb300.synth import workload as wl
+    return wl(config, n_families=n_families, seed=0)
 
 
 def global_bounds(fams):
@@ -413,6 +420,39 @@ def serving_stream(ctx, n_optimizers: int = 256, requests_each: int = 4, think_m
                     "submit -> result"}
 
 
+def config3_phase(ctx, torch, stream, flush, steps: int = 2, B: int = 64):
+    """Batched optimizer scoring at the config-3 shape: 64 candidate
+    (lambda, alpha) vectors x K = 8 x 20,000 families on a 48-taxon tree
+    (about 64 x 8 x 94 FP64 matrices built per round). Device time of the
+    batched mixed-precision call per round, and each candidate's dlnL
+    against FP64 at the same bins."""
+    from cafe5_gb300.inputs import RootPrior
+    w = workload_cfg(3)
+    F = w.families.n_families
+    tid = ctx.upload_tree(w.tree)
+    sid = ctx.upload_families(tid, w.families.counts)
+    ctx.set_prior(RootPrior.uniform(1100).vector())
+    kw = dict(model=1, precision="mixed_tf32x3")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    d_fam = torch.empty(B * F, dtype=torch.float64, device=dev)
+    d_tot = torch.empty(B, dtype=torch.float64, device=dev)
+    ms = time_steps(ctx, torch, stream, flush, tid, sid, w, B, steps, 1, d_fam, d_tot, kw, step0=30000)
+    cands = candidates(w, B, 31000)
+    cur = ctx.score_batch(tid, sid, cands, **kw)
+    ref = ctx.score_batch(tid, sid, cands, model=1, precision="fp64_binned")
+    per = []
+    for c, r in zip(cur, ref):
+        fin = np.isfinite(r.family_lnl)
+        per.append(float(np.max(np.abs(c.family_lnl[fin] - r.family_lnl[fin]) / np.abs(r.family_lnl[fin])))
+                   if fin.any() else 0.0)
+    ctx.free_families(sid)
+    return {"workload": w.name, "candidates": B, "K": 8, "families": F, "taxa": 48, "steps": steps,
+            "ms_per_round": ms / steps, "value": B * F * steps / (ms / 1e3), "unit": "family-lnL evals/s",
+            "max_rel_dlnl_vs_fp64": max(per), "median_rel_dlnl_vs_fp64": float(np.median(per)),
+            "n_fallback": int(max(c.n_fallback for c in cur)),
+            "note": "64 new (lambda, alpha) candidates per round, all 512 candidate-categories in one batched call"}
+
+
 def reconstruction_phase(ctx, tid, sid, w, fams, S, R, cpu_seconds: float, reps: int = 3):
     """Pupko joint reconstruction of every family x gamma category at the
     reference's global bounds (cafe_reconstruct): the log2-filtered kernel,
@@ -625,6 +665,11 @@ def run_ours(args):
     if rank == 0 and args.serving_clients > 0:
         serving = serving_phase(ctx, tid, sid, w, args.serving_clients, args.serving_requests, kw)
 
+    cfg3 = None
+    if rank == 0 and args.config3:
+        cfg3 = config3_phase(ctx, torch, stream, flush)
+        ctx.set_prior(prior)
+
     stream4 = None
     if rank == 0 and args.serving_optimizers > 0:
         stream4 = serving_stream(ctx, args.serving_optimizers)
@@ -690,6 +735,7 @@ def run_ours(args):
                         "h2d_bytes_per_step": int(fams.counts.nbytes), "d2h_bytes_per_step": int(B * (F * 8 + 8))},
                 "serving": serving,
                 "serving_stream": stream4,
+                "config3_batched": cfg3,
                 "reconstruction": recon,
                 "pvalues": pvals,
                 "gpu_launches": int(round(prof["launches"] / prof_steps * args.steps)),
