@@ -55,7 +55,7 @@ class Timings(C.Structure):
     _fields_ = [("matrix_ms", C.c_double), ("prune_ms", C.c_double), ("finish_ms", C.c_double),
                 ("other_ms", C.c_double), ("prune_flops", C.c_double), ("launches", C.c_int64),
                 ("prune_launches", C.c_int64), ("matrices_built", C.c_int64), ("host_keys_ms", C.c_double),
-                ("host_plan_ms", C.c_double), ("host_total_ms", C.c_double)]
+                ("host_plan_ms", C.c_double), ("host_total_ms", C.c_double), ("host_build_ms", C.c_double)]
 
 
 class OptConfig(C.Structure):

@@ -61,9 +61,17 @@ void MatCache::grow(size_t cap) {
         }
 }
 void MatCache::reserve(size_t n_entries) {
+    // fourfold growth: a long search keeps adding keys, and every growth
+    // rehashes the whole table
     size_t cap = slots_.empty() ? 1024 : slots_.size();
-    while (cap < 2 * n_entries) cap *= 2;
+    while (cap < 2 * n_entries) cap *= 4;
     if (cap != slots_.size()) grow(cap);
+}
+void MatCache::prefetch(const MatKey& k) const {
+    if (slots_.empty()) return;
+    const size_t i = home(k);
+    __builtin_prefetch(&slots_[i]);
+    __builtin_prefetch(&vals_[i]);
 }
 MatEntry* MatCache::find(const MatKey& k) {
     if (slots_.empty()) return nullptr;
@@ -106,10 +114,9 @@ void MatCache::erase(const MatKey& k) {
     --n_;
 }
 void MatCache::clear() {
-    slots_.clear();
-    vals_.clear();
+    // keep the table's size (a reset cache refills to about the same size)
+    for (Slot& sl : slots_) sl.used = false;
     n_ = 0;
-    mask_ = 0;
 }
 
 DevBuf::~DevBuf() {
@@ -454,7 +461,10 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P);
 // Allocate and enqueue K1 for the pending keys on `ws`. On failure the
 // keys' placeholder entries leave the cache again.
 int cache_build(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
+    const auto t0 = std::chrono::steady_clock::now();
     const int rc = cache_build_impl(C, ws, P);
+    if (C->prof.on && ws.sync)
+        C->prof.acc.host_build_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (rc) {
         for (const MatKey& k : P.keys) C->cache.erase(k);
         P.keys.clear();
@@ -1303,13 +1313,25 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     node_entry.assign((size_t)CT * T.n_nodes, nullptr);
     bool any_saturated = false;   // a key with 1 - 2a outside (0, 1): zero rows
     ws.sat_vec.assign((size_t)CT * T.n_nodes, 0);
+    // the request's keys first, with their table slots prefetched (a large
+    // cache misses in the CPU caches on every probe), then one
+    // find-or-insert per key
+    std::vector<MatKey>& keys = ws.key_vec;
+    keys.clear();
     for (int c : active) {
         const cafe_request& Q = Rs[c / K];
         const double m = gamma ? Q.multipliers[c % K] : 1.0;
         for (int v = 0; v < T.n_nodes; ++v) {
             if (T.parent[v] < 0) continue;
-            const double lam = Q.lambdas[T.lambda_index[v]] * m;
-            const MatKey key = make_key(msize, lam, T.branch_length[v]);
+            keys.push_back(make_key(msize, Q.lambdas[T.lambda_index[v]] * m, T.branch_length[v]));
+            C->cache.prefetch(keys.back());
+        }
+    }
+    size_t q = 0;
+    for (int c : active)
+        for (int v = 0; v < T.n_nodes; ++v) {
+            if (T.parent[v] < 0) continue;
+            const MatKey& key = keys[q++];
             node_entry[(size_t)c * T.n_nodes + v] = schedule(C, P, key);
             const double lq = (double)key.lq / 1000000000.0, tq = (double)key.tq / 1000.0;
             const double al = lq * tq / (1 + lq * tq), co = 1 - 2 * al;
@@ -1318,7 +1340,6 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
                 ws.sat_vec[(size_t)c * T.n_nodes + v] = 1;
             }
         }
-    }
     int rc = cache_build(C, ws, P);
     if (rc) return rc;
     // one pass over the entries: matrix pointers, and the builds to wait for
@@ -2232,6 +2253,7 @@ int cafe_ctx_create(const cafe_config* cfg, cafe_ctx** out) {
         cudaGetLastError();
     }
     C->serve_budget = fr / 4;
+    C->cache.reserve(1 << 17);   // 262,144 slots (16 MB of host memory): no rehash in a typical search
     const int n_streams = (cfg && cfg->n_streams > 0) ? cfg->n_streams : 4;
     for (int i = 0; i <= n_streams; ++i) {
         auto w = std::make_unique<Workspace>();

@@ -106,6 +106,7 @@ struct MatEntry {
 class MatCache {
    public:
     MatEntry* find(const MatKey& k);
+    void prefetch(const MatKey& k) const;   // bring k's home slot into the CPU caches
     // (entry, inserted)
     std::pair<MatEntry*, bool> try_emplace(const MatKey& k);
     void erase(const MatKey& k);
@@ -159,6 +160,7 @@ struct Workspace {
     PinnedBuf h_sim, h_simperm;        // p-values: simulated families staged for the device
     std::vector<PruneTile> tile_vec;
     std::vector<MatEntry*> entry_vec;   // cache entry of every (combined category, node)
+    std::vector<MatKey> key_vec;        // the request's matrix keys
     std::vector<uint8_t> sat_vec;       // its key is saturated (1 - 2a outside (0, 1))
     // CUDA graphs of the pruning phase: stream ops go through an op log;
     // a dry pass records their parameters as the graph's signature

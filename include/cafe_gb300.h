@@ -229,6 +229,8 @@ typedef struct {
     double host_keys_ms;         /* host: matrix keys, cache builds, pointer tables */
     double host_plan_ms;         /* host: conversion jobs, tiles, launch plans */
     double host_total_ms;        /* host: whole enqueue of the profiled calls */
+    double host_build_ms;        /* host: part of host_keys_ms spent enqueueing matrix builds
+                                    (job tables, cache memory, the K1 launch) */
 } cafe_timings;
 int cafe_profile_enable(cafe_ctx* ctx, int enable);
 int cafe_profile_read(cafe_ctx* ctx, cafe_timings* out);
