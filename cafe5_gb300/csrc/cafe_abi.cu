@@ -1468,6 +1468,11 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     return finish_batch(C, ws, info, gamma, scaled, dedupe ? S.d_ref.as<int64_t>() : nullptr, nullptr, d_fam, d_total);
 }
 
+bool small_request(const cafe_ctx* C, const cafe_request* R, int NB, int64_t F) {
+    const int K = R->model == CAFE_MODEL_GAMMA ? std::max(1, R->n_categories) : 1;
+    return F * NB * K < (int64_t)C->sm_count * 128;
+}
+
 // Requests' device timelines run one after another: each waits for the
 // previous request's last launch. Persistent tensor-core CTAs take every
 // register of an SM, so interleaving the launches of concurrent requests
@@ -1495,12 +1500,15 @@ int score_enqueue(cafe_ctx* C, Workspace& ws, const cafe_request* R, int NB, caf
     CK(ws.fam_lnl.reserve((size_t)std::max<int64_t>(F, 1) * NB * sizeof(double)), "family buffer");
     CK(ws.total.reserve((size_t)NB * sizeof(double)), "total");
     CK(cudaEventRecord(ws.ev_start, ws.stream), "event");
-    CK(gate_enter(C, ws), "gate");
+    // a request too small to fill the device (fewer family-categories than
+    // one 128-family tile per SM) runs beside the others instead of in turn
+    const bool gated = !small_request(C, R, NB, F);
+    if (gated) CK(gate_enter(C, ws), "gate");
     const auto t_host = std::chrono::steady_clock::now();
     int rc = enqueue_score(C, ws, R, NB, ws.fam_lnl.as<double>(), ws.total.as<double>(), info);
     if (rc) return rc;
     if (C->prof.on && ws.sync) C->prof.acc.host_total_ms += host_ms_since(t_host);
-    CK(gate_leave(C, ws), "gate");
+    if (gated) CK(gate_leave(C, ws), "gate");
     CK(cudaEventRecord(ws.ev_staged, ws.stream), "event");
     ws.staged = true;
     CK(cudaEventRecord(ws.ev_stop, ws.stream), "event");
@@ -2647,6 +2655,7 @@ struct Request {
     std::vector<double> lambdas, mult, probs;
     cafe_result* res = nullptr;
     size_t bytes = 0;          // admission footprint
+    bool small = false;        // too small to fill the device alone (runs beside others)
     int rc = CAFE_OK;
     bool done = false;
     std::chrono::steady_clock::time_point t_submit;
@@ -2698,7 +2707,10 @@ void server_loop(cafe_ctx* C, int wi) {
             // arrive meanwhile queue up and share the next launch)
             C->qcv.wait(lk, [&] {
                 if (C->stop) return true;
-                if (C->queue.empty() || C->batches_in_flight >= kMaxBatchesInFlight) return false;
+                if (C->queue.empty()) return false;
+                // small requests run side by side on every server stream
+                const bool small = C->queue.front()->small;
+                if (C->batches_in_flight >= (small ? (int)C->servers.size() : kMaxBatchesInFlight)) return false;
                 return C->in_flight == 0 || C->in_flight_bytes + C->queue.front()->bytes <= C->serve_budget;
             });
             if (C->stop && C->queue.empty()) return;
@@ -2818,6 +2830,8 @@ int cafe_submit(cafe_ctx* C, const cafe_request* req, cafe_result* res, uint64_t
     {
         std::lock_guard<std::mutex> lk(C->mu);
         r->bytes = request_footprint(C, r->req);
+        auto si = C->sets.find(r->req.set_id);
+        r->small = si != C->sets.end() && small_request(C, &r->req, 1, si->second->F);
     }
     std::lock_guard<std::mutex> lk(C->qmu);
     if (C->servers.empty()) {
