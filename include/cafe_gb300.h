@@ -384,8 +384,9 @@ typedef struct {
     double* conditional;         /* host [R][n_simulations] out, or NULL: sorted simulated likelihoods
                                     of root sizes 1..R */
     double* root_likelihood;     /* host [F][R] out, or NULL: observed root vectors (root sizes 1..R) */
-    double device_ms;            /* out: device time of both prunings */
-    double host_ms;              /* out: host time (simulation, sorting, p-values) */
+    double device_ms;            /* out: device span from the first pruning launch to the last (it
+                                    overlaps the host simulation) */
+    double host_ms;              /* out: host time (matrix copies, simulation, sorting, p-values) */
 } cafe_pvalues_out;
 
 /* compute_pvalues (src/probability.cpp:376-570) at the request's own
