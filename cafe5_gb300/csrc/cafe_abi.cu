@@ -772,6 +772,84 @@ int launch_fp64_tiles(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHos
     return CAFE_OK;
 }
 
+// Bins walked one family per thread-block cluster (k_prune64_cl): those whose
+// 32-family tiles of one candidate would occupy less than half of the SMs.
+// The choice depends on the family set and the category count only, so a
+// candidate gets the same bits alone and in a batch. The cluster gives each
+// CTA at least 64 rows of the bin.
+int fp64_cluster_size(int w) { return w >= 512 ? 8 : w >= 256 ? 4 : w >= 128 ? 2 : 1; }
+
+bool fp64_cluster_bin(const cafe_ctx* C, const TreeHost& T, int64_t count, int K, int w) {
+    return count > 0 && ((count + 31) / 32) * (int64_t)K * 2 < C->sm_count &&
+           prune64_cluster_smem(T.n_slots, w) <= prune64_cluster_max_smem();
+}
+
+// One tile per family of bin b for every category index in `active`.
+void add_cluster_tiles(std::vector<PruneTile>& out, const BinPlan& B, size_t b, const std::vector<int32_t>& active) {
+    const int w = B.widths[b];
+    for (int k : active)
+        for (int64_t i = 0; i < B.bin_count[b]; ++i) {
+            PruneTile t{};
+            t.first = (int)(B.bin_first[b] + i);
+            t.count = 1;
+            t.k = k;
+            t.S = w - 1;
+            t.R = w - 1;
+            out.push_back(t);
+        }
+}
+
+// Launch the one-family-per-cluster FP64 walk over `tiles` (grouped by bin,
+// bins ascending): one launch per bin, sized by the bin's width.
+int launch_fp64_cluster(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T, FamSet& S, int K,
+                        const std::vector<PruneTile>& tiles, const int64_t* d_perm, const int32_t* d_famR, int msize,
+                        bool scaled, double* out, cudaStream_t st, int prof_kind) {
+    if (tiles.empty()) return CAFE_OK;
+    const size_t n = tiles.size();
+    CK(ws.h_tiles_cl.reserve(n * sizeof(PruneTile)), "tiles");
+    CK(ws.tiles_cl.reserve(n * sizeof(PruneTile)), "tiles");
+    std::memcpy(ws.h_tiles_cl.p, tiles.data(), n * sizeof(PruneTile));
+    CK(op_h2d(ws, ws.tiles_cl.p, ws.h_tiles_cl.p, n * sizeof(PruneTile), st), "tiles");
+    Prune64Args a;
+    std::memset(&a, 0, sizeof a);
+    a.plan = T.plan;
+    a.counts = S.d_counts.as<int32_t>();
+    a.perm = d_perm;
+    a.mats = ws.mats.as<const double*>();
+    a.ld_mat = msize;
+    a.prior = C->d_prior.as<double>();
+    a.n_prior = (int)C->prior.size();
+    a.err = R->use_error_model ? C->d_err.as<double>() : nullptr;
+    a.err_rows = C->err_rows;
+    a.err_ndev = C->err_ndev;
+    a.fam_R = d_famR;
+    a.scaled = scaled ? 1 : 0;
+    a.model = R->model == CAFE_MODEL_GAMMA ? 1 : 0;
+    a.out = out;
+    a.K = K;
+    a.cat_probs = ws.catp.as<double>();
+    a.tile_families = 1;
+    const bool prof = ws.sync;
+    cudaEvent_t ev;
+    if (prof) C->prof.begin(prof_kind, st, &ev);
+    for (size_t i = 0; i < n;) {
+        size_t j = i;
+        while (j < n && tiles[j].S == tiles[i].S) ++j;
+        Prune64Args b;
+        std::memcpy(&b, &a, sizeof b);   // padding included: the bytes are a graph signature
+        b.tiles = ws.tiles_cl.as<PruneTile>() + i;
+        b.n_tiles = (int)(j - i);
+        b.W = tiles[i].S + 1;
+        const int cl = fp64_cluster_size(b.W);
+        const int n_cl = (int)std::min<int64_t>((int64_t)(j - i), (int64_t)C->sm_count * 8);
+        CK(op_launch(ws, 8, [&] { return launch_prune64_cluster(b, cl, n_cl, st); }, b, cl, n_cl, st),
+           "prune fp64 (cluster)");
+        i = j;
+    }
+    if (prof) C->prof.end(prof_kind, st, ev);
+    return CAFE_OK;
+}
+
 // Algorithmic flops of one family of a tile (the roofline basis), by the
 // tile's (S, R) and error-model use.
 double family_flops(const TreeHost& T, int S, int R, bool err) {
@@ -895,7 +973,13 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
     // tiles: 128 families (tensor cores) or 32 families (FP64, wide bins)
     // grouped by bin (bins ascend in width), so each bin's tiles are contiguous
     std::vector<PruneTile> tc_tiles, wide_tiles;
-    for (size_t b = 0; b < B.widths.size(); ++b)
+    std::vector<PruneTile>& cl_tiles = ws.cl_tile_vec;
+    cl_tiles.clear();
+    for (size_t b = 0; b < B.widths.size(); ++b) {
+        if (B.widths[b] > 256 && fp64_cluster_bin(C, T, B.bin_count[b], KC, B.widths[b])) {
+            add_cluster_tiles(cl_tiles, B, b, active);
+            continue;
+        }
         for (int k : active) {
             const int w = B.widths[b];
             const int step = w <= 256 ? 128 : 32;
@@ -909,8 +993,22 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
                 (w <= 256 ? tc_tiles : wide_tiles).push_back(t);
             }
         }
+    }
     const bool prof = ws.sync;
     cudaEvent_t ev;
+    // FP64 bins (wider than the tensor-core tiles): 32-family tiles, or one
+    // family per cluster where a bin is sparse; beside the tensor-core bins
+    // when those fork onto the auxiliary streams (profiled calls: after them)
+    bool wide_done = false;
+    auto launch_wide = [&]() -> int {
+        wide_done = true;
+        int rc = launch_fp64_tiles(C, ws, R, T, S, K, wide_tiles, ws.tiles64, ws.h_tiles64, B.d_perm.as<int64_t>(),
+                                   msize, msize, ws.cat.as<double>(), 3);
+        if (!rc)
+            rc = launch_fp64_cluster(C, ws, R, T, S, K, cl_tiles, B.d_perm.as<int64_t>(), B.d_famR.as<int32_t>(),
+                                     msize, true, ws.cat.as<double>(), ws.stream, 3);
+        return rc;
+    };
     if (!tc_tiles.empty()) {
         const size_t fl = (size_t)n_mat * Wm * Wm;
         CK(ws.tc_hi.reserve(fl * sizeof(float)), "tc matrices");
@@ -1036,6 +1134,10 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
                          st),
                "prune tc");
         }
+        if (fork && !prof) {
+            const int rcw = launch_wide();
+            if (rcw) return rcw;
+        }
         if (fork) {
             for (int q = 0; q < Workspace::kAux; ++q) {
                 CK(op_record(ws, ws.ev_join[q], ws.aux[q]), "join");
@@ -1054,9 +1156,10 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
 
         if (prof) C->prof.end(1, ws.stream, ev);
     }
-    int rc = launch_fp64_tiles(C, ws, R, T, S, K, wide_tiles, ws.tiles64, ws.h_tiles64, B.d_perm.as<int64_t>(), msize,
-                               msize, ws.cat.as<double>(), 3);
-    if (rc) return rc;
+    if (!wide_done) {
+        const int rc = launch_wide();
+        if (rc) return rc;
+    }
 
     // families the tensor-core pass could not represent: planned on the
     // device and recomputed in FP64 without a host round trip
@@ -1384,6 +1487,8 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     // tiles
     std::vector<PruneTile>& tiles = ws.tile_vec;
     tiles.clear();
+    std::vector<PruneTile>& cl_tiles = ws.cl_tile_vec;
+    cl_tiles.clear();
     const int TFm = 32;
     const int64_t* d_perm;
     const int32_t* d_famR = nullptr;
@@ -1404,8 +1509,12 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     } else {
         d_perm = S.bins.d_perm.as<int64_t>();
         d_famR = S.bins.d_famR.as<int32_t>();
+        for (size_t b = 0; b < S.bins.widths.size(); ++b)
+            if (fp64_cluster_bin(C, T, S.bins.bin_count[b], K, S.bins.widths[b]))
+                add_cluster_tiles(cl_tiles, S.bins, b, active);
         for (int c : active)
-            for (size_t b = 0; b < S.bins.widths.size(); ++b)
+            for (size_t b = 0; b < S.bins.widths.size(); ++b) {
+                if (fp64_cluster_bin(C, T, S.bins.bin_count[b], K, S.bins.widths[b])) continue;
                 for (int64_t i = 0; i < S.bins.bin_count[b]; i += TFm) {
                     PruneTile t{};
                     t.first = (int)(S.bins.bin_first[b] + i);
@@ -1415,6 +1524,7 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
                     t.R = S.bins.widths[b] - 1;
                     tiles.push_back(t);
                 }
+            }
     }
     const int n_tiles = (int)tiles.size();
     CK(ws.h_tiles.reserve(std::max(n_tiles, 1) * sizeof(PruneTile)), "tiles");
@@ -1465,6 +1575,10 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     }
     CK(launch_prune64(a, n_ctas, ws.stream), "prune");
     if (prof) C->prof.end(1, ws.stream, ev);
+    if (prof) C->prof.acc.prune_flops += tiles_flops(T, cl_tiles, R->use_error_model);
+    rc = launch_fp64_cluster(C, ws, R, T, S, CT, cl_tiles, d_perm, d_famR, msize, scaled, ws.cat.as<double>(),
+                             ws.stream, 1);
+    if (rc) return rc;
     return finish_batch(C, ws, info, gamma, scaled, dedupe ? S.d_ref.as<int64_t>() : nullptr, nullptr, d_fam, d_total);
 }
 
@@ -2241,7 +2355,7 @@ int cafe_ctx_create(const cafe_config* cfg, cafe_ctx** out) {
     cudaDeviceProp prop;
     cudaGetDeviceProperties(&prop, dev);
     C->sm_count = prop.multiProcessorCount;
-    if (tc_kernels_init() != cudaSuccess ||
+    if (tc_kernels_init() != cudaSuccess || prune64_cluster_init() != cudaSuccess ||
         cudaEventCreateWithFlags(&C->gate, cudaEventDisableTiming) != cudaSuccess) {
         delete C;
         return CAFE_ERR_CUDA;

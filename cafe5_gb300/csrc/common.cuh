@@ -98,6 +98,14 @@ struct Prune64Args {
 
 cudaError_t launch_prune64(const Prune64Args& a, int n_ctas, cudaStream_t s);
 
+// The same walk with one family per tile (count 1) and a thread-block
+// cluster of `cl` CTAs per family (rows split across the cluster); W is the
+// vector length of the launch's bin. `n_clusters` clusters loop over the tiles.
+size_t prune64_cluster_smem(int n_slots, int W);
+size_t prune64_cluster_max_smem();
+cudaError_t prune64_cluster_init();
+cudaError_t launch_prune64_cluster(const Prune64Args& a, int cl, int n_clusters, cudaStream_t s);
+
 struct FinishArgs {
     int64_t F;
     int K;                       // categories per candidate (1 for the base model)

@@ -18,7 +18,9 @@
 //                   reference's dense product with a one-hot vector adds only
 //                   exact zeros), or the error-model row sum over n-1, n, n+1
 //   internal child  factor[s] = sum_j M[s][j] L[j]   (an FP64 GEMM tile,
-//                   64 states x 32 families, K staged through shared memory)
+//                   64 states x 32 families, K staged through shared memory;
+//                   each sum as four FMA chains over j = 0, 1, 2, 3 mod 4 in
+//                   ascending j, combined as (s0 + s1) + (s2 + s3))
 // Internal nodes use states 0..S; the root uses rows 1..R (root index j is
 // root size j + 1, src/probability.cpp:206-219). With `scaled`, each node
 // vector is renormalised per family by a power of two and the exponents are
@@ -29,6 +31,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <cstring>
 
 namespace cafe {
 namespace {
@@ -106,7 +109,14 @@ __global__ void __launch_bounds__(NT) k_prune64(Prune64Args a) {
                     const double* L = slot_ptr(base, P.slot[ch], W);
                     const int ty = tid >> 4, tx = tid & 15;   // 16 x 16 threads: 4 rows x 2 families each
                     for (int r0 = 0; r0 < rows; r0 += RT) {
-                        double acc[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+                        // four partial sums per output, over j = 0, 1, 2, 3 (mod 4)
+                        double acc[4][2][4];
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+#pragma unroll
+                            for (int p = 0; p < 2; ++p)
+#pragma unroll
+                                for (int m = 0; m < 4; ++m) acc[q][p][m] = 0.0;
                         for (int j0 = 0; j0 <= S; j0 += KT) {
                             for (int e = tid; e < RT * KT; e += NT) {
                                 const int rr = e / KT, jj = e % KT;
@@ -119,14 +129,17 @@ __global__ void __launch_bounds__(NT) k_prune64(Prune64Args a) {
                                 Ls[jj][i] = (j <= S && i < cnt) ? L[(size_t)j * TF + i] : 0.0;
                             }
                             __syncthreads();
-#pragma unroll 8
-                            for (int jj = 0; jj < KT; ++jj) {
-                                const double b0 = Ls[jj][tx * 2], b1 = Ls[jj][tx * 2 + 1];
+#pragma unroll 2
+                            for (int jj = 0; jj < KT; jj += 4) {
 #pragma unroll
-                                for (int q = 0; q < 4; ++q) {
-                                    const double av = Ms[ty * 4 + q][jj];
-                                    acc[q][0] = fma(av, b0, acc[q][0]);
-                                    acc[q][1] = fma(av, b1, acc[q][1]);
+                                for (int m = 0; m < 4; ++m) {
+                                    const double b0 = Ls[jj + m][tx * 2], b1 = Ls[jj + m][tx * 2 + 1];
+#pragma unroll
+                                    for (int q = 0; q < 4; ++q) {
+                                        const double av = Ms[ty * 4 + q][jj + m];
+                                        acc[q][0][m] = fma(av, b0, acc[q][0][m]);
+                                        acc[q][1][m] = fma(av, b1, acc[q][1][m]);
+                                    }
                                 }
                             }
                             __syncthreads();
@@ -139,8 +152,9 @@ __global__ void __launch_bounds__(NT) k_prune64(Prune64Args a) {
                             for (int p = 0; p < 2; ++p) {
                                 const int i = tx * 2 + p;
                                 if (i >= cnt) continue;
+                                const double sum = (acc[q][p][0] + acc[q][p][1]) + (acc[q][p][2] + acc[q][p][3]);
                                 double* o = dst + (size_t)r * TF + i;
-                                *o = first ? acc[q][p] : *o * acc[q][p];
+                                *o = first ? sum : *o * sum;
                             }
                         }
                     }
@@ -243,6 +257,261 @@ __global__ void __launch_bounds__(NT) k_prune64(Prune64Args a) {
             }
         }
         __syncthreads();
+    }
+}
+
+// ---- the same walk for sparse bins: one family of one category per cluster ----
+//
+// A bin with few families leaves most SMs idle under 32-family tiles (one CTA
+// walks the whole tree per tile, and FP64 issue is the bound). Here a
+// thread-block cluster of CL CTAs walks one family: every CTA keeps a full
+// copy of the family's node vectors in shared memory and forms its own slice
+// of each node's rows (four lanes per row over column chunks of the matrix
+// staged in shared memory). After each node the CTAs exchange their slice
+// maxima (the power-of-two rescale, identical in every CTA) and then their
+// rows through distributed shared memory, each exchange closed by a cluster
+// barrier. Factors, products (the same four FMA chains per row), rescale
+// and root weighting are those of k_prune64, so a family gets the same bits
+// from either kernel; the walk's latency is spread over up to 8 SMs.
+constexpr int kClThreads = 256;
+constexpr int kClWarps = kClThreads / 32;
+constexpr int kClRows = kClThreads / 4;           // rows per pass (four lanes per row)
+constexpr int kClK = 32;                          // matrix columns staged per step
+constexpr int kClStage = kClRows * kClK / kClThreads;   // staged values per thread
+constexpr int kClMax = 8;
+
+__device__ __forceinline__ unsigned cl_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned cl_size() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned cl_id() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned cl_count() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+    return r;
+}
+// every thread of every CTA of the cluster; orders shared-memory stores
+// (local and remote) before the loads that follow it
+__device__ __forceinline__ void cl_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// store v at CTA `rank`'s copy of the shared-memory location p
+__device__ __forceinline__ void st_peer(double* p, unsigned rank, double v) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    unsigned ra;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+    asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(ra), "d"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(kClThreads) k_prune64_cl(Prune64Args a) {
+    extern __shared__ double s_vec[];   // [n_slots][W] node vectors of the family (full copy)
+    int* s_exp = reinterpret_cast<int*>(s_vec + (size_t)a.plan.n_slots * a.W);   // [n_slots]
+    __shared__ double Ms[kClRows][kClK + 4];   // matrix rows of this pass, one column chunk
+    __shared__ double s_part[kClMax];   // slice maxima, one per CTA of the cluster
+    __shared__ double s_red[kClWarps];
+    __shared__ int s_redi[kClWarps];
+
+    const TreePlan& P = a.plan;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const unsigned rank = cl_rank(), CL = cl_size();
+    const int W = a.W, ld = a.ld_mat;
+    cl_sync();   // every CTA of the cluster runs before the first remote store
+
+    for (int t = (int)cl_id(); t < a.n_tiles; t += (int)cl_count()) {
+        const PruneTile tile = a.tiles[t];
+        const int S = tile.S, R = tile.R, k = tile.k;
+        const int64_t f = a.perm[tile.first];
+        const double* const* mats = a.mats + (size_t)k * P.n_nodes;
+
+        for (int ii = 0; ii < P.n_internal; ++ii) {
+            const int v = P.internal[ii];
+            const bool is_root = (v == P.root);
+            const int rows = is_root ? R : S + 1;
+            const int row0 = is_root ? (tile.root_lo > 0 ? tile.root_lo : 1) : 0;
+            const int chunk = (rows + (int)CL - 1) / (int)CL;
+            const int r_lo = min(rows, (int)rank * chunk), r_hi = min(rows, r_lo + chunk);
+            const int vs = P.slot[v];
+            double* dst = s_vec + (size_t)vs * W;
+            int e_sum = 0;
+            for (int ci = P.cstart[ii]; ci < P.cstart[ii + 1]; ++ci) {
+                const int ch = P.child[ci];
+                const bool first = (ci == P.cstart[ii]);
+                const double* __restrict__ M = mats[ch];
+                const int lc = P.leaf_col[ch];
+                if (lc >= 0) {
+                    const int n = a.counts[(size_t)f * P.n_leaves + lc];
+                    for (int r = r_lo + tid; r < r_hi; r += kClThreads) {
+                        const double* Mr = M + (size_t)(row0 + r) * ld;
+                        double val = 0.0;
+                        if (a.err) {
+                            const double* pr = a.err + (size_t)(n < a.err_rows ? n : a.err_rows - 1) * a.err_ndev;
+                            const int off = n - (a.err_ndev - 1) / 2;
+                            for (int d = 0; d < a.err_ndev; ++d) {
+                                const int c = off + d;
+                                if (c < 0 || c > S) continue;
+                                val = fma(Mr[c], pr[d], val);
+                            }
+                        } else if (n >= 0 && n <= S) {
+                            val = Mr[n];
+                        }
+                        dst[r] = first ? val : dst[r] * val;
+                    }
+                } else {
+                    // dst[r] (*)= sum_j M[row0 + r][j] * L[j]: four lanes per row,
+                    // lane q the FMA chain over j = q (mod 4) in ascending j, then
+                    // (s0 + s1) + (s2 + s3), the sums of k_prune64 bit for bit.
+                    // Matrix chunks are staged coalesced, the next one loaded
+                    // into registers while the current one is used.
+                    const double* L = s_vec + (size_t)P.slot[ch] * W;
+                    const int rp = tid >> 2, q = tid & 3;
+                    for (int rb = r_lo; rb < r_hi; rb += kClRows) {
+                        const int nr = min(kClRows, r_hi - rb);
+                        double pre[kClStage];
+                        auto load_chunk = [&](int j0) {
+#pragma unroll
+                            for (int i = 0; i < kClStage; ++i) {
+                                const int rr = warp + kClWarps * i, j = j0 + lane;
+                                pre[i] = (rr < nr && j <= S) ? M[(size_t)(row0 + rb + rr) * ld + j] : 0.0;
+                            }
+                        };
+                        load_chunk(0);
+                        double acc = 0.0;
+                        for (int j0 = 0; j0 <= S; j0 += kClK) {
+#pragma unroll
+                            for (int i = 0; i < kClStage; ++i) Ms[warp + kClWarps * i][lane] = pre[i];
+                            __syncthreads();
+                            if (j0 + kClK <= S) load_chunk(j0 + kClK);
+#pragma unroll
+                            for (int i = 0; i < kClK / 4; ++i) {
+                                const int jj = q + 4 * i, j = j0 + jj;
+                                const double lv = j <= S ? L[j] : 0.0;
+                                acc = fma(Ms[rp][jj], lv, acc);
+                            }
+                            __syncthreads();
+                        }
+                        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+                        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+                        if (q == 0 && rp < nr) dst[rb + rp] = first ? acc : dst[rb + rp] * acc;
+                    }
+                    e_sum += s_exp[P.slot[ch]];
+                }
+                __syncthreads();
+            }
+            int e = 0;
+            if (a.scaled) {
+                // the node's maximum over all rows -> one power-of-two scale
+                double mx = 0.0;
+                for (int r = r_lo + tid; r < r_hi; r += kClThreads) {
+                    const double x = dst[r];
+                    mx = x > mx ? x : mx;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const double y = __shfl_xor_sync(0xffffffffu, mx, o);
+                    mx = y > mx ? y : mx;
+                }
+                if (lane == 0) s_red[warp] = mx;
+                __syncthreads();
+                if (tid < (int)CL) {
+                    double m = 0.0;
+                    for (int w = 0; w < kClWarps; ++w) m = s_red[w] > m ? s_red[w] : m;
+                    st_peer(&s_part[rank], (unsigned)tid, m);
+                }
+                cl_sync();
+                double m = 0.0;
+                for (unsigned q = 0; q < CL; ++q) m = s_part[q] > m ? s_part[q] : m;
+                if (m > 0.0 && isfinite(m)) frexp(m, &e);
+            }
+            // rescale this CTA's rows and send them to every other CTA
+            for (int r = r_lo + tid; r < r_hi; r += kClThreads) {
+                double x = dst[r];
+                if (e != 0) {
+                    x = scalbn(x, -e);
+                    dst[r] = x;
+                }
+                for (unsigned q = 0; q < CL; ++q)
+                    if (q != rank) st_peer(dst + r, q, x);
+            }
+            if (tid == 0) s_exp[vs] = e_sum + e;
+            cl_sync();
+        }
+
+        // ---- root weighting (K4), by the cluster's first CTA ----
+        const int rs = P.slot[P.root];
+        const double* root = s_vec + (size_t)rs * W;
+        if (rank == 0) {
+            if (a.root_out) {
+                for (int j = tid; j < R; j += kClThreads) a.root_out[(size_t)f * a.root_ld + j] = root[j];
+            } else {
+                const int Rf = a.fam_R ? a.fam_R[f] : R;
+                if (a.model == 0) {
+                    double best = -INFINITY;
+                    for (int j = tid; j < Rf; j += kClThreads) {
+                        const double eq = j < a.n_prior ? a.prior[j] : 0.0;
+                        const double vv = log(root[j]) + log(eq);
+                        best = vv > best ? vv : best;
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        const double y = __shfl_xor_sync(0xffffffffu, best, o);
+                        best = y > best ? y : best;
+                    }
+                    if (lane == 0) s_red[warp] = best;
+                    __syncthreads();
+                    if (tid == 0) {
+                        double b = -INFINITY;
+                        for (int w = 0; w < kClWarps; ++w) b = s_red[w] > b ? s_red[w] : b;
+                        a.out[(size_t)f * a.K + k] = b + (double)s_exp[rs] * 0.69314718055994530942;
+                    }
+                } else {
+                    double mx = 0.0;
+                    int nz = 0;
+                    for (int j = tid; j < Rf; j += kClThreads) {
+                        const double x = root[j];
+                        const double eq = j < a.n_prior ? a.prior[j] : 0.0;
+                        const double vv = x * eq;
+                        mx = vv > mx ? vv : mx;
+                        nz |= (x != 0.0);
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        const double y = __shfl_xor_sync(0xffffffffu, mx, o);
+                        mx = y > mx ? y : mx;
+                        nz |= __shfl_xor_sync(0xffffffffu, nz, o);
+                    }
+                    if (lane == 0) {
+                        s_red[warp] = mx;
+                        s_redi[warp] = nz;
+                    }
+                    __syncthreads();
+                    if (tid == 0) {
+                        double m = 0.0;
+                        int z = 0;
+                        for (int w = 0; w < kClWarps; ++w) {
+                            m = s_red[w] > m ? s_red[w] : m;
+                            z |= s_redi[w];
+                        }
+                        const double cat = m * a.cat_probs[k];
+                        double o;
+                        if (!z) o = a.scaled ? NAN : -1.0;   // all-zero root vector: family fails
+                        else if (a.scaled) o = log(cat) + (double)s_exp[rs] * 0.69314718055994530942;
+                        else o = cat;
+                        a.out[(size_t)f * a.K + k] = o;
+                    }
+                }
+            }
+        }
+        cl_sync();   // the root is read before the next family's rows arrive
     }
 }
 
@@ -402,6 +671,39 @@ cudaError_t launch_prune64(const Prune64Args& a, int n_ctas, cudaStream_t s) {
     size_t smem = sizeof(int) * (size_t)a.plan.n_slots * TF;
     k_prune64<<<n_ctas, NT, smem, s>>>(a);
     return cudaGetLastError();
+}
+
+size_t prune64_cluster_smem(int n_slots, int W) {
+    return (size_t)n_slots * W * sizeof(double) + (size_t)n_slots * sizeof(int);
+}
+
+// (the kernel also holds 19 KB of static shared memory; the opt-in limit is 227 KB)
+size_t prune64_cluster_max_smem() { return 160 * 1024; }
+
+cudaError_t prune64_cluster_init() {
+    return cudaFuncSetAttribute(k_prune64_cl, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)prune64_cluster_max_smem());
+}
+
+cudaError_t launch_prune64_cluster(const Prune64Args& a, int cl, int n_clusters, cudaStream_t s) {
+    if (a.n_tiles <= 0) return cudaSuccess;
+    if (cl < 1 || cl > kClMax || n_clusters < 1) return cudaErrorInvalidValue;
+    const size_t smem = prune64_cluster_smem(a.plan.n_slots, a.W);
+    if (smem > prune64_cluster_max_smem()) return cudaErrorInvalidValue;
+    cudaLaunchConfig_t cfg;
+    std::memset(&cfg, 0, sizeof cfg);
+    cfg.gridDim = dim3((unsigned)(n_clusters * cl), 1, 1);
+    cfg.blockDim = dim3(kClThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)cl;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_prune64_cl, a);
 }
 
 int finish_parts(int64_t F) {

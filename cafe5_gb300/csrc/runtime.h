@@ -155,6 +155,10 @@ struct Workspace {
     DevBuf tc_hi, tc_lo, tc_mi, tc_vhi, tc_vlo, conv, flags, fb_perm, tiles64, tiles_fb, parts, fb_count, phase,
         catids;
     PinnedBuf h_conv, h_mi, h_flags, h_tiles64, h_tiles_fb, h_tail, h_catids;
+    // FP64 bins walked one family per cluster
+    DevBuf tiles_cl;
+    PinnedBuf h_tiles_cl;
+    std::vector<PruneTile> cl_tile_vec;
     // reconstruction
     DevBuf rc_c, rc_state, rc_rmax, rc_mean, rc_count, rc_nfail, rc_parent, rc_bp, rc_lm, rc_lptr;
     PinnedBuf h_sim, h_simperm;        // p-values: simulated families staged for the device

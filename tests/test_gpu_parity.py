@@ -337,3 +337,48 @@ def test_mixed_results_do_not_depend_on_batch_composition(ctx):
     sub = w.families.counts[:300]
     c, d = _both(ctx, w.tree, sub, [0.002], model=1, mult=w.multipliers, probs=w.cat_probs)
     assert np.array_equal(d.family_lnl, b.family_lnl[:300])
+
+
+@pytest.mark.parametrize("wl,model", [(2, 0), (0, 1)], ids=["two_lambda_error_model", "gamma_k4"])
+def test_sparse_fp64_bins_walk_one_family_per_cluster(ctx, wl, model):
+    """FP64 bins too sparse to fill the GPU with 32-family tiles are walked
+    one family per thread-block cluster; their families get the same bits as
+    in a bin full enough for the 32-family tile walk, in fp64_binned and in
+    mixed_tf32x3 (whose bins above 256 states run in FP64). The small golden
+    cases of test_fp64_binned_matches_scaled_oracle run on the cluster walk
+    (every bin sparse) against the oracle."""
+    from cafe5_gb300.families import FamilySet, bin_families
+    from cafe5_gb300.inputs import ErrorModel, RootPrior
+    from cafe5_gb300.synth import workload
+    w = workload(wl, n_families=160, seed=41)
+    counts = w.families.counts.copy()
+    counts = counts[counts.max(axis=1) < 60]
+    counts[:3] += 230                        # bin 384
+    counts[3:6] += 330                       # bin 512
+    fams = FamilySet([str(i) for i in range(len(counts))], counts)
+    W, _, _ = bin_families(fams)
+    assert sorted(set(int(x) for x in W[:6])) == [384, 512]
+    K = 4 if model else 1
+    mult = [0.2, 0.6, 1.1, 2.1] if model else [1.0]
+    probs = [0.25] * 4 if model else [1.0]
+    reps = -(-(100 * 32) // K)               # 100 tiles per category: a bin this full takes the tile walk
+    wide = [np.tile(counts[i:i + 3], (reps // 3 + 1, 1))[:reps] for i in (0, 3)]
+    big = np.concatenate([wide[0], wide[1], counts[6:]])
+    pos_big = [0, 1, 2, reps, reps + 1, reps + 2]
+    err = ErrorModel.symmetric(0.05, 1100).table() if wl == 2 else None
+    prior = RootPrior.uniform(1100).vector()
+    lam_idx = w.lambda_of_node if wl == 2 else None
+    kw = dict(model=model, lambda_kind=1 if wl == 2 else 0, multipliers=mult, cat_probs=probs,
+              use_error_model=err is not None)
+    tid = ctx.upload_tree(w.tree, lam_idx)
+    ctx.set_prior(prior)
+    ctx.set_error_model(err)
+    small_sid = ctx.upload_families(tid, counts)
+    big_sid = ctx.upload_families(tid, big)
+    for precision in ("fp64_binned", "mixed_tf32x3"):
+        a = ctx.score(tid, small_sid, w.lambdas, precision=precision, **kw)
+        b = ctx.score(tid, big_sid, w.lambdas, precision=precision, **kw)
+        assert np.array_equal(a.family_lnl[:6], b.family_lnl[pos_big]), precision
+        assert np.array_equal(a.family_lnl[6:], b.family_lnl[2 * reps:]), precision
+    ctx.free_families(small_sid)
+    ctx.free_families(big_sid)
