@@ -70,8 +70,12 @@ def parse():
                     help="skip the p-value measurement")
     ap.add_argument("--no-config3", dest="config3", action="store_false",
                     help="skip the config-3 batched-candidates measurement")
+    ap.add_argument("--no-config2", dest="config2", action="store_false",
+                    help="skip the config-2 (two lambdas, error model, S-bins to 512) measurement")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default tensor-core launch shapes (no cafe_autotune before the warm-up)")
+    ap.add_argument("--profile-config2", action="store_true",
+                    help="two batched scores of the config-2 workload and nothing else (a small case for ncu)")
     ap.add_argument("--profile-only", action="store_true",
                     help="two batched scores of the workload and nothing else (a small case for ncu captures)")
     return ap.parse_args()
@@ -259,18 +263,19 @@ def run_reference(args):
     return 0
 
 
-def time_steps(ctx, torch, stream, flush, tid, sid, w, B, steps, warmup, d_fam, d_tot, kw, step0=0):
+def time_steps(ctx, torch, stream, flush, tid, sid, w, B, steps, warmup, d_fam, d_tot, kw, step0=0, make=None):
     """Device time (ms) of `steps` batched scores issued back to back after
     `warmup` untimed ones: the host prepares step i + 1 while the device
     runs step i, as a deployment's loop does. Between steps a 256 MB write
     on the same stream evicts L2; its time is inside the timed region."""
+    make = make or candidates
     for i in range(warmup):
-        ctx.score_batch_device(tid, sid, candidates(w, B, step0 - 1 - i), d_fam.data_ptr(), d_tot.data_ptr(),
+        ctx.score_batch_device(tid, sid, make(w, B, step0 - 1 - i), d_fam.data_ptr(), d_tot.data_ptr(),
                                stream.cuda_stream, **kw)
     torch.cuda.synchronize()
     if steps <= 0:
         return 0.0
-    cands = [candidates(w, B, step0 + i) for i in range(steps)]
+    cands = [make(w, B, step0 + i) for i in range(steps)]
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     flush.fill_(-1.0)
     e0.record(stream)
@@ -453,6 +458,63 @@ def config3_phase(ctx, torch, stream, flush, steps: int = 2, B: int = 64):
             "note": "64 new (lambda, alpha) candidates per round, all 512 candidate-categories in one batched call"}
 
 
+def config2_phase(ctx, torch, stream, flush, steps: int = 4, B: int = 4):
+    """The two-lambda local model with the error model: a 32-taxon tree whose
+    10-taxon clade runs at lambda2, epsilon 0.05, 50,000 families from a
+    heavy-tailed root (95 % Poisson(4), 5 % geometric(0.02); S-bins 32 to
+    512). Every bin goes into one request: bins up to 256 states on the
+    tensor cores, the sparse wider bins on the FP64 cluster walk, replayed as
+    one CUDA graph. B candidate (lambda1, lambda2) vectors per step; device
+    time per step, the FP64 path at the same bins, and the largest
+    per-family dlnL against it."""
+    from cafe5_gb300.families import bin_families
+    from cafe5_gb300.inputs import ErrorModel, RootPrior
+    w = workload_cfg(2)
+    F = w.families.n_families
+    Wb, _, _ = bin_families(w.families)
+    tid = ctx.upload_tree(w.tree, w.lambda_of_node)
+    sid = ctx.upload_families(tid, w.families.counts)
+    ctx.set_prior(RootPrior.uniform(1100).vector())
+    ctx.set_error_model(ErrorModel.symmetric(0.05, 1100).table())
+    base = dict(model=0, lambda_kind=1, use_error_model=True)
+
+    def make(w, B, step):
+        f = 1.0 + 1e-6 * (step % 10000)
+        return [dict(lambdas=[w.lambdas[0] * (1.0 + 0.01 * b) * f, w.lambdas[1] * (1.0 + 0.01 * b) * f])
+                for b in range(B)]
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    d_fam = torch.empty(B * F, dtype=torch.float64, device=dev)
+    d_tot = torch.empty(B, dtype=torch.float64, device=dev)
+    kw = dict(base, precision="mixed_tf32x3")
+    ms = time_steps(ctx, torch, stream, flush, tid, sid, w, B, steps, 3, d_fam, d_tot, kw, step0=20000, make=make)
+    kw64 = dict(base, precision="fp64_binned")
+    ms64 = time_steps(ctx, torch, stream, flush, tid, sid, w, B, 2, 1, d_fam, d_tot, kw64, step0=21000, make=make)
+    cands = make(w, B, 22000)
+    cur = ctx.score_batch(tid, sid, cands, **kw)
+    ref = ctx.score_batch(tid, sid, cands, **kw64)
+    per = []
+    for c, r in zip(cur, ref):
+        fin = np.isfinite(r.family_lnl)
+        per.append(float(np.max(np.abs(c.family_lnl[fin] - r.family_lnl[fin]) / np.abs(r.family_lnl[fin]))))
+    ctx.profile(True)
+    ctx.profile_read()
+    ctx.score_batch(tid, sid, cands, **kw)
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    ctx.free_families(sid)
+    ctx.set_error_model(None)
+    bins = {int(b): int((Wb == b).sum()) for b in sorted(set(int(x) for x in Wb))}
+    return {"workload": w.name, "candidates": B, "families": F, "taxa": 32, "bins": bins, "steps": steps,
+            "ms_per_step": ms / steps, "value": B * F * steps / (ms / 1e3), "unit": "family-lnL evals/s",
+            "fp64_binned_ms_per_step": ms64 / 2, "fp64_binned_value": B * F * 2 / (ms64 / 1e3),
+            "max_rel_dlnl_vs_fp64": max(per), "n_fallback": int(max(c.n_fallback for c in cur)),
+            "profiled_call_ms": {k: round(v, 3) for k, v in prof.items()
+                                 if k in ("matrix_ms", "prune_ms", "other_ms", "finish_ms")},
+            "note": "profiled_call_ms: one direct (unreplayed) call with per-launch events: prune_ms = "
+                    "tensor-core bins, other_ms = TF32 conversion + FP64 cluster walk of the bins above 256"}
+
+
 def reconstruction_phase(ctx, tid, sid, w, fams, S, R, cpu_seconds: float, reps: int = 3):
     """Pupko joint reconstruction of every family x gamma category at the
     reference's global bounds (cafe_reconstruct): the log2-filtered kernel,
@@ -583,6 +645,24 @@ def run_ours(args):
     torch.cuda.set_stream(stream)
     d_fam = torch.empty(B * F, dtype=torch.float64, device=dev)
     d_tot = torch.empty(B, dtype=torch.float64, device=dev)
+    if args.profile_config2:
+        # two batched mixed-precision scores of the config-2 workload (a small
+        # case for ncu captures of the FP64 cluster walk and the wide bins)
+        from cafe5_gb300.inputs import ErrorModel
+        w2 = workload_cfg(2)
+        tid2 = ctx.upload_tree(w2.tree, w2.lambda_of_node)
+        sid2 = ctx.upload_families(tid2, w2.families.counts)
+        ctx.set_prior(RootPrior.uniform(1100).vector())
+        ctx.set_error_model(ErrorModel.symmetric(0.05, 1100).table())
+        for i in range(2):
+            c = [dict(lambdas=[w2.lambdas[0] * (1.0 + 0.01 * b) * (1.0 + 1e-6 * i),
+                               w2.lambdas[1] * (1.0 + 0.01 * b) * (1.0 + 1e-6 * i)]) for b in range(B)]
+            r = ctx.score_batch(tid2, sid2, c, model=0, lambda_kind=1, use_error_model=True, precision=prec)
+        if rank == 0:
+            print(json.dumps({"profile_config2": True, "candidates": B, "families": w2.families.n_families,
+                              "neg_lnl": r[0].total}))
+        ctx.close()
+        return 0
     if args.profile_only:
         for i in range(2):
             ctx.score_batch_device(tid, sid, candidates(w, B, i), d_fam.data_ptr(), d_tot.data_ptr(),
@@ -670,6 +750,11 @@ def run_ours(args):
         cfg3 = config3_phase(ctx, torch, stream, flush)
         ctx.set_prior(prior)
 
+    cfg2 = None
+    if rank == 0 and args.config2:
+        cfg2 = config2_phase(ctx, torch, stream, flush)
+        ctx.set_prior(prior)
+
     stream4 = None
     if rank == 0 and args.serving_optimizers > 0:
         stream4 = serving_stream(ctx, args.serving_optimizers)
@@ -736,6 +821,7 @@ def run_ours(args):
                 "serving": serving,
                 "serving_stream": stream4,
                 "config3_batched": cfg3,
+                "config2_local_lambdas_error_model": cfg2,
                 "reconstruction": recon,
                 "pvalues": pvals,
                 "gpu_launches": int(round(prof["launches"] / prof_steps * args.steps)),
