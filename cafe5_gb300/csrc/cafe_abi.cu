@@ -1064,16 +1064,13 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             launches.push_back(L);
             i = j;
         }
-        CK(ws.tc_vhi.reserve((size_t)vrows * Wm * sizeof(float)), "tc vectors");
-        CK(ws.tc_vlo.reserve((size_t)vrows * Wm * sizeof(float)), "tc vectors");
+        CK(ws.tc_vec.reserve((size_t)vrows * Wm * sizeof(float)), "tc vectors");
         TcMaps maps;
         const int kbox = prune_tc_kchunk();
         int rc = cached_map(C, ws, 0, &maps.mat_hi, ws.tc_hi.as<float>(), (int64_t)n_mat * Wm, Wm, kbox);
         if (!rc) rc = cached_map(C, ws, 1, &maps.mat_lo, ws.tc_lo.as<float>(), (int64_t)n_mat * Wm, Wm, kbox);
-        if (!rc) rc = cached_map(C, ws, 2, &maps.vec_hi, ws.tc_vhi.as<float>(), vrows, Wm, kbox);
-        if (!rc) rc = cached_map(C, ws, 3, &maps.vec_lo, ws.tc_vlo.as<float>(), vrows, Wm, kbox);
-        if (!rc) rc = cached_map(C, ws, 4, &maps.vst_hi, ws.tc_vhi.as<float>(), vrows, Wm, 32);
-        if (!rc) rc = cached_map(C, ws, 5, &maps.vst_lo, ws.tc_vlo.as<float>(), vrows, Wm, 32);
+        if (!rc) rc = cached_map(C, ws, 2, &maps.vec, ws.tc_vec.as<float>(), vrows, Wm, kbox);
+        if (!rc) rc = cached_map(C, ws, 3, &maps.vst, ws.tc_vec.as<float>(), vrows, Wm, 32);
         if (rc) return rc;
         const int n_tc = (int)tc_tiles.size();
         CK(ws.tiles.reserve(n_tc * sizeof(PruneTile)), "tiles");
@@ -1087,8 +1084,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         a.perm = B.d_perm.as<int64_t>();
         a.mat_index = ws.tc_mi.as<int32_t>();
         a.Wm = Wm;
-        a.vec_hi = ws.tc_vhi.as<float>();
-        a.vec_lo = ws.tc_vlo.as<float>();
+        a.vec = ws.tc_vec.as<float>();
         a.n_slots = T.n_slots;
         a.prior = C->d_prior.as<double>();
         a.n_prior = (int)C->prior.size();

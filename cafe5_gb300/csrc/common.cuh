@@ -150,8 +150,7 @@ struct PruneTcArgs {
     const int32_t* mat_index;    // [K][n_nodes] converted-matrix index (-1 for the root); bit 30 set
                                  // when the key is saturated
     int Wm;                      // pitch of matrices and node vectors (elements)
-    float* vec_hi;               // node vectors, rows = CTA x slot x 128 families
-    float* vec_lo;
+    float* vec;                  // node vectors (FP32), rows = CTA x slot x 128 families
     int n_slots;
     const double* prior;
     int n_prior;
@@ -174,11 +173,11 @@ struct PruneTcArgs {
 };
 
 // Tensor maps travel by value (__grid_constant__); the host encodes them.
-// Operand loads use prune_tc_kchunk()-column boxes (mat_*, vec_*; 128-byte
+// Operand loads use prune_tc_kchunk()-column boxes (mat_*, vec; 128-byte
 // swizzle for 32 columns, 64-byte for 16); the epilogue stores node vectors
-// in 32-column boxes in the 128-byte swizzle (vst_*). Boxes are 32 rows.
+// in 32-column boxes in the 128-byte swizzle (vst). Boxes are 32 rows.
 struct TcMaps {
-    CUtensorMap mat_hi, mat_lo, vec_hi, vec_lo, vst_hi, vst_lo;
+    CUtensorMap mat_hi, mat_lo, vec, vst;
 };
 
 cudaError_t launch_prune_tc(const TcMaps& maps, const PruneTcArgs& a, int n_ctas, size_t smem, cudaStream_t s);

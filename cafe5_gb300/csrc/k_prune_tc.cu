@@ -69,7 +69,7 @@ constexpr int CW = CAFE_TC_CW;   // epilogue columns per TMEM load
 __host__ __device__ inline size_t stage_bytes(int Ws) { return (size_t)(2 * TM + 2 * Ws) * KC * sizeof(float); }
 __device__ __forceinline__ uint64_t desc_k(const void* p) { return KC == 32 ? tc::desc_sw128(p) : tc::desc_sw64(p); }
 
-// Pipeline stages, also home of the epilogue's 32 KB staging tile.
+// Pipeline stages, also home of the epilogue's two 16 KB staging tiles.
 __host__ __device__ inline size_t stages_region(int Ws, int stages) {
     const size_t st = (size_t)stages * stage_bytes(Ws), stg = (size_t)2 * TM * SC * sizeof(float);
     return st > stg ? st : stg;
@@ -291,20 +291,23 @@ __device__ __noinline__ int epi_maxexp(const NodeSrc<NC> ns, int W, int s_lo, in
     return maxe;
 }
 
-// Pass 2 (inner nodes; every thread of the CTA): the scaled product as
-// TF32 hi/lo into a staging tile in the 128-byte-swizzled layout, 32
-// columns at a time, written to the node's vector rows by TMA stores.
+// Pass 2 (inner nodes; every thread of the CTA): the scaled product in FP32
+// into a staging tile in the 128-byte-swizzled layout, 32 columns at a
+// time, written to the node's vector rows by TMA stores. The parent's GEMM
+// splits it into TF32 hi/lo as it loads it (split_row_tf32).
 template <int NC>
-__device__ __forceinline__ void epi_store(const NodeSrc<NC>& ns, int W, const float (&scl)[NC], float* stg_hi,
-                                          float* stg_lo, int tid, const CUtensorMap* map_hi, const CUtensorMap* map_lo,
-                                          int vrow) {
-    uint8_t* row_hi = reinterpret_cast<uint8_t*>(stg_hi) + (size_t)(tid >> 3) * 1024 + (size_t)(tid & 7) * 128;
-    uint8_t* row_lo = reinterpret_cast<uint8_t*>(stg_lo) + (size_t)(tid >> 3) * 1024 + (size_t)(tid & 7) * 128;
+__device__ __forceinline__ void epi_store(const NodeSrc<NC>& ns, int W, const float (&scl)[NC], float* stg, int tid,
+                                          const CUtensorMap* map, int vrow) {
+    // two staging tiles of TM x SC floats, used in turn: a chunk waits only
+    // for the stores of the chunk two back
     for (int c32 = 0; c32 < W; c32 += SC) {
-        if (c32 > 0) {
-            if (tid == 0) tc::bulk_wait_read0();     // the previous chunk's stores have read the tile
+        const int b = (c32 / SC) & 1;
+        float* tile = stg + (size_t)b * TM * SC;
+        if (c32 >= 2 * SC) {
+            if (tid == 0) tc::bulk_wait_read1();     // the chunk two back has read this tile
             __syncthreads();
         }
+        uint8_t* row = reinterpret_cast<uint8_t*>(tile) + (size_t)(tid >> 3) * 1024 + (size_t)(tid & 7) * 128;
         for (int col0 = c32; col0 < c32 + SC; col0 += CW) {
             uint32_t r[NC][CW];
             load_children(ns, col0, r);
@@ -317,37 +320,48 @@ __device__ __forceinline__ void epi_store(const NodeSrc<NC>& ns, int W, const fl
                 for (int j = 0; j < CW; ++j) p[j] *= __uint_as_float(r[c][j]) * scl[c];
 #pragma unroll
             for (int q = 0; q < CW / 4; ++q) {
-                float4 h, l;
-                h.x = tc::round_tf32(p[4 * q + 0]);
-                h.y = tc::round_tf32(p[4 * q + 1]);
-                h.z = tc::round_tf32(p[4 * q + 2]);
-                h.w = tc::round_tf32(p[4 * q + 3]);
-                l.x = tc::round_tf32(p[4 * q + 0] - h.x);
-                l.y = tc::round_tf32(p[4 * q + 1] - h.y);
-                l.z = tc::round_tf32(p[4 * q + 2] - h.z);
-                l.w = tc::round_tf32(p[4 * q + 3] - h.w);
                 const int j = ((col0 - c32) >> 2) + q;          // 16-byte piece of the 128-byte row
                 const int off = (j ^ (tid & 7)) << 4;
-                *reinterpret_cast<float4*>(row_hi + off) = h;
-                *reinterpret_cast<float4*>(row_lo + off) = l;
+                *reinterpret_cast<float4*>(row + off) = make_float4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
             }
         }
         tc::fence_proxy_async_shared();
         __syncthreads();
         if (tid == 0) {
-            for (int r = 0; r < TM / 32; ++r) {
-                tc::tma_store_2d(map_hi, c32, vrow + 32 * r, stg_hi + r * 32 * SC);
-                tc::tma_store_2d(map_lo, c32, vrow + 32 * r, stg_lo + r * 32 * SC);
-            }
+            for (int r = 0; r < TM / 32; ++r) tc::tma_store_2d(map, c32, vrow + 32 * r, tile + r * 32 * SC);
             tc::bulk_commit();
         }
     }
 }
 
+// Row `row` of an operand chunk holds the FP32 node vector (KC values, the
+// 16-byte pieces in swizzled order); write its TF32 hi part in place and the
+// lo part at the same position of `lo`: hi = tf32(v), lo = tf32(v - hi).
+__device__ __forceinline__ void split_row_tf32(float* hi, float* lo, int row) {
+    constexpr int NP = KC / 4;   // 16-byte pieces per row
+    float4* h = reinterpret_cast<float4*>(hi + (size_t)row * KC);
+    float4* l = reinterpret_cast<float4*>(lo + (size_t)row * KC);
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+        const int p = q ^ (row & (NP - 1));   // neighbouring rows start on different banks
+        const float4 v = h[p];
+        float4 a, b;
+        a.x = tc::round_tf32(v.x);
+        a.y = tc::round_tf32(v.y);
+        a.z = tc::round_tf32(v.z);
+        a.w = tc::round_tf32(v.w);
+        b.x = tc::round_tf32(v.x - a.x);
+        b.y = tc::round_tf32(v.y - a.y);
+        b.z = tc::round_tf32(v.z - a.z);
+        b.w = tc::round_tf32(v.w - a.w);
+        h[p] = a;
+        l[p] = b;
+    }
+}
+
 __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
     k_prune_tc(const __grid_constant__ CUtensorMap map_mhi, const __grid_constant__ CUtensorMap map_mlo,
-               const __grid_constant__ CUtensorMap map_vhi, const __grid_constant__ CUtensorMap map_vlo,
-               const __grid_constant__ CUtensorMap map_shi, const __grid_constant__ CUtensorMap map_slo,
+               const __grid_constant__ CUtensorMap map_vec, const __grid_constant__ CUtensorMap map_vst,
                const PruneTcArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -503,13 +517,13 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                         }
                         if (leaf && i >= NS) __syncthreads();      // stage free for every writer
                         if (tid == 0 && !abort_sh) {
-                            tc::mbar_expect_tx(&bar_full[st], (uint32_t)(((leaf ? 0 : 2 * TM) + 2 * W) * KC * sizeof(float)));
+                            tc::mbar_expect_tx(&bar_full[st], (uint32_t)(((leaf ? 0 : TM) + 2 * W) * KC * sizeof(float)));
                             if (!leaf) {
+                                // the FP32 node vector lands in the hi operand; the
+                                // consumer splits it into hi and lo in place
                                 const int vrow = (int)(vrow_cta + (int64_t)chi.slot * TM);
-                                for (int r = 0; r < TM / 32; ++r) {
-                                    tc::tma_load_2d(Ahi + r * 32 * KC, &map_vhi, kc * KC, vrow + 32 * r, &bar_full[st]);
-                                    tc::tma_load_2d(Alo + r * 32 * KC, &map_vlo, kc * KC, vrow + 32 * r, &bar_full[st]);
-                                }
+                                for (int r = 0; r < TM / 32; ++r)
+                                    tc::tma_load_2d(Ahi + r * 32 * KC, &map_vec, kc * KC, vrow + 32 * r, &bar_full[st]);
                             }
                             const int mrow = chi.mat * Wm;
                             for (int r = 0; r < W / 32; ++r) {
@@ -531,6 +545,25 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                     }
                     // ---- consume chunk j = i - (NS - 1) ----
                     const int j = i - (NS - 1);
+                    // an internal child's FP32 vector chunk: every thread waits
+                    // for it and splits its own row into the TF32 hi/lo operands
+                    if (j >= 0 && nd.c[j < n0 ? 0 : 1].leaf_col < 0) {
+                        const uint32_t cg = g + (uint32_t)j;
+                        const int st = (int)(cg % (uint32_t)NS);
+                        float* Ahi = reinterpret_cast<float*>(smem + st * sbytes);
+                        const bool ok = abort_sh || tc::mbar_wait(&bar_full[st], (cg / (uint32_t)NS) & 1);
+                        const bool fail = __syncthreads_or(!ok);
+                        if (fail) {
+                            if (tid == 0) {
+                                atomicExch(a.status, 1);
+                                abort_sh = 1;
+                            }
+                        } else if (!abort_sh) {
+                            split_row_tf32(Ahi, Ahi + TM * KC, tid);
+                            tc::fence_proxy_async_shared();
+                        }
+                        __syncthreads();
+                    }
                     if (j >= 0 && tid == 0 && !abort_sh) {
                         const int c = j < n0 ? 0 : 1;
                         const bool first = j == 0 || j == n0;
@@ -631,9 +664,9 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             long long t2 = timing ? clock64() : 0;
             flag |= nflag && !dead;
             if (!is_root) {
-                float* stg_hi = reinterpret_cast<float*>(smem);               // stage 0 as staging tile
-                float* stg_lo = stg_hi + TM * SC;
-                epi_store<2>(ns2, W, scl, stg_hi, stg_lo, tid, &map_shi, &map_slo, (int)(vrow_cta + (int64_t)vs * TM));
+                // stage 0 holds the two staging tiles
+                epi_store<2>(ns2, W, scl, reinterpret_cast<float*>(smem), tid, &map_vst,
+                             (int)(vrow_cta + (int64_t)vs * TM));
                 Esh[vs * TM + tid] = E;
             } else if (fam >= 0) {
                 double o = NAN;
@@ -805,7 +838,7 @@ cudaError_t launch_prune_tc(const TcMaps& m, const PruneTcArgs& a, int n_ctas, s
     if (a.n_tiles <= 0) return cudaSuccess;
     if (smem > (size_t)prune_tc_max_smem()) return cudaErrorInvalidValue;
     if (a.stages < 1 || a.stages > MAXST) return cudaErrorInvalidValue;
-    k_prune_tc<<<n_ctas, NTHREADS, smem, s>>>(m.mat_hi, m.mat_lo, m.vec_hi, m.vec_lo, m.vst_hi, m.vst_lo, a);
+    k_prune_tc<<<n_ctas, NTHREADS, smem, s>>>(m.mat_hi, m.mat_lo, m.vec, m.vst, a);
     return cudaGetLastError();
 }
 

@@ -148,11 +148,11 @@ struct Workspace {
         int cols = 0;
         int box = 0;
         CUtensorMap map;
-    } map_cache[6];
+    } map_cache[4];
     DevBuf scratch, tiles, mats, cat, fam_lnl, total, nfail, jobs, catp;
     PinnedBuf h_tiles, h_mats, h_jobs, h_out, h_catp;
     // tensor-core path
-    DevBuf tc_hi, tc_lo, tc_mi, tc_vhi, tc_vlo, conv, flags, fb_perm, tiles64, tiles_fb, parts, fb_count, phase,
+    DevBuf tc_hi, tc_lo, tc_mi, tc_vec, conv, flags, fb_perm, tiles64, tiles_fb, parts, fb_count, phase,
         catids;
     PinnedBuf h_conv, h_mi, h_flags, h_tiles64, h_tiles_fb, h_tail, h_catids;
     // FP64 bins walked one family per cluster

@@ -53,6 +53,8 @@ CAFE_DEV void tma_store_2d(const CUtensorMap* map, int x, int y, const void* src
 CAFE_DEV void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 // The shared-memory sources of this thread's bulk stores may be reused.
 CAFE_DEV void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// At most one of this thread's bulk store groups still reads shared memory.
+CAFE_DEV void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
 // This thread's bulk stores are complete in global memory.
 CAFE_DEV void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 CAFE_DEV void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
