@@ -35,6 +35,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -70,6 +71,8 @@ def parse():
                     help="skip the p-value measurement")
     ap.add_argument("--no-config3", dest="config3", action="store_false",
                     help="skip the config-3 batched-candidates measurement")
+    ap.add_argument("--no-config0", dest="config0", action="store_false",
+                    help="skip the config-0 (plain FP64 base model, dedupe, Nelder-Mead fit) measurement")
     ap.add_argument("--no-config2", dest="config2", action="store_false",
                     help="skip the config-2 (two lambdas, error model, S-bins to 512) measurement")
     ap.add_argument("--no-autotune", action="store_true",
@@ -515,6 +518,81 @@ def config2_phase(ctx, torch, stream, flush, steps: int = 4, B: int = 4):
                     "tensor-core bins, other_ms = TF32 conversion + FP64 cluster walk of the bins above 256"}
 
 
+def config0_phase(ctx, cpu_seconds: float, reps: int = 10):
+    """The plain base model in FP64: 12-taxon tree (root age 100), 1,000
+    families, single lambda, the reference's global S and R, uniform prior.
+    Latency of one score through the public API (host counts resident,
+    per-family lnL back to the host) for FP64_REF with and without the
+    reference's dedupe and for MIXED_TF32X3; the Nelder-Mead fit of lambda
+    (cafe_optimize: the host search, each evaluation one FP64_REF score on
+    the GPU) and, as the CPU baseline, the same search (cafe_nelder_mead)
+    over the oracle port's score on all host cores."""
+    from cafe5_gb300 import _lib, engine
+    from cafe5_gb300.inputs import RootPrior
+    import ctypes
+    w = workload_cfg(0)
+    F = w.families.n_families
+    S, R = global_bounds(w.families)
+    root_prior = RootPrior.uniform(R)
+    prior = root_prior.vector()
+    tid = ctx.upload_tree(w.tree)
+    sid = ctx.upload_families(tid, w.families.counts)
+    ctx.set_prior(prior)
+    ctx.set_error_model(None)
+    out = {"workload": w.name, "families": F, "taxa": 12, "S": S, "R": R}
+    for name, kw in (("fp64_ref", dict(precision="fp64_ref", S=S, R=R, dedupe=False)),
+                     ("fp64_ref_dedupe", dict(precision="fp64_ref", S=S, R=R, dedupe=True)),
+                     ("mixed_tf32x3", dict(precision="mixed_tf32x3"))):
+        ctx.score(tid, sid, [0.0025], **kw)
+        ts = []
+        for i in range(reps):
+            t0 = time.perf_counter()
+            r = ctx.score(tid, sid, [0.0025 * (1.0 + 1e-4 * (i + 1))], **kw)
+            ts.append((time.perf_counter() - t0) * 1e3)
+        med = float(np.median(ts))
+        out[name] = {"ms_per_score": med, "evals_per_s": F / (med / 1e3), "neg_lnl": r.total}
+    ctx.free_families(sid)
+    longest = max(w.tree.branch_length[v] for v in range(w.tree.n_nodes) if w.tree.parent[v] >= 0)
+    lam = engine.SingleLambda(0.01)
+    model = engine.BaseModel(lam, w.tree, w.families, S, R, ctx=ctx)
+    scorer = engine.LambdaOptimizerScorer(lam, model, root_prior, longest)
+    t0 = time.perf_counter()
+    res = engine.Optimizer(scorer).optimize(initial=[0.01])
+    fit = {"lambda": res.values[0], "neg_lnl": res.score, "iterations": res.num_iterations,
+           "evaluations": res.evaluations, "wall_ms": (time.perf_counter() - t0) * 1e3}
+    out["nm_fit_gpu"] = fit
+    if cpu_seconds > 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        ta = oracle.TreeArrays.from_tree(w.tree)
+        counts = np.ascontiguousarray(w.families.counts)
+        threads = os.cpu_count() or 1
+
+        def objective(xp, n, user):
+            x = xp[0]
+            if not x > 0:
+                return float("inf")
+            tot, _, _ = oracle.score(ta, counts, [x], prior=prior, S=S, R=R, dedupe=True, n_threads=threads)
+            return float("inf") if math.isnan(tot) else float(tot)
+
+        lib = _lib.load()
+        x0 = np.array([0.01])
+        best = np.zeros(1)
+        cfg = _lib.OptConfig(_lib.OPT_LAMBDA, 1, x0.ctypes.data, 300, 1.0, 2.0)
+        r = _lib.OptResult(best.ctypes.data, 0.0, 0, 0, 0)
+        cb = _lib.OBJECTIVE(objective)
+        t0 = time.perf_counter()
+        first = objective(x0.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 1, None)
+        rc = lib.cafe_nelder_mead(ctypes.byref(cfg), cb, None, ctypes.byref(r))
+        wall = (time.perf_counter() - t0) * 1e3
+        out["nm_fit_cpu_port"] = {"lambda": float(best[0]), "neg_lnl": r.score, "iterations": r.iterations,
+                                  "evaluations": r.evaluations + 1, "wall_ms": wall, "status": rc,
+                                  "cores": threads, "kind": "port", "initial_score": first}
+        out["fit_speedup_vs_cpu_port"] = wall / fit["wall_ms"]
+        out["same_fit"] = bool(float(best[0]) == fit["lambda"])
+    return out
+
+
 def reconstruction_phase(ctx, tid, sid, w, fams, S, R, cpu_seconds: float, reps: int = 3):
     """Pupko joint reconstruction of every family x gamma category at the
     reference's global bounds (cafe_reconstruct): the log2-filtered kernel,
@@ -755,6 +833,12 @@ def run_ours(args):
         cfg2 = config2_phase(ctx, torch, stream, flush)
         ctx.set_prior(prior)
 
+    cfg0 = None
+    if rank == 0 and args.config0:
+        cfg0 = config0_phase(ctx, args.cpu_seconds)
+        ctx.set_prior(prior)
+        ctx.set_error_model(None)
+
     stream4 = None
     if rank == 0 and args.serving_optimizers > 0:
         stream4 = serving_stream(ctx, args.serving_optimizers)
@@ -822,6 +906,7 @@ def run_ours(args):
                 "serving_stream": stream4,
                 "config3_batched": cfg3,
                 "config2_local_lambdas_error_model": cfg2,
+                "config0_base_fp64_fit": cfg0,
                 "reconstruction": recon,
                 "pvalues": pvals,
                 "gpu_launches": int(round(prof["launches"] / prof_steps * args.steps)),

@@ -839,7 +839,7 @@ int launch_fp64_cluster(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeH
         std::memcpy(&b, &a, sizeof b);   // padding included: the bytes are a graph signature
         b.tiles = ws.tiles_cl.as<PruneTile>() + i;
         b.n_tiles = (int)(j - i);
-        b.W = tiles[i].S + 1;
+        b.W = std::max(tiles[i].S + 1, tiles[i].R);
         const int cl = fp64_cluster_size(b.W);
         const int n_cl = (int)std::min<int64_t>((int64_t)(j - i), (int64_t)C->sm_count * 8);
         CK(op_launch(ws, 8, [&] { return launch_prune64_cluster(b, cl, n_cl, st); }, b, cl, n_cl, st),
@@ -1492,15 +1492,17 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     if (ref_mode) {
         const int64_t nf = dedupe ? (int64_t)S.unique.size() : F;
         d_perm = dedupe ? S.d_unique.as<int64_t>() : S.d_identity.as<int64_t>();
+        // few families: one per cluster (the same bits as the tile walk)
+        const bool cl = fp64_cluster_bin(C, T, nf, K, W);
         for (int c : active)
-            for (int64_t i = 0; i < nf; i += TFm) {
+            for (int64_t i = 0; i < nf; i += cl ? 1 : TFm) {
                 PruneTile t{};
                 t.first = (int)i;
-                t.count = (int)std::min<int64_t>(TFm, nf - i);
+                t.count = cl ? 1 : (int)std::min<int64_t>(TFm, nf - i);
                 t.k = c;
                 t.S = Sg;
                 t.R = Rg;
-                tiles.push_back(t);
+                (cl ? cl_tiles : tiles).push_back(t);
             }
     } else {
         d_perm = S.bins.d_perm.as<int64_t>();
