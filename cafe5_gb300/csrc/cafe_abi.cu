@@ -174,6 +174,7 @@ Workspace::~Workspace() {
     if (ev_stop) cudaEventDestroy(ev_stop);
     if (ev_staged) cudaEventDestroy(ev_staged);
     if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_jobs) cudaEventDestroy(ev_jobs);
     for (int q = 0; q < kAux; ++q) {
         if (aux[q]) cudaStreamDestroy(aux[q]);
         if (ev_join[q]) cudaEventDestroy(ev_join[q]);
@@ -186,6 +187,7 @@ int Workspace::init(int device) {
     if (cudaEventCreate(&ev_stop) != cudaSuccess) return CAFE_ERR_CUDA;
     if (cudaEventCreateWithFlags(&ev_staged, cudaEventDisableTiming) != cudaSuccess) return CAFE_ERR_CUDA;
     if (cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming) != cudaSuccess) return CAFE_ERR_CUDA;
+    if (cudaEventCreateWithFlags(&ev_jobs, cudaEventDisableTiming) != cudaSuccess) return CAFE_ERR_CUDA;
     for (int q = 0; q < kAux; ++q) {
         if (cudaStreamCreateWithFlags(&aux[q], cudaStreamNonBlocking) != cudaSuccess) return CAFE_ERR_CUDA;
         if (cudaEventCreateWithFlags(&ev_join[q], cudaEventDisableTiming) != cudaSuccess) return CAFE_ERR_CUDA;
@@ -443,17 +445,15 @@ struct PendingJobs {
 };
 
 void cache_reset(cafe_ctx* C) {
-    for (auto& sl : C->slabs) cudaFree(sl.p);
+    for (auto& sl : C->slabs) {
+        cudaFree(sl.p);
+        if (sl.ev_alloc) cudaEventDestroy(sl.ev_alloc);
+    }
     C->slabs.clear();
     for (cudaEvent_t e : C->batch_events) cudaEventDestroy(e);
     C->batch_events.clear();
     C->cache.clear();
     C->cache_bytes = 0;
-}
-
-double* cache_lookup(cafe_ctx* C, const MatKey& k) {
-    const MatEntry* e = C->cache.find(k);
-    return e ? e->d : nullptr;
 }
 
 int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P);
@@ -476,6 +476,15 @@ int cache_build(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
 int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
     const size_t n = P.keys.size();
     if (!n) return CAFE_OK;
+    // builds run on the request's stream (K1 beside the pruning of an earlier
+    // request takes shared memory the tensor-core CTAs need: slower overall);
+    // users on other streams wait on the ready event below
+    const cudaStream_t bs = ws.stream;
+    AllocScope scope(bs);
+    if (ws.jobs_pending) {   // the previous build's copy out of h_jobs has run
+        CK(cudaEventSynchronize(ws.ev_jobs), "jobs");
+        ws.jobs_pending = false;
+    }
     size_t total = 0;
     int max_size = 0;
     for (auto& k : P.keys) {
@@ -492,9 +501,13 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
         CK(t_alloc_stream ? cudaMallocAsync(&sl.p, sl.size, t_alloc_stream) : cudaMalloc(&sl.p, sl.size),
            "matrix cache");
         sl.used = 0;
+        CK(cudaEventCreateWithFlags(&sl.ev_alloc, cudaEventDisableTiming), "event");
+        CK(cudaEventRecord(sl.ev_alloc, bs), "event");
         C->slabs.push_back(sl);
     }
     Slab& slab = C->slabs.back();
+    // a slab another workspace allocated is written only after its allocation
+    CK(cudaStreamWaitEvent(bs, slab.ev_alloc, 0), "event");
     void* chunk = static_cast<char*>(slab.p) + slab.used;
     slab.used += need;
     C->cache_bytes += total;
@@ -518,17 +531,21 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
         P.entries[i]->chunk = batch;
         cur += (size_t)k.size * k.size * sizeof(double);
     }
-    CK(cudaMemcpyAsync(ws.jobs.p, J, n * sizeof(MatrixJob), cudaMemcpyHostToDevice, ws.stream), "jobs");
+    CK(cudaMemcpyAsync(ws.jobs.p, J, n * sizeof(MatrixJob), cudaMemcpyHostToDevice, bs), "jobs");
+    if (ws.ev_jobs) {
+        CK(cudaEventRecord(ws.ev_jobs, bs), "event");
+        ws.jobs_pending = true;
+    }
     const bool prof = ws.sync;
     cudaEvent_t ev;
-    if (prof) C->prof.begin(0, ws.stream, &ev);
-    CK(launch_matrix_build(ws.jobs.as<MatrixJob>(), (int)n, max_size, ws.stream), "matrix build");
+    if (prof) C->prof.begin(0, bs, &ev);
+    CK(launch_matrix_build(ws.jobs.as<MatrixJob>(), (int)n, max_size, bs), "matrix build");
     if (prof) {
-        C->prof.end(0, ws.stream, ev);
+        C->prof.end(0, bs, ev);
         C->prof.acc.matrices_built += (int64_t)n;
     }
-    // requests on other streams order themselves after this build
-    CK(cudaEventRecord(ready, ws.stream), "event");
+    // every stream that reads these matrices orders itself after this build
+    CK(cudaEventRecord(ready, bs), "event");
     P.keys.clear();
     P.entries.clear();
     return CAFE_OK;
@@ -2571,10 +2588,11 @@ int cafe_matrix_get(cafe_ctx* C, double lambda, double branch_length, int matrix
     if (!C || !out || matrix_size < 1) return fail(C, CAFE_ERR_INVALID, "bad matrix_get arguments");
     std::lock_guard<std::mutex> lk(C->mu);
     cudaSetDevice(C->device);
-    double* d = cache_lookup(C, make_key(matrix_size, lambda, branch_length));
-    if (!d)
+    const MatEntry* e = C->cache.find(make_key(matrix_size, lambda, branch_length));
+    if (!e || !e->d)
         return fail(C, CAFE_ERR_MISSING_MATRIX, "Failed to find matrix for %d,%g,%g", matrix_size, branch_length, lambda);
-    CK(cudaMemcpy(out, d, (size_t)matrix_size * matrix_size * sizeof(double), cudaMemcpyDeviceToHost), "matrix_get");
+    CK(cudaEventSynchronize(C->batch_events[e->chunk]), "matrix_get");   // its build has run
+    CK(cudaMemcpy(out, e->d, (size_t)matrix_size * matrix_size * sizeof(double), cudaMemcpyDeviceToHost), "matrix_get");
     return CAFE_OK;
 }
 

@@ -129,6 +129,7 @@ class MatCache {
 struct Slab {
     void* p = nullptr;
     size_t size = 0, used = 0;
+    cudaEvent_t ev_alloc = nullptr;   // after its stream-ordered allocation
 };
 
 // Per-request device workspace (one per stream).
@@ -138,6 +139,8 @@ struct Workspace {
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     cudaEvent_t ev_staged = nullptr;   // after the last request's host->device staging copies
     bool staged = false;
+    cudaEvent_t ev_jobs = nullptr;     // after the last build's job-table copy out of h_jobs
+    bool jobs_pending = false;
     static constexpr int kAux = 3;     // streams for concurrent per-bin launches
     cudaStream_t aux[kAux] = {nullptr, nullptr, nullptr};
     cudaEvent_t ev_fork = nullptr;
