@@ -494,10 +494,11 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
     // (16-candidate config-1 steps: 3.43 -> 3.24 ms); a larger one runs in
     // line, since streaming gigabytes of matrices beside the pruning evicts
     // its working set from L2 (64-candidate K = 8 rounds: 116 -> 127 ms).
-    // Profiled calls build in line, so each kernel is timed alone. Slab and
+    // Synchronous calls build in line (nothing of theirs to hide behind), and
+    // so do profiled calls, so each kernel is timed alone. Slab and
     // job-table growth follow the build's stream; every user of the
     // matrices waits on the ready event below.
-    const bool beside = ws.build && !(C->prof.on && ws.sync) && total <= ((size_t)256 << 20);
+    const bool beside = ws.build && !ws.build_inline && !(C->prof.on && ws.sync) && total <= ((size_t)256 << 20);
     const cudaStream_t bs = beside ? ws.build : ws.stream;
     AllocScope scope(bs);
     if (ws.jobs_pending) {   // the previous build's copy out of h_jobs has run
@@ -1732,6 +1733,12 @@ int score_complete(cafe_ctx* C, Workspace& ws, const cafe_request* R, int NB, ca
 
 int score_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, int NB, cafe_result* res) {
     ScoreInfo info;
+    // nothing of this workspace is in flight for a build to hide behind
+    struct Inline {
+        Workspace& w;
+        explicit Inline(Workspace& x) : w(x) { w.build_inline = true; }
+        ~Inline() { w.build_inline = false; }
+    } in_line(ws);
     int rc = score_enqueue(C, ws, R, NB, res, &info);
     if (rc) return rc;
     return score_complete(C, ws, R, NB, res, info);

@@ -140,6 +140,7 @@ struct Workspace {
     cudaEvent_t ev_staged = nullptr;   // after the last request's host->device staging copies
     bool staged = false;
     cudaStream_t build = nullptr;      // K1 builds (overlap the previous request's pruning)
+    bool build_inline = false;         // this call builds on `stream` (synchronous calls)
     cudaEvent_t ev_jobs = nullptr;     // after the last build's job-table copy out of h_jobs
     bool jobs_pending = false;
     static constexpr int kAux = 3;     // streams for concurrent per-bin launches
