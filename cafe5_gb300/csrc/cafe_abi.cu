@@ -501,7 +501,7 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
     const bool beside = ws.build && !ws.build_inline && !(C->prof.on && ws.sync) && total <= ((size_t)256 << 20);
     const cudaStream_t bs = beside ? ws.build : ws.stream;
     AllocScope scope(bs);
-    if (ws.jobs_pending) {   // the previous build's copy out of h_jobs has run
+    if (ws.jobs_pending) {   // the previous build has read h_jobs and ws.jobs
         CK(cudaEventSynchronize(ws.ev_jobs), "jobs");
         ws.jobs_pending = false;
     }
@@ -546,10 +546,6 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
         cur += (size_t)k.size * k.size * sizeof(double);
     }
     CK(cudaMemcpyAsync(ws.jobs.p, J, n * sizeof(MatrixJob), cudaMemcpyHostToDevice, bs), "jobs");
-    if (ws.ev_jobs) {
-        CK(cudaEventRecord(ws.ev_jobs, bs), "event");
-        ws.jobs_pending = true;
-    }
     const bool prof = ws.sync;
     cudaEvent_t ev;
     if (prof) C->prof.begin(0, bs, &ev);
@@ -557,6 +553,13 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
     if (prof) {
         C->prof.end(0, bs, ev);
         C->prof.acc.matrices_built += (int64_t)n;
+    }
+    // h_jobs and ws.jobs stay untouched until this build has read them (the
+    // next build may run on the other stream, so stream order alone does
+    // not protect a reallocation of ws.jobs)
+    if (ws.ev_jobs) {
+        CK(cudaEventRecord(ws.ev_jobs, bs), "event");
+        ws.jobs_pending = true;
     }
     // every stream that reads these matrices orders itself after this build
     CK(cudaEventRecord(ready, bs), "event");

@@ -141,7 +141,7 @@ struct Workspace {
     bool staged = false;
     cudaStream_t build = nullptr;      // K1 builds (overlap the previous request's pruning)
     bool build_inline = false;         // this call builds on `stream` (synchronous calls)
-    cudaEvent_t ev_jobs = nullptr;     // after the last build's job-table copy out of h_jobs
+    cudaEvent_t ev_jobs = nullptr;     // after the last build (its job table read)
     bool jobs_pending = false;
     static constexpr int kAux = 3;     // streams for concurrent per-bin launches
     cudaStream_t aux[kAux] = {nullptr, nullptr, nullptr};
