@@ -278,3 +278,39 @@ def test_families_update_rebuilds_derived_tables(ctx):
         f = ctx.score(tid, sid2, [0.002], model=1, multipliers=w.multipliers, cat_probs=w.cat_probs,
                       precision=pr, S=S, R=R)
         assert np.array_equal(e.family_lnl, f.family_lnl)
+
+
+def test_back_to_back_device_calls_match_synchronous_calls(ctx):
+    """Device-pointer calls issued back to back build each call's matrices on
+    a build stream while the previous call still prunes, and alternate
+    between two workspaces; every call's per-family lnL and total equal the
+    same request scored synchronously (matrices built in line), bit for bit,
+    in both precisions."""
+    import torch
+    from cafe5_gb300.inputs import RootPrior
+    from cafe5_gb300.synth import workload
+    w = workload(1, n_families=3000, seed=38)
+    tid, sid = _setup(ctx, w.tree, w.families.counts, prior=RootPrior.uniform(400).vector())
+    F = w.families.n_families
+    B, steps = 4, 6
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    for precision in ("mixed_tf32x3", "fp64_binned"):
+        kw = dict(model=1, precision=precision)
+        cands = [[dict(lambdas=[0.002 * (1 + 0.01 * b) * (1 + 1e-5 * (s + 1) + (0.1 if precision == "fp64_binned" else 0))],
+                       multipliers=w.multipliers, cat_probs=w.cat_probs) for b in range(B)] for s in range(steps)]
+        fam = [torch.empty(B * F, dtype=torch.float64, device=dev) for _ in range(steps)]
+        tot = [torch.empty(B, dtype=torch.float64, device=dev) for _ in range(steps)]
+        with torch.cuda.stream(stream):
+            for s in range(steps):
+                ctx.score_batch_device(tid, sid, cands[s], fam[s].data_ptr(), tot[s].data_ptr(), stream.cuda_stream,
+                                       **kw)
+        stream.synchronize()
+        for s in range(steps):
+            ref = ctx.score_batch(tid, sid, cands[s], **kw)
+            got = fam[s].view(B, F).cpu().numpy()
+            got_tot = tot[s].cpu().numpy()
+            for b in range(B):
+                assert np.array_equal(got[b], ref[b].family_lnl), (precision, s, b)
+                assert got_tot[b] == ref[b].total, (precision, s, b)
+    ctx.free_families(sid)
