@@ -116,8 +116,11 @@ def _keep_nonzero(counts: np.ndarray) -> np.ndarray:
     return counts[counts.max(axis=1) > 0]
 
 
-def workload(config: int, n_families: Optional[int] = None, seed: int = 0) -> Workload:
-    """Synthetic stand-ins for the five benchmark configurations."""
+def workload(config: int, n_families: Optional[int] = None, seed: int = 0, gamma=None) -> Workload:
+    """Synthetic stand-ins for the five benchmark configurations. `gamma(alpha,
+    K)` -> (probabilities, multipliers) is get_gamma (the library's by
+    default); a caller that must not load the library passes its own."""
+    gamma = gamma or discrete_gamma
     if config == 0:
         tree = yule_tree(12, 100.0, seed)
         F = n_families or 1000
@@ -133,7 +136,7 @@ def workload(config: int, n_families: Optional[int] = None, seed: int = 0) -> Wo
     if config == 1:
         tree = yule_tree(24, 150.0, seed)
         F = n_families or 10000
-        probs, mult = discrete_gamma(0.5, 4)
+        probs, mult = gamma(0.5, 4)
         rng = np.random.default_rng(seed + 1)
         k = rng.integers(0, 4, F)
         lam = 0.002 * np.asarray(mult)[k]
@@ -182,7 +185,7 @@ def workload(config: int, n_families: Optional[int] = None, seed: int = 0) -> Wo
     if config == 3:
         tree = yule_tree(48, 200.0, seed)
         F = n_families or 20000
-        probs, mult = discrete_gamma(0.5, 8)
+        probs, mult = gamma(0.5, 8)
         rng = np.random.default_rng(seed + 1)
         k = rng.integers(0, 8, F)
         lam = 0.002 * np.asarray(mult)[k]

@@ -14,13 +14,35 @@
 #include <omp.h>
 #endif
 
-/* src/probability.cpp:82-91. The reference serves n, r < 100 from a cache
- * and n < 1024 from an lgamma table (probability.cpp:55-80); both hold the
- * same libm lgamma values used here directly. */
+/* src/probability.cpp:55-91. The reference serves lgamma(n) for integral
+ * 0 <= n < 1024 from a table (lgamma2, init_lgamma_cache) and chooseln(n,
+ * r) for integral n, r < 100 from a second table built from the first.
+ * Both tables hold the values of the direct libm expressions, so caching
+ * here changes speed only: the tables are filled once when the library is
+ * loaded, and the sum is formed in the same order as the direct form. */
+#define G_LGAMMA_N 1024
+#define G_CHOOSE_N 100
+static double g_lgamma_tab[G_LGAMMA_N];
+static double g_choose_tab[G_CHOOSE_N][G_CHOOSE_N];
+
+static double g_lgamma2(double n) {
+    if (n >= 0 && n < G_LGAMMA_N && (n - (int)n < 0.00000000001)) return g_lgamma_tab[(int)n];
+    return lgamma(n);
+}
+
+__attribute__((constructor)) static void g_tables_init(void) {
+    for (int i = 0; i < G_LGAMMA_N; i++) g_lgamma_tab[i] = lgamma(i);
+    for (int i = 0; i < G_CHOOSE_N; i++)
+        for (int j = 0; j < G_CHOOSE_N; j++)
+            g_choose_tab[i][j] = g_lgamma2(i + 1) - g_lgamma2(j + 1) - g_lgamma2(i - j + 1);
+}
+
 double oracle_chooseln(double n, double r) {
     if (r == 0 || (n == 0 && r == 0)) return 0;
     if (n <= 0 || r <= 0) return log(0.0);
-    return lgamma(n + 1) - lgamma(r + 1) - lgamma(n - r + 1);
+    if (n < G_CHOOSE_N && r < G_CHOOSE_N && (n - (int)n < 0.00000000001) && (r - (int)r < 0.00000000001))
+        return g_choose_tab[(int)n][(int)r];
+    return g_lgamma2(n + 1) - g_lgamma2(r + 1) - g_lgamma2(n - r + 1);
 }
 
 /* src/probability.cpp:104-148: Eqn (1) of Hahn et al. 2005, one exp and
@@ -47,6 +69,127 @@ double oracle_transition(double lambda, double t, int s, int c) {
     double coeff = 1 - 2 * alpha;
     if (coeff > 0 && coeff != 1) return oracle_bd_rate(s, c, log(alpha), coeff);
     return 0.0;
+}
+
+/* ---- gamma discretisation (src/gamma.cpp) ----
+ * Published algorithms (Applied Statistics AS 70, AS 32, AS 91) in the
+ * order of operations the reference evaluates them. */
+
+/* AS 70, src/gamma.cpp:187-203: rational approximation of the standard
+ * normal quantile in y = sqrt(ln(1 / p1^2)). */
+static double g_normal_quantile(double p) {
+    static const double num[5] = {-.322232431088, -1.0, -.342242088547, -.0204231210245, -.453642210148e-4};
+    static const double den[5] = {.0993484626060, .588581570495, .531103462366, .103537752850, .0038560700634};
+    double p1 = p < 0.5 ? p : 1 - p;
+    if (p1 < 1e-20) return -9999;
+    double y = sqrt(log(1 / (p1 * p1)));
+    double n = num[4], d = den[4];
+    for (int i = 3; i >= 0; i--) {
+        n = n * y + num[i];
+        d = d * y + den[i];
+    }
+    double z = y + n / d;
+    return p < 0.5 ? -z : z;
+}
+
+/* AS 32, src/gamma.cpp:66-125: I(x, p) by the series when x <= 1 or x < p,
+ * else by the continued fraction (its convergents as the ratio of two
+ * recurrences, both scaled down by 1e30 when they grow past it). The
+ * continued fraction stops when two successive convergents agree within
+ * 1e-8 absolute and relative, and returns with the earlier one. */
+static double g_incomplete_gamma(double x, double p, double lng) {
+    const double accurate = 1e-8, overflow = 1e30;
+    if (x == 0) return 0;
+    if (x < 0 || p <= 0) return -1;
+    double factor = exp(p * log(x) - x - lng);
+    if (!(x > 1 && x >= p)) {
+        double gin = 1, term = 1, rn = p;
+        for (;;) {
+            rn += 1;
+            term *= x / rn;
+            gin += term;
+            if (!(term > accurate)) break;
+        }
+        return gin * (factor / p);
+    }
+    double a = 1 - p, b = a + x + 1, term = 0;
+    double pn[6] = {1, x, x + 1, x * (a + x + 1), 0, 0};
+    double gin = pn[2] / pn[3];
+    for (;;) {
+        a += 1;
+        b += 2;
+        term += 1;
+        double an = a * term;
+        pn[4] = b * pn[2] - an * pn[0];
+        pn[5] = b * pn[3] - an * pn[1];
+        if (pn[5] != 0) {
+            double rn = pn[4] / pn[5];
+            double dif = fabs(gin - rn);
+            if (dif <= accurate && dif <= accurate * rn) return 1 - factor * gin;
+            gin = rn;
+        }
+        memmove(pn, pn + 2, 4 * sizeof(double));
+        if (!(fabs(pn[2]) < overflow))
+            for (int i = 0; i < 4; i++) pn[i] /= overflow;
+    }
+}
+
+/* AS 91, src/gamma.cpp:138-185: chi-square(v) quantile; a starting value
+ * (small v against -ln p, v <= 0.32 by Newton steps, else Wilson-Hilferty
+ * through AS 70) refined by seventh-order steps on AS 32 until the
+ * relative change is at most 5e-7. */
+static double g_chi2_quantile(double prob, double v) {
+    const double e = .5e-6, aa = .6931471805;
+    if (prob < .000002 || prob > .999998 || v <= 0) return -1;
+    double g = lgamma(v / 2), xx = v / 2, c = xx - 1, ch;
+    if (v < -1.24 * log(prob)) {
+        ch = pow((prob * xx * exp(g + xx * aa)), 1 / xx);
+        if (ch - e < 0) return ch;
+    } else if (v <= .32) {
+        double a = log(1 - prob), q;
+        ch = 0.4;
+        do {
+            q = ch;
+            double p1 = 1 + ch * (4.67 + ch);
+            double p2 = ch * (6.73 + ch * (6.66 + ch));
+            double t = -0.5 + (4.67 + 2 * ch) / p1 - (6.73 + ch * (13.32 + 3 * ch)) / p2;
+            ch -= (1 - exp(a + g + .5 * ch + c * aa) * p2 / p1) / t;
+        } while (fabs(q / ch - 1) - .01 > 0);
+    } else {
+        double x = g_normal_quantile(prob), p1 = 0.222222 / v;
+        ch = v * pow((x * sqrt(p1) + 1 - p1), 3.0);
+        if (ch > 2.2 * v + 6) ch = -2 * (log(1 - prob) - c * log(.5 * ch) + g);
+    }
+    for (;;) {
+        double q = ch, p1 = .5 * ch, t = g_incomplete_gamma(p1, xx, g);
+        if (t < 0) return -1;
+        double p2 = prob - t;
+        t = p2 * exp(xx * aa + g + p1 - c * log(ch));
+        double b = t / ch, a = 0.5 * t - b * c;
+        double s1 = (210 + a * (140 + a * (105 + a * (84 + a * (70 + 60 * a))))) / 420;
+        double s2 = (420 + a * (735 + a * (966 + a * (1141 + 1278 * a)))) / 2520;
+        double s3 = (210 + a * (462 + a * (707 + 932 * a))) / 2520;
+        double s4 = (252 + a * (672 + 1182 * a) + c * (294 + a * (889 + 1740 * a))) / 5040;
+        double s5 = (84 + 264 * a + c * (175 + 606 * a)) / 2520;
+        double s6 = (120 + c * (346 + 127 * c)) / 5040;
+        ch += t * (1 + 0.5 * t * s1 - b * c * (s1 - b * (s2 - b * (s3 - b * (s4 - b * (s5 - b * s6))))));
+        if (!(fabs(q / ch - 1) > e)) return ch;
+    }
+}
+
+/* src/gamma.cpp:15-52 (median = 1) as get_gamma calls it (:225-241):
+ * rate k = the Gamma(alpha, alpha) quantile at (2k + 1) / 2K, i.e.
+ * point_chi2(., 2 alpha) / (2 alpha), rescaled so the rates sum to K. */
+int oracle_discrete_gamma(int K, double alpha, double* probs, double* multipliers) {
+    if (K < 1 || !(alpha > 0)) return -1;
+    double beta = alpha, gap05 = 1.0 / (2.0 * K), factor = alpha / beta * K, t = 0;
+    for (int i = 0; i < K; i++) multipliers[i] = g_chi2_quantile((i * 2.0 + 1) * gap05, 2.0 * alpha) / (2.0 * beta);
+    for (int i = 0; i < K; i++) t += multipliers[i];
+    for (int i = 0; i < K; i++) {
+        multipliers[i] *= factor / t;
+        probs[i] = 1.0 / K;
+    }
+    return 0;
 }
 
 /* src/matrix_cache.h:49-62: matrices are computed at lambda truncated to

@@ -42,6 +42,14 @@ void oracle_fill_matrix(double lambda, double t, int size, double* out);
 void oracle_multiply(const double* m, int size, const double* v, int s_min, int s_max,
                      int c_min, int c_max, double* result);
 
+/* get_gamma (src/gamma.cpp:225-241 over discrete_gamma, :15-52, with
+ * median = 1 and beta = alpha): K category probabilities (1/K each) and the
+ * median rate multipliers, through AS 91 (point_chi2), AS 32
+ * (incomplete_gamma) and AS 70 (point_normal), step for step so the
+ * multipliers carry the reference's bits. Returns 0, or -1 for alpha <= 0
+ * or K < 1. */
+int oracle_discrete_gamma(int K, double alpha, double* probs, double* multipliers);
+
 /* Prunes one family with matrices given per node (node_matrix[i] is the
  * size x size matrix of the branch above node i; unused for the root).
  * Writes the root vector (R values, index j <-> root size j+1). With

@@ -24,10 +24,20 @@ class _Tree(C.Structure):
                 ("lambda_index", C.c_void_p), ("leaf_col", C.c_void_p)]
 
 
+def reference_dir() -> Optional[str]:
+    """The CAFE5 reference checkout the `ref` recipe compiles: the directory
+    named by the CAFE_REFERENCE environment variable, else the checkout this
+    build's fixtures came from when it exists; None when neither is there
+    (then only the restatement is built)."""
+    d = os.environ.get("CAFE_REFERENCE") or "/root/reference"
+    return d if os.path.isdir(os.path.join(d, "src")) else None
+
+
 def build(ref: bool = False) -> None:
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if ref and os.path.isdir("/root/reference/src"):
-        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref"], check=True)
+    d = reference_dir()
+    if ref and d:
+        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", f"REF={d}"], check=True)
 
 
 def lib():
@@ -48,6 +58,8 @@ def lib():
         _lib.oracle_fill_matrix.argtypes = [d, d, i, p]
         _lib.oracle_quantize.argtypes = [d, d, p, p]
         _lib.oracle_multiply.argtypes = [p, i, p, i, i, i, i, p]
+        _lib.oracle_discrete_gamma.restype = i
+        _lib.oracle_discrete_gamma.argtypes = [i, d, p, p]
         _lib.oracle_prune.restype = i
         _lib.oracle_prune.argtypes = [C.POINTER(_Tree), p, p, i, p, i, i, i, i, i, p, p]
         _lib.oracle_score.restype = i
@@ -67,6 +79,18 @@ def lib():
 
 def _ptr(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data
+
+
+def discrete_gamma(alpha: float, K: int):
+    """(category probabilities, rate multipliers) of get_gamma for K median
+    categories -- the oracle's own restatement, bit for bit the reference's."""
+    if K <= 1:
+        return [1.0], [1.0]
+    probs = np.zeros(K)
+    mult = np.zeros(K)
+    if lib().oracle_discrete_gamma(K, float(alpha), probs.ctypes.data, mult.ctypes.data):
+        raise ValueError(f"discrete gamma needs alpha > 0 (got {alpha})")
+    return probs.tolist(), mult.tolist()
 
 
 def bd_rate(s, c, log_alpha, coeff):

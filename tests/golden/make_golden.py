@@ -17,9 +17,10 @@ tests, and stores inputs plus hex-float outputs:
   ref_simulations.json  the simulator action with the engine seeded: root
                      sizes and every simulated node size
 
-Only this script reads the reference (it needs /root/reference and the
-built harness); the tests read the committed JSON. Usage:
-    make -C oracle ref && python tests/golden/make_golden.py
+Only this script reads the reference (the checkout named by the
+CAFE_REFERENCE environment variable, and the harness built from it); the
+tests read the committed JSON. Usage:
+    CAFE_REFERENCE=<checkout> make -C oracle ref && python tests/golden/make_golden.py
 """
 from __future__ import annotations
 

@@ -25,3 +25,18 @@ def test_reference_arm_prints_the_contract_line():
     assert base["kind"] in ("port", "reference") and base["cores"] >= 1 and base["value"] == line["value"]
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_maps_only_the_oracle():
+    """The timed reference arm must not run any of the product: after a run,
+    the process has mapped the oracle's library and not libcafe_gb300.so
+    (the workload's gamma multipliers come from the oracle's get_gamma)."""
+    code = ("import sys, bench; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0', "
+            "'--families', '200', '--candidates', '2']; bench.main(); maps = open('/proc/self/maps').read(); "
+            "print('product=%d oracle=%d' % ('libcafe_gb300' in maps, 'libcafe_oracle' in maps))")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = r.stdout.strip().splitlines()
+    line = json.loads(out[-2])
+    assert line["config"]["candidates_per_step"] == 2 and line["config"]["families_per_gpu"] == 200
+    assert out[-1] == "product=0 oracle=1", out[-1]

@@ -166,6 +166,23 @@ def test_discrete_gamma_matches_reference():
         assert probs == [float.fromhex(x) for x in g["probs"]]
 
 
+def test_oracle_discrete_gamma_bits_match_reference():
+    """The oracle's own AS 91 / AS 32 / AS 70 restatement (used where the
+    library must not be loaded, e.g. the timed reference arm) carries the
+    reference's bits, and agrees with the library's over a sweep of shapes
+    that reaches every branch of AS 91 (small v, v <= 0.32, Wilson-Hilferty)
+    and both branches of AS 32."""
+    for g in load_json("ref_matrices.json")["gamma"]:
+        probs, mult = oracle.discrete_gamma(g["alpha"], g["K"])
+        assert [m.hex() for m in mult] == [float.fromhex(x).hex() for x in g["multipliers"]], (g["K"], g["alpha"])
+        assert probs == [float.fromhex(x) for x in g["probs"]]
+    for a in (0.02, 0.1, 0.16, 0.37, 0.5, 0.51, 1.0, 1.7, 3.3, 12.0, 80.0):
+        for K in (2, 3, 4, 5, 8, 16):
+            assert oracle.discrete_gamma(a, K) == discrete_gamma(a, K), (a, K)
+    with pytest.raises(ValueError):
+        oracle.discrete_gamma(0.0, 4)
+
+
 @pytest.mark.parametrize("case", CASES, ids=[c.name for c in CASES])
 def test_oracle_matches_reference_end_to_end(case):
     ta = oracle.TreeArrays.from_tree(case.tree, case.lambda_of_node)
