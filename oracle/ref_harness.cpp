@@ -155,6 +155,7 @@ void usage() {
         "   [--repeat N] [--quiet]\n"
         "   [--optimize lambda|alpha|lambda_alpha|lambda_epsilon --initial x1,..]\n"
         "   [--reconstruct] [--pvalues N_SIMULATIONS --seed S] [--simulate N --seed S]\n"
+        "   [--exclude-zero-root] [--estimate-bounds] [--dump-input]\n"
         "cafe_ref_harness nm rosen|wall|bowl|product <maxiters> x1,..\n");
 }
 
@@ -221,7 +222,7 @@ int main(int argc, char** argv) {
     std::vector<double> lambdas, gmult, gprob;
     double alpha = -1;
     int gk = 0, S = -1, R = -1, repeat = 1;
-    bool quiet = false, recon = false;
+    bool quiet = false, recon = false, zero_root = false, dump = false, estimate_bounds = false;
     int n_sim = 0, n_simulate = 0;
     unsigned long seed = 10;
     for (int i = 1; i < argc; ++i) {
@@ -250,6 +251,9 @@ int main(int argc, char** argv) {
         else if (a == "--pvalues") n_sim = std::stoi(next());
         else if (a == "--seed") seed = std::stoul(next());
         else if (a == "--simulate") n_simulate = std::stoi(next());
+        else if (a == "--exclude-zero-root") zero_root = true;
+        else if (a == "--dump-input") dump = true;
+        else if (a == "--estimate-bounds") estimate_bounds = true;
         else { usage(); return 2; }
     }
     if (tree_path.empty() || fam_path.empty() || lambdas.empty()) { usage(); return 2; }
@@ -264,11 +268,36 @@ int main(int argc, char** argv) {
             read_gene_families(f, tree.get(), families);
         }
         // Global bounds exactly as user_data::read_gene_family_data computes
-        // them (src/user_data.cpp:39-48) unless overridden.
+        // them (src/user_data.cpp:39-48) unless overridden: over every family
+        // read, before any filter.
         int mx = 0;
         for (auto& gf : families) mx = std::max(mx, gf.get_max_size());
+        int est_fam = -1, est_root = -1;
+        if (estimate_bounds) {
+            // the estimate action's own bounds: user_data::read_gene_family_data
+            // on the same file, starting from user_data's defaults
+            // (src/user_data.cpp:24-48, src/user_data.h:26-27)
+            input_parameters ip;
+            ip.input_file_path = fam_path;
+            user_data ud;
+            std::vector<gene_family> again;
+            ud.read_gene_family_data(ip, ud.max_family_size, ud.max_root_family_size, tree.get(), &again);
+            est_fam = ud.max_family_size;
+            est_root = ud.max_root_family_size;
+        }
+        // the estimate action's default filter, applied after the bounds
+        // (exclude_zero_root_families, src/core.cpp:190-205, over
+        // gene_family::exists_at_root; cafexp.cpp reads the data files first)
+        if (zero_root)
+            families.erase(std::remove_if(families.begin(), families.end(),
+                                          [&](const gene_family& gf) { return !gf.exists_at_root(tree.get()); }),
+                           families.end());
         int max_root = std::max(30, static_cast<int>(std::rint(mx * 1.25)));
         int max_fam = mx + std::max(50, mx / 5);
+        if (estimate_bounds) {
+            max_fam = est_fam;
+            max_root = est_root;
+        }
         if (S >= 0) max_fam = S;
         if (R >= 0) max_root = R;
 
@@ -286,6 +315,42 @@ int main(int argc, char** argv) {
             em.reset(new error_model());
             std::ifstream f(err_path);
             read_error_model_file(f, em.get());
+        }
+
+        if (dump) {
+            // what the reference's readers made of the inputs: the tree in
+            // prefix order (name, parent, branch length), every family's
+            // counts at the leaves in that order, the lambda index of every
+            // node of a lambda tree, and the error model's rows
+            std::vector<const clade*> nodes;
+            tree->apply_prefix_order([&](const clade* c) { nodes.push_back(c); });
+            std::map<const clade*, int> at;
+            for (size_t i = 0; i < nodes.size(); ++i) at[nodes[i]] = (int)i;
+            for (size_t i = 0; i < nodes.size(); ++i) {
+                const clade* c = nodes[i];
+                std::printf("node %zu %s %d %a\n", i, c->get_taxon_name().c_str(),
+                            c->get_parent() ? at[c->get_parent()] : -1, c->get_branch_length());
+            }
+            std::printf("families %zu\n", families.size());
+            for (auto& gf : families) {
+                std::printf("gf %s", gf.id().c_str());
+                for (auto* c : nodes)
+                    if (c->is_leaf()) std::printf(" %d", gf.get_species_size(c->get_taxon_name()));
+                std::printf("\n");
+            }
+            if (ltree) {
+                auto idx = ltree->get_lambda_index_map();
+                for (auto* c : nodes) std::printf("lambda_index %s %d\n", c->get_taxon_name().c_str(), idx[c->get_taxon_name()]);
+            }
+            if (em) {
+                for (size_t n = 0; n < em->get_max_family_size(); ++n) {
+                    std::printf("erow %zu", n);
+                    for (double x : em->get_probs(n)) std::printf(" %a", x);
+                    std::printf("\n");
+                }
+            }
+            std::printf("bounds %d %d\n", max_fam, max_root);
+            return 0;
         }
 
         std::unique_ptr<root_equilibrium_distribution> prior;

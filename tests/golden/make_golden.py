@@ -111,7 +111,7 @@ def parse_recon(out: str, ids, n_nodes):
 
 def make_case(name, tree, fams, lambdas, *, lam_idx=None, model="base", mult=None, probs=None,
               err=None, S=None, R=None, prior="uniform", note="", alpha=None, K=None, optimize=None,
-              initial=None, recon=False):
+              initial=None, recon=False, estimate_bounds=False):
     with tempfile.TemporaryDirectory() as d:
         tp, fp = os.path.join(d, "t.nwk"), os.path.join(d, "f.tab")
         nwk = tree.to_newick()
@@ -137,6 +137,8 @@ def make_case(name, tree, fams, lambdas, *, lam_idx=None, model="base", mult=Non
             args += ["--gamma-mult", ",".join(repr(x) for x in mult), "--gamma-prob", ",".join(repr(x) for x in probs)]
         if S is not None:
             args += ["--max-family", str(S), "--max-root", str(R)]
+        if estimate_bounds:
+            args += ["--estimate-bounds"]
         if optimize is not None:
             search = parse_search(run(args + ["--optimize", optimize, "--initial",
                                               ",".join(repr(x) for x in initial)]))
@@ -355,5 +357,149 @@ def main():
               open(os.path.join(HERE, "ref_optimizer.json"), "w"), indent=1)
 
 
+# -- the reference's own example inputs --------------------------------------
+# Paths are relative to the reference checkout; tests/golden/stage_examples.py
+# copies the same files into tests/golden/_refdata/ (git-ignored) for the GPU
+# tests, which compare against the values written here.
+EXAMPLES = [
+    dict(name="mammals_base", tree="examples/mammals_tree.txt", families="examples/mammal_gene_families.txt",
+         lambdas=[0.01], note="the mammals example at lambda 0.01: -lnL 210925.6422469711"),
+    dict(name="primates_base", tree="Test_data/Primate_data/12Primates.tree",
+         families="Test_data/Primate_data/12Primate_genefamilies.tab", lambdas=[0.00453],
+         note="the Primates test data at lambda 0.00453: -lnL 159140.7143496017"),
+    dict(name="mammals_error_model", tree="examples/mammals_tree.txt",
+         families="examples/mammal_gene_families.txt", error="examples/errormodel_0.1.txt", lambdas=[0.01],
+         note="the mammals example with its error-model file"),
+    dict(name="mammals_two_lambdas", tree="examples/mammals_tree.txt",
+         families="examples/mammal_gene_families.txt", lambda_tree="examples/chimphuman_separate_lambda.txt",
+         lambdas=[0.01, 0.02], note="the chimp/human lambda tree"),
+    dict(name="primates_rootdist", tree="Test_data/Primate_data/12Primates.tree",
+         families="Test_data/Primate_data/12Primate_genefamilies.tab", rootdist="Test_data/Primate_data/Root_dist.txt",
+         lambdas=[0.00453], note="the Primates root-size distribution as the prior"),
+    dict(name="mammals_gamma_k4", tree="examples/mammals_tree.txt", families="examples/mammal_gene_families.txt",
+         lambdas=[0.01], gamma=(4, 0.5), note="gamma K=4 alpha=0.5: a family underflows -> +inf"),
+]
+
+
+def reference_checkout():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    d = oracle.reference_dir()
+    if d is None:
+        raise SystemExit("set CAFE_REFERENCE to the reference checkout")
+    return d
+
+
+def rootdist_spec(path):
+    pairs = []
+    for ln in open(path):
+        tok = ln.split()
+        if len(tok) >= 2:
+            pairs.append(f"{int(tok[0])}={int(tok[1])}")
+    return "rootdist:" + ",".join(pairs)
+
+
+def canonical_dump(text: str) -> str:
+    """The harness's --dump-input lines with every hex float re-printed by
+    Python (C's %a and float.hex differ in trailing zeros)."""
+    out = []
+    for ln in text.splitlines():
+        tok = ln.split()
+        if tok[0] == "node":
+            tok[4] = float.fromhex(tok[4]).hex()
+        elif tok[0] == "erow":
+            tok[2:] = [float.fromhex(x).hex() for x in tok[2:]]
+        out.append(" ".join(tok))
+    return "\n".join(out) + "\n"
+
+
+def examples_main():
+    import hashlib
+    ref = reference_checkout()
+    meta, arrays = [], {}
+    for ex in EXAMPLES:
+        args = ["--tree", os.path.join(ref, ex["tree"]), "--families", os.path.join(ref, ex["families"]),
+                "--lambdas", ",".join(repr(x) for x in ex["lambdas"]), "--exclude-zero-root", "--estimate-bounds"]
+        if ex.get("error"):
+            args += ["--error", os.path.join(ref, ex["error"])]
+        if ex.get("lambda_tree"):
+            args += ["--lambda-tree", os.path.join(ref, ex["lambda_tree"])]
+        prior = rootdist_spec(os.path.join(ref, ex["rootdist"])) if ex.get("rootdist") else "uniform"
+        args += ["--prior", prior]
+        if ex.get("gamma"):
+            args += ["--gamma-k", str(ex["gamma"][0]), "--gamma-alpha", repr(ex["gamma"][1])]
+        dump = canonical_dump(run(args + ["--dump-input"]))
+        out = parse_output(run(args))
+        fam_ids = [ln.split()[1] for ln in dump.splitlines() if ln.startswith("gf ")]
+        m = {k: v for k, v in ex.items()}
+        m.update({"prior": prior, "S": out["S"], "R": out["R"], "total_hex": out["total_hex"],
+                  "n_families": len(fam_ids), "parse_sha256": hashlib.sha256(dump.encode()).hexdigest()})
+        if ex.get("gamma"):
+            # per-family lnL of the gamma model: log of family_likelihood
+            cats = out["cat"]
+            fam = [np.log(float.fromhex(cats[i][0]["fam_lh"])) if i in cats else np.nan for i in fam_ids]
+        else:
+            fam = [float.fromhex(out["fam"][i]) for i in fam_ids]
+        arrays[ex["name"] + "_fam_lnl"] = np.asarray(fam, dtype=np.float64)
+        meta.append(m)
+        print(ex["name"], m["n_families"], m["S"], m["R"], float.fromhex(m["total_hex"]))
+    json.dump({"generator": "tests/golden/make_golden.py --examples", "cases": meta},
+              open(os.path.join(HERE, "ref_examples.json"), "w"), indent=1)
+    np.savez_compressed(os.path.join(HERE, "ref_examples.npz"), **arrays)
+
+
+def configs_main():
+    """Subsets of the larger benchmark shapes scored by the reference at its
+    own global bounds: the two-lambda + error-model shape at S ~ 600 and
+    the 48-taxon K = 8 gamma shape."""
+    cases = []
+    w2 = workload(2, n_families=50000, seed=0)
+    mx = w2.families.max_counts()
+    order = np.argsort(-mx, kind="stable")
+    rng = np.random.default_rng(21)
+    pick = np.concatenate([order[:6], rng.choice(order[6:], 34, replace=False)])
+    pick.sort()
+    f2 = FamilySet([w2.families.ids[i] for i in pick], np.ascontiguousarray(w2.families.counts[pick]))
+    err = "maxcnt: 700\ncntdiff: -1 0 1\n0 0 0.95 0.05\n1 0.05 0.9 0.05\n"
+    cases.append(make_case("cfg2_two_lambdas_error_S600", w2.tree, f2, [0.0015, 0.006], lam_idx=w2.lambda_of_node,
+                           err=err, estimate_bounds=True,
+                           note="config-2 shape at the reference's global bound: the 6 largest families of the "
+                                "50,000 and 34 others"))
+    w3 = workload(3, n_families=20000, seed=0)
+    f3 = FamilySet(w3.families.ids[:300], np.ascontiguousarray(w3.families.counts[:300]))
+    cases.append(make_case("cfg3_gamma_k8_48taxa_underflow", w3.tree, f3, [0.002], model="gamma",
+                           mult=w3.multipliers, probs=w3.cat_probs, estimate_bounds=True,
+                           note="config-3 shape: 48 taxa, K=8, alpha=0.5, the first 300 families; some "
+                                "families underflow in the smallest category, so the reference returns +inf"))
+    # 300 families whose every category is finite in the reference's
+    # arithmetic (selected with the oracle, which is bit-exact with it)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from cafe5_gb300.families import global_bounds as gb
+    S3, R3 = gb(w3.families)
+    cand = np.ascontiguousarray(w3.families.counts[:4000])
+    _, fam3, _ = oracle.score(oracle.TreeArrays.from_tree(w3.tree), cand, [0.002], model=1,
+                              multipliers=w3.multipliers, cat_probs=w3.cat_probs,
+                              prior=RootPrior.uniform(R3).vector(), S=S3, R=R3, dedupe=False)
+    ok = np.nonzero(np.isfinite(fam3))[0]      # a failed family's lnL is NaN
+    # the 300 finite families with the largest counts, in their input order
+    ok = np.sort(ok[np.argsort(-cand[ok].max(axis=1), kind="stable")[:300]])
+    f3f = FamilySet([w3.families.ids[i] for i in ok], np.ascontiguousarray(cand[ok]))
+    cases.append(make_case("cfg3_gamma_k8_48taxa_finite", w3.tree, f3f, [0.002], model="gamma",
+                           mult=w3.multipliers, probs=w3.cat_probs, estimate_bounds=True,
+                           note="config-3 shape: 48 taxa, K=8, alpha=0.5 (get_gamma's multipliers); of the first "
+                                "4,000 families, the 300 with the largest counts among those whose every category "
+                                "is finite in FP64 (only 5 are: the smallest category underflows the others)"))
+    for c in cases:
+        print(c["name"], c["S"], c["R"], float.fromhex(c["expected"]["total_hex"]))
+    json.dump({"generator": "tests/golden/make_golden.py --configs", "cases": cases},
+              open(os.path.join(HERE, "ref_configs.json"), "w"))
+
+
 if __name__ == "__main__":
-    main()
+    if "--examples" in sys.argv:
+        examples_main()
+    elif "--configs" in sys.argv:
+        configs_main()
+    else:
+        main()

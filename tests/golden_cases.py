@@ -112,8 +112,10 @@ def case_from_json(c) -> Case:
         cat=cat, recon=recon_from_json(c.get("recon")))
 
 
-def load_cases() -> List[Case]:
-    return [case_from_json(c) for c in load_json("ref_cases.json")["cases"]]
+def load_cases(name: str = "ref_cases.json") -> List[Case]:
+    """ref_cases.json: the known-answer and small synthetic cases;
+    ref_configs.json: subsets of the larger benchmark shapes."""
+    return [case_from_json(c) for c in load_json(name)["cases"]]
 
 
 def load_searches():
@@ -186,3 +188,73 @@ def load_simulation_cases() -> List[SimulationCase]:
             err=ErrorModel.parse(c["error_model"]) if c["error_model"] else None, alpha=c["alpha"], K=c["K"],
             lambda_used=np.array([hexf(x) for x in c["lambda_hex"]]), sizes=_ints(c["sizes"])))
     return out
+
+
+# ---- the reference's example data (tests/golden/ref_examples.json) ----------
+
+REFDATA = os.path.join(GOLDEN, "_refdata")
+
+
+def example_cases():
+    return load_json("ref_examples.json")["cases"]
+
+
+def example_path(rel: str) -> Optional[str]:
+    """A staged example input (tests/golden/stage_examples.py), else the file
+    in the reference checkout named by CAFE_REFERENCE; None if neither."""
+    p = os.path.join(REFDATA, rel)
+    if os.path.exists(p):
+        return p
+    ref = os.environ.get("CAFE_REFERENCE")
+    if ref and os.path.exists(os.path.join(ref, rel)):
+        return os.path.join(ref, rel)
+    return None
+
+
+def example_available(c) -> bool:
+    return all(example_path(c[k]) for k in ("tree", "families", "error", "lambda_tree", "rootdist") if c.get(k))
+
+
+def read_example(c):
+    """(tree, all families read, families after the zero-root filter, lambda
+    tree or None, ErrorModel or None, RootPrior) through this package's
+    readers, as the estimate action reads them."""
+    from cafe5_gb300.families import exclude_zero_root_families, global_bounds, read_families
+    tree = parse_newick(open(example_path(c["tree"])).read())
+    fams = read_families(example_path(c["families"]), tree)
+    kept = exclude_zero_root_families(fams, tree)
+    ltree = parse_newick(open(example_path(c["lambda_tree"])).read(), lambda_tree=True) if c.get("lambda_tree") else None
+    em = ErrorModel.parse(open(example_path(c["error"])).read()) if c.get("error") else None
+    S, R = global_bounds(fams)
+    if c.get("rootdist"):
+        rd = {}
+        for ln in open(example_path(c["rootdist"])):
+            tok = ln.split()
+            if len(tok) >= 2:
+                rd[int(tok[0])] = int(tok[1])
+        prior = RootPrior.from_rootdist(rd)
+    else:
+        prior = RootPrior.uniform(R)
+    return tree, fams, kept, ltree, em, prior, S, R
+
+
+def canonical_input_text(tree: Tree, kept, S: int, R: int, ltree=None, em=None) -> str:
+    """The same lines the reference harness's --dump-input prints (nodes in
+    prefix order with parent and branch length, every kept family's leaf
+    counts in that order, the lambda index of every node, the error model's
+    rows, the bounds), floats as Python hex."""
+    out = []
+    for v in range(tree.n_nodes):
+        out.append(f"node {v} {tree.name[v]} {tree.parent[v]} {float(tree.branch_length[v]).hex()}")
+    out.append(f"families {kept.n_families}")
+    for fid, row in zip(kept.ids, kept.counts):
+        out.append("gf " + fid + "".join(f" {int(x)}" for x in row))
+    if ltree is not None:
+        by_name = {ltree.name[v]: ltree.lambda_index[v] - 1 for v in range(ltree.n_nodes)}
+        for v in range(tree.n_nodes):
+            out.append(f"lambda_index {tree.name[v]} {by_name.get(tree.name[v], 0)}")
+    if em is not None:
+        for n, row in enumerate(em.rows):
+            out.append(f"erow {n}" + "".join(" " + float(x).hex() for x in row))
+    out.append(f"bounds {S} {R}")
+    return "\n".join(out) + "\n"

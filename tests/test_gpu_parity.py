@@ -21,6 +21,9 @@ from golden_cases import load_cases, load_json
 pytestmark = pytest.mark.gpu
 
 CASES = load_cases()
+# subsets of the larger shapes: two lambdas + error model at the reference's
+# global bound S = 488 (bins up to 512), 48 taxa with K = 8
+CONFIG_CASES = load_cases("ref_configs.json")
 REL = 1e-10
 
 
@@ -82,7 +85,7 @@ def _score_case(ctx, case, precision="fp64_ref", prior=None, **kw):
     return r
 
 
-@pytest.mark.parametrize("case", CASES, ids=[c.name for c in CASES])
+@pytest.mark.parametrize("case", CASES + CONFIG_CASES, ids=[c.name for c in CASES + CONFIG_CASES])
 @pytest.mark.parametrize("dedupe", [False, True])
 def test_fp64_ref_matches_reference(ctx, case, dedupe):
     """Plain FP64 path vs the reference's own -lnL and per-family lnL
@@ -106,7 +109,9 @@ def test_fp64_ref_matches_reference(ctx, case, dedupe):
                 assert abs(r.category_lnl[f, k] - lc) <= REL * abs(lc)
 
 
-@pytest.mark.parametrize("case", [c for c in CASES if not math.isinf(c.total) or c.name == "syn_base_underflow"],
+@pytest.mark.parametrize("case", [c for c in CASES + CONFIG_CASES
+                                  if not math.isinf(c.total) or c.name in ("syn_base_underflow",
+                                                                           "cfg3_gamma_k8_48taxa_underflow")],
                          ids=lambda c: c.name)
 def test_fp64_binned_matches_scaled_oracle(ctx, case):
     """Per-family S-bins with power-of-two rescale vs the rescaled oracle at
@@ -220,6 +225,31 @@ def _both(ctx, tree, counts, lambdas, lam_idx=None, kind=0, model=0, mult=(1.0,)
     return a, b
 
 
+def _scaled_oracle_binned(tree, counts, lambdas, lam_idx=None, kind=0, model=0, mult=(1.0,), probs=(1.0,), err=None,
+                          prior=None):
+    """The rescaled FP64 oracle at the GPU's per-family bins: (total, fam)."""
+    from cafe5_gb300.families import FamilySet, bin_families
+    from cafe5_gb300.inputs import RootPrior
+    W, Sb, Rb = bin_families(FamilySet([str(i) for i in range(len(counts))], counts))
+    if prior is None:
+        prior = RootPrior.uniform(1100).vector()
+    ta = oracle.TreeArrays.from_tree(tree, lam_idx)
+    tot, fam, _ = oracle.score(ta, counts, lambdas, lambda_kind=kind, model=model, multipliers=list(mult),
+                               cat_probs=list(probs), prior=prior, err_rows=err, fam_S=Sb, fam_R=Rb, scaled=True,
+                               dedupe=False)
+    return tot, fam
+
+
+def _check_vs_oracle(b, ref_total, ref_fam):
+    """The tensor-core path against the FP64 oracle, family by family."""
+    fin = np.isfinite(ref_fam)
+    assert np.array_equal(fin, np.isfinite(b.family_lnl))
+    rel = np.abs(b.family_lnl[fin] - ref_fam[fin]) / np.abs(ref_fam[fin])
+    assert rel.max() <= MIXED_REL, f"max rel dlnL vs oracle {rel.max():.3e}"
+    if math.isfinite(ref_total):
+        assert abs(b.total - ref_total) <= MIXED_REL * abs(ref_total)
+
+
 def _check_mixed(a, b):
     fin = np.isfinite(a.family_lnl)
     assert np.array_equal(fin, np.isfinite(b.family_lnl))
@@ -233,9 +263,40 @@ def _check_mixed(a, b):
 
 @pytest.mark.parametrize("lam", [0.002, 0.0007, 0.0035])
 def test_mixed_gamma_config1_shape(ctx, lam):
+    """3,000 families of the config-1 shape (24 taxa, K = 4): the tensor-core
+    path against the rescaled FP64 oracle and against FP64_BINNED, 1e-6
+    relative per family."""
     from cafe5_gb300.synth import workload
     w = workload(1, n_families=3000, seed=21)
     a, b = _both(ctx, w.tree, w.families.counts, [lam], model=1, mult=w.multipliers, probs=w.cat_probs)
+    _check_mixed(a, b)
+    _check_vs_oracle(b, *_scaled_oracle_binned(w.tree, w.families.counts, [lam], model=1, mult=w.multipliers,
+                                               probs=w.cat_probs))
+
+
+def test_mixed_config3_shape_vs_oracle(ctx):
+    """2,000 families of the config-3 shape (48 taxa, K = 8, alpha = 0.5):
+    finite in the rescaled oracle where the reference's own FP64 underflows
+    (3,995 of its first 4,000 families); the tensor-core path within 1e-6
+    of the oracle on every family."""
+    from cafe5_gb300.synth import workload
+    w = workload(3, n_families=2000, seed=0)
+    a, b = _both(ctx, w.tree, w.families.counts, [0.002], model=1, mult=w.multipliers, probs=w.cat_probs)
+    tot, fam = _scaled_oracle_binned(w.tree, w.families.counts, [0.002], model=1, mult=w.multipliers,
+                                     probs=w.cat_probs)
+    assert math.isfinite(tot)
+    _check_vs_oracle(b, tot, fam)
+    _check_mixed(a, b)
+
+
+def test_mixed_config2_wide_bins_vs_oracle(ctx):
+    """The two-lambda + error-model families of ref_configs.json (the
+    largest counts of the 50,000-family set: bins up to 512) on the mixed
+    path against the rescaled oracle at the same bins."""
+    case = [c for c in CONFIG_CASES if c.name == "cfg2_two_lambdas_error_S600"][0]
+    a, b = _both(ctx, case.tree, case.counts, case.lambdas, lam_idx=case.lambda_of_node, kind=1, err=case.err_rows)
+    _check_vs_oracle(b, *_scaled_oracle_binned(case.tree, case.counts, case.lambdas, lam_idx=case.lambda_of_node,
+                                               kind=1, err=case.err_rows))
     _check_mixed(a, b)
 
 
@@ -251,6 +312,8 @@ def test_mixed_error_model_two_lambdas(ctx):
     case = [c for c in CASES if c.name == "syn_multilambda_error_32taxa"][0]
     a, b = _both(ctx, case.tree, case.counts, case.lambdas, lam_idx=case.lambda_of_node, kind=1, err=case.err_rows)
     _check_mixed(a, b)
+    _check_vs_oracle(b, *_scaled_oracle_binned(case.tree, case.counts, case.lambdas, lam_idx=case.lambda_of_node,
+                                               kind=1, err=case.err_rows))
 
 
 def test_mixed_polytomy_and_underflow_cases(ctx):

@@ -17,6 +17,7 @@ from golden_cases import load_cases, load_json
 
 KAT = load_json("reference_kats.json")
 CASES = load_cases()
+CONFIG_CASES = load_cases("ref_configs.json")
 
 
 def approx5(a, b, rel=1.1920929e-5):
@@ -183,7 +184,7 @@ def test_oracle_discrete_gamma_bits_match_reference():
         oracle.discrete_gamma(0.0, 4)
 
 
-@pytest.mark.parametrize("case", CASES, ids=[c.name for c in CASES])
+@pytest.mark.parametrize("case", CASES + CONFIG_CASES, ids=[c.name for c in CASES + CONFIG_CASES])
 def test_oracle_matches_reference_end_to_end(case):
     ta = oracle.TreeArrays.from_tree(case.tree, case.lambda_of_node)
     tot, fam, cat = oracle.score(ta, case.counts, case.lambdas, lambda_kind=case.lambda_kind, model=case.model,
