@@ -958,6 +958,10 @@ TcShape tc_shape(cafe_ctx* C, const TreeHost& T, int W) {
     return sh;
 }
 
+// Share of the 1e-6 per-family budget (|dlnL| / |lnL|) left to FP32 range
+// loss; TF32x3 rounding takes the rest.
+constexpr double kRangeTau = 1e-7;
+
 // MIXED_TF32X3: tensor-core tiles for bins <= 256 states, FP64 tiles for
 // wider bins and for families the tensor-core pass flags. Caller holds C->mu;
 // hm holds the FP64 matrix of every (category, node).
@@ -1132,6 +1136,11 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         a.cat_probs = ws.catp.as<double>();
         a.flags = d_flags;
         a.status = d_status;
+        // range-error bounds of the category terms: zero for every term the
+        // tensor cores do not write (FP64 bins, candidates not pruned)
+        CK(ws.cerr.reserve((size_t)std::max<int64_t>(F, 1) * K * sizeof(float)), "range bounds");
+        CK(op_memset(ws, ws.cerr.p, 0, (size_t)std::max<int64_t>(F, 1) * K * sizeof(float), ws.stream), "range bounds");
+        a.out_err = ws.cerr.as<float>();
         a.phase_clocks = nullptr;
         static const bool phase_env = getenv("CAFE_TC_PHASES") != nullptr;
         if (phase_env) {
@@ -1191,9 +1200,21 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         if (rc) return rc;
     }
 
-    // families the tensor-core pass could not represent: planned on the
-    // device and recomputed in FP64 without a host round trip
+    // families the tensor-core pass could not represent, or whose result FP32's
+    // range may have cost accuracy: planned on the device and recomputed in
+    // FP64 without a host round trip
     if (!tc_tiles.empty()) {
+        RangeFlagArgs rf;
+        std::memset(&rf, 0, sizeof rf);
+        rf.cat = ws.cat.as<double>();
+        rf.err = ws.cerr.as<float>();
+        rf.F = F;
+        rf.K = K;
+        rf.KC = KC;
+        rf.tau = kRangeTau;
+        rf.flags = d_flags;
+        rf.any_flag = d_status + 3;
+        CK(op_launch(ws, 9, [&] { return launch_range_flags(rf, ws.stream); }, rf, ws.stream), "range flags");
         FallbackPlanArgs fp;
         std::memset(&fp, 0, sizeof fp);
         fp.flags = d_flags;

@@ -163,6 +163,8 @@ struct PruneTcArgs {
     int model;                   // 0 base (a zero family is -inf), 1 gamma (a zero family is NaN: failed)
     const double* cat_probs;
     int32_t* flags;              // [F] set when a family must be recomputed in FP64
+    float* out_err;              // [F][K] bound on the relative error of each category term from FP32
+                                 // range loss (values below 2^-126 flushed), or null
     int32_t* status;             // [1] nonzero when a bounded wait gave up
     int tmem_cols;
     int Ws;                      // widest bin of this launch (shared-memory B rows)
@@ -181,6 +183,22 @@ struct TcMaps {
 };
 
 cudaError_t launch_prune_tc(const TcMaps& maps, const PruneTcArgs& a, int n_ctas, size_t smem, cudaStream_t s);
+
+// Families whose tensor-core result may have lost accuracy to FP32's range:
+// for every (family, candidate), the category terms' range-error bounds
+// weighted by the terms' shares of the family likelihood; over
+// tau x |lnL| the family is flagged for the FP64 recompute.
+struct RangeFlagArgs {
+    const double* cat;           // [F][K] natural log of each category term
+    const float* err;            // [F][K] relative bound of each term
+    int64_t F;
+    int K;                       // combined (candidate, category) indices
+    int KC;                      // categories per candidate
+    double tau;
+    int32_t* flags;              // [F]
+    int32_t* any_flag;           // set to 1 when a family is flagged
+};
+cudaError_t launch_range_flags(const RangeFlagArgs& a, cudaStream_t s);
 size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages, int n_internal);
 int prune_tc_kchunk();   // K columns per operand box of k_prune_tc (its load maps' box width)
 int prune_tc_max_smem(); // dynamic shared memory one k_prune_tc CTA may use

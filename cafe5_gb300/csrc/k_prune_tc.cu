@@ -34,6 +34,17 @@
 //    log is written.
 //  * A family whose factors are too far apart, or whose root vector is all
 //    zero, is flagged; the host recomputes flagged families in FP64.
+//  * FP32 range: a factor value below 2^-126 is flushed (or denormal) where
+//    FP64 keeps it, which matters where the children's preferred states are
+//    far apart (large counts, short branches). Every node vector carries an
+//    absolute error bound E (in its own normalised units): a factor of an
+//    internal child is off by at most E_child + 8 W 2^-126 (flushed matrix
+//    entries, flushed lo parts and products; rows of M sum to <= 1), a leaf
+//    factor by a few 2^-126 where its value is below 2^-100; the product's
+//    bound is u_A (f_B + u_B) + u_B f_A per state, scaled like the product.
+//    At the root the bound of the best prior-weighted row, relative to it,
+//    is written per (family, category); families whose weighted bound
+//    exceeds tau |lnL| are recomputed in FP64 (k_range_flags).
 //
 // Every mbarrier wait is bounded; on time-out the kernel records a status,
 // waits (bounded) for its own copies, frees TMEM and returns.
@@ -41,6 +52,8 @@
 #include "tc_ptx.cuh"
 
 #include <math.h>
+
+#include <algorithm>
 
 namespace cafe {
 namespace {
@@ -121,7 +134,18 @@ struct NodeSrc {
     Src s[NC];
     int Eacc;     // sum of the internal children's power-of-two exponents
     bool flag;
+    float ue[NC]; // absolute error bound of the child's factor (unscaled units): every state of an
+                  // internal child; a leaf's only where its value is below 2^-100
+    bool leaf[NC];
 };
+
+constexpr float kTiny = 0x1p-126f;   // smallest normal FP32 value
+
+// Absolute error bound of factor c at a state whose unscaled value is raw.
+template <int NC>
+__device__ __forceinline__ float fac_err(const NodeSrc<NC>& ns, int c, float raw) {
+    return ns.leaf[c] ? (raw < 0x1p-100f ? ns.ue[c] : 0.0f) : ns.ue[c];
+}
 
 // Leaf weights of this thread's family: up to three (column, weight) pairs
 // (one-hot column n, or the error model's columns n-1, n, n+1).
@@ -132,7 +156,7 @@ struct LeafW {
 
 template <int NC>
 __device__ __forceinline__ void setup_src(const PruneTcArgs& a, const ChildInfo* ch, int nch, const int* Esh,
-                                          uint32_t tmem_lane, int64_t fam, int tid, int S, int W,
+                                          const float* Erh, uint32_t tmem_lane, int64_t fam, int tid, int S, int W,
                                           const int (&count)[NC], NodeSrc<NC>& ns, LeafW (&lw)[NC], int* cmask_sh) {
     ns.Eacc = 0;
     ns.flag = false;
@@ -148,13 +172,18 @@ __device__ __forceinline__ void setup_src(const PruneTcArgs& a, const ChildInfo*
         }
         sc.unit = c >= nch;
         sc.taddr = 0;
+        ns.ue[c] = 0.0f;
+        ns.leaf[c] = false;
         if (sc.unit) continue;
         const ChildInfo ci = ch[c];
         sc.taddr = tmem_lane + (uint32_t)(ci.tcol * W);
         if (ci.leaf_col < 0) {
             ns.Eacc += Esh[ci.slot * TM + tid];
+            ns.ue[c] = Erh[ci.slot * TM + tid] + (float)(8 * W) * kTiny;
             continue;
         }
+        ns.leaf[c] = true;
+        ns.ue[c] = (a.err ? 8.0f : 2.0f) * kTiny;
         if (fam < 0) continue;        // padding row: zero factor
         const int n = count[c];
         unsigned bits = 0;
@@ -230,9 +259,10 @@ __device__ __forceinline__ void load_children(const NodeSrc<NC>& ns, int col0, u
 template <int NC>
 __device__ __forceinline__ void epi_scan(const NodeSrc<NC>& ns, int W, bool is_root, int Rf, const float* prior_f,
                                          const float (&scl)[NC], float& maxp, float& best_f, float& best_p,
-                                         float& best_q) {
+                                         float& best_q, float& best_err) {
+    static_assert(NC == 2, "two factors per node");
     maxp = 0.0f;
-    best_f = best_p = best_q = 0.0f;
+    best_f = best_p = best_q = best_err = 0.0f;
     for (int col0 = 0; col0 < W; col0 += CW) {
         uint32_t r[NC][CW];
         load_children(ns, col0, r);
@@ -259,6 +289,11 @@ __device__ __forceinline__ void epi_scan(const NodeSrc<NC>& ns, int W, bool is_r
                         best_p = p[j];
                         best_q = q;
                     }
+                    // range-error bound of this row of the root product
+                    const float r0 = __uint_as_float(r[0][j]), r1 = __uint_as_float(r[1][j]);
+                    const float f0 = r0 * scl[0], f1 = r1 * scl[1];
+                    const float u0 = fac_err(ns, 0, r0) * scl[0], u1 = fac_err(ns, 1, r1) * scl[1];
+                    best_err = fmaxf(best_err, (u0 * (f1 + u1) + u1 * f0) * q);
                 }
             }
         }
@@ -297,7 +332,9 @@ __device__ __noinline__ int epi_maxexp(const NodeSrc<NC> ns, int W, int s_lo, in
 // splits it into TF32 hi/lo as it loads it (split_row_tf32).
 template <int NC>
 __device__ __forceinline__ void epi_store(const NodeSrc<NC>& ns, int W, const float (&scl)[NC], float* stg, int tid,
-                                          const CUtensorMap* map, int vrow) {
+                                          const CUtensorMap* map, int vrow, float& err) {
+    static_assert(NC == 2, "two factors per node");
+    err = 0.0f;
     // two staging tiles of TM x SC floats, used in turn: a chunk waits only
     // for the stores of the chunk two back
     for (int c32 = 0; c32 < W; c32 += SC) {
@@ -318,6 +355,12 @@ __device__ __forceinline__ void epi_store(const NodeSrc<NC>& ns, int W, const fl
             for (int c = 0; c < NC; ++c)
 #pragma unroll
                 for (int j = 0; j < CW; ++j) p[j] *= __uint_as_float(r[c][j]) * scl[c];
+#pragma unroll
+            for (int j = 0; j < CW; ++j) {
+                const float r0 = __uint_as_float(r[0][j]), r1 = __uint_as_float(r[1][j]);
+                const float u0 = fac_err(ns, 0, r0) * scl[0], u1 = fac_err(ns, 1, r1) * scl[1];
+                err = fmaxf(err, u0 * (r1 * scl[1] + u1) + u1 * (r0 * scl[0]));
+            }
 #pragma unroll
             for (int q = 0; q < CW / 4; ++q) {
                 const int j = ((col0 - c32) >> 2) + q;          // 16-byte piece of the 128-byte row
@@ -377,7 +420,8 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
     const TreePlan& P = a.plan;
     const size_t sbytes = stage_bytes(a.Ws);
     int* Esh = reinterpret_cast<int*>(smem + stages_region(a.Ws, NS));   // [n_slots][TM]
-    NodeInfo* nodes = reinterpret_cast<NodeInfo*>(Esh + (size_t)a.n_slots * TM);   // [n_internal]
+    float* Erh = reinterpret_cast<float*>(Esh + (size_t)a.n_slots * TM);   // [n_slots][TM] error bounds
+    NodeInfo* nodes = reinterpret_cast<NodeInfo*>(Erh + (size_t)a.n_slots * TM);   // [n_internal]
 
     for (int j = tid; j < 256; j += NTHREADS) prior_f[j] = j < a.n_prior ? (float)a.prior[j] : 0.0f;
     if (warp == 0) tc::tmem_alloc(&tmem_sh, (uint32_t)a.tmem_cols);
@@ -461,7 +505,7 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             NodeSrc<2> ns2;
             LeafW lw[2];
             const int cnt_cur[2] = {cnt_next[0], cnt_next[1]};
-            setup_src<2>(a, nd.c, nch, Esh, tmem + lane_base, fam, tid, S, W, cnt_cur, ns2, lw, cmask);
+            setup_src<2>(a, nd.c, nch, Esh, Erh, tmem + lane_base, fam, tid, S, W, cnt_cur, ns2, lw, cmask);
             // counts of the next node's leaves, in flight during this node
             if (ii + 1 < P.n_internal) {
                 const NodeInfo& nx = nodes[ii + 1];
@@ -620,8 +664,8 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             float scl[2] = {1.0f, 1.0f};
             int E = ns2.Eacc;
             bool nflag = ns2.flag;
-            float maxp, bf, bp, bq;
-            epi_scan<2>(ns2, W, is_root, Rf, prior_f, scl, maxp, bf, bp, bq);
+            float maxp, bf, bp, bq, be;
+            epi_scan<2>(ns2, W, is_root, Rf, prior_f, scl, maxp, bf, bp, bq, be);
             // Without an error model, every state-0 entry is exact: row 0 of
             // every matrix is delta(s, 0), so L[0] is 1 (scaled by a power of
             // two) when all leaves below are 0, else 0, and it is then the
@@ -652,12 +696,13 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                     E = ns2.Eacc + maxe;
                 }
                 if (is_root) {
-                    float m2, f2, p2, q2;
-                    epi_scan<2>(ns2, W, true, Rf, prior_f, scl, m2, f2, p2, q2);
+                    float m2, f2, p2, q2, e2;
+                    epi_scan<2>(ns2, W, true, Rf, prior_f, scl, m2, f2, p2, q2, e2);
                     if (need) {
                         bf = f2;
                         bp = p2;
                         bq = q2;
+                        be = e2;
                     }
                 }
             }
@@ -665,9 +710,12 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             flag |= nflag && !dead;
             if (!is_root) {
                 // stage 0 holds the two staging tiles
+                float ev;
                 epi_store<2>(ns2, W, scl, reinterpret_cast<float*>(smem), tid, &map_vst,
-                             (int)(vrow_cta + (int64_t)vs * TM));
+                             (int)(vrow_cta + (int64_t)vs * TM), ev);
                 Esh[vs * TM + tid] = E;
+                // the stored vector's bound: the product's, plus values flushed on the store
+                Erh[vs * TM + tid] = fminf(ev + kTiny, 1e30f);
             } else if (fam >= 0) {
                 double o = NAN;
                 const double best = (double)bp * (double)bq;
@@ -676,6 +724,7 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                     o = log(best * a.cat_probs[k]) + (double)E * 0.69314718055994530942;
                 else flag = true;
                 a.out[(size_t)fam * a.K + k] = o;
+                if (a.out_err) a.out_err[(size_t)fam * a.K + k] = (dead || flag || !(bf > 0.0f)) ? 0.0f : be / bf;
             }
             long long t3 = timing ? clock64() : 0;
             tc::fence_before();
@@ -791,7 +840,49 @@ __global__ void __launch_bounds__(256) k_fallback_plan(FallbackPlanArgs a) {
     }
 }
 
+// One thread per (family, candidate): the category terms' range-error
+// bounds weighted by their shares of the family likelihood; a family over
+// tau |lnL| is flagged for the FP64 recompute. Terms that are not finite
+// (a dead or failed category) carry no weight; a family none of whose
+// terms is finite is left to the finish.
+__global__ void __launch_bounds__(256) k_range_flags(RangeFlagArgs a) {
+    const int n_cand = a.K / a.KC;
+    const int64_t n = a.F * n_cand;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t f = i / n_cand;
+        const int b = (int)(i % n_cand);
+        const double* c = a.cat + (size_t)f * a.K + (size_t)b * a.KC;
+        const float* e = a.err + (size_t)f * a.K + (size_t)b * a.KC;
+        double m = -INFINITY;
+        for (int k = 0; k < a.KC; ++k)
+            if (isfinite(c[k])) m = fmax(m, c[k]);
+        if (!(m > -INFINITY)) continue;
+        double w = 0.0, we = 0.0;
+        for (int k = 0; k < a.KC; ++k) {
+            if (!isfinite(c[k])) continue;
+            const double x = exp(c[k] - m);
+            w += x;
+            we += x * (double)e[k];
+        }
+        if (!(we != 0.0)) continue;      // no range loss in any term (or a candidate that was not pruned)
+        const double lnl = m + log(w);
+        const double bound = we / w;
+        if (!(bound <= a.tau * fabs(lnl))) {
+            atomicOr(&a.flags[f], 2);
+            atomicOr(a.any_flag, 1);
+        }
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_range_flags(const RangeFlagArgs& a, cudaStream_t s) {
+    const int64_t n = a.F * (a.K / a.KC);
+    if (n <= 0) return cudaSuccess;
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
+    k_range_flags<<<blocks, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
 
 // k_prune_tc's dynamic shared-memory limit is raised once, to the most a
 // CTA may use, so launches of different widths need no per-launch change.
@@ -825,7 +916,8 @@ int prune_tc_max_smem() {
 }
 
 size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages, int n_internal) {
-    return stages_region(Ws, stages) + (size_t)n_slots * TM * sizeof(int) + (size_t)n_internal * sizeof(NodeInfo) + 1024;
+    return stages_region(Ws, stages) + (size_t)n_slots * TM * (sizeof(int) + sizeof(float)) +
+           (size_t)n_internal * sizeof(NodeInfo) + 1024;
 }
 
 cudaError_t launch_convert_tc(const ConvertJob* d_jobs, int n_jobs, TcBuffers b, cudaStream_t s) {

@@ -158,7 +158,7 @@ struct Workspace {
     PinnedBuf h_tiles, h_mats, h_jobs, h_out, h_catp;
     // tensor-core path
     DevBuf tc_hi, tc_lo, tc_mi, tc_vec, conv, flags, fb_perm, tiles64, tiles_fb, parts, fb_count, phase,
-        catids;
+        catids, cerr;
     PinnedBuf h_conv, h_mi, h_flags, h_tiles64, h_tiles_fb, h_tail, h_catids;
     // FP64 bins walked one family per cluster
     DevBuf tiles_cl;

@@ -58,6 +58,8 @@ def _run(ctx, n_families, seed, scaled):
 
     # the same matrices, in caller-owned device memory
     msize = max(R, S) + 1
+    ctx.matrices_build([lam], [w.tree.branch_length[v] for v in range(w.tree.n_nodes) if w.tree.parent[v] >= 0],
+                       msize)
     dev = torch.device("cuda", 0)
     keep = []
     ptrs = (ctypes.c_void_p * w.tree.n_nodes)()
