@@ -27,8 +27,9 @@ EXPORTS = [
     "cafe_score_device", "cafe_submit", "cafe_poll", "cafe_serving_stats", "cafe_profile_enable",
     "cafe_profile_read", "cafe_prune_fp64_noalloc", "cafe_optimize", "cafe_discrete_gamma",
     "cafe_nelder_mead", "cafe_score_batch", "cafe_score_batch_device", "cafe_serving_counters", "cafe_autotune",
-    "cafe_reconstruct", "cafe_branch_probabilities", "cafe_pvalues", "cafe_simulate",
+    "cafe_reconstruct", "cafe_branch_probabilities", "cafe_pvalues", "cafe_simulate", "cafe_debug_set",
 ]
+DEBUG_TC_WAIT_LIMIT = 1
 OPT_LAMBDA, OPT_LAMBDA_ALPHA, OPT_LAMBDA_EPSILON, OPT_ALPHA = 0, 1, 2, 3
 
 
@@ -151,6 +152,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
         "cafe_branch_probabilities": (i, [p, P(Request), p, p]),
         "cafe_pvalues": (i, [p, P(Request), P(PvaluesOut)]),
         "cafe_simulate": (i, [p, P(Request), P(Simulation)]),
+        "cafe_debug_set": (i, [p, i, i64]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

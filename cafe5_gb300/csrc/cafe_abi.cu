@@ -1136,6 +1136,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         a.cat_probs = ws.catp.as<double>();
         a.flags = d_flags;
         a.status = d_status;
+        a.debug_wait_limit = C->debug_wait_limit;
         // range-error bounds of the category terms: zero for every term the
         // tensor cores do not write (FP64 bins, candidates not pruned)
         CK(ws.cerr.reserve((size_t)std::max<int64_t>(F, 1) * K * sizeof(float)), "range bounds");
@@ -2374,6 +2375,17 @@ int branch_prob_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, const in
 extern "C" {
 
 int cafe_version(void) { return 1; }
+
+int cafe_debug_set(cafe_ctx* C, int knob, int64_t value) {
+    if (!C) return CAFE_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(C->mu);
+    if (knob == CAFE_DEBUG_TC_WAIT_LIMIT) {
+        if (value < 0 || value > ((int64_t)1 << 30)) return fail(C, CAFE_ERR_INVALID, "wait limit out of range");
+        C->debug_wait_limit = (int)value;
+        return CAFE_OK;
+    }
+    return fail(C, CAFE_ERR_INVALID, "unknown debug knob %d", knob);
+}
 
 const char* cafe_status_string(int s) {
     switch (s) {

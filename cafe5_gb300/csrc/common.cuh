@@ -172,6 +172,8 @@ struct PruneTcArgs {
     int64_t vrow_base;           // first node-vector row of this launch
     unsigned long long* phase_clocks;   // optional [6]: SM clocks of thread 0 in child setup, GEMMs,
                                         // epilogue, root bookkeeping, end-of-node barrier; tile-nodes
+    int debug_wait_limit;        // > 0: the wait for a node's GEMMs gives up after this many polls
+                                 // minus one (tests of the time-out path); 0: the default bound
 };
 
 // Tensor maps travel by value (__grid_constant__); the host encodes them.

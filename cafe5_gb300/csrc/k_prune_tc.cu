@@ -216,20 +216,18 @@ __device__ __forceinline__ void setup_src(const PruneTcArgs& a, const ChildInfo*
 // descriptor reads: a 128-byte row r keeps its 16-byte piece j at
 // j ^ (r % 8); a 64-byte row at j ^ ((r >> 1) % 4).
 __device__ __forceinline__ void write_leaf_row(float* tile, int r, const LeafW& L, int kc, bool lo) {
-    uint8_t* row = reinterpret_cast<uint8_t*>(tile) + (size_t)r * (KC * sizeof(float));
+    float* row = tile + (size_t)r * KC;
     const int c0 = kc * KC;
+    const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll
-    for (int j = 0; j < KC / 4; ++j) {
-        float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int j = 0; j < KC / 4; ++j) reinterpret_cast<float4*>(row)[j] = z;
+    // then the (at most three) nonzero columns, each at its swizzled place
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const int q = L.col[d] - c0 - 4 * j;
-#pragma unroll
-            for (int e = 0; e < 4; ++e)
-                if (q == e) v[e] = lo ? L.lo[d] : L.hi[d];
-        }
-        const int pj = KC == 32 ? (j ^ (r & 7)) : (j ^ ((r >> 1) & 3));
-        *reinterpret_cast<float4*>(row + (pj << 4)) = make_float4(v[0], v[1], v[2], v[3]);
+    for (int d = 0; d < 3; ++d) {
+        const int e = L.col[d] - c0;
+        if (L.col[d] < 0 || e < 0 || e >= KC) continue;
+        const int pj = KC == 32 ? ((e >> 2) ^ (r & 7)) : ((e >> 2) ^ ((r >> 1) & 3));
+        row[(pj << 2) + (e & 3)] = lo ? L.lo[d] : L.hi[d];
     }
 }
 
@@ -259,10 +257,12 @@ __device__ __forceinline__ void load_children(const NodeSrc<NC>& ns, int col0, u
 template <int NC>
 __device__ __forceinline__ void epi_scan(const NodeSrc<NC>& ns, int W, bool is_root, int Rf, const float* prior_f,
                                          const float (&scl)[NC], float& maxp, float& best_f, float& best_p,
-                                         float& best_q, float& best_err) {
+                                         float& best_q, float& best_err, float (&fmx)[NC], float (&fmn)[NC]) {
     static_assert(NC == 2, "two factors per node");
     maxp = 0.0f;
     best_f = best_p = best_q = best_err = 0.0f;
+    fmx[0] = fmx[1] = 0.0f;
+    fmn[0] = fmn[1] = 1.0f;
     for (int col0 = 0; col0 < W; col0 += CW) {
         uint32_t r[NC][CW];
         load_children(ns, col0, r);
@@ -275,7 +275,14 @@ __device__ __forceinline__ void epi_scan(const NodeSrc<NC>& ns, int W, bool is_r
             for (int j = 0; j < CW; ++j) p[j] *= __uint_as_float(r[c][j]) * scl[c];
         if (!is_root) {
 #pragma unroll
-            for (int j = 0; j < CW; ++j) maxp = fmaxf(maxp, p[j]);
+            for (int j = 0; j < CW; ++j) {
+                maxp = fmaxf(maxp, p[j]);
+                const float r0 = __uint_as_float(r[0][j]), r1 = __uint_as_float(r[1][j]);
+                fmx[0] = fmaxf(fmx[0], r0);
+                fmx[1] = fmaxf(fmx[1], r1);
+                fmn[0] = fminf(fmn[0], r0);
+                fmn[1] = fminf(fmn[1], r1);
+            }
         } else {
 #pragma unroll
             for (int j = 0; j < CW; ++j) {
@@ -332,9 +339,8 @@ __device__ __noinline__ int epi_maxexp(const NodeSrc<NC> ns, int W, int s_lo, in
 // splits it into TF32 hi/lo as it loads it (split_row_tf32).
 template <int NC>
 __device__ __forceinline__ void epi_store(const NodeSrc<NC>& ns, int W, const float (&scl)[NC], float* stg, int tid,
-                                          const CUtensorMap* map, int vrow, float& err) {
+                                          const CUtensorMap* map, int vrow) {
     static_assert(NC == 2, "two factors per node");
-    err = 0.0f;
     // two staging tiles of TM x SC floats, used in turn: a chunk waits only
     // for the stores of the chunk two back
     for (int c32 = 0; c32 < W; c32 += SC) {
@@ -355,12 +361,6 @@ __device__ __forceinline__ void epi_store(const NodeSrc<NC>& ns, int W, const fl
             for (int c = 0; c < NC; ++c)
 #pragma unroll
                 for (int j = 0; j < CW; ++j) p[j] *= __uint_as_float(r[c][j]) * scl[c];
-#pragma unroll
-            for (int j = 0; j < CW; ++j) {
-                const float r0 = __uint_as_float(r[0][j]), r1 = __uint_as_float(r[1][j]);
-                const float u0 = fac_err(ns, 0, r0) * scl[0], u1 = fac_err(ns, 1, r1) * scl[1];
-                err = fmaxf(err, u0 * (r1 * scl[1] + u1) + u1 * (r0 * scl[0]));
-            }
 #pragma unroll
             for (int q = 0; q < CW / 4; ++q) {
                 const int j = ((col0 - c32) >> 2) + q;          // 16-byte piece of the 128-byte row
@@ -389,14 +389,14 @@ __device__ __forceinline__ void split_row_tf32(float* hi, float* lo, int row) {
         const int p = q ^ (row & (NP - 1));   // neighbouring rows start on different banks
         const float4 v = h[p];
         float4 a, b;
-        a.x = tc::round_tf32(v.x);
-        a.y = tc::round_tf32(v.y);
-        a.z = tc::round_tf32(v.z);
-        a.w = tc::round_tf32(v.w);
-        b.x = tc::round_tf32(v.x - a.x);
-        b.y = tc::round_tf32(v.y - a.y);
-        b.z = tc::round_tf32(v.z - a.z);
-        b.w = tc::round_tf32(v.w - a.w);
+        a.x = tc::round_tf32_bits(v.x);
+        a.y = tc::round_tf32_bits(v.y);
+        a.z = tc::round_tf32_bits(v.z);
+        a.w = tc::round_tf32_bits(v.w);
+        b.x = tc::round_tf32_bits(v.x - a.x);
+        b.y = tc::round_tf32_bits(v.y - a.y);
+        b.z = tc::round_tf32_bits(v.z - a.z);
+        b.w = tc::round_tf32_bits(v.w - a.w);
         h[p] = a;
         l[p] = b;
     }
@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                const PruneTcArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    __shared__ __align__(8) uint64_t bar_full[MAXST], bar_empty[MAXST], bar_done;
+    __shared__ __align__(8) uint64_t bar_full[MAXST], bar_empty[MAXST], bar_done, bar_drain;
     __shared__ uint32_t tmem_sh;
     __shared__ int abort_sh;
     __shared__ int cmask_sh[2][2];  // [node parity][child]: K chunks holding a leaf column of the tile
@@ -431,6 +431,7 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             tc::mbar_init(&bar_empty[q], 1);
         }
         tc::mbar_init(&bar_done, 1);
+        tc::mbar_init(&bar_drain, 1);
         tc::mbar_init_fence();
         abort_sh = 0;
     }
@@ -644,7 +645,8 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                 g += (uint32_t)n_chunks;        // every thread tracks the stage sequence
                 __syncthreads();
                 if (!abort_sh) {
-                    if (!tc::mbar_wait(&bar_done, dn & 1)) {
+                    // (a test hook can make this wait give up after limit - 1 polls)
+                    if (!tc::mbar_wait(&bar_done, dn & 1, a.debug_wait_limit > 0 ? a.debug_wait_limit - 1 : (1 << 24))) {
                         atomicExch(a.status, 2);
                         abort_sh = 1;
                     }
@@ -664,8 +666,8 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             float scl[2] = {1.0f, 1.0f};
             int E = ns2.Eacc;
             bool nflag = ns2.flag;
-            float maxp, bf, bp, bq, be;
-            epi_scan<2>(ns2, W, is_root, Rf, prior_f, scl, maxp, bf, bp, bq, be);
+            float maxp, bf, bp, bq, be, fmx[2], fmn[2];
+            epi_scan<2>(ns2, W, is_root, Rf, prior_f, scl, maxp, bf, bp, bq, be, fmx, fmn);
             // Without an error model, every state-0 entry is exact: row 0 of
             // every matrix is delta(s, 0), so L[0] is 1 (scaled by a power of
             // two) when all leaves below are 0, else 0, and it is then the
@@ -696,8 +698,8 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                     E = ns2.Eacc + maxe;
                 }
                 if (is_root) {
-                    float m2, f2, p2, q2, e2;
-                    epi_scan<2>(ns2, W, true, Rf, prior_f, scl, m2, f2, p2, q2, e2);
+                    float m2, f2, p2, q2, e2, x2[2], n2[2];
+                    epi_scan<2>(ns2, W, true, Rf, prior_f, scl, m2, f2, p2, q2, e2, x2, n2);
                     if (need) {
                         bf = f2;
                         bp = p2;
@@ -710,11 +712,18 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             flag |= nflag && !dead;
             if (!is_root) {
                 // stage 0 holds the two staging tiles
-                float ev;
                 epi_store<2>(ns2, W, scl, reinterpret_cast<float*>(smem), tid, &map_vst,
-                             (int)(vrow_cta + (int64_t)vs * TM), ev);
+                             (int)(vrow_cta + (int64_t)vs * TM));
                 Esh[vs * TM + tid] = E;
-                // the stored vector's bound: the product's, plus values flushed on the store
+                // the stored vector's bound, from the factors' maxima: u_A (f_B + u_B)
+                // + u_B f_A over all states, with a leaf factor's u counted only
+                // if it fell below 2^-100 somewhere; plus values flushed on the store
+                float u0 = ns2.ue[0], u1 = ns2.ue[1];
+                if (ns2.leaf[0] && !(fmn[0] < 0x1p-100f)) u0 = 0.0f;
+                if (ns2.leaf[1] && !(fmn[1] < 0x1p-100f)) u1 = 0.0f;
+                u0 *= scl[0];
+                u1 *= scl[1];
+                const float ev = u0 * (fmx[1] * scl[1] + u1) + u1 * (fmx[0] * scl[0]);
                 Erh[vs * TM + tid] = fminf(ev + kTiny, 1e30f);
             } else if (fam >= 0) {
                 double o = NAN;
@@ -754,6 +763,12 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
     if (tid == 0) tc::bulk_wait0();
     tc::fence_before();
     __syncthreads();
+    // after a time-out the MMAs this thread issued may still be running:
+    // they complete before TMEM goes away (a full-length bounded wait)
+    if (abort_sh && tid == 0) {
+        tc::mma_commit(&bar_drain);
+        tc::mbar_wait(&bar_drain, 0, 1 << 24);
+    }
     if (abort_sh && tid == 0)
         for (int q = 0; q < MAXST; ++q)
             if (q < NS && last_full[q]) tc::mbar_wait(&bar_full[q], last_full_parity[q], 1 << 20);

@@ -225,6 +225,7 @@ struct cafe_ctx {
     size_t cache_bytes = 0, cache_cap = 0;
     uint64_t request_stamp = 0;
     std::map<int, std::pair<int, int>> tuned;   // bin width -> (CTAs per SM, stages) chosen by cafe_autotune
+    int debug_wait_limit = 0;    // cafe_debug_set: polls before the tensor-core wait for a node's GEMMs gives up
     // workspaces: [0] for synchronous calls, [1..] for the serving loop
     std::vector<std::unique_ptr<cafe::Workspace>> ws;
     std::unique_ptr<cafe::Workspace> ws_alt;   // second workspace of the device-pointer calls

@@ -154,5 +154,12 @@ CAFE_DEV float round_tf32(float x) {
     return __uint_as_float(r);
 }
 
+// The same rounding by integer arithmetic on the bit pattern (finite
+// values): adding half a TF32 unit (bit 12) to the magnitude and clearing
+// the 13 low mantissa bits rounds |x| to nearest, ties away from zero, for
+// either sign (sign-magnitude encoding). Cheaper than the conversion
+// instruction where a whole operand tile is split.
+CAFE_DEV float round_tf32_bits(float x) { return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u); }
+
 }  // namespace tc
 }  // namespace cafe

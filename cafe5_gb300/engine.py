@@ -299,6 +299,10 @@ class Context:
         self._check(self.lib.cafe_simulate(self.h, C.byref(req), C.byref(io)))
         return sizes, lam
 
+    def debug_set(self, knob: int, value: int):
+        """Test hooks (cafe_debug_set); see include/cafe_gb300.h."""
+        self._check(self.lib.cafe_debug_set(self.h, int(knob), int(value)))
+
     def profile(self, enable: bool = True):
         self._check(self.lib.cafe_profile_enable(self.h, 1 if enable else 0))
 

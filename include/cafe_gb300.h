@@ -104,6 +104,15 @@ const char* cafe_last_error(const cafe_ctx* ctx);
 const char* cafe_status_string(int status);
 int cafe_version(void);
 
+/* Test hooks (no counterpart in the reference). CAFE_DEBUG_TC_WAIT_LIMIT:
+ * value n > 0 makes the tensor-core kernel's wait for a node's GEMMs give
+ * up after n - 1 polls (1: at once); 0 restores the default bound of 2^24
+ * polls. With 1 a test can check that the kernel drains its own copies and
+ * MMAs, frees TMEM, and the call returns CAFE_ERR_TIMEOUT with the context
+ * still usable. */
+typedef enum { CAFE_DEBUG_TC_WAIT_LIMIT = 1 } cafe_debug_knob;
+int cafe_debug_set(cafe_ctx* ctx, int knob, int64_t value);
+
 /* ---- inputs ---------------------------------------------------------- */
 /* Species tree (clade, src/clade.h:25-121). Nodes are numbered so that the
  * children of every node appear in increasing index (Newick order), which
