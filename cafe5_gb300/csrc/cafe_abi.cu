@@ -958,37 +958,6 @@ TcShape tc_shape(cafe_ctx* C, const TreeHost& T, int W) {
     return sh;
 }
 
-// Launch shape of the warp-specialised walk for one bin width: as many
-// tiles in flight per CTA as TMEM (2 W columns each) and registers allow,
-// then as many ring stages (2 to 4) as shared memory holds.
-struct WsShape {
-    int nctx = 0, stages = 0, tmem_cols = 0;
-    size_t smem = 0;
-};
-
-WsShape ws_shape(const TreeHost& T, int W, bool err) {
-    WsShape sh;
-    const size_t cap = (size_t)prune_ws_max_smem();
-    if (T.max_children > 2) return sh;
-    for (int nctx = W <= 64 ? 3 : (W <= 128 ? 2 : 1); nctx >= 1; --nctx) {
-        int cols = 32;
-        while (cols < 2 * nctx * W) cols *= 2;
-        if (cols > 512) continue;
-        for (int st = 4; st >= 2; --st) {
-            const size_t sm =
-                prune_ws_smem_bytes(W, T.n_slots, st, (int)T.internal.size(), T.n_leaves, T.n_nodes, nctx, err);
-            if (sm <= cap) {
-                sh.nctx = nctx;
-                sh.stages = st;
-                sh.tmem_cols = cols;
-                sh.smem = sm;
-                return sh;
-            }
-        }
-    }
-    return sh;
-}
-
 // Share of the 1e-6 per-family budget (|dlnL| / |lnL|) left to FP32 range
 // loss; TF32x3 rounding takes the rest.
 constexpr double kRangeTau = 1e-7;
@@ -1105,11 +1074,10 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         // concurrently: TMEM (512 columns per SM) and shared memory set how
         // many tiles of a bin share an SM
         struct BinLaunch {
-            int W, tmem_cols, stages, per_sm, n_ctas, nctx;
+            int W, tmem_cols, stages, per_sm, n_ctas;
             size_t smem;
             int64_t first_tile, n_tiles, vrow_base;
         };
-        static const bool classic = getenv("CAFE_TC_CLASSIC") != nullptr;
         std::vector<BinLaunch> launches;
         int64_t vrows = 0;
         for (size_t i = 0; i < tc_tiles.size();) {
@@ -1117,24 +1085,6 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             while (j < tc_tiles.size() && tc_tiles[j].S == tc_tiles[i].S) ++j;
             BinLaunch L{};
             L.W = tc_tiles[i].S + 1;
-            const WsShape wsh = classic ? WsShape{} : ws_shape(T, L.W, R->use_error_model != 0);
-            if (wsh.nctx > 0) {
-                // warp-specialised walk: one CTA per SM, nctx tiles in flight
-                L.nctx = wsh.nctx;
-                L.tmem_cols = wsh.tmem_cols;
-                L.stages = wsh.stages;
-                L.smem = wsh.smem;
-                L.per_sm = 1;
-                L.first_tile = (int64_t)i;
-                L.n_tiles = (int64_t)(j - i);
-                L.n_ctas = (int)std::max<int64_t>(
-                    1, std::min<int64_t>((L.n_tiles + L.nctx - 1) / L.nctx, (int64_t)C->sm_count));
-                L.vrow_base = vrows;
-                vrows += (int64_t)L.n_ctas * L.nctx * T.n_slots * 128;
-                launches.push_back(L);
-                i = j;
-                continue;
-            }
             const TcShape shape = tc_shape(C, T, L.W);
             if (shape.per_sm < 1) return fail(C, CAFE_ERR_INVALID, "tensor-core tile does not fit shared memory");
             L.tmem_cols = shape.tmem_cols;
@@ -1195,8 +1145,8 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         a.phase_clocks = nullptr;
         static const bool phase_env = getenv("CAFE_TC_PHASES") != nullptr;
         if (phase_env) {
-            CK(ws.phase.reserve(16 * sizeof(unsigned long long)), "phase clocks");
-            CK(cudaMemsetAsync(ws.phase.p, 0, 16 * sizeof(unsigned long long), ws.stream), "phase clocks");
+            CK(ws.phase.reserve(6 * sizeof(unsigned long long)), "phase clocks");
+            CK(cudaMemsetAsync(ws.phase.p, 0, 6 * sizeof(unsigned long long), ws.stream), "phase clocks");
             a.phase_clocks = ws.phase.as<unsigned long long>();
         }
         if (prof) {
@@ -1220,14 +1170,9 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             b.stages = L.stages;
             b.vrow_base = L.vrow_base;
             cudaStream_t st = fork ? ws.aux[li % Workspace::kAux] : ws.stream;
-            if (L.nctx > 0)
-                CK(op_launch(ws, 10, [&] { return launch_prune_ws(maps, b, L.nctx, L.n_ctas, L.smem, st); }, maps, b,
-                             L.nctx, L.n_ctas, L.smem, st),
-                   "prune ws");
-            else
-                CK(op_launch(ws, 5, [&] { return launch_prune_tc(maps, b, L.n_ctas, L.smem, st); }, maps, b, L.n_ctas,
-                             L.smem, st),
-                   "prune tc");
+            CK(op_launch(ws, 5, [&] { return launch_prune_tc(maps, b, L.n_ctas, L.smem, st); }, maps, b, L.n_ctas, L.smem,
+                         st),
+               "prune tc");
         }
         if (fork && !prof) {
             const int rcw = launch_wide();
@@ -1241,24 +1186,12 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         }
 
         if (phase_env) {
-            unsigned long long h[16];
+            unsigned long long h[6];
             CK(cudaMemcpyAsync(h, ws.phase.p, sizeof(h), cudaMemcpyDeviceToHost, ws.stream), "phase clocks");
             CK(cudaStreamSynchronize(ws.stream), "phase clocks");
-            if (classic) {
-                const double n = (double)h[5] + 1e-9;
-                fprintf(stderr, "k_prune_tc clocks per tile-node: setup %.0f gemm %.0f epilogue %.0f root %.0f sync %.0f (%llu tile-nodes)\n",
-                        h[0] / n, h[1] / n, h[2] / n, h[3] / n, h[4] / n, h[5]);
-            } else {
-                // role totals summed over CTAs; per tile-node of the context threads
-                const double nodes = (double)h[12] + 1e-9, chunks = (double)h[13] + 1e-9;
-                fprintf(stderr,
-                        "k_prune_ws: %llu tile-nodes %llu chunks; kernel %.3g clk (sum over CTAs) | producer: pick %.3g "
-                        "empty %.3g busy %.3g | mma per chunk: wait %.0f issue %.0f | context per tile-node: setup %.0f "
-                        "build %.0f acc-wait %.0f scan %.0f store %.0f end %.0f\n",
-                        h[12], h[13], (double)h[14], (double)h[0], (double)h[1], (double)h[2], h[5] / chunks,
-                        h[6] / chunks, h[11] / nodes, h[4] / nodes, h[7] / nodes, h[8] / nodes, h[9] / nodes,
-                        h[10] / nodes);
-            }
+            const double n = (double)h[5] + 1e-9;
+            fprintf(stderr, "k_prune_tc clocks per tile-node: setup %.0f gemm %.0f epilogue %.0f root %.0f sync %.0f (%llu tile-nodes)\n",
+                    h[0] / n, h[1] / n, h[2] / n, h[3] / n, h[4] / n, h[5]);
         }
 
         if (prof) C->prof.end(1, ws.stream, ev);
@@ -2493,7 +2426,7 @@ int cafe_ctx_create(const cafe_config* cfg, cafe_ctx** out) {
     cudaDeviceProp prop;
     cudaGetDeviceProperties(&prop, dev);
     C->sm_count = prop.multiProcessorCount;
-    if (tc_kernels_init() != cudaSuccess || prune_ws_init() != cudaSuccess || prune64_cluster_init() != cudaSuccess ||
+    if (tc_kernels_init() != cudaSuccess || prune64_cluster_init() != cudaSuccess ||
         cudaEventCreateWithFlags(&C->gate, cudaEventDisableTiming) != cudaSuccess) {
         delete C;
         return CAFE_ERR_CUDA;

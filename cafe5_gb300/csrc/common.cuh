@@ -186,17 +186,6 @@ struct TcMaps {
 
 cudaError_t launch_prune_tc(const TcMaps& maps, const PruneTcArgs& a, int n_ctas, size_t smem, cudaStream_t s);
 
-// The warp-specialised walk (k_prune_ws): `nctx` tiles in flight per CTA
-// (1 to 3; the CTA has 64 + 128 nctx threads and 2 nctx W TMEM columns),
-// `a.stages` ring stages (2 to 4), one CTA per SM. Node vectors are written
-// to a.vec directly (pitch Wm); the maps it reads are mat_hi, mat_lo, vec.
-size_t prune_ws_smem_bytes(int W, int n_slots, int stages, int n_internal, int n_leaves, int n_nodes, int nctx,
-                           bool err);
-int prune_ws_max_smem();
-cudaError_t prune_ws_init();
-cudaError_t launch_prune_ws(const TcMaps& maps, const PruneTcArgs& a, int nctx, int n_ctas, size_t smem,
-                            cudaStream_t s);
-
 // Families whose tensor-core result may have lost accuracy to FP32's range:
 // for every (family, candidate), the category terms' range-error bounds
 // weighted by the terms' shares of the family likelihood; over

@@ -219,8 +219,10 @@ __device__ __forceinline__ void write_leaf_row(float* tile, int r, const LeafW& 
     float* row = tile + (size_t)r * KC;
     const int c0 = kc * KC;
     const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    // pieces visited in swizzled order, so neighbouring rows hit different banks
+    const int sw = KC == 32 ? (r & 7) : ((r >> 1) & 3);
 #pragma unroll
-    for (int j = 0; j < KC / 4; ++j) reinterpret_cast<float4*>(row)[j] = z;
+    for (int j = 0; j < KC / 4; ++j) reinterpret_cast<float4*>(row)[j ^ sw] = z;
     // then the (at most three) nonzero columns, each at its swizzled place
 #pragma unroll
     for (int d = 0; d < 3; ++d) {

@@ -35,33 +35,6 @@ CAFE_DEV bool mbar_wait(uint64_t* b, uint32_t parity, int limit = (1 << 24)) {
     return false;
 }
 
-// Plain arrival (count 1, no transaction bytes).
-CAFE_DEV void mbar_arrive(uint64_t* b) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
-}
-
-// Named barrier `id` over `n` threads (a multiple of 32); id 0 is __syncthreads.
-CAFE_DEV void named_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
-// Named barrier that also ORs a predicate over its threads.
-CAFE_DEV bool named_sync_or(int id, int n, bool p) {
-    uint32_t r;
-    asm volatile(
-        "{\n .reg .pred a, b;\n setp.ne.u32 a, %1, 0;\n bar.red.or.pred b, %2, %3, a;\n selp.u32 %0, 1, 0, b;\n}\n"
-        : "=r"(r)
-        : "r"((uint32_t)p), "r"(id), "r"(n)
-        : "memory");
-    return r != 0;
-}
-// Shared-memory counters handed between roles of a CTA.
-CAFE_DEV int ld_acquire_shared(const int* p) {
-    int v;
-    asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
-    return v;
-}
-CAFE_DEV void st_release_shared(int* p, int v) {
-    asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
-}
-
 // 2D TMA tile load (box given by the tensor map) into shared memory,
 // completion counted in bytes on `bar`.
 CAFE_DEV void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
