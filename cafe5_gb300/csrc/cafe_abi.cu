@@ -924,9 +924,9 @@ struct TcShape {
     size_t smem = 0;
 };
 
-int tc_by_smem(const TreeHost& T, int W, int stages, size_t* smem) {
+int tc_by_smem(const TreeHost& T, int W, int stages, size_t* smem, int nsplit = 1) {
     *smem = prune_tc_smem_bytes(W, T.n_slots, stages, (int)T.internal.size());
-    if (*smem > (size_t)prune_tc_max_smem()) return 0;
+    if (*smem > (size_t)prune_tc_max_smem(nsplit)) return 0;
     return (int)((227 * 1024) / (*smem + 1024));
 }
 
@@ -962,7 +962,12 @@ TcShape tc_shape(cafe_ctx* C, const TreeHost& T, int W) {
 // loss; TF32x3 rounding takes the rest.
 constexpr double kRangeTau = 1e-7;
 
-// MIXED_TF32X3: tensor-core tiles for bins <= 256 states, FP64 tiles for
+// Widest bin on the tensor cores: one CTA per tile up to 256 states (both
+// children's factors in 2 W <= 512 TMEM columns), a pair of CTAs (half the
+// states each) for 384 and 512.
+constexpr int kTcMaxW = 512;
+
+// MIXED_TF32X3: tensor-core tiles for bins <= 512 states, FP64 tiles for
 // wider bins and for families the tensor-core pass flags. Caller holds C->mu;
 // hm holds the FP64 matrix of every (category, node).
 int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T, FamSet& S, int K, int CT,
@@ -975,7 +980,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
     const int msize = B.W_max;
     int Wm = 0;
     for (int w : B.widths)
-        if (w <= 256) Wm = std::max(Wm, w);
+        if (w <= kTcMaxW) Wm = std::max(Wm, w);
     info->scaled = true;
 
     // request-local matrix list and conversion to TF32 operands (a cache
@@ -1014,13 +1019,13 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
     std::vector<PruneTile>& cl_tiles = ws.cl_tile_vec;
     cl_tiles.clear();
     for (size_t b = 0; b < B.widths.size(); ++b) {
-        if (B.widths[b] > 256 && fp64_cluster_bin(C, T, B.bin_count[b], KC, B.widths[b])) {
+        if (B.widths[b] > kTcMaxW && fp64_cluster_bin(C, T, B.bin_count[b], KC, B.widths[b])) {
             add_cluster_tiles(cl_tiles, B, b, active);
             continue;
         }
         for (int k : active) {
             const int w = B.widths[b];
-            const int step = w <= 256 ? 128 : 32;
+            const int step = w <= kTcMaxW ? 128 : 32;
             for (int64_t i = 0; i < B.bin_count[b]; i += step) {
                 PruneTile t{};
                 t.first = (int)(B.bin_first[b] + i);
@@ -1028,7 +1033,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
                 t.k = k;
                 t.S = w - 1;
                 t.R = w - 1;
-                (w <= 256 ? tc_tiles : wide_tiles).push_back(t);
+                (w <= kTcMaxW ? tc_tiles : wide_tiles).push_back(t);
             }
         }
     }
@@ -1074,9 +1079,23 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         // concurrently: TMEM (512 columns per SM) and shared memory set how
         // many tiles of a bin share an SM
         struct BinLaunch {
-            int W, tmem_cols, stages, per_sm, n_ctas;
+            int W, tmem_cols, stages, per_sm, n_ctas, nsplit;
             size_t smem;
             int64_t first_tile, n_tiles, vrow_base;
+        };
+        // Bins of 128 states or more split each tile over a cluster of
+        // nsplit CTAs (4 or 2; W / nsplit a multiple of 32 and at least 64)
+        // when the bin is sparse enough that every tile still gets SMs of
+        // its own: a lone tile's walk is bound by what one SM can stream.
+        // Bins over 256 states always split (both children's factors, 2 W
+        // columns, would not fit one CTA's TMEM).
+        auto pick_split = [&](int W, int64_t n_tiles) {
+            for (int ns : {4, 2}) {
+                const int wn = W / ns;
+                if (W % ns || wn % 32 || wn < 64 || wn > 256) continue;
+                if (n_tiles * ns <= (int64_t)C->sm_count) return ns;
+            }
+            return W > 256 ? 2 : 1;
         };
         std::vector<BinLaunch> launches;
         int64_t vrows = 0;
@@ -1085,6 +1104,32 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             while (j < tc_tiles.size() && tc_tiles[j].S == tc_tiles[i].S) ++j;
             BinLaunch L{};
             L.W = tc_tiles[i].S + 1;
+            L.first_tile = (int64_t)i;
+            L.n_tiles = (int64_t)(j - i);
+            L.nsplit = pick_split(L.W, L.n_tiles);
+            if (L.nsplit > 1) {
+                // the deepest pipeline of W / nsplit B rows that fits
+                const int wn = L.W / L.nsplit;
+                L.tmem_cols = 32;
+                while (L.tmem_cols < 2 * wn) L.tmem_cols *= 2;
+                L.per_sm = 1;
+                for (int st = 4; st >= 1 && !L.stages; --st)
+                    if (tc_by_smem(T, wn, st, &L.smem, L.nsplit) >= 1) L.stages = st;
+                if (!L.stages) return fail(C, CAFE_ERR_INVALID, "tensor-core tile does not fit shared memory");
+                // over half an SM's shared memory: two cluster CTAs (of this or
+                // another cluster launch) never share an SM, so no CTA holding
+                // TMEM waits on a peer that waits for that SM's TMEM
+                L.smem = std::min(std::max(L.smem, (size_t)120 * 1024), (size_t)prune_tc_max_smem(L.nsplit));
+                const int64_t clusters =
+                    std::max<int64_t>(1, std::min<int64_t>(L.n_tiles, (int64_t)C->sm_count / L.nsplit));
+                L.n_ctas = (int)(L.nsplit * clusters);
+                L.vrow_base = vrows;
+                vrows += clusters * T.n_slots * 128;
+                launches.push_back(L);
+                i = j;
+                continue;
+            }
+            L.nsplit = 1;
             const TcShape shape = tc_shape(C, T, L.W);
             if (shape.per_sm < 1) return fail(C, CAFE_ERR_INVALID, "tensor-core tile does not fit shared memory");
             L.tmem_cols = shape.tmem_cols;
@@ -1094,8 +1139,6 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             // pad shared memory so no more CTAs of this launch than TMEM allows share an SM
             L.smem = std::max(L.smem, (size_t)((227 * 1024) / L.per_sm) - 2048);
             L.smem = std::min(L.smem, (size_t)prune_tc_max_smem());
-            L.first_tile = (int64_t)i;
-            L.n_tiles = (int64_t)(j - i);
             L.n_ctas = (int)std::max<int64_t>(1, std::min<int64_t>(L.n_tiles, (int64_t)C->sm_count * L.per_sm));
             L.vrow_base = vrows;
             vrows += (int64_t)L.n_ctas * T.n_slots * 128;
@@ -1159,17 +1202,20 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             CK(op_record(ws, ws.ev_fork, ws.stream), "fork");
             for (int q = 0; q < Workspace::kAux; ++q) CK(op_wait(ws, ws.aux[q], ws.ev_fork), "fork");
         }
-        for (size_t li = 0; li < launches.size(); ++li) {
+        // widest bins (the longest walks) first, each on its own stream
+        for (size_t q = 0; q < launches.size(); ++q) {
+            const size_t li = launches.size() - 1 - q;
             const BinLaunch& L = launches[li];
             PruneTcArgs b;
             std::memcpy(&b, &a, sizeof b);     // padding included: the bytes are a graph signature
             b.tiles = ws.tiles.as<PruneTile>() + L.first_tile;
             b.n_tiles = (int)L.n_tiles;
             b.tmem_cols = L.tmem_cols;
-            b.Ws = L.W;
+            b.nsplit = L.nsplit;
+            b.Ws = L.W / L.nsplit;
             b.stages = L.stages;
             b.vrow_base = L.vrow_base;
-            cudaStream_t st = fork ? ws.aux[li % Workspace::kAux] : ws.stream;
+            cudaStream_t st = fork ? ws.aux[q % Workspace::kAux] : ws.stream;
             CK(op_launch(ws, 5, [&] { return launch_prune_tc(maps, b, L.n_ctas, L.smem, st); }, maps, b, L.n_ctas, L.smem,
                          st),
                "prune tc");
@@ -1222,7 +1268,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         fp.perm = B.d_perm.as<int64_t>();
         fp.n_bins = 0;
         for (size_t b = 0; b < B.widths.size() && fp.n_bins < 16; ++b) {
-            if (B.widths[b] > 256) continue;
+            if (B.widths[b] > kTcMaxW) continue;
             fp.bin_width[fp.n_bins] = B.widths[b];
             fp.bin_first[fp.n_bins] = B.bin_first[b];
             fp.bin_count[fp.n_bins] = B.bin_count[b];

@@ -167,7 +167,9 @@ struct PruneTcArgs {
                                  // range loss (values below 2^-126 flushed), or null
     int32_t* status;             // [1] nonzero when a bounded wait gave up
     int tmem_cols;
-    int Ws;                      // widest bin of this launch (shared-memory B rows)
+    int nsplit;                  // 1: one CTA per tile; 2 or 4: a cluster of nsplit CTAs per tile, CTA h
+                                 // computing states [h W/nsplit, (h + 1) W/nsplit) of every node
+    int Ws;                      // B rows per stage: the launch's bin width / nsplit
     int stages;                  // pipeline stages (1 to 4)
     int64_t vrow_base;           // first node-vector row of this launch
     unsigned long long* phase_clocks;   // optional [6]: SM clocks of thread 0 in child setup, GEMMs,
@@ -203,7 +205,7 @@ struct RangeFlagArgs {
 cudaError_t launch_range_flags(const RangeFlagArgs& a, cudaStream_t s);
 size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages, int n_internal);
 int prune_tc_kchunk();   // K columns per operand box of k_prune_tc (its load maps' box width)
-int prune_tc_max_smem(); // dynamic shared memory one k_prune_tc CTA may use
+int prune_tc_max_smem(int nsplit = 1);   // dynamic shared memory one k_prune_tc CTA may use (per split)
 
 // Device-side plan of the FP64 recompute of flagged families: compacts the
 // flagged families of each listed bin (in permutation order) into fb_perm

@@ -54,6 +54,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <cstring>
 
 namespace cafe {
 namespace {
@@ -70,6 +71,12 @@ static_assert(KC == 32 || KC == 16, "K chunk of 16 or 32 columns");
 constexpr int SC = 32;    // columns per staging tile of the epilogue's TMA stores (128-byte swizzle)
 constexpr int MAXST = 4;  // pipeline stages at most
 constexpr int NTHREADS = 128;
+constexpr int kXN = 9;           // values per family in one pair exchange
+// root rows the prior table holds: bins up to 256 states in one CTA, up to
+// 512 in a pair (the single-CTA kernel keeps the smaller table: four CTAs
+// of the 64-state bin fill an SM's shared memory to the last kilobyte)
+template <int NSPLIT>
+__host__ __device__ constexpr int prior_rows() { return NSPLIT > 1 ? 512 : 256; }
 
 #ifndef CAFE_TC_CW
 #define CAFE_TC_CW 16
@@ -141,6 +148,48 @@ struct NodeSrc {
 
 constexpr float kTiny = 0x1p-126f;   // smallest normal FP32 value
 
+// Handshakes among the NSPLIT CTAs of a cluster (NSPLIT > 1).
+struct ClusterX {
+    uint32_t seq;    // handshakes so far (the same in every thread of every CTA)
+    uint32_t rank;   // this CTA's rank in the cluster
+    const float* buf;   // the buffer of the last handshake: [NSPLIT - 1][kXN][TM]
+};
+
+// One handshake: this thread's N values go to the same family's slot in
+// every other CTA's buffer (sender s at position (s - r - 1) mod NSPLIT of
+// receiver r), every thread arrives on every other CTA's barrier
+// (releasing its stores), then waits (bounded) for the others'
+// arrivals. Handshakes alternate between two buffers and two barriers, so
+// no CTA can be more than one handshake ahead of what the others have
+// read. Returns false in every thread of the CTA when some wait gave up.
+template <int NSPLIT, int N>
+__device__ __forceinline__ bool cluster_exchange(ClusterX& cx, float* xbuf, uint64_t* bar_x, const float* mine,
+                                                 int tid) {
+    const uint32_t slot = cx.seq & 1, parity = (cx.seq >> 1) & 1;
+    cx.seq++;
+    float* buf = xbuf + (size_t)slot * (NSPLIT - 1) * kXN * TM;
+#pragma unroll
+    for (int d = 1; d < NSPLIT; ++d) {
+        const uint32_t r = (cx.rank + d) % NSPLIT;
+        const int p = (int)((cx.rank + NSPLIT - r - 1) % NSPLIT);
+#pragma unroll
+        for (int i = 0; i < N; ++i) tc::st_cluster_f32(tc::mapa(buf + ((size_t)p * kXN + i) * TM + tid, r), mine[i]);
+    }
+#pragma unroll
+    for (int d = 1; d < NSPLIT; ++d) tc::mbar_arrive_remote(tc::mapa(&bar_x[slot], (cx.rank + d) % NSPLIT));
+    const bool ok = tc::mbar_wait_cluster(&bar_x[slot], parity);
+    cx.buf = buf;
+    return __syncthreads_or(!ok) == 0;
+}
+
+// Value i of CTA r's last handshake for this thread's family.
+template <int NSPLIT>
+__device__ __forceinline__ float xval(const ClusterX& cx, uint32_t r, const float* mine, int i, int tid) {
+    if (r == cx.rank) return mine[i];
+    const int p = (int)((r + NSPLIT - cx.rank - 1) % NSPLIT);
+    return cx.buf[((size_t)p * kXN + i) * TM + tid];
+}
+
 // Absolute error bound of factor c at a state whose unscaled value is raw.
 template <int NC>
 __device__ __forceinline__ float fac_err(const NodeSrc<NC>& ns, int c, float raw) {
@@ -157,7 +206,8 @@ struct LeafW {
 template <int NC>
 __device__ __forceinline__ void setup_src(const PruneTcArgs& a, const ChildInfo* ch, int nch, const int* Esh,
                                           const float* Erh, uint32_t tmem_lane, int64_t fam, int tid, int S, int W,
-                                          const int (&count)[NC], NodeSrc<NC>& ns, LeafW (&lw)[NC], int* cmask_sh) {
+                                          int Wt, const int (&count)[NC], NodeSrc<NC>& ns, LeafW (&lw)[NC],
+                                          int* cmask_sh) {
     ns.Eacc = 0;
     ns.flag = false;
 #pragma unroll
@@ -176,7 +226,7 @@ __device__ __forceinline__ void setup_src(const PruneTcArgs& a, const ChildInfo*
         ns.leaf[c] = false;
         if (sc.unit) continue;
         const ChildInfo ci = ch[c];
-        sc.taddr = tmem_lane + (uint32_t)(ci.tcol * W);
+        sc.taddr = tmem_lane + (uint32_t)(ci.tcol * Wt);   // Wt TMEM columns per child
         if (ci.leaf_col < 0) {
             ns.Eacc += Esh[ci.slot * TM + tid];
             ns.ue[c] = Erh[ci.slot * TM + tid] + (float)(8 * W) * kTiny;
@@ -255,9 +305,11 @@ __device__ __forceinline__ void load_children(const NodeSrc<NC>& ns, int col0, u
 // Pass 1 over the product of the children's factors, each scaled by
 // scl[c]: its maximum over the states (inner node), or the largest
 // prior-weighted value over root rows 1..Rf (root; index j = state j + 1).
+// The W TMEM columns hold states s_off .. s_off + W - 1.
 // Warp-collective (TMEM loads).
 template <int NC>
-__device__ __forceinline__ void epi_scan(const NodeSrc<NC>& ns, int W, bool is_root, int Rf, const float* prior_f,
+__device__ __forceinline__ void epi_scan(const NodeSrc<NC>& ns, int W, int s_off, bool is_root, int Rf,
+                                         const float* prior_f,
                                          const float (&scl)[NC], float& maxp, float& best_f, float& best_p,
                                          float& best_q, float& best_err, float (&fmx)[NC], float (&fmn)[NC]) {
     static_assert(NC == 2, "two factors per node");
@@ -288,7 +340,7 @@ __device__ __forceinline__ void epi_scan(const NodeSrc<NC>& ns, int W, bool is_r
         } else {
 #pragma unroll
             for (int j = 0; j < CW; ++j) {
-                const int s = col0 + j;
+                const int s = s_off + col0 + j;
                 if (s >= 1 && s <= Rf) {
                     maxp = fmaxf(maxp, p[j]);
                     const float q = prior_f[s - 1];
@@ -311,10 +363,10 @@ __device__ __forceinline__ void epi_scan(const NodeSrc<NC>& ns, int W, bool is_r
 
 // Exact path (warp-collective; lanes that do not need it ignore the
 // result): the largest per-state sum of the factors' binary exponents over
-// states [s_lo, s_hi). Arguments travel by value so the caller's copies
-// stay in registers.
+// states [s_lo, s_hi) (the W TMEM columns hold states s_off ..). Arguments
+// travel by value so the caller's copies stay in registers.
 template <int NC>
-__device__ __noinline__ int epi_maxexp(const NodeSrc<NC> ns, int W, int s_lo, int s_hi) {
+__device__ __noinline__ int epi_maxexp(const NodeSrc<NC> ns, int W, int s_off, int s_lo, int s_hi) {
     int maxe = -100000;
     for (int col0 = 0; col0 < W; col0 += CW) {
         uint32_t r[NC][CW];
@@ -328,7 +380,7 @@ __device__ __noinline__ int epi_maxexp(const NodeSrc<NC> ns, int W, int s_lo, in
             for (int j = 0; j < CW; ++j) ex[j] += bexp(__uint_as_float(r[c][j]));
 #pragma unroll
         for (int j = 0; j < CW; ++j) {
-            const int s = col0 + j;
+            const int s = s_off + col0 + j;
             if (s >= s_lo && s < s_hi && ex[j] > maxe) maxe = ex[j];
         }
     }
@@ -337,11 +389,12 @@ __device__ __noinline__ int epi_maxexp(const NodeSrc<NC> ns, int W, int s_lo, in
 
 // Pass 2 (inner nodes; every thread of the CTA): the scaled product in FP32
 // into a staging tile in the 128-byte-swizzled layout, 32 columns at a
-// time, written to the node's vector rows by TMA stores. The parent's GEMM
-// splits it into TF32 hi/lo as it loads it (split_row_tf32).
+// time, written to the node's vector rows by TMA stores (columns x_off ..
+// x_off + W - 1). The parent's GEMM splits it into TF32 hi/lo as it loads
+// it (split_row_tf32).
 template <int NC>
 __device__ __forceinline__ void epi_store(const NodeSrc<NC>& ns, int W, const float (&scl)[NC], float* stg, int tid,
-                                          const CUtensorMap* map, int vrow) {
+                                          const CUtensorMap* map, int vrow, int x_off) {
     static_assert(NC == 2, "two factors per node");
     // two staging tiles of TM x SC floats, used in turn: a chunk waits only
     // for the stores of the chunk two back
@@ -373,7 +426,7 @@ __device__ __forceinline__ void epi_store(const NodeSrc<NC>& ns, int W, const fl
         tc::fence_proxy_async_shared();
         __syncthreads();
         if (tid == 0) {
-            for (int r = 0; r < TM / 32; ++r) tc::tma_store_2d(map, c32, vrow + 32 * r, tile + r * 32 * SC);
+            for (int r = 0; r < TM / 32; ++r) tc::tma_store_2d(map, x_off + c32, vrow + 32 * r, tile + r * 32 * SC);
             tc::bulk_commit();
         }
     }
@@ -404,19 +457,37 @@ __device__ __forceinline__ void split_row_tf32(float* hi, float* lo, int row) {
     }
 }
 
-__global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
+// NSPLIT = 2 or 4: a cluster of NSPLIT CTAs shares each tile -- bins of
+// 384 and 512 states, whose two children's factors would need 2 W > 512
+// TMEM columns, and sparse bins of 128 to 256 states, whose few tiles would
+// otherwise walk the tree on few SMs. CTA h keeps output states
+// [h Wn, h Wn + Wn), Wn = W / NSPLIT, of both children in TMEM (B operand:
+// those rows of each matrix; A operand: the child's whole vector). The
+// per-family statistics the epilogue's decisions rest on (maxima, minima,
+// the best root row, the exponent sums) are exchanged through distributed
+// shared memory, so every CTA takes the same decisions and scales its
+// states alike; each stores its columns of the node vector, and a
+// handshake after the stores' completion lets the parent's GEMM read them
+// all. Every handshake wait is bounded.
+template <int NSPLIT>
+__global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
     k_prune_tc(const __grid_constant__ CUtensorMap map_mhi, const __grid_constant__ CUtensorMap map_mlo,
                const __grid_constant__ CUtensorMap map_vec, const __grid_constant__ CUtensorMap map_vst,
                const PruneTcArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     __shared__ __align__(8) uint64_t bar_full[MAXST], bar_empty[MAXST], bar_done, bar_drain;
+    __shared__ __align__(8) uint64_t bar_x[2];     // cluster handshakes (NSPLIT > 1), in turn
+    // [2][NSPLIT - 1][kXN][TM]: the other CTAs' values, per handshake
+    __shared__ float xbuf[NSPLIT > 1 ? 2 * (NSPLIT - 1) * kXN * TM : 1];
     __shared__ uint32_t tmem_sh;
     __shared__ int abort_sh;
     __shared__ int cmask_sh[2][2];  // [node parity][child]: K chunks holding a leaf column of the tile
-    __shared__ float prior_f[256];
+    __shared__ float prior_f[prior_rows<NSPLIT>()];
 
     const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t h = NSPLIT > 1 ? tc::cluster_rank() : 0u;   // this CTA's share of the states
+    const int cid = (int)blockIdx.x / NSPLIT, n_cl = (int)gridDim.x / NSPLIT;
     const int Wm = a.Wm;
     const int NS = a.stages;
     const TreePlan& P = a.plan;
@@ -425,7 +496,7 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
     float* Erh = reinterpret_cast<float*>(Esh + (size_t)a.n_slots * TM);   // [n_slots][TM] error bounds
     NodeInfo* nodes = reinterpret_cast<NodeInfo*>(Erh + (size_t)a.n_slots * TM);   // [n_internal]
 
-    for (int j = tid; j < 256; j += NTHREADS) prior_f[j] = j < a.n_prior ? (float)a.prior[j] : 0.0f;
+    for (int j = tid; j < prior_rows<NSPLIT>(); j += NTHREADS) prior_f[j] = j < a.n_prior ? (float)a.prior[j] : 0.0f;
     if (warp == 0) tc::tmem_alloc(&tmem_sh, (uint32_t)a.tmem_cols);
     if (tid == 0) {
         for (int q = 0; q < MAXST; ++q) {
@@ -434,12 +505,20 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
         }
         tc::mbar_init(&bar_done, 1);
         tc::mbar_init(&bar_drain, 1);
+        if (NSPLIT > 1) {
+            // one arrival per thread of every other CTA (a count of at least 1)
+            tc::mbar_init(&bar_x[0], (NSPLIT > 1 ? NSPLIT - 1 : 1) * NTHREADS);
+            tc::mbar_init(&bar_x[1], (NSPLIT > 1 ? NSPLIT - 1 : 1) * NTHREADS);
+        }
         tc::mbar_init_fence();
         abort_sh = 0;
     }
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
+    // every CTA's barriers are initialised before the first remote arrival
+    if (NSPLIT > 1) tc::cluster_sync_all();
+    ClusterX cx{0u, h, nullptr};
     const uint32_t tmem = tmem_sh;
     const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
 
@@ -447,17 +526,21 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
     uint32_t dn = 0;         // completions of bar_done observed (all threads)
     int last_full[MAXST] = {0, 0, 0, 0};            // thread 0: stage has a TMA not yet waited for
     uint32_t last_full_parity[MAXST] = {0, 0, 0, 0};
-    const int64_t vrow_cta = a.vrow_base + (int64_t)blockIdx.x * a.n_slots * TM;
+    // node-vector rows of this tile (the CTAs of a cluster share them, each
+    // writing its own columns)
+    const int64_t vrow_cta = a.vrow_base + (int64_t)cid * a.n_slots * TM;
     unsigned long long ph[6] = {0, 0, 0, 0, 0, 0};
     const bool timing = a.phase_clocks != nullptr && tid == 0;
 
-    for (int t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
+    for (int t = cid; t < a.n_tiles; t += n_cl) {
         const PruneTile tile = a.tiles[t];
         const int cnt = tile.count, k = tile.k, S = tile.S, W = tile.S + 1;
+        const int Wn = W / NSPLIT;              // output states (TMEM columns) per child in this CTA
+        const int s_off = (int)h * Wn;          // this CTA's first output state
         const int64_t fam = tid < cnt ? a.perm[tile.first + tid] : -1;
         const int Rf = (fam >= 0 && a.fam_R) ? a.fam_R[fam] : tile.R;
         const int32_t* mi = a.mat_index + (size_t)k * P.n_nodes;
-        const uint32_t idesc = tc::idesc_tf32(TM, W);
+        const uint32_t idesc = tc::idesc_tf32(TM, Wn);
         bool flag = false;
         bool dead = false;   // an exact zero vector through a saturated branch: the family's term is 0
 
@@ -502,13 +585,25 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             int* cmask = cmask_sh[ii & 1];
             const long long ts = timing ? clock64() : 0;
             // the previous nodes' TMA stores must be complete before this node
-            // overwrites their staging tile or reads their rows back
+            // overwrites their staging tile or reads their rows back (in a
+            // cluster: the other CTAs' columns as well)
             if (tid == 0) tc::bulk_wait0();
+            if (NSPLIT > 1) {
+                if (tid == 0) tc::fence_proxy_async_global();
+                __syncthreads();
+                if (!cluster_exchange<NSPLIT, 0>(cx, xbuf, bar_x, nullptr, tid)) {
+                    if (tid == 0) {
+                        atomicExch(a.status, 1);
+                        abort_sh = 1;
+                    }
+                }
+                if (tid == 0) tc::fence_proxy_async_global();
+            }
             // child sources; leaf weights and the K chunks they touch
             NodeSrc<2> ns2;
             LeafW lw[2];
             const int cnt_cur[2] = {cnt_next[0], cnt_next[1]};
-            setup_src<2>(a, nd.c, nch, Esh, Erh, tmem + lane_base, fam, tid, S, W, cnt_cur, ns2, lw, cmask);
+            setup_src<2>(a, nd.c, nch, Esh, Erh, tmem + lane_base, fam, tid, S, W, Wn, cnt_cur, ns2, lw, cmask);
             // counts of the next node's leaves, in flight during this node
             if (ii + 1 < P.n_internal) {
                 const NodeInfo& nx = nodes[ii + 1];
@@ -564,7 +659,7 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                         }
                         if (leaf && i >= NS) __syncthreads();      // stage free for every writer
                         if (tid == 0 && !abort_sh) {
-                            tc::mbar_expect_tx(&bar_full[st], (uint32_t)(((leaf ? 0 : TM) + 2 * W) * KC * sizeof(float)));
+                            tc::mbar_expect_tx(&bar_full[st], (uint32_t)(((leaf ? 0 : TM) + 2 * Wn) * KC * sizeof(float)));
                             if (!leaf) {
                                 // the FP32 node vector lands in the hi operand; the
                                 // consumer splits it into hi and lo in place
@@ -572,8 +667,8 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                                 for (int r = 0; r < TM / 32; ++r)
                                     tc::tma_load_2d(Ahi + r * 32 * KC, &map_vec, kc * KC, vrow + 32 * r, &bar_full[st]);
                             }
-                            const int mrow = chi.mat * Wm;
-                            for (int r = 0; r < W / 32; ++r) {
+                            const int mrow = chi.mat * Wm + s_off;     // this CTA's output states
+                            for (int r = 0; r < Wn / 32; ++r) {
                                 tc::tma_load_2d(Bhi + r * 32 * KC, &map_mhi, kc * KC, mrow + 32 * r, &bar_full[st]);
                                 tc::tma_load_2d(Blo + r * 32 * KC, &map_mlo, kc * KC, mrow + 32 * r, &bar_full[st]);
                             }
@@ -627,7 +722,7 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                         if (tc::mbar_wait(&bar_full[st], u & 1)) {
                             last_full[st] = 0;
                             tc::fence_after();
-                            const uint32_t d = tmem + (uint32_t)(chi.tcol * W);
+                            const uint32_t d = tmem + (uint32_t)(chi.tcol * Wn);
 #pragma unroll
                             for (int ks = 0; ks < KC / 8; ++ks) {
                                 const uint64_t ah = desc_k(Ahi + ks * 8), al = desc_k(Alo + ks * 8);
@@ -669,7 +764,37 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             int E = ns2.Eacc;
             bool nflag = ns2.flag;
             float maxp, bf, bp, bq, be, fmx[2], fmn[2];
-            epi_scan<2>(ns2, W, is_root, Rf, prior_f, scl, maxp, bf, bp, bq, be, fmx, fmn);
+            epi_scan<2>(ns2, Wn, s_off, is_root, Rf, prior_f, scl, maxp, bf, bp, bq, be, fmx, fmn);
+            if (NSPLIT > 1) {
+                // every CTA's statistics: maxima, minima, the best root row
+                // (combined in rank order, so a tie goes to the first in state
+                // order, as in one CTA's scan)
+                const float mine[kXN] = {maxp, fmx[0], fmx[1], fmn[0], fmn[1], bf, bp, bq, be};
+                if (!cluster_exchange<NSPLIT, kXN>(cx, xbuf, bar_x, mine, tid)) {
+                    if (tid == 0) {
+                        atomicExch(a.status, 1);
+                        abort_sh = 1;
+                    }
+                    cx.buf = nullptr;
+                }
+                if (cx.buf) {
+#pragma unroll
+                    for (int r = 0; r < NSPLIT; ++r) {
+                        const float f = xval<NSPLIT>(cx, r, mine, 5, tid);
+                        maxp = fmaxf(maxp, xval<NSPLIT>(cx, r, mine, 0, tid));
+                        fmx[0] = fmaxf(fmx[0], xval<NSPLIT>(cx, r, mine, 1, tid));
+                        fmx[1] = fmaxf(fmx[1], xval<NSPLIT>(cx, r, mine, 2, tid));
+                        fmn[0] = fminf(fmn[0], xval<NSPLIT>(cx, r, mine, 3, tid));
+                        fmn[1] = fminf(fmn[1], xval<NSPLIT>(cx, r, mine, 4, tid));
+                        be = fmaxf(be, xval<NSPLIT>(cx, r, mine, 8, tid));
+                        if (r == 0 || f > bf) {
+                            bf = f;
+                            bp = xval<NSPLIT>(cx, r, mine, 6, tid);
+                            bq = xval<NSPLIT>(cx, r, mine, 7, tid);
+                        }
+                    }
+                }
+            }
             // Without an error model, every state-0 entry is exact: row 0 of
             // every matrix is delta(s, 0), so L[0] is 1 (scaled by a power of
             // two) when all leaves below are 0, else 0, and it is then the
@@ -684,11 +809,23 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                 scl[0] = pow2f(kk);
                 E -= kk;
             }
-            if (__any_sync(0xffffffffu, need)) {
+            // (in a pair the decision is the same in both CTAs: it rests on the
+            // exchanged statistics of the same families)
+            if (NSPLIT > 1 ? __syncthreads_or(need) != 0 : __any_sync(0xffffffffu, need)) {
                 // underflow: rescale by the largest per-state exponent sum, so the
                 // product's maximum is in [2^-2, 1) unless the factors are more
                 // than 2^250 apart (then FP64 recomputes the family)
-                int maxe = epi_maxexp<2>(ns2, W, is_root ? 1 : 0, is_root ? Rf + 1 : W);
+                int maxe = epi_maxexp<2>(ns2, Wn, s_off, is_root ? 1 : 0, is_root ? Rf + 1 : W);
+                if (NSPLIT > 1) {
+                    const float mine[1] = {__int_as_float(maxe)};
+                    if (cluster_exchange<NSPLIT, 1>(cx, xbuf, bar_x, mine, tid)) {
+#pragma unroll
+                        for (int r = 0; r < NSPLIT; ++r) maxe = max(maxe, __float_as_int(xval<NSPLIT>(cx, r, mine, 0, tid)));
+                    } else if (tid == 0) {
+                        atomicExch(a.status, 1);
+                        abort_sh = 1;
+                    }
+                }
                 if (need) {
                     if (maxe < -250) {
                         nflag = true;
@@ -701,7 +838,25 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                 }
                 if (is_root) {
                     float m2, f2, p2, q2, e2, x2[2], n2[2];
-                    epi_scan<2>(ns2, W, true, Rf, prior_f, scl, m2, f2, p2, q2, e2, x2, n2);
+                    epi_scan<2>(ns2, Wn, s_off, true, Rf, prior_f, scl, m2, f2, p2, q2, e2, x2, n2);
+                    if (NSPLIT > 1) {
+                        const float mine[4] = {f2, p2, q2, e2};
+                        if (cluster_exchange<NSPLIT, 4>(cx, xbuf, bar_x, mine, tid)) {
+#pragma unroll
+                            for (int r = 0; r < NSPLIT; ++r) {
+                                const float f = xval<NSPLIT>(cx, r, mine, 0, tid);
+                                e2 = fmaxf(e2, xval<NSPLIT>(cx, r, mine, 3, tid));
+                                if (r == 0 || f > f2) {
+                                    f2 = f;
+                                    p2 = xval<NSPLIT>(cx, r, mine, 1, tid);
+                                    q2 = xval<NSPLIT>(cx, r, mine, 2, tid);
+                                }
+                            }
+                        } else if (tid == 0) {
+                            atomicExch(a.status, 1);
+                            abort_sh = 1;
+                        }
+                    }
                     if (need) {
                         bf = f2;
                         bp = p2;
@@ -714,8 +869,8 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             flag |= nflag && !dead;
             if (!is_root) {
                 // stage 0 holds the two staging tiles
-                epi_store<2>(ns2, W, scl, reinterpret_cast<float*>(smem), tid, &map_vst,
-                             (int)(vrow_cta + (int64_t)vs * TM));
+                epi_store<2>(ns2, Wn, scl, reinterpret_cast<float*>(smem), tid, &map_vst,
+                             (int)(vrow_cta + (int64_t)vs * TM), s_off);
                 Esh[vs * TM + tid] = E;
                 // the stored vector's bound, from the factors' maxima: u_A (f_B + u_B)
                 // + u_B f_A over all states, with a leaf factor's u counted only
@@ -727,7 +882,7 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                 u1 *= scl[1];
                 const float ev = u0 * (fmx[1] * scl[1] + u1) + u1 * (fmx[0] * scl[0]);
                 Erh[vs * TM + tid] = fminf(ev + kTiny, 1e30f);
-            } else if (fam >= 0) {
+            } else if (fam >= 0 && h == 0) {     // (a cluster's first CTA writes the term)
                 double o = NAN;
                 const double best = (double)bp * (double)bq;
                 if (dead) o = a.model == 0 ? -INFINITY : NAN;   // log 0 (base) / a failed family (gamma)
@@ -751,7 +906,7 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
                 ph[5] += 1;           // tile-nodes
             }
         }
-        if (flag && fam >= 0) {
+        if (flag && fam >= 0 && h == 0) {
             atomicOr(&a.flags[fam], 1);
             atomicOr(a.status + 3, 1);     // "some family is flagged"
         }
@@ -776,16 +931,26 @@ __global__ void __launch_bounds__(NTHREADS, CAFE_TC_MINB)
             if (q < NS && last_full[q]) tc::mbar_wait(&bar_full[q], last_full_parity[q], 1 << 20);
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)a.tmem_cols);
+    // no CTA of a cluster exits while another may still write into its
+    // shared memory or arrive on its barriers (every wait before this is
+    // bounded)
+    if (NSPLIT > 1) tc::cluster_sync_all();
 }
 
-// FP64 matrix -> TF32 hi/lo operands (row-major, pitch Wm).
-__global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict__ jobs, TcBuffers b) {
-    const ConvertJob J = jobs[blockIdx.x];
+// FP64 matrix -> TF32 hi/lo operands (row-major, pitch Wm); each block
+// converts `rows` rows of one matrix (a matrix of side 512 spreads over 64
+// blocks, so a few hundred matrices fill the GPU).
+__global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict__ jobs, TcBuffers b, int rows) {
     const int Wm = b.Wm;
-    const size_t base = (size_t)J.mat * Wm * Wm;
-    for (int idx = threadIdx.x; idx < Wm * Wm; idx += blockDim.x) {
-        const int s = idx / Wm, c = idx % Wm;
-        const float x = (float)J.src[(size_t)s * J.ld + c];
+    const int per_mat = (Wm + rows - 1) / rows;
+    const ConvertJob J = jobs[blockIdx.x / per_mat];
+    const int r0 = (int)(blockIdx.x % per_mat) * rows;
+    const int n = (min(Wm, r0 + rows) - r0) * Wm;
+    const size_t base = ((size_t)J.mat * Wm + r0) * Wm;
+    const double* src = J.src + (size_t)r0 * J.ld;
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+        const int s = idx / Wm, c = idx - s * Wm;
+        const float x = (float)src[(size_t)s * J.ld + c];
         const float h = tc::round_tf32(x);
         b.hi[base + idx] = h;
         b.lo[base + idx] = tc::round_tf32(x - h);
@@ -904,7 +1069,12 @@ cudaError_t launch_range_flags(const RangeFlagArgs& a, cudaStream_t s) {
 // k_prune_tc's dynamic shared-memory limit is raised once, to the most a
 // CTA may use, so launches of different widths need no per-launch change.
 cudaError_t tc_kernels_init() {
-    return cudaFuncSetAttribute(k_prune_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, prune_tc_max_smem());
+    cudaError_t e = cudaFuncSetAttribute(k_prune_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, prune_tc_max_smem(1));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_prune_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, prune_tc_max_smem(2));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_prune_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, prune_tc_max_smem(4));
+    return e;
 }
 
 cudaError_t launch_fallback_plan(const FallbackPlanArgs& a, cudaStream_t s) {
@@ -915,21 +1085,25 @@ cudaError_t launch_fallback_plan(const FallbackPlanArgs& a, cudaStream_t s) {
 int prune_tc_kchunk() { return KC; }
 
 // Dynamic shared memory one k_prune_tc CTA may use: the device's per-block
-// opt-in limit minus the kernel's static shared memory.
-int prune_tc_max_smem() {
-    static int cached = -1;
-    if (cached < 0) {
+// opt-in limit minus the kernel instance's static shared memory (the
+// cluster instances hold the handshake buffers).
+int prune_tc_max_smem(int nsplit) {
+    static int cached[5] = {-1, -1, -1, -1, -1};
+    if (nsplit != 1 && nsplit != 2 && nsplit != 4) return 0;
+    if (cached[nsplit] < 0) {
         int dev = 0, optin = 0;
         cudaFuncAttributes fa{};
+        const void* fn = nsplit == 1 ? (const void*)k_prune_tc<1> : nsplit == 2 ? (const void*)k_prune_tc<2>
+                                                                              : (const void*)k_prune_tc<4>;
         if (cudaGetDevice(&dev) != cudaSuccess ||
             cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
-            cudaFuncGetAttributes(&fa, (const void*)k_prune_tc) != cudaSuccess) {
+            cudaFuncGetAttributes(&fa, fn) != cudaSuccess) {
             cudaGetLastError();
             return 0;
         }
-        cached = optin - (int)fa.sharedSizeBytes;
+        cached[nsplit] = optin - (int)fa.sharedSizeBytes;
     }
-    return cached;
+    return cached[nsplit];
 }
 
 size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages, int n_internal) {
@@ -939,16 +1113,40 @@ size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages, int n_internal) {
 
 cudaError_t launch_convert_tc(const ConvertJob* d_jobs, int n_jobs, TcBuffers b, cudaStream_t s) {
     if (n_jobs <= 0) return cudaSuccess;
-    k_convert_tc<<<n_jobs, 256, 0, s>>>(d_jobs, b);
+    const int rows = std::max(1, std::min(b.Wm, 4096 / std::max(1, b.Wm)));
+    const int per_mat = (b.Wm + rows - 1) / rows;
+    k_convert_tc<<<(unsigned)(n_jobs * per_mat), 256, 0, s>>>(d_jobs, b, rows);
     return cudaGetLastError();
 }
 
 cudaError_t launch_prune_tc(const TcMaps& m, const PruneTcArgs& a, int n_ctas, size_t smem, cudaStream_t s) {
     if (a.n_tiles <= 0) return cudaSuccess;
-    if (smem > (size_t)prune_tc_max_smem()) return cudaErrorInvalidValue;
+    if (smem > (size_t)prune_tc_max_smem(a.nsplit)) return cudaErrorInvalidValue;
     if (a.stages < 1 || a.stages > MAXST) return cudaErrorInvalidValue;
-    k_prune_tc<<<n_ctas, NTHREADS, smem, s>>>(m.mat_hi, m.mat_lo, m.vec, m.vst, a);
-    return cudaGetLastError();
+    if (a.nsplit == 1) {
+        k_prune_tc<1><<<n_ctas, NTHREADS, smem, s>>>(m.mat_hi, m.mat_lo, m.vec, m.vst, a);
+        return cudaGetLastError();
+    }
+    // a cluster of nsplit CTAs per tile, each with Ws = W / nsplit output
+    // states (a multiple of 32: whole 32-row TMA boxes) of both children
+    if ((a.nsplit != 2 && a.nsplit != 4) || n_ctas % a.nsplit || a.Ws % 32 || a.Ws > 256 ||
+        a.tmem_cols < 2 * a.Ws || a.tmem_cols > 512)
+        return cudaErrorInvalidValue;
+    cudaLaunchConfig_t cfg;
+    std::memset(&cfg, 0, sizeof cfg);
+    cfg.gridDim = dim3((unsigned)n_ctas, 1, 1);
+    cfg.blockDim = dim3(NTHREADS, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)a.nsplit;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (a.nsplit == 2) return cudaLaunchKernelEx(&cfg, k_prune_tc<2>, m.mat_hi, m.mat_lo, m.vec, m.vst, a);
+    return cudaLaunchKernelEx(&cfg, k_prune_tc<4>, m.mat_hi, m.mat_lo, m.vec, m.vst, a);
 }
 
 }  // namespace cafe

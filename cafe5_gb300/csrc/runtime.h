@@ -143,10 +143,10 @@ struct Workspace {
     bool build_inline = false;         // this call builds on `stream` (synchronous calls)
     cudaEvent_t ev_jobs = nullptr;     // after the last build (its job table read)
     bool jobs_pending = false;
-    static constexpr int kAux = 3;     // streams for concurrent per-bin launches
-    cudaStream_t aux[kAux] = {nullptr, nullptr, nullptr};
+    static constexpr int kAux = 8;     // streams for concurrent per-bin launches (one per bin)
+    cudaStream_t aux[kAux] = {};
     cudaEvent_t ev_fork = nullptr;
-    cudaEvent_t ev_join[kAux] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev_join[kAux] = {};
     struct MapCache {
         const void* ptr = nullptr;
         int64_t rows = 0;

@@ -161,5 +161,47 @@ CAFE_DEV float round_tf32(float x) {
 // instruction where a whole operand tile is split.
 CAFE_DEV float round_tf32_bits(float x) { return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u); }
 
+// ---- a pair of CTAs in one thread-block cluster ----
+CAFE_DEV uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// Every thread of every CTA of the cluster; orders shared-memory accesses
+// (release / acquire at cluster scope). Waits without a limit: only used
+// where every CTA is known to arrive (after bounded waits only).
+CAFE_DEV void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// The address of this shared-memory location in CTA `rank` of the cluster.
+CAFE_DEV uint32_t mapa(const void* p, uint32_t rank) {
+    uint32_t ra;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(smem_u32(p)), "r"(rank));
+    return ra;
+}
+CAFE_DEV void st_cluster_f32(uint32_t ra, float v) {
+    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(ra), "f"(v) : "memory");
+}
+// One arrival on an mbarrier of another CTA of the cluster, releasing this
+// thread's earlier writes (its remote stores included) at cluster scope.
+CAFE_DEV void mbar_arrive_remote(uint32_t ra_bar) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(ra_bar) : "memory");
+}
+// Bounded wait on this CTA's mbarrier, acquiring at cluster scope what the
+// arrivals (possibly remote) released.
+CAFE_DEV bool mbar_wait_cluster(uint64_t* b, uint32_t parity, int limit = (1 << 24)) {
+    for (int i = 0; i < limit; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, "
+            "1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(smem_u32(b)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
 }  // namespace tc
 }  // namespace cafe

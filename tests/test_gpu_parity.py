@@ -386,14 +386,38 @@ def test_mixed_saturated_gamma_many_families_stays_on_tensor_cores(ctx):
 
 
 def test_mixed_wide_bins_hybrid(ctx):
-    """Families needing more than 256 states run on FP64 tiles in the same
-    request; the rest on the tensor cores."""
+    """Families needing more than 256 states (bin 384: a pair of CTAs per
+    tile) in the same request as families of the single-CTA bins."""
     from cafe5_gb300.synth import workload
     w = workload(0, n_families=600, seed=23)
     counts = w.families.counts.copy()
     counts[:7] += 230            # bins 384 (counts ~240-260)
     a, b = _both(ctx, w.tree, counts, [0.0025])
     _check_mixed(a, b)
+
+
+def test_mixed_pair_tiles_vs_oracle_and_tile_walk(ctx):
+    """Bins 384 and 512 on the tensor cores: each 128-family tile is shared by
+    a cluster of two CTAs, each computing half the states and exchanging the
+    per-family statistics. 160 gamma (K = 4) families of the config-1 tree
+    with counts of 230-400 against the rescaled FP64 oracle at 1e-6; then the
+    same families tiled 40 times (200 tiles per bin, more than the pairs the
+    GPU holds, so every pair walks several tiles) give the same bits. The
+    range bound must leave most families on the tensor cores."""
+    from cafe5_gb300.synth import workload
+    w = workload(1, n_families=400, seed=31)
+    counts = w.families.counts[w.families.counts.max(axis=1) < 40][:160].copy()
+    counts[:80] += 230                  # bin 384
+    counts[80:] += 330                  # bin 512
+    mult, probs = w.multipliers, w.cat_probs
+    a, b = _both(ctx, w.tree, counts, [0.002], model=1, mult=mult, probs=probs)
+    assert b.n_fallback < len(counts) // 4, f"{b.n_fallback} of {len(counts)} families recomputed in FP64"
+    _check_mixed(a, b)
+    _check_vs_oracle(b, *_scaled_oracle_binned(w.tree, counts, [0.002], model=1, mult=mult, probs=probs))
+    big = np.tile(counts, (40, 1))
+    c, d = _both(ctx, w.tree, big, [0.002], model=1, mult=mult, probs=probs)
+    for r in range(40):
+        assert np.array_equal(d.family_lnl[r * len(counts):(r + 1) * len(counts)], b.family_lnl), r
 
 
 def test_mixed_results_do_not_depend_on_batch_composition(ctx):
@@ -411,8 +435,9 @@ def test_mixed_results_do_not_depend_on_batch_composition(ctx):
 def test_sparse_fp64_bins_walk_one_family_per_cluster(ctx, wl, model):
     """FP64 bins too sparse to fill the GPU with 32-family tiles are walked
     one family per thread-block cluster; their families get the same bits as
-    in a bin full enough for the 32-family tile walk, in fp64_binned and in
-    mixed_tf32x3 (whose bins above 256 states run in FP64). The small golden
+    in a bin full enough for the 32-family tile walk in fp64_binned, and
+    mixed_tf32x3 (bins 384 and 512 on the tensor cores, in CTA pairs) gives
+    the same bits in both sets as well. The small golden
     cases of test_fp64_binned_matches_scaled_oracle run on the cluster walk
     (every bin sparse) against the oracle."""
     from cafe5_gb300.families import FamilySet, bin_families
