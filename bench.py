@@ -740,6 +740,17 @@ def pvalue_phase(ctx, tid, sid, w, fams, S, R, cpu_seconds: float, n_sim: int = 
            "simulated_families": R * n_sim, "observed_families": F, "S": S,
            "note": "whole cafe_pvalues call; the simulation is sequential on the host (the reference's "
                    "mt19937 stream), both prunings on the GPU"}
+    # the opt-in device-sampled mode: every step on the GPU, the same
+    # distributions but not the reference's random stream
+    ctx.pvalues(tid, sid, lam, S=S, R=R, n_simulations=50, seed=1, device_sampling=True)
+    t0 = time.perf_counter()
+    rd = ctx.pvalues(tid, sid, lam, S=S, R=R, n_simulations=n_sim, seed=10, device_sampling=True)
+    wall_d = (time.perf_counter() - t0) * 1e3
+    out["device_sampled"] = {"value": pruned / (wall_d / 1e3), "wall_ms": wall_d, "device_ms": rd["device_ms"],
+                             "host_ms": rd["host_ms"],
+                             "mean_abs_dp_vs_reference_stream": float(np.mean(np.abs(rd["pvalues"] - r["pvalues"]))),
+                             "note": "device_sampling = 1: draws, grouping, pruning, sort and ranks on the GPU "
+                                     "(counter-based generator; equal in distribution, not the reference's stream)"}
     if cpu_seconds > 0:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle

@@ -78,7 +78,7 @@ class TuneResult(C.Structure):
 
 class ServingInfo(C.Structure):
     _fields_ = [("batches", C.c_int64), ("merged", C.c_int64), ("retried", C.c_int64), ("enqueue_ms", C.c_double),
-                ("wait_ms", C.c_double), ("device_ms", C.c_double)]
+                ("wait_ms", C.c_double), ("device_ms", C.c_double), ("overlap_ms", C.c_double)]
 
 
 class Reconstruction(C.Structure):
@@ -90,7 +90,7 @@ class Reconstruction(C.Structure):
 class PvaluesOut(C.Structure):
     _fields_ = [("n_simulations", C.c_int), ("seed", C.c_uint32), ("pvalues", C.c_void_p),
                 ("conditional", C.c_void_p), ("root_likelihood", C.c_void_p), ("device_ms", C.c_double),
-                ("host_ms", C.c_double)]
+                ("host_ms", C.c_double), ("device_sampling", C.c_int)]
 
 
 class Simulation(C.Structure):

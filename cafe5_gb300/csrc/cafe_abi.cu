@@ -169,7 +169,8 @@ cudaError_t PinnedBuf::reserve(size_t n) {
 Workspace::~Workspace() {
     for (auto& g : graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
-    if (stream) cudaStreamDestroy(stream);
+    if (stream_hi) cudaStreamDestroy(stream_hi);
+    if (stream_lo) cudaStreamDestroy(stream_lo);
     if (ev_start) cudaEventDestroy(ev_start);
     if (ev_stop) cudaEventDestroy(ev_stop);
     if (ev_staged) cudaEventDestroy(ev_staged);
@@ -188,7 +189,10 @@ int Workspace::init(int device) {
     // pruning CTAs leave free
     int least = 0, greatest = 0;
     cudaDeviceGetStreamPriorityRange(&least, &greatest);
-    if (cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, greatest) != cudaSuccess) return CAFE_ERR_CUDA;
+    if (cudaStreamCreateWithPriority(&stream_hi, cudaStreamNonBlocking, greatest) != cudaSuccess) return CAFE_ERR_CUDA;
+    if (cudaStreamCreateWithPriority(&stream_lo, cudaStreamNonBlocking, std::min(least, greatest + 1)) != cudaSuccess)
+        return CAFE_ERR_CUDA;
+    stream = stream_hi;
     if (cudaEventCreate(&ev_start) != cudaSuccess) return CAFE_ERR_CUDA;
     if (cudaEventCreate(&ev_stop) != cudaSuccess) return CAFE_ERR_CUDA;
     if (cudaEventCreateWithFlags(&ev_staged, cudaEventDisableTiming) != cudaSuccess) return CAFE_ERR_CUDA;
@@ -1687,11 +1691,12 @@ bool small_request(const cafe_ctx* C, const cafe_request* R, int NB, int64_t F) 
     return F * NB * K < (int64_t)C->sm_count * 128;
 }
 
-// Requests' device timelines run one after another: each waits for the
-// previous request's last launch. Persistent tensor-core CTAs take every
-// register of an SM, so interleaving the launches of concurrent requests
-// would starve their small kernels; ordered, each request runs at full
-// speed while host work and copies of the others overlap. Caller holds C->mu.
+// Direct calls on the context's own workspaces (cafe_score_batch_device)
+// keep their device timelines in call order: each waits for the previous
+// call's last launch. Serving batches do not: their work overlaps on the
+// device (the matrix cache is append-only while anything is in flight, and
+// every other buffer a batch writes belongs to its workspace). Caller
+// holds C->mu.
 cudaError_t gate_enter(cafe_ctx* C, Workspace& ws) {
     return C->gate_set ? cudaStreamWaitEvent(ws.stream, C->gate, 0) : cudaSuccess;
 }
@@ -1714,15 +1719,10 @@ int score_enqueue(cafe_ctx* C, Workspace& ws, const cafe_request* R, int NB, caf
     CK(ws.fam_lnl.reserve((size_t)std::max<int64_t>(F, 1) * NB * sizeof(double)), "family buffer");
     CK(ws.total.reserve((size_t)NB * sizeof(double)), "total");
     CK(cudaEventRecord(ws.ev_start, ws.stream), "event");
-    // a request too small to fill the device (fewer family-categories than
-    // one 128-family tile per SM) runs beside the others instead of in turn
-    const bool gated = !small_request(C, R, NB, F);
-    if (gated) CK(gate_enter(C, ws), "gate");
     const auto t_host = std::chrono::steady_clock::now();
     int rc = enqueue_score(C, ws, R, NB, ws.fam_lnl.as<double>(), ws.total.as<double>(), info);
     if (rc) return rc;
     if (C->prof.on && ws.sync) C->prof.acc.host_total_ms += host_ms_since(t_host);
-    if (gated) CK(gate_leave(C, ws), "gate");
     CK(cudaEventRecord(ws.ev_staged, ws.stream), "event");
     ws.staged = true;
     CK(cudaEventRecord(ws.ev_stop, ws.stream), "event");
@@ -2109,6 +2109,163 @@ int host_sampler_init(cafe_ctx* C, Workspace& ws, const cafe_request* R, const T
 
 // ---- p-values
 
+// compute_pvalues with the simulated families drawn on the GPU (k_pvalue.cu:
+// a counter-based generator, one thread per family; the same distributions
+// as the reference's draws, not its stream). Every step runs on the device:
+// the row CDFs, the draws, the grouping of the simulated families into
+// 32-family tiles of equal (root size, state bound), their pruning with the
+// root fixed, the per-root-size sort and the p-value search; the host only
+// copies the results back.
+int pvalues_device(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_pvalues_out* out) {
+    const auto t_host0 = std::chrono::steady_clock::now();
+    ReconSetup Z;
+    int rc = recon_setup(C, ws, R, false, &Z);
+    if (rc) return rc;
+    TreeHost& T = *Z.T;
+    FamSet& FS = *Z.S;
+    const int S = Z.Smax, RR = Z.Rmax, msize = Z.msize, nsim = out->n_simulations, n = T.n_nodes;
+    if (nsim > kSortRowsMaxP)
+        return fail(C, CAFE_ERR_INVALID, "device sampling takes at most %d simulations per root size", kSortRowsMaxP);
+    const int n_ps = std::max(RR, S) + 1;
+    if (n_ps > msize) return fail(C, CAFE_ERR_INVALID, "parent sizes beyond the matrices");
+    const int64_t F = FS.F;
+    const int L = T.n_leaves;
+    const int64_t NS = (int64_t)RR * nsim;
+    const int n_keys = RR * (S + 1);
+    const int64_t max_tiles = NS / 32 + n_keys + 1;
+    const int Wmax = std::max(S + 1, RR);
+    DevBuf d_cdf, d_sizes, d_sim, d_keys, d_hist, d_cursor, d_perm, d_tiles, d_ntiles, d_simL, d_obsL, d_pv, d_tree,
+        d_otiles;
+    CK(d_cdf.reserve((size_t)n * n_ps * S * sizeof(double)), "row cdfs");
+    CK(d_sizes.reserve((size_t)NS * n * sizeof(int32_t)), "simulated families");
+    CK(d_sim.reserve(std::max<size_t>((size_t)NS * L, 1) * sizeof(int32_t)), "simulated families");
+    CK(d_keys.reserve((size_t)NS * sizeof(int32_t)), "simulated families");
+    CK(d_hist.reserve((size_t)n_keys * sizeof(int32_t)), "simulation plan");
+    CK(d_cursor.reserve((size_t)n_keys * sizeof(int32_t)), "simulation plan");
+    CK(d_perm.reserve((size_t)NS * sizeof(int64_t)), "simulation plan");
+    CK(d_tiles.reserve((size_t)max_tiles * sizeof(PruneTile)), "tiles");
+    CK(d_ntiles.reserve(16), "tiles");
+    CK(d_simL.reserve((size_t)NS * sizeof(double)), "simulated likelihoods");
+    CK(d_obsL.reserve(std::max<size_t>((size_t)F * RR, 1) * sizeof(double)), "root vectors");
+    CK(d_pv.reserve(std::max<size_t>((size_t)F, 1) * sizeof(double)), "p-values");
+    // prefix order, parents and leaf columns of the tree
+    const std::vector<int> prefix = prefix_order(T);
+    std::vector<int32_t> tree_tab(3 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        tree_tab[i] = prefix[i];
+        tree_tab[n + i] = T.parent[i];
+        tree_tab[2 * n + i] = T.leaf_col[i];
+    }
+    CK(d_tree.reserve(tree_tab.size() * sizeof(int32_t)), "tree");
+    CK(cudaMemcpy(d_tree.p, tree_tab.data(), tree_tab.size() * sizeof(int32_t), cudaMemcpyHostToDevice), "tree");
+    // observed families: states 0..S, root sizes 1..R
+    std::vector<PruneTile> otiles;
+    for (int64_t f = 0; f < F; f += 32) {
+        PruneTile t{};
+        t.first = (int)f;
+        t.count = (int)std::min<int64_t>(32, F - f);
+        t.S = S;
+        t.R = RR;
+        t.root_lo = 1;
+        otiles.push_back(t);
+    }
+    if (!otiles.empty()) {
+        CK(d_otiles.reserve(otiles.size() * sizeof(PruneTile)), "tiles");
+        CK(cudaMemcpy(d_otiles.p, otiles.data(), otiles.size() * sizeof(PruneTile), cudaMemcpyHostToDevice), "tiles");
+    }
+    const int n_ctas_max = C->n_ctas;
+    CK(ws.scratch.reserve((size_t)n_ctas_max * T.n_slots * Wmax * 32 * sizeof(double)), "scratch");
+    double host_ms = host_ms_since(t_host0);
+
+    Prune64Args a{};
+    a.plan = T.plan;
+    a.mats = ws.mats.as<const double*>();
+    a.ld_mat = msize;
+    a.scratch = ws.scratch.as<double>();
+    a.scratch_per_cta = (int64_t)T.n_slots * Wmax * 32;
+    a.K = 1;
+    a.tile_families = 32;
+    a.W = Wmax;
+    CK(cudaEventRecord(ws.ev_start, ws.stream), "event");
+    if (!otiles.empty()) {
+        Prune64Args o = a;
+        o.tiles = d_otiles.as<PruneTile>();
+        o.n_tiles = (int)otiles.size();
+        o.counts = FS.d_counts.as<int32_t>();
+        o.perm = FS.d_identity.as<int64_t>();
+        o.root_out = d_obsL.as<double>();
+        o.root_ld = RR;
+        CK(launch_prune64(o, std::max(1, std::min((int)otiles.size(), n_ctas_max)), ws.stream), "prune root vectors");
+    }
+    CK(launch_cdf_build(ws.mats.as<const double*>(), n, msize, S, n_ps, d_cdf.as<double>(), ws.stream), "row cdfs");
+    CK(cudaMemsetAsync(d_hist.p, 0, (size_t)n_keys * sizeof(int32_t), ws.stream), "simulation plan");
+    SimDrawArgs sd{};
+    sd.cdf = d_cdf.as<double>();
+    sd.prefix = d_tree.as<int32_t>();
+    sd.parent = d_tree.as<int32_t>() + n;
+    sd.leaf_col = d_tree.as<int32_t>() + 2 * n;
+    sd.n_nodes = n;
+    sd.n_leaves = L;
+    sd.root = T.root;
+    sd.n_ps = n_ps;
+    sd.S = S;
+    sd.n_sim = nsim;
+    sd.n_families = NS;
+    sd.key = sim_seed_key(out->seed);
+    sd.sizes = d_sizes.as<int32_t>();
+    sd.counts = d_sim.as<int32_t>();
+    sd.keys = d_keys.as<int32_t>();
+    sd.hist = d_hist.as<int32_t>();
+    CK(launch_sim_draw(sd, ws.stream), "simulation draws");
+    SimPlanArgs sp{};
+    sp.hist = d_hist.as<int32_t>();
+    sp.n_keys = n_keys;
+    sp.S = S;
+    sp.cursor = d_cursor.as<int32_t>();
+    sp.tiles = d_tiles.as<PruneTile>();
+    sp.max_tiles = max_tiles;
+    sp.n_tiles = d_ntiles.as<int32_t>();
+    CK(launch_sim_plan(sp, ws.stream), "simulation plan");
+    CK(launch_sim_scatter(d_keys.as<int32_t>(), NS, d_cursor.as<int32_t>(), d_perm.as<int64_t>(), ws.stream),
+       "simulation plan");
+    Prune64Args p = a;
+    p.tiles = d_tiles.as<PruneTile>();
+    p.n_tiles = 0;
+    p.n_tiles_dev = d_ntiles.as<int32_t>();
+    p.counts = d_sim.as<int32_t>();
+    p.perm = d_perm.as<int64_t>();
+    p.root_out = d_simL.as<double>();
+    p.root_ld = 1;
+    CK(launch_prune64(p, (int)std::max<int64_t>(1, std::min<int64_t>(max_tiles, n_ctas_max)), ws.stream),
+       "prune simulated families");
+    CK(launch_sort_rows(d_simL.as<double>(), RR, nsim, ws.stream), "sort");
+    PvalueSearchArgs ps{};
+    ps.counts = FS.d_counts.as<int32_t>();
+    ps.F = F;
+    ps.n_leaves = L;
+    ps.obs = d_obsL.as<double>();
+    ps.sorted = d_simL.as<double>();
+    ps.R = RR;
+    ps.n_sim = nsim;
+    ps.out = d_pv.as<double>();
+    CK(launch_pvalue_search(ps, ws.stream), "p-values");
+    CK(cudaEventRecord(ws.ev_stop, ws.stream), "event");
+    if (F) CK(cudaMemcpyAsync(out->pvalues, d_pv.p, (size_t)F * sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "d2h");
+    if (out->conditional)
+        CK(cudaMemcpyAsync(out->conditional, d_simL.p, (size_t)NS * sizeof(double), cudaMemcpyDeviceToHost, ws.stream),
+           "d2h");
+    if (out->root_likelihood && F)
+        CK(cudaMemcpyAsync(out->root_likelihood, d_obsL.p, (size_t)F * RR * sizeof(double), cudaMemcpyDeviceToHost,
+                           ws.stream),
+           "d2h");
+    CK(cudaStreamSynchronize(ws.stream), "p-values");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ws.ev_start, ws.ev_stop);
+    out->device_ms = ms;
+    out->host_ms = host_ms;     // the host only plans and copies; it draws nothing
+    return CAFE_OK;
+}
+
 // compute_pvalues (src/probability.cpp:376-570). The simulation runs on the
 // host because its random stream is the reference's: one std::mt19937
 // seeded by the caller, drawing in the reference's order (create_family,
@@ -2125,6 +2282,7 @@ int pvalues_sync(cafe_ctx* C, Workspace& ws, const cafe_request* R, cafe_pvalues
         ws.staged = false;
     }
     if (!out || !out->pvalues || out->n_simulations < 1) return fail(C, CAFE_ERR_INVALID, "bad p-value arguments");
+    if (out->device_sampling) return pvalues_device(C, ws, R, out);
     const auto t_host0 = std::chrono::steady_clock::now();
     double host_ms = 0.0;
     ReconSetup Z;
@@ -2472,7 +2630,7 @@ int cafe_ctx_create(const cafe_config* cfg, cafe_ctx** out) {
     cudaDeviceProp prop;
     cudaGetDeviceProperties(&prop, dev);
     C->sm_count = prop.multiProcessorCount;
-    if (tc_kernels_init() != cudaSuccess || prune64_cluster_init() != cudaSuccess ||
+    if (tc_kernels_init() != cudaSuccess || prune64_cluster_init() != cudaSuccess || pvalue_kernels_init() != cudaSuccess ||
         cudaEventCreateWithFlags(&C->gate, cudaEventDisableTiming) != cudaSuccess) {
         delete C;
         return CAFE_ERR_CUDA;
@@ -2522,6 +2680,7 @@ int cafe_ctx_destroy(cafe_ctx* C) {
     cudaDeviceSynchronize();
     cache_reset(C);
     if (C->gate) cudaEventDestroy(C->gate);
+    if (C->serve_epoch) cudaEventDestroy(C->serve_epoch);
     delete C;
     return CAFE_OK;
 }
@@ -2931,6 +3090,7 @@ void server_loop(cafe_ctx* C, int wi) {
     for (;;) {
         std::vector<std::shared_ptr<Request>> batch;
         size_t bytes = 0;
+        bool behind = false;     // another batch is in flight: this one runs at the lower priority
         {
             std::unique_lock<std::mutex> lk(C->qmu);
             // admit when the queue has work and the footprint fits (an idle
@@ -2963,6 +3123,7 @@ void server_loop(cafe_ctx* C, int wi) {
             C->in_flight += (int)batch.size();
             C->in_flight_bytes += bytes;
             C->batches_in_flight++;
+            behind = C->batches_in_flight > 1;
         }
         const int n = (int)batch.size();
         std::vector<cafe_request> reqs(n);
@@ -2976,8 +3137,11 @@ void server_loop(cafe_ctx* C, int wi) {
         const auto t0 = std::chrono::steady_clock::now();
         {
             // enqueue under the context lock; the GPU work of this batch then
-            // overlaps with batches running on the other streams
+            // overlaps with batches running on the other streams (this
+            // workspace's previous batch has completed, so it may switch
+            // streams)
             std::unique_lock<std::mutex> lk(C->mu);
+            ws.stream = behind ? ws.stream_lo : ws.stream_hi;
             rc = score_enqueue(C, ws, reqs.data(), n, res.data(), &info);
         }
         const auto t1 = std::chrono::steady_clock::now();
@@ -2993,6 +3157,19 @@ void server_loop(cafe_ctx* C, int wi) {
             si.enqueue_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
             si.wait_ms += std::chrono::duration<double, std::milli>(t2 - t1).count();
             if (rc == CAFE_OK) si.device_ms += res[0].device_ms;
+            // this batch's device interval against the recent ones: the time
+            // they ran side by side
+            float s0 = 0.0f, s1 = 0.0f;
+            if (rc == CAFE_OK && C->serve_epoch && cudaEventElapsedTime(&s0, C->serve_epoch, ws.ev_start) == cudaSuccess &&
+                cudaEventElapsedTime(&s1, C->serve_epoch, ws.ev_stop) == cudaSuccess) {
+                for (const auto& iv : C->serve_intervals) {
+                    const float lo = std::max(iv.first, s0), hi = std::min(iv.second, s1);
+                    if (hi > lo) si.overlap_ms += hi - lo;
+                }
+                C->serve_intervals.emplace_back(s0, s1);
+                if (C->serve_intervals.size() > 32) C->serve_intervals.pop_front();
+            }
+            cudaGetLastError();
         }
         if (rc != CAFE_OK && n > 1) {
             // one bad request must not fail the others: run them one by one
@@ -3068,6 +3245,11 @@ int cafe_submit(cafe_ctx* C, const cafe_request* req, cafe_result* res, uint64_t
     std::lock_guard<std::mutex> lk(C->qmu);
     if (C->servers.empty()) {
         C->stop = false;
+        // the epoch of the batches' device intervals, on a serving stream
+        // with nothing queued
+        C->serve_intervals.clear();
+        if (!C->serve_epoch && cudaEventCreate(&C->serve_epoch) != cudaSuccess) C->serve_epoch = nullptr;
+        if (C->serve_epoch && C->ws.size() > 1) cudaEventRecord(C->serve_epoch, C->ws[1]->stream);
         for (size_t i = 1; i < C->ws.size(); ++i) C->servers.emplace_back(server_loop, C, (int)i);
     }
     *ticket = C->next_ticket++;

@@ -188,6 +188,49 @@ struct TcMaps {
 
 cudaError_t launch_prune_tc(const TcMaps& maps, const PruneTcArgs& a, int n_ctas, size_t smem, cudaStream_t s);
 
+// ---- device-sampled p-value simulations (k_pvalue.cu) ----
+struct SimDrawArgs {
+    const double* cdf;           // [n_nodes][n_ps][S] cumulative weights of each (node, parent size) row
+    const int32_t* prefix;       // [n_nodes] prefix order
+    const int32_t* parent;       // [n_nodes], -1 at the root
+    const int32_t* leaf_col;     // [n_nodes] counts column of a leaf, -1 for internal nodes
+    int n_nodes, n_leaves, root, n_ps, S, n_sim;
+    int64_t n_families;          // R x n_sim; family fi has root size fi / n_sim + 1
+    uint64_t key;                // sim_seed_key(seed)
+    int32_t* sizes;              // [n_families][n_nodes] scratch
+    int32_t* counts;             // [n_families][n_leaves] out: leaf counts
+    int32_t* keys;               // [n_families] out: root index x (S + 1) + state bound
+    int32_t* hist;               // [R x (S + 1)] zeroed in, families per key out
+};
+struct SimPlanArgs {
+    const int32_t* hist;
+    int n_keys;
+    int S;
+    int32_t* cursor;             // [n_keys] out: first family slot of each key (the scatter's cursor)
+    PruneTile* tiles;            // [max_tiles] out: 32-family tiles of equal (root size, bound)
+    int64_t max_tiles;
+    int32_t* n_tiles;            // [1] out
+};
+struct PvalueSearchArgs {
+    const int32_t* counts;       // [F][n_leaves] observed families
+    int64_t F;
+    int n_leaves;
+    const double* obs;           // [F][R] observed root values (root sizes 1..R)
+    const double* sorted;        // [R][n_sim] sorted simulated values
+    int R, n_sim;
+    double* out;                 // [F] p-values
+};
+constexpr int kSortRowsMaxP = 16384;   // simulations per root size the device sort takes
+uint64_t sim_seed_key(uint32_t seed);
+cudaError_t pvalue_kernels_init();
+cudaError_t launch_cdf_build(const double* const* mats, int n_nodes, int msize, int S, int n_ps, double* cdf,
+                             cudaStream_t s);
+cudaError_t launch_sim_draw(const SimDrawArgs& a, cudaStream_t s);
+cudaError_t launch_sim_plan(const SimPlanArgs& a, cudaStream_t s);
+cudaError_t launch_sim_scatter(const int32_t* keys, int64_t n, int32_t* cursor, int64_t* perm, cudaStream_t s);
+cudaError_t launch_sort_rows(double* v, int rows, int n, cudaStream_t s);
+cudaError_t launch_pvalue_search(const PvalueSearchArgs& a, cudaStream_t s);
+
 // Families whose tensor-core result may have lost accuracy to FP32's range:
 // for every (family, candidate), the category terms' range-error bounds
 // weighted by the terms' shares of the family likelihood; over

@@ -134,7 +134,11 @@ struct Slab {
 
 // Per-request device workspace (one per stream).
 struct Workspace {
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;     // the stream of the current request: stream_hi or stream_lo
+    // Serving batches admitted while another batch runs go to stream_lo (one
+    // priority step lower): their blocks fill the SMs the earlier batch
+    // leaves idle instead of competing with it.
+    cudaStream_t stream_hi = nullptr, stream_lo = nullptr;
     bool sync = false;                 // a synchronous-call workspace (profiled when profiling is on)
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     cudaEvent_t ev_staged = nullptr;   // after the last request's host->device staging copies
@@ -246,6 +250,8 @@ struct cafe_ctx {
     std::vector<double> latencies_ms;
     int batches_in_flight = 0;
     cafe_serving_info serving{};     // serving counters
+    cudaEvent_t serve_epoch = nullptr;                    // recorded when the server threads start
+    std::deque<std::pair<float, float>> serve_intervals;  // recent batches' device [start, end] (ms from the epoch)
     // last launch of the most recent request: the next request's device work
     // starts after it
     cudaEvent_t gate = nullptr;

@@ -271,16 +271,18 @@ class Context:
         return out
 
     def pvalues(self, tree_id, set_id, lambdas, *, S: int, R: int, n_simulations: int = 1000, seed: int = 10,
-                lambda_kind=0) -> dict:
+                lambda_kind=0, device_sampling: bool = False) -> dict:
         """cafe_pvalues (compute_pvalues): per-family p-values, the sorted
         conditional distributions [R][n_simulations] and the observed root
-        vectors [F][R]."""
+        vectors [F][R]. device_sampling draws the simulated families on the
+        GPU (not the reference's random stream: equal in distribution)."""
         req, keep = self.make_request(tree_id, set_id, lambdas, lambda_kind=lambda_kind, S=S, R=R)
         F, _ = self._set_shape.get(set_id, (0, 0))
         pv = np.zeros(F)
         cd = np.zeros((R, n_simulations))
         rl = np.zeros((F, R))
-        out = _lib.PvaluesOut(n_simulations, seed & 0xFFFFFFFF, _p(pv), _p(cd), _p(rl), 0.0, 0.0)
+        out = _lib.PvaluesOut(n_simulations, seed & 0xFFFFFFFF, _p(pv), _p(cd), _p(rl), 0.0, 0.0,
+                              1 if device_sampling else 0)
         self._check(self.lib.cafe_pvalues(self.h, C.byref(req), C.byref(out)))
         return {"pvalues": pv, "conditional": cd, "root_likelihood": rl, "device_ms": out.device_ms,
                 "host_ms": out.host_ms}
@@ -321,7 +323,7 @@ class Context:
         self._check(self.lib.cafe_serving_counters(self.h, C.byref(si)))
         return {"completed": n.value, "p50_ms": p50.value, "p99_ms": p99.value, "in_flight": inf.value,
                 "batches": si.batches, "merged": si.merged, "retried": si.retried, "enqueue_ms": si.enqueue_ms,
-                "wait_ms": si.wait_ms, "device_ms": si.device_ms}
+                "wait_ms": si.wait_ms, "device_ms": si.device_ms, "overlap_ms": si.overlap_ms}
 
 
 _default_ctx: Optional[Context] = None

@@ -285,6 +285,9 @@ typedef struct {
     double enqueue_ms;           /* host time enqueuing batches (context lock held) */
     double wait_ms;              /* host time waiting for batches to finish */
     double device_ms;            /* device time of the batches (events) */
+    double overlap_ms;           /* device time during which batches ran side by side: the summed pairwise
+                                    intersections of the batches' event intervals (0 when every batch ran
+                                    alone) */
 } cafe_serving_info;
 int cafe_serving_counters(cafe_ctx* ctx, cafe_serving_info* out);
 
@@ -396,6 +399,11 @@ typedef struct {
     double device_ms;            /* out: device span from the first pruning launch to the last (it
                                     overlaps the host simulation) */
     double host_ms;              /* out: host time (matrix copies, simulation, sorting, p-values) */
+    int device_sampling;         /* in: 0 = the reference's std::mt19937 stream drawn on the host (the
+                                    reference's families and p-values, bit for bit); 1 = every simulated
+                                    family drawn on the GPU from a counter-based generator seeded by
+                                    `seed` (the same distributions, not the reference's stream: p-values
+                                    agree in distribution only; at most 16,384 simulations per root size) */
 } cafe_pvalues_out;
 
 /* compute_pvalues (src/probability.cpp:376-570) at the request's own

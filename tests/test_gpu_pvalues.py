@@ -93,3 +93,54 @@ def test_model_mirror_pvalues(ctx):
     m = BaseModel(SingleLambda(case.lambdas[0]), case.tree, fams, case.S, case.R, ctx=ctx)
     pv = m.compute_pvalues(n_simulations=case.n_sim, seed=case.seed)
     assert np.array_equal(pv, case.pvalues)
+
+
+def _ks(a, b):
+    """Two-sample Kolmogorov-Smirnov statistic of two samples."""
+    a, b = np.sort(a), np.sort(b)
+    x = np.concatenate([a, b])
+    return np.max(np.abs(np.searchsorted(a, x, side="right") / len(a) - np.searchsorted(b, x, side="right") / len(b)))
+
+
+def test_device_sampled_pvalues_agree_in_distribution(ctx):
+    """device_sampling = 1 draws every simulated family on the GPU from a
+    counter-based generator: the reference's distributions, not its
+    mt19937 stream, so the check is statistical. 200 families of the
+    config-0 shape (12 taxa, R = 30), 1,000 simulations per root size:
+      * per root size, the two-sample Kolmogorov-Smirnov statistic between
+        the device-sampled simulated likelihoods and those of the
+        reference's stream (the same FP64 pruning, so equal families give
+        equal values) stays below the 0.1 % critical value
+        1.95 sqrt(2 / 1000) = 0.087;
+      * every family's p-value is within 0.12 of the oracle's (two
+        independent empirical distributions of 1,000 draws; the largest KS
+        distance bounds the difference), and the mean difference is below
+        0.03;
+      * the observed root vectors are those of the reference-stream path;
+      * the same seed gives the same bits, another seed other draws."""
+    from cafe5_gb300.families import global_bounds
+    from cafe5_gb300.synth import workload
+    w = workload(0, n_families=200, seed=4)
+    S, R = global_bounds(w.families)
+    n_sim = 1000
+    tid = ctx.upload_tree(w.tree)
+    sid = ctx.upload_families(tid, w.families.counts)
+    kw = dict(S=S, R=R, n_simulations=n_sim, seed=777)
+    host = ctx.pvalues(tid, sid, [0.0025], **kw)
+    dev = ctx.pvalues(tid, sid, [0.0025], device_sampling=True, **kw)
+    again = ctx.pvalues(tid, sid, [0.0025], device_sampling=True, **kw)
+    other = ctx.pvalues(tid, sid, [0.0025], device_sampling=True, **dict(kw, seed=778))
+    assert np.array_equal(dev["pvalues"], again["pvalues"])
+    assert np.array_equal(dev["conditional"], again["conditional"])
+    assert not np.array_equal(dev["conditional"], other["conditional"])
+    assert np.array_equal(dev["root_likelihood"], host["root_likelihood"])
+    cd_dev, cd_host = dev["conditional"], host["conditional"]
+    assert np.all(np.diff(cd_dev, axis=1) >= 0)          # sorted per root size
+    crit = 1.95 * np.sqrt(2.0 / n_sim)
+    ks = np.array([_ks(cd_dev[j], cd_host[j]) for j in range(R)])
+    assert ks.max() < crit, (ks.argmax(), ks.max(), crit)
+    ta = oracle.TreeArrays.from_tree(w.tree)
+    pv, _, _ = oracle.pvalues(ta, w.families.counts, [0.0025], S=S, R=R, n_sim=n_sim, seed=777)
+    d = np.abs(dev["pvalues"] - pv)
+    assert d.max() <= 0.12 and d.mean() < 0.03, (d.max(), d.mean())
+    ctx.free_families(sid)
