@@ -1060,6 +1060,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         const size_t fl = (size_t)n_mat * Wm * Wm;
         CK(ws.tc_hi.reserve(fl * sizeof(float)), "tc matrices");
         CK(ws.tc_lo.reserve(fl * sizeof(float)), "tc matrices");
+        CK(ws.tc_tr.reserve(fl * sizeof(float)), "tc matrices");
         CK(ws.h_conv.reserve(jobs.size() * sizeof(ConvertJob)), "convert jobs");
         CK(ws.conv.reserve(jobs.size() * sizeof(ConvertJob)), "convert jobs");
         std::memcpy(ws.h_conv.p, jobs.data(), jobs.size() * sizeof(ConvertJob));
@@ -1072,6 +1073,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         std::memset(&tb, 0, sizeof tb);
         tb.hi = ws.tc_hi.as<float>();
         tb.lo = ws.tc_lo.as<float>();
+        tb.tr = ws.tc_tr.as<float>();
         tb.Wm = Wm;
         if (prof) C->prof.begin(3, ws.stream, &ev);
         const ConvertJob* cj = ws.conv.as<ConvertJob>();
@@ -1169,6 +1171,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         a.perm = B.d_perm.as<int64_t>();
         a.mat_index = ws.tc_mi.as<int32_t>();
         a.Wm = Wm;
+        a.mat_tr = ws.tc_tr.as<float>();
         a.vec = ws.tc_vec.as<float>();
         a.n_slots = T.n_slots;
         a.prior = C->d_prior.as<double>();

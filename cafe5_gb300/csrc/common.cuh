@@ -136,6 +136,7 @@ struct ConvertJob {
 struct TcBuffers {
     float* hi;           // [n_mat][Wm][Wm] TF32 hi part, row-major M[s][c]
     float* lo;           // [n_mat][Wm][Wm] TF32 lo part
+    float* tr;           // [n_mat][Wm][Wm] FP32 transpose: tr[c][s] = M[s][c] (leaf factors)
     int Wm;
 };
 
@@ -150,6 +151,7 @@ struct PruneTcArgs {
     const int32_t* mat_index;    // [K][n_nodes] converted-matrix index (-1 for the root); bit 30 set
                                  // when the key is saturated
     int Wm;                      // pitch of matrices and node vectors (elements)
+    const float* mat_tr;         // [n_mat][Wm][Wm] FP32 transposed matrices (row c = column c of M)
     float* vec;                  // node vectors (FP32), rows = CTA x slot x 128 families
     int n_slots;
     const double* prior;

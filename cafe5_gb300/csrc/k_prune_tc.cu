@@ -18,12 +18,12 @@
 //    tcgen05.mma; the accumulators of up to two children sit side by side in
 //    TMEM.
 //  * Leaf child: its factor is the matrix column of the observed count (or
-//    the error model's weighted sum of three columns), computed as the same
-//    GEMM with a one-hot (or three-hot) A tile that the threads write into
-//    shared memory in the swizzled operand layout: D = A (B_hi + B_lo), plus
-//    A_lo B_hi for error-model weights. Only the K chunks that hold a count
-//    of the tile are issued. Every child's factor then sits in TMEM and the
-//    epilogue reads no global memory.
+//    the error model's weighted sum of three columns): each thread reads its
+//    family's column as a row of the transposed FP32 matrix and writes it
+//    into the child's TMEM columns (tcgen05.st), while the node's first
+//    operand chunk is in flight; a node whose children are both leaves runs
+//    no GEMM. Every child's factor then sits in TMEM and the epilogue reads
+//    no global memory.
 //  * Epilogue (thread f owns family f = TMEM lane f): the product over
 //    children is rescaled by the largest per-state sum of the factors'
 //    binary exponents, so the product's maximum is ~1 and nothing
@@ -200,26 +200,48 @@ __device__ __forceinline__ float fac_err(const NodeSrc<NC>& ns, int c, float raw
 // (one-hot column n, or the error model's columns n-1, n, n+1).
 struct LeafW {
     int col[3];
-    float hi[3], lo[3];
+    float w[3];
 };
+
+// The leaf weights of a family with count n (a padding row: none). False
+// when the count has no column in the bin (the family is recomputed in FP64).
+__device__ __forceinline__ bool leaf_weights(const PruneTcArgs& a, int64_t fam, int n, int S, LeafW& L) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        L.col[d] = -1;
+        L.w[d] = 0.0f;
+    }
+    if (fam < 0) return true;
+    bool any = false;
+    if (a.err) {
+        const double* pr = a.err + (size_t)(n < a.err_rows ? n : a.err_rows - 1) * a.err_ndev;
+        const int off = n - (a.err_ndev - 1) / 2;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int col = off + d;
+            if (d < a.err_ndev && col >= 0 && col <= S && pr[d] > 0) {
+                L.col[d] = col;
+                L.w[d] = (float)pr[d];
+                any = true;
+            }
+        }
+    } else if (n >= 0 && n <= S) {
+        L.col[0] = n;
+        L.w[0] = 1.0f;
+        any = true;
+    }
+    return any;
+}
 
 template <int NC>
 __device__ __forceinline__ void setup_src(const PruneTcArgs& a, const ChildInfo* ch, int nch, const int* Esh,
                                           const float* Erh, uint32_t tmem_lane, int64_t fam, int tid, int S, int W,
-                                          int Wt, const int (&count)[NC], NodeSrc<NC>& ns, LeafW (&lw)[NC],
-                                          int* cmask_sh) {
+                                          int Wt, const int (&count)[NC], NodeSrc<NC>& ns) {
     ns.Eacc = 0;
     ns.flag = false;
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
         Src& sc = ns.s[c];
-        LeafW& L = lw[c];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            L.col[d] = -1;
-            L.hi[d] = 0.0f;
-            L.lo[d] = 0.0f;
-        }
         sc.unit = c >= nch;
         sc.taddr = 0;
         ns.ue[c] = 0.0f;
@@ -234,53 +256,64 @@ __device__ __forceinline__ void setup_src(const PruneTcArgs& a, const ChildInfo*
         }
         ns.leaf[c] = true;
         ns.ue[c] = (a.err ? 8.0f : 2.0f) * kTiny;
-        if (fam < 0) continue;        // padding row: zero factor
-        const int n = count[c];
-        unsigned bits = 0;
-        if (a.err) {
-            const double* pr = a.err + (size_t)(n < a.err_rows ? n : a.err_rows - 1) * a.err_ndev;
-            const int off = n - (a.err_ndev - 1) / 2;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                const int col = off + d;
-                if (d < a.err_ndev && col >= 0 && col <= S && pr[d] > 0) {
-                    const float w = (float)pr[d];
-                    L.col[d] = col;
-                    L.hi[d] = tc::round_tf32(w);
-                    L.lo[d] = tc::round_tf32(w - L.hi[d]);
-                    bits |= 1u << (col / KC);
-                }
-            }
-        } else if (n >= 0 && n <= S) {
-            L.col[0] = n;
-            L.hi[0] = 1.0f;
-            bits = 1u << (n / KC);
-        }
-        if (!bits) ns.flag = true;
-        else atomicOr(cmask_sh + c, (int)bits);
+        LeafW L;
+        if (!leaf_weights(a, fam, count[c], S, L)) ns.flag = true;   // a count past the bin: FP64 recomputes
     }
 }
 
-// This thread's row of the leaf A tile for K chunk kc (columns
-// [kc KC, kc KC + KC)), written into the swizzled K-major layout the MMA
-// descriptor reads: a 128-byte row r keeps its 16-byte piece j at
-// j ^ (r % 8); a 64-byte row at j ^ ((r >> 1) % 4).
-__device__ __forceinline__ void write_leaf_row(float* tile, int r, const LeafW& L, int kc, bool lo) {
-    float* row = tile + (size_t)r * KC;
-    const int c0 = kc * KC;
-    const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    // pieces visited in swizzled order, so neighbouring rows hit different banks
-    const int sw = KC == 32 ? (r & 7) : ((r >> 1) & 3);
+// A leaf child's factor into its TMEM columns (warp-collective): column j
+// of this thread's row is sum_d w_d M[s_off + j][col_d], read as row col_d
+// of the transposed FP32 matrix tr (pitch Wm). A padding row stores zeros.
+// A single column (no error model) is loaded 32 states at a time, all
+// loads in flight together: one round trip to L2 per 32 states (W is a
+// multiple of 32).
+__device__ __noinline__ void gather_leaf(const float* __restrict__ tr, int Wm, const LeafW& L, uint32_t taddr, int W,
+                                         int s_off) {
+    // tcgen05.st is warp-collective: every lane takes the same branch (the
+    // weighted one as soon as any lane of the warp has more than one column)
+    if (__all_sync(0xffffffffu, L.col[1] < 0 && L.col[2] < 0)) {
+        const float w = L.w[0];
+        const float4* p = reinterpret_cast<const float4*>(tr + (size_t)(L.col[0] < 0 ? 0 : L.col[0]) * Wm + s_off);
+        for (int col0 = 0; col0 < W; col0 += 32) {
+            float4 x[8];
 #pragma unroll
-    for (int j = 0; j < KC / 4; ++j) reinterpret_cast<float4*>(row)[j ^ sw] = z;
-    // then the (at most three) nonzero columns, each at its swizzled place
+            for (int q = 0; q < 8; ++q) x[q] = L.col[0] >= 0 ? __ldg(p + col0 / 4 + q) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const int e = L.col[d] - c0;
-        if (L.col[d] < 0 || e < 0 || e >= KC) continue;
-        const int pj = KC == 32 ? ((e >> 2) ^ (r & 7)) : ((e >> 2) ^ ((r >> 1) & 3));
-        row[(pj << 2) + (e & 3)] = lo ? L.lo[d] : L.hi[d];
+            for (int h = 0; h < 2; ++h) {
+                float v[16];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    v[4 * q] = w * x[4 * h + q].x;
+                    v[4 * q + 1] = w * x[4 * h + q].y;
+                    v[4 * q + 2] = w * x[4 * h + q].z;
+                    v[4 * q + 3] = w * x[4 * h + q].w;
+                }
+                tc::tmem_st16(taddr + (uint32_t)(col0 + 16 * h), v);
+            }
+        }
+    } else {
+        for (int col0 = 0; col0 < W; col0 += 16) {
+            float v[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = 0.0f;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                if (L.col[d] < 0) continue;
+                const float4* p = reinterpret_cast<const float4*>(tr + (size_t)L.col[d] * Wm + s_off + col0);
+                const float w = L.w[d];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float4 x = __ldg(p + q);
+                    v[4 * q] = fmaf(w, x.x, v[4 * q]);
+                    v[4 * q + 1] = fmaf(w, x.y, v[4 * q + 1]);
+                    v[4 * q + 2] = fmaf(w, x.z, v[4 * q + 2]);
+                    v[4 * q + 3] = fmaf(w, x.w, v[4 * q + 3]);
+                }
+            }
+            tc::tmem_st16(taddr + (uint32_t)col0, v);
+        }
     }
+    tc::tmem_wait_st();
 }
 
 // CW values of a child's factor starting at column col0 (issue only for
@@ -482,7 +515,6 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
     __shared__ float xbuf[NSPLIT > 1 ? 2 * (NSPLIT - 1) * kXN * TM : 1];
     __shared__ uint32_t tmem_sh;
     __shared__ int abort_sh;
-    __shared__ int cmask_sh[2][2];  // [node parity][child]: K chunks holding a leaf column of the tile
     __shared__ float prior_f[prior_rows<NSPLIT>()];
 
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -565,10 +597,6 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
             }
             nodes[ii] = e;
         }
-        if (tid == 0) {
-            cmask_sh[0][0] = cmask_sh[0][1] = 0;
-            cmask_sh[1][0] = cmask_sh[1][1] = 0;
-        }
         __syncthreads();
         const int32_t* fam_counts = a.counts + (size_t)(fam >= 0 ? fam : 0) * P.n_leaves;
         int cnt_next[2] = {0, 0};
@@ -582,7 +610,6 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
             const bool is_root = nd.is_root != 0;
             const int vs = nd.slot;
             const int nch = nd.nch;
-            int* cmask = cmask_sh[ii & 1];
             const long long ts = timing ? clock64() : 0;
             // the previous nodes' TMA stores must be complete before this node
             // overwrites their staging tile or reads their rows back (in a
@@ -599,11 +626,10 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                 }
                 if (tid == 0) tc::fence_proxy_async_global();
             }
-            // child sources; leaf weights and the K chunks they touch
+            // child sources
             NodeSrc<2> ns2;
-            LeafW lw[2];
             const int cnt_cur[2] = {cnt_next[0], cnt_next[1]};
-            setup_src<2>(a, nd.c, nch, Esh, Erh, tmem + lane_base, fam, tid, S, W, Wn, cnt_cur, ns2, lw, cmask);
+            setup_src<2>(a, nd.c, nch, Esh, Erh, tmem + lane_base, fam, tid, S, W, Wn, cnt_cur, ns2);
             // counts of the next node's leaves, in flight during this node
             if (ii + 1 < P.n_internal) {
                 const NodeInfo& nx = nodes[ii + 1];
@@ -613,35 +639,37 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
             }
             __syncthreads();
 
-            // ---------------- one GEMM per child into TMEM ----------------
-            // K chunks of both children form one list (CTA-uniform); thread 0
-            // runs the TMA loads up to NS - 1 chunks ahead of the MMAs. A leaf
-            // chunk's A tile is written by all threads into its stage.
+            // ---------------- one GEMM per internal child into TMEM ----------------
+            // K chunks of the internal children form one list (CTA-uniform);
+            // thread 0 runs the TMA loads up to NS - 1 chunks ahead of the MMAs.
+            // Leaf children's factors are gathered into TMEM meanwhile.
             long long t0 = timing ? clock64() : 0;
             {
                 const int kpc = W / KC;             // K chunks per child
-                unsigned cm[2];
+                int nk[2];
 #pragma unroll
-                for (int c = 0; c < 2; ++c) {
-                    if (c >= nch) {
-                        cm[c] = 0;
-                    } else if (nd.c[c].leaf_col >= 0) {
-                        cm[c] = (unsigned)cmask[c];
-                        if (!cm[c]) cm[c] = 1;      // all-zero leaf tile: still initialise D
-                    } else {
-                        cm[c] = (1u << kpc) - 1;
-                    }
-                }
-                const int n0 = __popc(cm[0]);
-                const int n_chunks = n0 + __popc(cm[1]);
+                for (int c = 0; c < 2; ++c) nk[c] = (c < nch && nd.c[c].leaf_col < 0) ? kpc : 0;
+                const int n0 = nk[0];
+                const int n_chunks = n0 + nk[1];
+                // leaf factors (CTA-uniform): after the first chunk's loads are
+                // issued, or at once when the node runs no GEMM
+                auto gather_leaves = [&]() {
+                    if (__shfl_sync(0xffffffffu, abort_sh, 0)) return;   // warp-uniform: the stores are collective
+#pragma unroll
+                    for (int c = 0; c < 2; ++c)
+                        if (c < nch && nd.c[c].leaf_col >= 0) {
+                            LeafW L;
+                            leaf_weights(a, fam, cnt_cur[c], S, L);
+                            gather_leaf(a.mat_tr + (size_t)nd.c[c].mat * Wm * Wm, Wm, L, ns2.s[c].taddr, Wn, s_off);
+                        }
+                };
+                if (n_chunks == 0) gather_leaves();
                 for (int i = 0; i < n_chunks + NS - 1; ++i) {
                     // ---- produce chunk i ----
                     if (i < n_chunks) {
                         const int c = i < n0 ? 0 : 1;
-                        const int kc = (int)__fns(cm[c], 0, (c == 0 ? i : i - n0) + 1);
+                        const int kc = c == 0 ? i : i - n0;
                         const ChildInfo chi = nd.c[c];
-                        const bool leaf = chi.leaf_col >= 0;
-                        const bool with_lo = !leaf || a.err != nullptr;
                         const uint32_t cg = g + (uint32_t)i;
                         const int st = (int)(cg % (uint32_t)NS);
                         const uint32_t u = cg / (uint32_t)NS;
@@ -657,16 +685,13 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                             atomicExch(a.status, 1);
                             abort_sh = 1;
                         }
-                        if (leaf && i >= NS) __syncthreads();      // stage free for every writer
                         if (tid == 0 && !abort_sh) {
-                            tc::mbar_expect_tx(&bar_full[st], (uint32_t)(((leaf ? 0 : TM) + 2 * Wn) * KC * sizeof(float)));
-                            if (!leaf) {
-                                // the FP32 node vector lands in the hi operand; the
-                                // consumer splits it into hi and lo in place
-                                const int vrow = (int)(vrow_cta + (int64_t)chi.slot * TM);
-                                for (int r = 0; r < TM / 32; ++r)
-                                    tc::tma_load_2d(Ahi + r * 32 * KC, &map_vec, kc * KC, vrow + 32 * r, &bar_full[st]);
-                            }
+                            tc::mbar_expect_tx(&bar_full[st], (uint32_t)((TM + 2 * Wn) * KC * sizeof(float)));
+                            // the FP32 node vector lands in the hi operand; the
+                            // consumer splits it into hi and lo in place
+                            const int vrow = (int)(vrow_cta + (int64_t)chi.slot * TM);
+                            for (int r = 0; r < TM / 32; ++r)
+                                tc::tma_load_2d(Ahi + r * 32 * KC, &map_vec, kc * KC, vrow + 32 * r, &bar_full[st]);
                             const int mrow = chi.mat * Wm + s_off;     // this CTA's output states
                             for (int r = 0; r < Wn / 32; ++r) {
                                 tc::tma_load_2d(Bhi + r * 32 * KC, &map_mhi, kc * KC, mrow + 32 * r, &bar_full[st]);
@@ -675,21 +700,13 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                             last_full[st] = 1;
                             last_full_parity[st] = u & 1;
                         }
-                        if (leaf) {
-                            // on a time-out every thread still walks the same barriers
-                            if (!abort_sh) {
-                                write_leaf_row(Ahi, tid, lw[c], kc, false);
-                                if (with_lo) write_leaf_row(Alo, tid, lw[c], kc, true);
-                                tc::fence_proxy_async_shared();
-                            }
-                            __syncthreads();
-                        }
+                        if (i == 0) gather_leaves();
                     }
                     // ---- consume chunk j = i - (NS - 1) ----
                     const int j = i - (NS - 1);
-                    // an internal child's FP32 vector chunk: every thread waits
-                    // for it and splits its own row into the TF32 hi/lo operands
-                    if (j >= 0 && nd.c[j < n0 ? 0 : 1].leaf_col < 0) {
+                    // the child's FP32 vector chunk: every thread waits for it
+                    // and splits its own row into the TF32 hi/lo operands
+                    if (j >= 0) {
                         const uint32_t cg = g + (uint32_t)j;
                         const int st = (int)(cg % (uint32_t)NS);
                         float* Ahi = reinterpret_cast<float*>(smem + st * sbytes);
@@ -710,7 +727,6 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                         const int c = j < n0 ? 0 : 1;
                         const bool first = j == 0 || j == n0;
                         const ChildInfo chi = nd.c[c];
-                        const bool with_lo = chi.leaf_col < 0 || a.err != nullptr;
                         const uint32_t cg = g + (uint32_t)j;
                         const int st = (int)(cg % (uint32_t)NS);
                         const uint32_t u = cg / (uint32_t)NS;
@@ -729,7 +745,7 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                                 const uint64_t bh = desc_k(Bhi + ks * 8), bl = desc_k(Blo + ks * 8);
                                 tc::mma_tf32(d, ah, bh, idesc, (first && ks == 0) ? 0u : 1u);
                                 tc::mma_tf32(d, ah, bl, idesc, 1);
-                                if (with_lo) tc::mma_tf32(d, al, bh, idesc, 1);
+                                tc::mma_tf32(d, al, bh, idesc, 1);
                             }
                             tc::mma_commit(&bar_empty[st]);
                         } else {
@@ -753,10 +769,6 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
             }
             __syncthreads();
             if (abort_sh) break;
-            if (tid == 0) {
-                cmask_sh[(ii + 1) & 1][0] = 0;
-                cmask_sh[(ii + 1) & 1][1] = 0;
-            }
             long long t1 = timing ? clock64() : 0;
 
             // ---------------- epilogue: product over children ----------------
@@ -937,23 +949,31 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
     if (NSPLIT > 1) tc::cluster_sync_all();
 }
 
-// FP64 matrix -> TF32 hi/lo operands (row-major, pitch Wm); each block
-// converts `rows` rows of one matrix (a matrix of side 512 spreads over 64
-// blocks, so a few hundred matrices fill the GPU).
-__global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict__ jobs, TcBuffers b, int rows) {
+// FP64 matrix -> TF32 hi/lo operands (row-major, pitch Wm) and the FP32
+// transpose tr[c][s] = M[s][c] (a leaf factor, column c of M, as one row).
+// A block converts a band of 32 rows of one matrix, 32 columns at a time
+// through a shared-memory tile, so the row-major and the transposed stores
+// both write whole 128-byte lines. Wm is a multiple of 32.
+__global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict__ jobs, TcBuffers b) {
+    __shared__ float tile[32][33];
     const int Wm = b.Wm;
-    const int per_mat = (Wm + rows - 1) / rows;
-    const ConvertJob J = jobs[blockIdx.x / per_mat];
-    const int r0 = (int)(blockIdx.x % per_mat) * rows;
-    const int n = (min(Wm, r0 + rows) - r0) * Wm;
-    const size_t base = ((size_t)J.mat * Wm + r0) * Wm;
-    const double* src = J.src + (size_t)r0 * J.ld;
-    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
-        const int s = idx / Wm, c = idx - s * Wm;
-        const float x = (float)src[(size_t)s * J.ld + c];
-        const float h = tc::round_tf32(x);
-        b.hi[base + idx] = h;
-        b.lo[base + idx] = tc::round_tf32(x - h);
+    const int bands = Wm / 32;
+    const ConvertJob J = jobs[blockIdx.x / bands];
+    const int s0 = (int)(blockIdx.x % bands) * 32;
+    const size_t base = (size_t)J.mat * Wm * Wm;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int c0 = 0; c0 < Wm; c0 += 32) {
+        for (int r = ty; r < 32; r += 8) {
+            const int s = s0 + r, c = c0 + tx;
+            const float x = (float)J.src[(size_t)s * J.ld + c];
+            const float h = tc::round_tf32(x);
+            b.hi[base + (size_t)s * Wm + c] = h;
+            b.lo[base + (size_t)s * Wm + c] = tc::round_tf32(x - h);
+            tile[r][tx] = x;
+        }
+        __syncthreads();
+        for (int r = ty; r < 32; r += 8) b.tr[base + (size_t)(c0 + r) * Wm + s0 + tx] = tile[tx][r];
+        __syncthreads();
     }
 }
 
@@ -1113,9 +1133,8 @@ size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages, int n_internal) {
 
 cudaError_t launch_convert_tc(const ConvertJob* d_jobs, int n_jobs, TcBuffers b, cudaStream_t s) {
     if (n_jobs <= 0) return cudaSuccess;
-    const int rows = std::max(1, std::min(b.Wm, 4096 / std::max(1, b.Wm)));
-    const int per_mat = (b.Wm + rows - 1) / rows;
-    k_convert_tc<<<(unsigned)(n_jobs * per_mat), 256, 0, s>>>(d_jobs, b, rows);
+    if (b.Wm % 32) return cudaErrorInvalidValue;
+    k_convert_tc<<<(unsigned)(n_jobs * (b.Wm / 32)), 256, 0, s>>>(d_jobs, b);
     return cudaGetLastError();
 }
 
