@@ -626,10 +626,9 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-// 2D FP32 tensor map [rows][cols] with 32-row boxes: box_cols = 16 uses the
-// 64-byte swizzle (operand loads), box_cols = 32 the 128-byte swizzle
-// (node-vector stores).
-int encode_map(cafe_ctx* C, CUtensorMap* m, const float* base, int64_t rows, int cols, int box_cols) {
+// 2D FP32 tensor map [rows][cols] with boxes of box_rows x box_cols:
+// box_cols = 16 uses the 64-byte swizzle, box_cols = 32 the 128-byte swizzle.
+int encode_map(cafe_ctx* C, CUtensorMap* m, const float* base, int64_t rows, int cols, int box_cols, int box_rows) {
     static EncodeTiledFn enc = nullptr;
     if (!enc) {
         cudaDriverEntryPointQueryResult q;
@@ -642,7 +641,8 @@ int encode_map(cafe_ctx* C, CUtensorMap* m, const float* base, int64_t rows, int
     }
     cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)cols * sizeof(float)};
-    cuuint32_t box[2] = {(cuuint32_t)box_cols, 32};
+    if (box_rows < 1 || box_rows > 256 || box_rows > rows) return fail(C, CAFE_ERR_INVALID, "tensor map box of %d rows", box_rows);
+    cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
     cuuint32_t es[2] = {1, 1};
     const CUtensorMapSwizzle sw = box_cols == 16 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B;
     const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, es,
@@ -653,10 +653,10 @@ int encode_map(cafe_ctx* C, CUtensorMap* m, const float* base, int64_t rows, int
 }
 
 int cached_map(cafe_ctx* C, Workspace& ws, int slot, CUtensorMap* out, const float* base, int64_t rows, int cols,
-               int box_cols) {
+               int box_cols, int box_rows) {
     Workspace::MapCache& mc = ws.map_cache[slot];
-    if (mc.ptr != base || mc.rows != rows || mc.cols != cols || mc.box != box_cols) {
-        int rc = encode_map(C, &mc.map, base, rows, cols, box_cols);
+    if (mc.ptr != base || mc.rows != rows || mc.cols != cols || mc.box != box_cols || mc.box_rows != box_rows) {
+        int rc = encode_map(C, &mc.map, base, rows, cols, box_cols, box_rows);
         if (rc) {
             mc.ptr = nullptr;
             return rc;
@@ -665,6 +665,7 @@ int cached_map(cafe_ctx* C, Workspace& ws, int slot, CUtensorMap* out, const flo
         mc.rows = rows;
         mc.cols = cols;
         mc.box = box_cols;
+        mc.box_rows = box_rows;
     }
     *out = mc.map;
     return CAFE_OK;
@@ -1152,13 +1153,21 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             i = j;
         }
         CK(ws.tc_vec.reserve((size_t)vrows * Wm * sizeof(float)), "tc vectors");
+        // node vectors move in boxes of one tile's 128 rows; each launch's
+        // matrix maps have boxes of its Ws rows (one TMA instruction per
+        // operand and chunk)
         TcMaps maps;
         const int kbox = prune_tc_kchunk();
-        int rc = cached_map(C, ws, 0, &maps.mat_hi, ws.tc_hi.as<float>(), (int64_t)n_mat * Wm, Wm, kbox);
-        if (!rc) rc = cached_map(C, ws, 1, &maps.mat_lo, ws.tc_lo.as<float>(), (int64_t)n_mat * Wm, Wm, kbox);
-        if (!rc) rc = cached_map(C, ws, 2, &maps.vec, ws.tc_vec.as<float>(), vrows, Wm, kbox);
-        if (!rc) rc = cached_map(C, ws, 3, &maps.vst, ws.tc_vec.as<float>(), vrows, Wm, 32);
+        int rc = cached_map(C, ws, 2, &maps.vec, ws.tc_vec.as<float>(), vrows, Wm, kbox, 128);
+        if (!rc) rc = cached_map(C, ws, 3, &maps.vst, ws.tc_vec.as<float>(), vrows, Wm, 32, 128);
         if (rc) return rc;
+        auto launch_maps = [&](int Ws, TcMaps* m) {
+            *m = maps;
+            const int q = 4 + 2 * (Ws / 32 - 1);      // Ws: a multiple of 32 up to 256
+            int r = cached_map(C, ws, q, &m->mat_hi, ws.tc_hi.as<float>(), (int64_t)n_mat * Wm, Wm, kbox, Ws);
+            if (!r) r = cached_map(C, ws, q + 1, &m->mat_lo, ws.tc_lo.as<float>(), (int64_t)n_mat * Wm, Wm, kbox, Ws);
+            return r;
+        };
         const int n_tc = (int)tc_tiles.size();
         CK(ws.tiles.reserve(n_tc * sizeof(PruneTile)), "tiles");
         CK(ws.h_tiles.reserve(n_tc * sizeof(PruneTile)), "tiles");
@@ -1195,8 +1204,8 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         a.phase_clocks = nullptr;
         static const bool phase_env = getenv("CAFE_TC_PHASES") != nullptr;
         if (phase_env) {
-            CK(ws.phase.reserve(6 * sizeof(unsigned long long)), "phase clocks");
-            CK(cudaMemsetAsync(ws.phase.p, 0, 6 * sizeof(unsigned long long), ws.stream), "phase clocks");
+            CK(ws.phase.reserve(kPhases * sizeof(unsigned long long)), "phase clocks");
+            CK(cudaMemsetAsync(ws.phase.p, 0, kPhases * sizeof(unsigned long long), ws.stream), "phase clocks");
             a.phase_clocks = ws.phase.as<unsigned long long>();
         }
         if (prof) {
@@ -1223,7 +1232,11 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             b.stages = L.stages;
             b.vrow_base = L.vrow_base;
             cudaStream_t st = fork ? ws.aux[q % Workspace::kAux] : ws.stream;
-            CK(op_launch(ws, 5, [&] { return launch_prune_tc(maps, b, L.n_ctas, L.smem, st); }, maps, b, L.n_ctas, L.smem,
+            if (b.Ws % 32 || b.Ws < 32 || b.Ws > 256) return fail(C, CAFE_ERR_INVALID, "tensor-core tile of %d rows", b.Ws);
+            TcMaps lm;
+            const int rcm = launch_maps(b.Ws, &lm);
+            if (rcm) return rcm;
+            CK(op_launch(ws, 5, [&] { return launch_prune_tc(lm, b, L.n_ctas, L.smem, st); }, lm, b, L.n_ctas, L.smem,
                          st),
                "prune tc");
         }
@@ -1239,12 +1252,18 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         }
 
         if (phase_env) {
-            unsigned long long h[6];
+            unsigned long long h[kPhases];
             CK(cudaMemcpyAsync(h, ws.phase.p, sizeof(h), cudaMemcpyDeviceToHost, ws.stream), "phase clocks");
             CK(cudaStreamSynchronize(ws.stream), "phase clocks");
             const double n = (double)h[5] + 1e-9;
             fprintf(stderr, "k_prune_tc clocks per tile-node: setup %.0f gemm %.0f epilogue %.0f root %.0f sync %.0f (%llu tile-nodes)\n",
                     h[0] / n, h[1] / n, h[2] / n, h[3] / n, h[4] / n, h[5]);
+            fprintf(stderr, "  per tile-node: store wait %.0f leaf gather %.0f; per chunk (%.2f per tile-node): stage wait %.0f "
+                    "TMA wait %.0f split %.0f MMA issue %.0f (of which the stage's wait %.0f); last-MMA wait per tile-node %.0f\n",
+                    h[12] / n, h[13] / n, h[11] / n, h[6] / (h[11] + 1e-9), h[7] / (h[11] + 1e-9), h[8] / (h[11] + 1e-9),
+                    h[9] / (h[11] + 1e-9), h[14] / (h[11] + 1e-9), h[10] / n);
+            fprintf(stderr, "  TMA issue per chunk %.0f; barriers per tile-node: after the chunks %.0f, after the last MMAs %.0f\n",
+                    h[15] / (h[11] + 1e-9), h[16] / n, h[17] / n);
         }
 
         if (prof) C->prof.end(1, ws.stream, ev);

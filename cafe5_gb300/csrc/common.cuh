@@ -142,6 +142,8 @@ struct TcBuffers {
 
 cudaError_t launch_convert_tc(const ConvertJob* d_jobs, int n_jobs, TcBuffers b, cudaStream_t s);
 
+constexpr int kPhases = 18;   // k_prune_tc phase counters (CAFE_TC_PHASES)
+
 struct PruneTcArgs {
     TreePlan plan;
     const PruneTile* tiles;      // 128-family tiles; S = W - 1 of the tile's bin
@@ -174,8 +176,9 @@ struct PruneTcArgs {
     int Ws;                      // B rows per stage: the launch's bin width / nsplit
     int stages;                  // pipeline stages (1 to 4)
     int64_t vrow_base;           // first node-vector row of this launch
-    unsigned long long* phase_clocks;   // optional [6]: SM clocks of thread 0 in child setup, GEMMs,
-                                        // epilogue, root bookkeeping, end-of-node barrier; tile-nodes
+    unsigned long long* phase_clocks;   // optional [kPhases]: SM clocks of thread 0 in child setup, GEMMs,
+                                        // epilogue, root bookkeeping, end-of-node barrier; tile-nodes;
+                                        // then the GEMM chain's parts (k_prune_tc.cu)
     int debug_wait_limit;        // > 0: the wait for a node's GEMMs gives up after this many polls
                                  // minus one (tests of the time-out path); 0: the default bound
 };
@@ -183,7 +186,8 @@ struct PruneTcArgs {
 // Tensor maps travel by value (__grid_constant__); the host encodes them.
 // Operand loads use prune_tc_kchunk()-column boxes (mat_*, vec; 128-byte
 // swizzle for 32 columns, 64-byte for 16); the epilogue stores node vectors
-// in 32-column boxes in the 128-byte swizzle (vst). Boxes are 32 rows.
+// in 32-column boxes in the 128-byte swizzle (vst). Vector boxes are one
+// tile's 128 rows; matrix boxes are the launch's Ws rows.
 struct TcMaps {
     CUtensorMap mat_hi, mat_lo, vec, vst;
 };

@@ -420,6 +420,32 @@ __device__ __noinline__ int epi_maxexp(const NodeSrc<NC> ns, int W, int s_off, i
     return maxe;
 }
 
+// Columns c32 .. c32 + SC - 1 of this thread's row of the scaled product
+// into a staging tile in the 128-byte-swizzled layout (warp-collective:
+// TMEM loads).
+template <int NC>
+__device__ __forceinline__ void epi_fill_chunk(const NodeSrc<NC>& ns, int c32, const float (&scl)[NC], float* tile,
+                                               int tid) {
+    uint8_t* row = reinterpret_cast<uint8_t*>(tile) + (size_t)(tid >> 3) * 1024 + (size_t)(tid & 7) * 128;
+    for (int col0 = c32; col0 < c32 + SC; col0 += CW) {
+        uint32_t r[NC][CW];
+        load_children(ns, col0, r);
+        float p[CW];
+#pragma unroll
+        for (int j = 0; j < CW; ++j) p[j] = 1.0f;
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+#pragma unroll
+            for (int j = 0; j < CW; ++j) p[j] *= __uint_as_float(r[c][j]) * scl[c];
+#pragma unroll
+        for (int q = 0; q < CW / 4; ++q) {
+            const int j = ((col0 - c32) >> 2) + q;          // 16-byte piece of the 128-byte row
+            const int off = (j ^ (tid & 7)) << 4;
+            *reinterpret_cast<float4*>(row + off) = make_float4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
+        }
+    }
+}
+
 // Pass 2 (inner nodes; every thread of the CTA): the scaled product in FP32
 // into a staging tile in the 128-byte-swizzled layout, 32 columns at a
 // time, written to the node's vector rows by TMA stores (columns x_off ..
@@ -438,29 +464,68 @@ __device__ __forceinline__ void epi_store(const NodeSrc<NC>& ns, int W, const fl
             if (tid == 0) tc::bulk_wait_read1();     // the chunk two back has read this tile
             __syncthreads();
         }
-        uint8_t* row = reinterpret_cast<uint8_t*>(tile) + (size_t)(tid >> 3) * 1024 + (size_t)(tid & 7) * 128;
+        epi_fill_chunk<NC>(ns, c32, scl, tile, tid);
+        tc::fence_proxy_async_shared();
+        __syncthreads();
+        if (tid == 0) {
+            tc::tma_store_2d(map, x_off + c32, vrow, tile);     // one TM-row box
+            tc::bulk_commit();
+        }
+    }
+}
+
+// One pass for an inner node whose vector fits the two staging tiles
+// (W <= 2 SC, one CTA per tile): the statistics of epi_scan and, at the
+// same time, the unscaled product into the staging tiles (tile c32 / SC).
+// Warp-collective.
+template <int NC>
+__device__ __forceinline__ void epi_scan_fill(const NodeSrc<NC>& ns, int W, float* stg, int tid, float& maxp,
+                                              float (&fmx)[NC], float (&fmn)[NC]) {
+    static_assert(NC == 2, "two factors per node");
+    maxp = 0.0f;
+    fmx[0] = fmx[1] = 0.0f;
+    fmn[0] = fmn[1] = 1.0f;
+    for (int c32 = 0; c32 < W; c32 += SC) {
+        uint8_t* row = reinterpret_cast<uint8_t*>(stg + (size_t)(c32 / SC) * TM * SC) + (size_t)(tid >> 3) * 1024 +
+                       (size_t)(tid & 7) * 128;
         for (int col0 = c32; col0 < c32 + SC; col0 += CW) {
             uint32_t r[NC][CW];
             load_children(ns, col0, r);
             float p[CW];
 #pragma unroll
-            for (int j = 0; j < CW; ++j) p[j] = 1.0f;
-#pragma unroll
-            for (int c = 0; c < NC; ++c)
-#pragma unroll
-                for (int j = 0; j < CW; ++j) p[j] *= __uint_as_float(r[c][j]) * scl[c];
+            for (int j = 0; j < CW; ++j) {
+                const float r0 = __uint_as_float(r[0][j]), r1 = __uint_as_float(r[1][j]);
+                p[j] = (1.0f * r0) * r1;      // the same rounding as epi_fill_chunk with unit scales
+                maxp = fmaxf(maxp, p[j]);
+                fmx[0] = fmaxf(fmx[0], r0);
+                fmx[1] = fmaxf(fmx[1], r1);
+                fmn[0] = fminf(fmn[0], r0);
+                fmn[1] = fminf(fmn[1], r1);
+            }
 #pragma unroll
             for (int q = 0; q < CW / 4; ++q) {
-                const int j = ((col0 - c32) >> 2) + q;          // 16-byte piece of the 128-byte row
+                const int j = ((col0 - c32) >> 2) + q;
                 const int off = (j ^ (tid & 7)) << 4;
                 *reinterpret_cast<float4*>(row + off) = make_float4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
             }
         }
-        tc::fence_proxy_async_shared();
-        __syncthreads();
-        if (tid == 0) {
-            for (int r = 0; r < TM / 32; ++r) tc::tma_store_2d(map, x_off + c32, vrow + 32 * r, tile + r * 32 * SC);
-            tc::bulk_commit();
+    }
+}
+
+// This thread's staged row times a power of two s (exact unless a value
+// was already below the FP32 normal range before the scaling).
+__device__ __forceinline__ void rescale_row(float* stg, int tid, int W, float s) {
+    for (int c32 = 0; c32 < W; c32 += SC) {
+        float4* row = reinterpret_cast<float4*>(reinterpret_cast<uint8_t*>(stg + (size_t)(c32 / SC) * TM * SC) +
+                                                (size_t)(tid >> 3) * 1024 + (size_t)(tid & 7) * 128);
+#pragma unroll
+        for (int q = 0; q < SC / 4; ++q) {
+            float4 v = row[q];
+            v.x *= s;
+            v.y *= s;
+            v.z *= s;
+            v.w *= s;
+            row[q] = v;
         }
     }
 }
@@ -561,7 +626,16 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
     // node-vector rows of this tile (the CTAs of a cluster share them, each
     // writing its own columns)
     const int64_t vrow_cta = a.vrow_base + (int64_t)cid * a.n_slots * TM;
-    unsigned long long ph[6] = {0, 0, 0, 0, 0, 0};
+    // thread 0's clocks (CAFE_TC_PHASES): [0..4] node phases, [5] tile-nodes,
+    // [6] waits for a free stage, [7] waits for a chunk's TMA, [8] split and
+    // barriers, [9] MMA issue, [10] wait for the node's last MMAs, [11] chunks,
+    // [12] wait for the previous node's stores, [13] leaf gathers, [14] the MMA
+    // issuer's wait for a chunk, [15] TMA issue, [16] and [17] the barriers
+    // after the chunk loop and after the last MMAs
+    // (kept in shared memory: only thread 0 touches them, and they cost no registers)
+    __shared__ unsigned long long ph[kPhases];
+    if (tid == 0)
+        for (int q = 0; q < kPhases; ++q) ph[q] = 0;
     const bool timing = a.phase_clocks != nullptr && tid == 0;
 
     for (int t = cid; t < a.n_tiles; t += n_cl) {
@@ -615,6 +689,7 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
             // overwrites their staging tile or reads their rows back (in a
             // cluster: the other CTAs' columns as well)
             if (tid == 0) tc::bulk_wait0();
+            if (timing) ph[12] += clock64() - ts;
             if (NSPLIT > 1) {
                 if (tid == 0) tc::fence_proxy_async_global();
                 __syncthreads();
@@ -663,7 +738,11 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                             gather_leaf(a.mat_tr + (size_t)nd.c[c].mat * Wm * Wm, Wm, L, ns2.s[c].taddr, Wn, s_off);
                         }
                 };
-                if (n_chunks == 0) gather_leaves();
+                if (n_chunks == 0) {
+                    const long long tg = timing ? clock64() : 0;
+                    gather_leaves();
+                    if (timing) ph[13] += clock64() - tg;
+                }
                 for (int i = 0; i < n_chunks + NS - 1; ++i) {
                     // ---- produce chunk i ----
                     if (i < n_chunks) {
@@ -681,26 +760,33 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                         // the first NS chunks of a node find their stages free: the
                         // previous node's MMAs completed before its epilogue and its
                         // staging-tile stores were waited for at the node start
+                        const long long te = timing ? clock64() : 0;
                         if (tid == 0 && !abort_sh && i >= NS && !tc::mbar_wait(&bar_empty[st], (u - 1) & 1)) {
                             atomicExch(a.status, 1);
                             abort_sh = 1;
                         }
+                        if (timing) ph[6] += clock64() - te;
+                        const long long ti = timing ? clock64() : 0;
                         if (tid == 0 && !abort_sh) {
                             tc::mbar_expect_tx(&bar_full[st], (uint32_t)((TM + 2 * Wn) * KC * sizeof(float)));
                             // the FP32 node vector lands in the hi operand; the
                             // consumer splits it into hi and lo in place
+                            // one box each: the vector's TM rows, the matrices' Wn rows
+                            // (TMA issue is slow enough per instruction to count)
                             const int vrow = (int)(vrow_cta + (int64_t)chi.slot * TM);
-                            for (int r = 0; r < TM / 32; ++r)
-                                tc::tma_load_2d(Ahi + r * 32 * KC, &map_vec, kc * KC, vrow + 32 * r, &bar_full[st]);
+                            tc::tma_load_2d(Ahi, &map_vec, kc * KC, vrow, &bar_full[st]);
                             const int mrow = chi.mat * Wm + s_off;     // this CTA's output states
-                            for (int r = 0; r < Wn / 32; ++r) {
-                                tc::tma_load_2d(Bhi + r * 32 * KC, &map_mhi, kc * KC, mrow + 32 * r, &bar_full[st]);
-                                tc::tma_load_2d(Blo + r * 32 * KC, &map_mlo, kc * KC, mrow + 32 * r, &bar_full[st]);
-                            }
+                            tc::tma_load_2d(Bhi, &map_mhi, kc * KC, mrow, &bar_full[st]);
+                            tc::tma_load_2d(Blo, &map_mlo, kc * KC, mrow, &bar_full[st]);
                             last_full[st] = 1;
                             last_full_parity[st] = u & 1;
                         }
-                        if (i == 0) gather_leaves();
+                        if (timing) ph[15] += clock64() - ti;
+                        if (i == 0) {
+                            const long long tg = timing ? clock64() : 0;
+                            gather_leaves();
+                            if (timing) ph[13] += clock64() - tg;
+                        }
                     }
                     // ---- consume chunk j = i - (NS - 1) ----
                     const int j = i - (NS - 1);
@@ -710,7 +796,9 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                         const uint32_t cg = g + (uint32_t)j;
                         const int st = (int)(cg % (uint32_t)NS);
                         float* Ahi = reinterpret_cast<float*>(smem + st * sbytes);
+                        const long long tf = timing ? clock64() : 0;
                         const bool ok = abort_sh || tc::mbar_wait(&bar_full[st], (cg / (uint32_t)NS) & 1);
+                        const long long tf1 = timing ? clock64() : 0;
                         const bool fail = __syncthreads_or(!ok);
                         if (fail) {
                             if (tid == 0) {
@@ -722,6 +810,11 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                             tc::fence_proxy_async_shared();
                         }
                         __syncthreads();
+                        if (timing) {
+                            ph[7] += tf1 - tf;
+                            ph[8] += clock64() - tf1;
+                            ph[11] += 1;
+                        }
                     }
                     if (j >= 0 && tid == 0 && !abort_sh) {
                         const int c = j < n0 ? 0 : 1;
@@ -735,9 +828,11 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                         const float* Alo = Ahi + TM * KC;
                         const float* Bhi = Alo + TM * KC;
                         const float* Blo = Bhi + a.Ws * KC;
+                        const long long tm = timing ? clock64() : 0;
                         if (tc::mbar_wait(&bar_full[st], u & 1)) {
                             last_full[st] = 0;
                             tc::fence_after();
+                            if (timing) ph[14] += clock64() - tm;
                             const uint32_t d = tmem + (uint32_t)(chi.tcol * Wn);
 #pragma unroll
                             for (int ks = 0; ks < KC / 8; ++ks) {
@@ -748,6 +843,7 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                                 tc::mma_tf32(d, al, bh, idesc, 1);
                             }
                             tc::mma_commit(&bar_empty[st]);
+                            if (timing) ph[9] += clock64() - tm;
                         } else {
                             atomicExch(a.status, 1);
                             abort_sh = 1;
@@ -756,7 +852,10 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                 }
                 if (tid == 0 && !abort_sh) tc::mma_commit(&bar_done);
                 g += (uint32_t)n_chunks;        // every thread tracks the stage sequence
+                const long long tq = timing ? clock64() : 0;
                 __syncthreads();
+                const long long td = timing ? clock64() : 0;
+                if (timing) ph[16] += td - tq;
                 if (!abort_sh) {
                     // (a test hook can make this wait give up after limit - 1 polls)
                     if (!tc::mbar_wait(&bar_done, dn & 1, a.debug_wait_limit > 0 ? a.debug_wait_limit - 1 : (1 << 24))) {
@@ -765,9 +864,12 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                     }
                 }
                 dn++;
+                if (timing) ph[10] += clock64() - td;
                 tc::fence_after();
             }
+            const long long tz = timing ? clock64() : 0;
             __syncthreads();
+            if (timing) ph[17] += clock64() - tz;
             if (abort_sh) break;
             long long t1 = timing ? clock64() : 0;
 
@@ -776,7 +878,16 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
             int E = ns2.Eacc;
             bool nflag = ns2.flag;
             float maxp, bf, bp, bq, be, fmx[2], fmn[2];
-            epi_scan<2>(ns2, Wn, s_off, is_root, Rf, prior_f, scl, maxp, bf, bp, bq, be, fmx, fmn);
+            // one CTA per tile and a vector that fits the staging tiles: the
+            // statistics and the unscaled product in one pass over TMEM
+            const bool fused = NSPLIT == 1 && !is_root && Wn <= 2 * SC;
+            float* stg = reinterpret_cast<float*>(smem);     // stage 0 holds the two staging tiles
+            if (fused) {
+                epi_scan_fill<2>(ns2, Wn, stg, tid, maxp, fmx, fmn);
+                bf = bp = bq = be = 0.0f;
+            } else {
+                epi_scan<2>(ns2, Wn, s_off, is_root, Rf, prior_f, scl, maxp, bf, bp, bq, be, fmx, fmn);
+            }
             if (NSPLIT > 1) {
                 // every CTA's statistics: maxima, minima, the best root row
                 // (combined in rank order, so a tie goes to the first in state
@@ -880,9 +991,28 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
             long long t2 = timing ? clock64() : 0;
             flag |= nflag && !dead;
             if (!is_root) {
-                // stage 0 holds the two staging tiles
-                epi_store<2>(ns2, Wn, scl, reinterpret_cast<float*>(smem), tid, &map_vst,
-                             (int)(vrow_cta + (int64_t)vs * TM), s_off);
+                float flush = kTiny;   // values flushed on the store, in the stored vector's units
+                if (fused) {
+                    // a warp with a family on the exact path writes its rows again
+                    // with the factors scaled before the product; otherwise a
+                    // family brought back to [0.5, 1) is scaled in place, where a
+                    // value below 2^-126 before the scaling was flushed
+                    if (__any_sync(0xffffffffu, need)) {
+                        for (int c32 = 0; c32 < Wn; c32 += SC) epi_fill_chunk<2>(ns2, c32, scl, stg + (size_t)(c32 / SC) * TM * SC, tid);
+                    } else if (scl[0] != 1.0f) {
+                        rescale_row(stg, tid, Wn, scl[0]);
+                        flush = kTiny * scl[0];
+                    }
+                    tc::fence_proxy_async_shared();
+                    __syncthreads();
+                    if (tid == 0) {
+                        const int vrow = (int)(vrow_cta + (int64_t)vs * TM);
+                        for (int c32 = 0; c32 < Wn; c32 += SC) tc::tma_store_2d(&map_vst, c32, vrow, stg + (size_t)(c32 / SC) * TM * SC);
+                        tc::bulk_commit();
+                    }
+                } else {
+                    epi_store<2>(ns2, Wn, scl, stg, tid, &map_vst, (int)(vrow_cta + (int64_t)vs * TM), s_off);
+                }
                 Esh[vs * TM + tid] = E;
                 // the stored vector's bound, from the factors' maxima: u_A (f_B + u_B)
                 // + u_B f_A over all states, with a leaf factor's u counted only
@@ -893,7 +1023,7 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                 u0 *= scl[0];
                 u1 *= scl[1];
                 const float ev = u0 * (fmx[1] * scl[1] + u1) + u1 * (fmx[0] * scl[0]);
-                Erh[vs * TM + tid] = fminf(ev + kTiny, 1e30f);
+                Erh[vs * TM + tid] = fminf(ev + flush, 1e30f);
             } else if (fam >= 0 && h == 0) {     // (a cluster's first CTA writes the term)
                 double o = NAN;
                 const double best = (double)bp * (double)bq;
@@ -927,7 +1057,7 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
     }
 
     if (timing)
-        for (int q = 0; q < 6; ++q) atomicAdd(&a.phase_clocks[q], ph[q]);
+        for (int q = 0; q < kPhases; ++q) atomicAdd(&a.phase_clocks[q], ph[q]);
     // teardown: no copy of ours may still be landing when TMEM goes away
     if (tid == 0) tc::bulk_wait0();
     tc::fence_before();
