@@ -1166,6 +1166,8 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             const int q = 4 + 2 * (Ws / 32 - 1);      // Ws: a multiple of 32 up to 256
             int r = cached_map(C, ws, q, &m->mat_hi, ws.tc_hi.as<float>(), (int64_t)n_mat * Wm, Wm, kbox, Ws);
             if (!r) r = cached_map(C, ws, q + 1, &m->mat_lo, ws.tc_lo.as<float>(), (int64_t)n_mat * Wm, Wm, kbox, Ws);
+            // leaf blocks: W x W (read only where W <= 64, one CTA per tile)
+            if (!r) r = cached_map(C, ws, 20 + (Ws / 32 - 1), &m->tr, ws.tc_tr.as<float>(), (int64_t)n_mat * Wm, Wm, 32, Ws);
             return r;
         };
         const int n_tc = (int)tc_tiles.size();

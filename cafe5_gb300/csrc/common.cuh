@@ -187,9 +187,11 @@ struct PruneTcArgs {
 // Operand loads use prune_tc_kchunk()-column boxes (mat_*, vec; 128-byte
 // swizzle for 32 columns, 64-byte for 16); the epilogue stores node vectors
 // in 32-column boxes in the 128-byte swizzle (vst). Vector boxes are one
-// tile's 128 rows; matrix boxes are the launch's Ws rows.
+// tile's 128 rows; matrix boxes are the launch's Ws rows. tr: the FP32
+// transposed matrices in boxes of 32 columns x the launch's W rows (leaf
+// blocks of bins up to 64 states).
 struct TcMaps {
-    CUtensorMap mat_hi, mat_lo, vec, vst;
+    CUtensorMap mat_hi, mat_lo, vec, vst, tr;
 };
 
 cudaError_t launch_prune_tc(const TcMaps& maps, const PruneTcArgs& a, int n_ctas, size_t smem, cudaStream_t s);

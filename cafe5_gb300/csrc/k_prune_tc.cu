@@ -316,6 +316,39 @@ __device__ __noinline__ void gather_leaf(const float* __restrict__ tr, int Wm, c
     tc::tmem_wait_st();
 }
 
+// A leaf child's factor into its TMEM columns (warp-collective), read from
+// the W x W block of the transposed FP32 matrix that a TMA load placed in
+// shared memory: W / 32 boxes of W rows x 32 columns, 128-byte swizzled
+// (box b holds columns 32 b .. 32 b + 31; the 16-byte piece q of row r
+// lies at piece q ^ (r & 7)). Column j of this thread's row is
+// sum_d w_d tr[col_d][j], summed in the order of the global-memory gather.
+__device__ __forceinline__ void gather_leaf_smem(const float* blk, int W, const LeafW& L, uint32_t taddr) {
+    for (int col0 = 0; col0 < W; col0 += 16) {
+        float v[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = 0.0f;
+        const uint8_t* box = reinterpret_cast<const uint8_t*>(blk + (size_t)(col0 / 32) * W * 32);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int r = L.col[d];
+            if (r < 0) continue;
+            const uint8_t* row = box + (size_t)r * 128;
+            const float w = L.w[d];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int piece = ((col0 & 31) >> 2) + q;
+                const float4 x = *reinterpret_cast<const float4*>(row + ((piece ^ (r & 7)) << 4));
+                v[4 * q] = fmaf(w, x.x, v[4 * q]);
+                v[4 * q + 1] = fmaf(w, x.y, v[4 * q + 1]);
+                v[4 * q + 2] = fmaf(w, x.z, v[4 * q + 2]);
+                v[4 * q + 3] = fmaf(w, x.w, v[4 * q + 3]);
+            }
+        }
+        tc::tmem_st16(taddr + (uint32_t)col0, v);
+    }
+    tc::tmem_wait_st();
+}
+
 // CW values of a child's factor starting at column col0 (issue only for
 // TMEM children; the unit factor is filled at once).
 __device__ __forceinline__ void load_unit(uint32_t (&out)[CW]) {
@@ -571,10 +604,10 @@ template <int NSPLIT>
 __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
     k_prune_tc(const __grid_constant__ CUtensorMap map_mhi, const __grid_constant__ CUtensorMap map_mlo,
                const __grid_constant__ CUtensorMap map_vec, const __grid_constant__ CUtensorMap map_vst,
-               const PruneTcArgs a) {
+               const __grid_constant__ CUtensorMap map_tr, const PruneTcArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    __shared__ __align__(8) uint64_t bar_full[MAXST], bar_empty[MAXST], bar_done, bar_drain;
+    __shared__ __align__(8) uint64_t bar_full[MAXST], bar_empty[MAXST], bar_done, bar_drain, bar_leaf;
     __shared__ __align__(8) uint64_t bar_x[2];     // cluster handshakes (NSPLIT > 1), in turn
     // [2][NSPLIT - 1][kXN][TM]: the other CTAs' values, per handshake
     __shared__ float xbuf[NSPLIT > 1 ? 2 * (NSPLIT - 1) * kXN * TM : 1];
@@ -602,6 +635,7 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
         }
         tc::mbar_init(&bar_done, 1);
         tc::mbar_init(&bar_drain, 1);
+        tc::mbar_init(&bar_leaf, 1);
         if (NSPLIT > 1) {
             // one arrival per thread of every other CTA (a count of at least 1)
             tc::mbar_init(&bar_x[0], (NSPLIT > 1 ? NSPLIT - 1 : 1) * NTHREADS);
@@ -621,6 +655,8 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
 
     uint32_t g = 0;          // chunks issued so far (same in every thread)
     uint32_t dn = 0;         // completions of bar_done observed (all threads)
+    uint32_t ln = 0;         // leaf-block loads issued (all threads)
+    int leaf_pending = 0;    // thread 0: a leaf-block load not yet waited for
     int last_full[MAXST] = {0, 0, 0, 0};            // thread 0: stage has a TMA not yet waited for
     uint32_t last_full_parity[MAXST] = {0, 0, 0, 0};
     // node-vector rows of this tile (the CTAs of a cluster share them, each
@@ -728,14 +764,57 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                 const int n_chunks = n0 + nk[1];
                 // leaf factors (CTA-uniform): after the first chunk's loads are
                 // issued, or at once when the node runs no GEMM
+                // bins of up to 64 states (one CTA per tile): each leaf child's
+                // W x W block of the transposed matrix comes by TMA into a free
+                // operand area of chunk 0's stage (the lo operand, which chunk
+                // 0's split writes only after the gather; a node without GEMMs
+                // uses the hi area too), while chunk 0's operands load
+                const bool smem_leaf = NSPLIT == 1 && W * W <= TM * KC;
+                int n_leaf = 0;
+#pragma unroll
+                for (int c = 0; c < 2; ++c) n_leaf += (c < nch && nd.c[c].leaf_col >= 0) ? 1 : 0;
+                float* leaf_area[2];
+                {
+                    float* a_hi = reinterpret_cast<float*>(smem + (g % (uint32_t)NS) * sbytes);
+                    leaf_area[0] = n_chunks ? a_hi + TM * KC : a_hi;
+                    leaf_area[1] = a_hi + TM * KC;
+                }
+                const bool leaf_tma = smem_leaf && n_leaf > 0;
+                if (leaf_tma && tid == 0 && !abort_sh) {
+                    tc::fence_proxy_async_shared();     // this CTA's earlier reads of the area come first
+                    tc::mbar_expect_tx(&bar_leaf, (uint32_t)(n_leaf * W * W * sizeof(float)));
+                    int q = 0;
+#pragma unroll
+                    for (int c = 0; c < 2; ++c)
+                        if (c < nch && nd.c[c].leaf_col >= 0) {
+                            for (int b = 0; b < W / 32; ++b)
+                                tc::tma_load_2d(leaf_area[q] + (size_t)b * W * 32, &map_tr, 32 * b, nd.c[c].mat * Wm, &bar_leaf);
+                            ++q;
+                        }
+                    leaf_pending = 1;
+                }
                 auto gather_leaves = [&]() {
                     if (__shfl_sync(0xffffffffu, abort_sh, 0)) return;   // warp-uniform: the stores are collective
+                    if (leaf_tma) {
+                        const bool ok = tc::mbar_wait(&bar_leaf, ln & 1);
+                        if (!__all_sync(0xffffffffu, ok)) {
+                            if ((tid & 31) == 0) {
+                                atomicExch(a.status, 1);
+                                abort_sh = 1;
+                            }
+                            return;
+                        }
+                        if (tid == 0) leaf_pending = 0;
+                    }
+                    int q = 0;
 #pragma unroll
                     for (int c = 0; c < 2; ++c)
                         if (c < nch && nd.c[c].leaf_col >= 0) {
                             LeafW L;
                             leaf_weights(a, fam, cnt_cur[c], S, L);
-                            gather_leaf(a.mat_tr + (size_t)nd.c[c].mat * Wm * Wm, Wm, L, ns2.s[c].taddr, Wn, s_off);
+                            if (leaf_tma) gather_leaf_smem(leaf_area[q], W, L, ns2.s[c].taddr);
+                            else gather_leaf(a.mat_tr + (size_t)nd.c[c].mat * Wm * Wm, Wm, L, ns2.s[c].taddr, Wn, s_off);
+                            ++q;
                         }
                 };
                 if (n_chunks == 0) {
@@ -852,6 +931,7 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                 }
                 if (tid == 0 && !abort_sh) tc::mma_commit(&bar_done);
                 g += (uint32_t)n_chunks;        // every thread tracks the stage sequence
+                if (leaf_tma) ln++;
                 const long long tq = timing ? clock64() : 0;
                 __syncthreads();
                 const long long td = timing ? clock64() : 0;
@@ -1068,9 +1148,11 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
         tc::mma_commit(&bar_drain);
         tc::mbar_wait(&bar_drain, 0, 1 << 24);
     }
-    if (abort_sh && tid == 0)
+    if (abort_sh && tid == 0) {
         for (int q = 0; q < MAXST; ++q)
             if (q < NS && last_full[q]) tc::mbar_wait(&bar_full[q], last_full_parity[q], 1 << 20);
+        if (leaf_pending) tc::mbar_wait(&bar_leaf, ln & 1, 1 << 20);
+    }
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)a.tmem_cols);
     // no CTA of a cluster exits while another may still write into its
@@ -1273,7 +1355,7 @@ cudaError_t launch_prune_tc(const TcMaps& m, const PruneTcArgs& a, int n_ctas, s
     if (smem > (size_t)prune_tc_max_smem(a.nsplit)) return cudaErrorInvalidValue;
     if (a.stages < 1 || a.stages > MAXST) return cudaErrorInvalidValue;
     if (a.nsplit == 1) {
-        k_prune_tc<1><<<n_ctas, NTHREADS, smem, s>>>(m.mat_hi, m.mat_lo, m.vec, m.vst, a);
+        k_prune_tc<1><<<n_ctas, NTHREADS, smem, s>>>(m.mat_hi, m.mat_lo, m.vec, m.vst, m.tr, a);
         return cudaGetLastError();
     }
     // a cluster of nsplit CTAs per tile, each with Ws = W / nsplit output
@@ -1294,8 +1376,8 @@ cudaError_t launch_prune_tc(const TcMaps& m, const PruneTcArgs& a, int n_ctas, s
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    if (a.nsplit == 2) return cudaLaunchKernelEx(&cfg, k_prune_tc<2>, m.mat_hi, m.mat_lo, m.vec, m.vst, a);
-    return cudaLaunchKernelEx(&cfg, k_prune_tc<4>, m.mat_hi, m.mat_lo, m.vec, m.vst, a);
+    if (a.nsplit == 2) return cudaLaunchKernelEx(&cfg, k_prune_tc<2>, m.mat_hi, m.mat_lo, m.vec, m.vst, m.tr, a);
+    return cudaLaunchKernelEx(&cfg, k_prune_tc<4>, m.mat_hi, m.mat_lo, m.vec, m.vst, m.tr, a);
 }
 
 }  // namespace cafe

@@ -158,7 +158,8 @@ struct Workspace {
         int box = 0;
         int box_rows = 0;
         CUtensorMap map;
-    } map_cache[20];   // [2] vector loads, [3] vector stores, [4 + 2 (Ws/32 - 1) + {0, 1}] matrix hi / lo
+    } map_cache[28];   // [2] vector loads, [3] vector stores, [4 + 2 (Ws/32 - 1) + {0, 1}] matrix hi / lo,
+                       // [20 + Ws/32 - 1] transposed matrices
     DevBuf scratch, tiles, mats, cat, fam_lnl, total, nfail, jobs, catp;
     PinnedBuf h_tiles, h_mats, h_jobs, h_out, h_catp;
     // tensor-core path
