@@ -628,7 +628,8 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
 
 // 2D FP32 tensor map [rows][cols] with boxes of box_rows x box_cols:
 // box_cols = 16 uses the 64-byte swizzle, box_cols = 32 the 128-byte swizzle.
-int encode_map(cafe_ctx* C, CUtensorMap* m, const float* base, int64_t rows, int cols, int box_cols, int box_rows) {
+int encode_map(cafe_ctx* C, CUtensorMap* m, const float* base, int64_t rows, int cols, int box_cols, int box_rows,
+               int64_t depth_stride = 0) {
     static EncodeTiledFn enc = nullptr;
     if (!enc) {
         cudaDriverEntryPointQueryResult q;
@@ -639,13 +640,16 @@ int encode_map(cafe_ctx* C, CUtensorMap* m, const float* base, int64_t rows, int
             return fail(C, CAFE_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
         }
     }
-    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)cols * sizeof(float)};
+    // depth_stride > 0: a third dimension of 2 planes that many elements
+    // apart (one box holds the same rows of both)
+    cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, 2};
+    cuuint64_t strides[2] = {(cuuint64_t)cols * sizeof(float), (cuuint64_t)depth_stride * sizeof(float)};
     if (box_rows < 1 || box_rows > 256 || box_rows > rows) return fail(C, CAFE_ERR_INVALID, "tensor map box of %d rows", box_rows);
-    cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
-    cuuint32_t es[2] = {1, 1};
+    if (depth_stride < 0 || (depth_stride * sizeof(float)) % 16) return fail(C, CAFE_ERR_INVALID, "tensor map plane stride");
+    cuuint32_t box[3] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows, 2};
+    cuuint32_t es[3] = {1, 1, 1};
     const CUtensorMapSwizzle sw = box_cols == 16 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B;
-    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, es,
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, depth_stride > 0 ? 3 : 2, (void*)base, dims, strides, box, es,
                            CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(C, CAFE_ERR_CUDA, "tensor map encode failed (%d)", (int)r);
@@ -653,10 +657,11 @@ int encode_map(cafe_ctx* C, CUtensorMap* m, const float* base, int64_t rows, int
 }
 
 int cached_map(cafe_ctx* C, Workspace& ws, int slot, CUtensorMap* out, const float* base, int64_t rows, int cols,
-               int box_cols, int box_rows) {
+               int box_cols, int box_rows, int64_t depth_stride = 0) {
     Workspace::MapCache& mc = ws.map_cache[slot];
-    if (mc.ptr != base || mc.rows != rows || mc.cols != cols || mc.box != box_cols || mc.box_rows != box_rows) {
-        int rc = encode_map(C, &mc.map, base, rows, cols, box_cols, box_rows);
+    if (mc.ptr != base || mc.rows != rows || mc.cols != cols || mc.box != box_cols || mc.box_rows != box_rows ||
+        mc.depth != depth_stride) {
+        int rc = encode_map(C, &mc.map, base, rows, cols, box_cols, box_rows, depth_stride);
         if (rc) {
             mc.ptr = nullptr;
             return rc;
@@ -666,6 +671,7 @@ int cached_map(cafe_ctx* C, Workspace& ws, int slot, CUtensorMap* out, const flo
         mc.cols = cols;
         mc.box = box_cols;
         mc.box_rows = box_rows;
+        mc.depth = depth_stride;
     }
     *out = mc.map;
     return CAFE_OK;
@@ -1059,8 +1065,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
     };
     if (!tc_tiles.empty()) {
         const size_t fl = (size_t)n_mat * Wm * Wm;
-        CK(ws.tc_hi.reserve(fl * sizeof(float)), "tc matrices");
-        CK(ws.tc_lo.reserve(fl * sizeof(float)), "tc matrices");
+        CK(ws.tc_hi.reserve(2 * fl * sizeof(float)), "tc matrices");     // hi, then lo
         CK(ws.tc_tr.reserve(fl * sizeof(float)), "tc matrices");
         CK(ws.h_conv.reserve(jobs.size() * sizeof(ConvertJob)), "convert jobs");
         CK(ws.conv.reserve(jobs.size() * sizeof(ConvertJob)), "convert jobs");
@@ -1073,7 +1078,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         TcBuffers tb;
         std::memset(&tb, 0, sizeof tb);
         tb.hi = ws.tc_hi.as<float>();
-        tb.lo = ws.tc_lo.as<float>();
+        tb.lo = ws.tc_hi.as<float>() + fl;
         tb.tr = ws.tc_tr.as<float>();
         tb.Wm = Wm;
         if (prof) C->prof.begin(3, ws.stream, &ev);
@@ -1163,11 +1168,11 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         if (rc) return rc;
         auto launch_maps = [&](int Ws, TcMaps* m) {
             *m = maps;
-            const int q = 4 + 2 * (Ws / 32 - 1);      // Ws: a multiple of 32 up to 256
-            int r = cached_map(C, ws, q, &m->mat_hi, ws.tc_hi.as<float>(), (int64_t)n_mat * Wm, Wm, kbox, Ws);
-            if (!r) r = cached_map(C, ws, q + 1, &m->mat_lo, ws.tc_lo.as<float>(), (int64_t)n_mat * Wm, Wm, kbox, Ws);
+            const int q = 4 + (Ws / 32 - 1);      // Ws: a multiple of 32 up to 256
+            const int64_t fl = (int64_t)n_mat * Wm * Wm;
+            int r = cached_map(C, ws, q, &m->mat, ws.tc_hi.as<float>(), (int64_t)n_mat * Wm, Wm, kbox, Ws, fl);
             // leaf blocks: W x W (read only where W <= 64, one CTA per tile)
-            if (!r) r = cached_map(C, ws, 20 + (Ws / 32 - 1), &m->tr, ws.tc_tr.as<float>(), (int64_t)n_mat * Wm, Wm, 32, Ws);
+            if (!r) r = cached_map(C, ws, 12 + (Ws / 32 - 1), &m->tr, ws.tc_tr.as<float>(), (int64_t)n_mat * Wm, Wm, 32, Ws);
             return r;
         };
         const int n_tc = (int)tc_tiles.size();

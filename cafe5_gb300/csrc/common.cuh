@@ -184,14 +184,15 @@ struct PruneTcArgs {
 };
 
 // Tensor maps travel by value (__grid_constant__); the host encodes them.
-// Operand loads use prune_tc_kchunk()-column boxes (mat_*, vec; 128-byte
+// Operand loads use prune_tc_kchunk()-column boxes (mat, vec; 128-byte
 // swizzle for 32 columns, 64-byte for 16); the epilogue stores node vectors
 // in 32-column boxes in the 128-byte swizzle (vst). Vector boxes are one
-// tile's 128 rows; matrix boxes are the launch's Ws rows. tr: the FP32
-// transposed matrices in boxes of 32 columns x the launch's W rows (leaf
-// blocks of bins up to 64 states).
+// tile's 128 rows. mat is 3D: the TF32 hi and lo matrices, one buffer
+// [2][n_mat Wm][Wm], in boxes of the launch's Ws rows x both halves. tr:
+// the FP32 transposed matrices in boxes of 32 columns x the launch's W
+// rows (leaf blocks of bins up to 64 states).
 struct TcMaps {
-    CUtensorMap mat_hi, mat_lo, vec, vst, tr;
+    CUtensorMap mat, vec, vst, tr;
 };
 
 cudaError_t launch_prune_tc(const TcMaps& maps, const PruneTcArgs& a, int n_ctas, size_t smem, cudaStream_t s);

@@ -602,9 +602,9 @@ __device__ __forceinline__ void split_row_tf32(float* hi, float* lo, int row) {
 // all. Every handshake wait is bounded.
 template <int NSPLIT>
 __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
-    k_prune_tc(const __grid_constant__ CUtensorMap map_mhi, const __grid_constant__ CUtensorMap map_mlo,
-               const __grid_constant__ CUtensorMap map_vec, const __grid_constant__ CUtensorMap map_vst,
-               const __grid_constant__ CUtensorMap map_tr, const PruneTcArgs a) {
+    k_prune_tc(const __grid_constant__ CUtensorMap map_mat, const __grid_constant__ CUtensorMap map_vec,
+               const __grid_constant__ CUtensorMap map_vst, const __grid_constant__ CUtensorMap map_tr,
+               const PruneTcArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     __shared__ __align__(8) uint64_t bar_full[MAXST], bar_empty[MAXST], bar_done, bar_drain, bar_leaf;
@@ -835,7 +835,8 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                         float* Ahi = reinterpret_cast<float*>(base);
                         float* Alo = Ahi + TM * KC;
                         float* Bhi = Alo + TM * KC;
-                        float* Blo = Bhi + a.Ws * KC;
+                        float* Blo = Bhi + a.Ws * KC;   // (the matrix box lands hi, then lo)
+                        (void)Blo;
                         // the first NS chunks of a node find their stages free: the
                         // previous node's MMAs completed before its epilogue and its
                         // staging-tile stores were waited for at the node start
@@ -855,8 +856,7 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                             const int vrow = (int)(vrow_cta + (int64_t)chi.slot * TM);
                             tc::tma_load_2d(Ahi, &map_vec, kc * KC, vrow, &bar_full[st]);
                             const int mrow = chi.mat * Wm + s_off;     // this CTA's output states
-                            tc::tma_load_2d(Bhi, &map_mhi, kc * KC, mrow, &bar_full[st]);
-                            tc::tma_load_2d(Blo, &map_mlo, kc * KC, mrow, &bar_full[st]);
+                            tc::tma_load_3d(Bhi, &map_mat, kc * KC, mrow, 0, &bar_full[st]);   // hi, then lo at Blo
                             last_full[st] = 1;
                             last_full_parity[st] = u & 1;
                         }
@@ -864,6 +864,9 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                         if (i == 0) {
                             const long long tg = timing ? clock64() : 0;
                             gather_leaves();
+                            // the leaf block lies in chunk 0's lo operand area, which
+                            // chunk 0's split overwrites: every thread's reads first
+                            if (leaf_tma) __syncthreads();
                             if (timing) ph[13] += clock64() - tg;
                         }
                     }
@@ -878,12 +881,11 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                         const long long tf = timing ? clock64() : 0;
                         const bool ok = abort_sh || tc::mbar_wait(&bar_full[st], (cg / (uint32_t)NS) & 1);
                         const long long tf1 = timing ? clock64() : 0;
-                        const bool fail = __syncthreads_or(!ok);
-                        if (fail) {
-                            if (tid == 0) {
-                                atomicExch(a.status, 1);
-                                abort_sh = 1;
-                            }
+                        // (a thread whose wait gave up stops the CTA: the MMAs are
+                        // issued only if no thread did, which the barrier shows)
+                        if (!ok) {
+                            atomicExch(a.status, 1);
+                            abort_sh = 1;
                         } else if (!abort_sh) {
                             split_row_tf32(Ahi, Ahi + TM * KC, tid);
                             tc::fence_proxy_async_shared();
@@ -1355,7 +1357,7 @@ cudaError_t launch_prune_tc(const TcMaps& m, const PruneTcArgs& a, int n_ctas, s
     if (smem > (size_t)prune_tc_max_smem(a.nsplit)) return cudaErrorInvalidValue;
     if (a.stages < 1 || a.stages > MAXST) return cudaErrorInvalidValue;
     if (a.nsplit == 1) {
-        k_prune_tc<1><<<n_ctas, NTHREADS, smem, s>>>(m.mat_hi, m.mat_lo, m.vec, m.vst, m.tr, a);
+        k_prune_tc<1><<<n_ctas, NTHREADS, smem, s>>>(m.mat, m.vec, m.vst, m.tr, a);
         return cudaGetLastError();
     }
     // a cluster of nsplit CTAs per tile, each with Ws = W / nsplit output
@@ -1376,8 +1378,8 @@ cudaError_t launch_prune_tc(const TcMaps& m, const PruneTcArgs& a, int n_ctas, s
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    if (a.nsplit == 2) return cudaLaunchKernelEx(&cfg, k_prune_tc<2>, m.mat_hi, m.mat_lo, m.vec, m.vst, m.tr, a);
-    return cudaLaunchKernelEx(&cfg, k_prune_tc<4>, m.mat_hi, m.mat_lo, m.vec, m.vst, m.tr, a);
+    if (a.nsplit == 2) return cudaLaunchKernelEx(&cfg, k_prune_tc<2>, m.mat, m.vec, m.vst, m.tr, a);
+    return cudaLaunchKernelEx(&cfg, k_prune_tc<4>, m.mat, m.vec, m.vst, m.tr, a);
 }
 
 }  // namespace cafe

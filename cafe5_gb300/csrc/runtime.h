@@ -157,13 +157,14 @@ struct Workspace {
         int cols = 0;
         int box = 0;
         int box_rows = 0;
+        int64_t depth = 0;
         CUtensorMap map;
-    } map_cache[28];   // [2] vector loads, [3] vector stores, [4 + 2 (Ws/32 - 1) + {0, 1}] matrix hi / lo,
-                       // [20 + Ws/32 - 1] transposed matrices
+    } map_cache[20];   // [2] vector loads, [3] vector stores, [4 + Ws/32 - 1] matrices (hi and lo planes),
+                       // [12 + Ws/32 - 1] transposed matrices
     DevBuf scratch, tiles, mats, cat, fam_lnl, total, nfail, jobs, catp;
     PinnedBuf h_tiles, h_mats, h_jobs, h_out, h_catp;
     // tensor-core path
-    DevBuf tc_hi, tc_lo, tc_tr, tc_mi, tc_vec, conv, flags, fb_perm, tiles64, tiles_fb, parts, fb_count, phase,
+    DevBuf tc_hi, tc_tr, tc_mi, tc_vec, conv, flags, fb_perm, tiles64, tiles_fb, parts, fb_count, phase,
         catids, cerr;
     PinnedBuf h_conv, h_mi, h_flags, h_tiles64, h_tiles_fb, h_tail, h_catids;
     // FP64 bins walked one family per cluster

@@ -44,6 +44,15 @@ CAFE_DEV void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint6
         "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
         : "memory");
 }
+// 3D TMA tile load (box given by the tensor map) into shared memory,
+// completion counted in bytes on `bar`.
+CAFE_DEV void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+            smem_u32(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
 // 2D TMA tile store from shared memory (bulk-group completion).
 CAFE_DEV void tma_store_2d(const CUtensorMap* map, int x, int y, const void* src) {
     asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"((uint64_t)map),
