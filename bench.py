@@ -600,7 +600,7 @@ def config2_phase(ctx, torch, stream, flush, steps: int = 4, B: int = 4):
             "profiled_call_ms": {k: round(v, 3) for k, v in prof.items()
                                  if k in ("matrix_ms", "prune_ms", "other_ms", "finish_ms")},
             "note": "profiled_call_ms: one direct (unreplayed) call with per-launch events: prune_ms = "
-                    "tensor-core bins, other_ms = TF32 conversion + FP64 cluster walk of the bins above 256"}
+                    "tensor-core bins (384 and 512 in CTA pairs), other_ms = TF32 conversion"}
 
 
 def config0_phase(ctx, cpu_seconds: float, reps: int = 10):

@@ -1595,9 +1595,9 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     if (C->prof.on) C->prof.acc.host_keys_ms += host_ms_since(t_keys);
     CK(ws.cat.reserve((size_t)std::max<int64_t>(F, 1) * CT * sizeof(double)), "category buffer");
     if (R->precision == CAFE_PREC_MIXED_TF32X3) {
-        // saturated keys (1 - 2a < 0) and polytomies stay on the FP64 path
-        // polytomies stay on the FP64 path; saturated keys run on the tensor
-        // cores (a family that is exactly zero through one ends there)
+        // polytomies stay on the FP64 path; saturated keys (1 - 2a < 0) run
+        // on the tensor cores (a family that is exactly zero through one ends
+        // there)
         const bool to_fp64 = T.max_children > 2;
         (void)any_saturated;
         if (!to_fp64) {

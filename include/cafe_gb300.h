@@ -50,9 +50,10 @@ typedef enum { CAFE_LAMBDA_SINGLE = 0, CAFE_LAMBDA_MULTIPLE = 1 } cafe_lambda_ki
  *   MIXED_TF32X3 per-family S bins on the tensor cores (tcgen05, kind::tf32):
  *                each operand is split into two TF32 parts (hi, lo), products
  *                hi*hi + hi*lo + lo*hi accumulate in FP32, node vectors carry
- *                integer power-of-two exponents; bins wider than 256 states,
- *                saturated categories and families whose factors lose range
- *                are computed in FP64_BINNED */
+ *                integer power-of-two exponents; bins wider than 512 states,
+ *                trees with a node of more than two children, and families
+ *                whose factors lose FP32 range (a per-family error bound) are
+ *                computed in FP64_BINNED */
 typedef enum {
     CAFE_PREC_FP64_REF = 0,
     CAFE_PREC_FP64_BINNED = 1,
