@@ -976,6 +976,7 @@ def run_ours(args):
     roof["other_ms_per_step"] = prof["other_ms"] / prof_steps
     roof["finish_ms_per_step"] = prof["finish_ms"] / prof_steps
     roof["host_enqueue_ms_per_step"] = prof["host_total_ms"] / prof_steps
+    roof["host_ms_per_step"] = {k: prof[k] / prof_steps for k in ("host_keys_ms", "host_build_ms", "host_plan_ms")}
 
     base = None
     if rank == 0 and world == 1 and args.cpu_seconds > 0:

@@ -7,31 +7,38 @@
 // mapped onto tcgen05:
 //
 //  * One CTA (4 warps) owns a tile of 128 families of one gamma category and
-//    one S-bin of width W (<= 256) and walks the tree in post-order.
+//    one S-bin of width W and walks the tree in post-order (bins of 384 and
+//    512 states, and sparse bins of 128 to 256, share a tile among a
+//    cluster of 2 or 4 CTAs, each computing a slice of the output states).
 //  * Internal child c: D[f][s] = sum_j L_c[f][j] M_c[s][j] is one
 //    M=128 x N=W x K=W GEMM: A = node vectors (128 families x W states,
 //    K-major), B = the transition matrix (W x W, K-major: row s, column j).
 //    Operands are FP32 pairs hi + lo, each rounded to TF32, and
 //    D = A_hi B_hi + A_hi B_lo + A_lo B_hi (the lo*lo term is below the
-//    TF32x3 error). Tiles of 32 K-columns (one 128-byte swizzle row) are
-//    staged by TMA into two shared-memory stages; one thread issues TMA and
-//    tcgen05.mma; the accumulators of up to two children sit side by side in
-//    TMEM.
+//    TF32x3 error). K chunks of 32 columns (one 128-byte swizzle row) are
+//    staged by TMA in 1 to 4 shared-memory stages, one box per operand: the
+//    node vector arrives in FP32 and every thread splits its own row into
+//    hi (in place) and lo; the matrix's hi and lo planes arrive in one 3D
+//    box. One thread issues TMA and tcgen05.mma; the accumulators of the
+//    two children sit side by side in TMEM.
 //  * Leaf child: its factor is the matrix column of the observed count (or
 //    the error model's weighted sum of three columns): each thread reads its
 //    family's column as a row of the transposed FP32 matrix and writes it
-//    into the child's TMEM columns (tcgen05.st), while the node's first
-//    operand chunk is in flight; a node whose children are both leaves runs
-//    no GEMM. Every child's factor then sits in TMEM and the epilogue reads
-//    no global memory.
+//    into the child's TMEM columns (tcgen05.st). Bins up to 64 states read
+//    the rows from a W x W block of the transpose that one TMA load puts in
+//    shared memory beside the node's first operand chunk; wider bins read
+//    them from global memory. A node whose children are both leaves runs no
+//    GEMM. Every child's factor then sits in TMEM and the epilogue reads no
+//    global memory.
 //  * Epilogue (thread f owns family f = TMEM lane f): the product over
 //    children is rescaled by the largest per-state sum of the factors'
 //    binary exponents, so the product's maximum is ~1 and nothing
 //    underflows unless the factors are >2^250 apart; the exponent goes into
-//    the family's integer exponent. The node vector is stored as TF32 hi/lo
-//    for the parent's GEMM. At the root the vector is weighted by the prior
-//    in FP64 (root index j = state j + 1) and the category term's natural
-//    log is written.
+//    the family's integer exponent. The node vector is stored in FP32 for
+//    the parent's GEMM (bins up to 64 states: one pass over TMEM stages the
+//    product and its statistics together). At the root the vector is
+//    weighted by the prior in FP64 (root index j = state j + 1) and the
+//    category term's natural log is written.
 //  * A family whose factors are too far apart, or whose root vector is all
 //    zero, is flagged; the host recomputes flagged families in FP64.
 //  * FP32 range: a factor value below 2^-126 is flushed (or denormal) where
