@@ -559,9 +559,9 @@ def config2_phase(ctx, torch, stream, flush, steps: int = 4, B: int = 4):
     """The two-lambda local model with the error model: a 32-taxon tree whose
     10-taxon clade runs at lambda2, epsilon 0.05, 50,000 families from a
     heavy-tailed root (95 % Poisson(4), 5 % geometric(0.02); S-bins 32 to
-    512). Every bin goes into one request: bins up to 256 states on the
-    tensor cores, the sparse wider bins on the FP64 cluster walk, replayed as
-    one CUDA graph. B candidate (lambda1, lambda2) vectors per step; device
+    512). Every bin goes into one request on the tensor cores (bins of 384
+    and 512 states in CTA pairs), replayed as one CUDA graph. B candidate
+    (lambda1, lambda2) vectors per step; device
     time per step, the FP64 path at the same bins, and the largest
     per-family dlnL against it."""
     from cafe5_gb300.families import bin_families
@@ -596,7 +596,7 @@ def config2_phase(ctx, torch, stream, flush, steps: int = 4, B: int = 4):
         per.append(float(np.max(np.abs(c.family_lnl[fin] - r.family_lnl[fin]) / np.abs(r.family_lnl[fin]))))
     ctx.profile(True)
     ctx.profile_read()
-    ctx.score_batch(tid, sid, candidates(w, B, 43000), **kw)     # new candidates: matrices built
+    ctx.score_batch(tid, sid, make(w, B, 23000), **kw)     # new candidates: matrices built
     prof = ctx.profile_read()
     ctx.profile(False)
     ctx.free_families(sid)
