@@ -1023,6 +1023,10 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
     int32_t* d_flags = ws.flags.as<int32_t>();
     int32_t* d_status = d_flags + std::max<int64_t>(F, 1);
     CK(op_memset(ws, ws.flags.p, 0, (size_t)std::max<int64_t>(F, 1) * sizeof(int32_t) + 64, ws.stream), "flags");
+    // which category terms the FP64 pass recomputes, [F][K]
+    CK(ws.term_flags.reserve((size_t)std::max<int64_t>(F, 1) * K), "term flags");
+    uint8_t* d_term = ws.term_flags.as<uint8_t>();
+    CK(op_memset(ws, ws.term_flags.p, 0, (size_t)std::max<int64_t>(F, 1) * K, ws.stream), "term flags");
 
     // tiles: 128 families (tensor cores) or 32 families (FP64, wide bins)
     // grouped by bin (bins ascend in width), so each bin's tiles are contiguous
@@ -1201,6 +1205,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         a.model = gamma ? 1 : 0;
         a.cat_probs = ws.catp.as<double>();
         a.flags = d_flags;
+        a.term_flags = d_term;
         a.status = d_status;
         a.debug_wait_limit = C->debug_wait_limit;
         // range-error bounds of the category terms: zero for every term the
@@ -1293,11 +1298,45 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         rf.KC = KC;
         rf.tau = kRangeTau;
         rf.flags = d_flags;
+        rf.term_flags = d_term;
         rf.any_flag = d_status + 3;
         CK(op_launch(ws, 9, [&] { return launch_range_flags(rf, ws.stream); }, rf, ws.stream), "range flags");
+        static const bool flag_env = getenv("CAFE_DEBUG_FLAGS") != nullptr;
+        if (flag_env && op_issue(ws)) {
+            // diagnostics: which families the FP64 pass will recompute, and why
+            // (bit 1: the tensor-core walk could not represent a category term;
+            // bit 2: the weighted FP32 range bound), and which category terms
+            // the walk left unwritten
+            std::vector<int32_t> hf((size_t)F);
+            std::vector<double> hc((size_t)F * K);
+            CK(cudaMemcpyAsync(hf.data(), d_flags, (size_t)F * sizeof(int32_t), cudaMemcpyDeviceToHost, ws.stream), "flags");
+            CK(cudaMemcpyAsync(hc.data(), ws.cat.p, (size_t)F * K * sizeof(double), cudaMemcpyDeviceToHost, ws.stream), "flags");
+            CK(cudaStreamSynchronize(ws.stream), "flags");
+            int64_t n1 = 0, n2 = 0, n12 = 0, terms = 0;
+            std::vector<int64_t> by_cat((size_t)KC, 0);
+            for (int64_t f = 0; f < F; ++f) {
+                const int v = hf[(size_t)f];
+                n1 += (v & 1) != 0;
+                n2 += (v & 2) != 0;
+                n12 += (v & 3) == 3;
+                if (v & 1)
+                    for (int k = 0; k < K; ++k)
+                        if (std::isnan(hc[(size_t)f * K + k])) {
+                            terms++;
+                            by_cat[(size_t)(k % KC)]++;
+                        }
+            }
+            fprintf(stderr, "flags: %lld families (walk %lld, range %lld, both %lld); unwritten terms %lld of %lld; by category:",
+                    (long long)(n1 + n2 - n12), (long long)n1, (long long)n2, (long long)n12, (long long)terms,
+                    (long long)(F * K));
+            for (int k = 0; k < KC; ++k) fprintf(stderr, " %lld", (long long)by_cat[(size_t)k]);
+            fprintf(stderr, "\n");
+        }
         FallbackPlanArgs fp;
         std::memset(&fp, 0, sizeof fp);
         fp.flags = d_flags;
+        fp.term_flags = d_term;
+        fp.K = K;
         fp.perm = B.d_perm.as<int64_t>();
         fp.n_bins = 0;
         for (size_t b = 0; b < B.widths.size() && fp.n_bins < 16; ++b) {
@@ -1312,7 +1351,9 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         const int64_t max_tiles = (int64_t)active.size() * (F / 32 + fp.n_bins + 1);
         CK(ws.fb_perm.reserve((size_t)std::max<int64_t>(F, 1) * sizeof(int64_t)), "fallback");
         CK(ws.tiles_fb.reserve((size_t)max_tiles * sizeof(PruneTile)), "fallback");
+        CK(ws.fb_bins.reserve(32 * sizeof(int64_t)), "fallback");
         fp.fb_perm = ws.fb_perm.as<int64_t>();
+        fp.fb_bins = ws.fb_bins.as<int64_t>();
         fp.fb_tiles = ws.tiles_fb.as<PruneTile>();
         fp.out_counts = d_status + 1;     // [families, tiles]
         fp.any_flag = d_status + 3;
@@ -1347,6 +1388,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         a.cat_probs = ws.catp.as<double>();
         a.tile_families = 32;
         a.W = msize;
+        a.term_mask = d_term;     // only the flagged terms of each tile are written
         if (prof) C->prof.begin(3, ws.stream, &ev);
         CK(op_launch(ws, 7, [&] { return launch_prune64(a, n_ctas, ws.stream); }, a, n_ctas, ws.stream),
            "fallback prune");
@@ -1366,7 +1408,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
 int enqueue_mixed_graph(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T, FamSet& S, int K, int CT,
                         const std::vector<int32_t>& active, double** hm, double* d_fam, double* d_total,
                         ScoreInfo* info) {
-    static const bool phase_env = getenv("CAFE_TC_PHASES") != nullptr;
+    static const bool phase_env = getenv("CAFE_TC_PHASES") != nullptr || getenv("CAFE_DEBUG_FLAGS") != nullptr;
     ws.oplog.clear();
     if (C->prof.on || phase_env) {
         ws.op_mode = Workspace::kOpRun;

@@ -91,6 +91,7 @@ struct Prune64Args {
     int tile_families;           // families per tile (<= 32)
     int W;                       // max vector length over tiles (S + 1 or R)
     const int32_t* n_tiles_dev;  // optional: tile count read from device memory
+    const uint8_t* term_mask;    // optional [F][K]: only the terms set here are written
     double* root_out;            // optional (unscaled runs): root vector of every family,
                                  // root_out[f * root_ld + j] = L(root size root_lo + j); no reduction
     int root_ld;
@@ -167,6 +168,7 @@ struct PruneTcArgs {
     int model;                   // 0 base (a zero family is -inf), 1 gamma (a zero family is NaN: failed)
     const double* cat_probs;
     int32_t* flags;              // [F] set when a family must be recomputed in FP64
+    uint8_t* term_flags;         // [F][K] set with it for the category term that needs the recompute
     float* out_err;              // [F][K] bound on the relative error of each category term from FP32
                                  // range loss (values below 2^-126 flushed), or null
     int32_t* status;             // [1] nonzero when a bounded wait gave up
@@ -252,6 +254,8 @@ struct RangeFlagArgs {
     int KC;                      // categories per candidate
     double tau;
     int32_t* flags;              // [F]
+    uint8_t* term_flags;         // [F][K]: the terms of a flagged family whose share of the bound is over
+                                 // tau / (2 KC), which the FP64 pass recomputes (the rest stay under tau / 2)
     int32_t* any_flag;           // set to 1 when a family is flagged
 };
 cudaError_t launch_range_flags(const RangeFlagArgs& a, cudaStream_t s);
@@ -259,12 +263,16 @@ size_t prune_tc_smem_bytes(int Ws, int n_slots, int stages, int n_internal);
 int prune_tc_kchunk();   // K columns per operand box of k_prune_tc (its load maps' box width)
 int prune_tc_max_smem(int nsplit = 1);   // dynamic shared memory one k_prune_tc CTA may use (per split)
 
-// Device-side plan of the FP64 recompute of flagged families: compacts the
-// flagged families of each listed bin (in permutation order) into fb_perm
-// and writes 32-family tiles for every listed category; out_counts[0] = families,
-// out_counts[1] = tiles.
+// Device-side plan of the FP64 recompute of flagged category terms:
+// k_fallback_plan compacts the flagged families of each listed bin (in
+// permutation order) into fb_perm; k_fallback_tiles then writes a 32-family
+// tile for every (chunk of 32 compacted families, listed category) in which
+// some family has that term flagged (tile order is immaterial: each tile
+// writes its own terms). out_counts[0] = families, out_counts[1] = tiles.
 struct FallbackPlanArgs {
     const int32_t* flags;        // [F]
+    const uint8_t* term_flags;   // [F][K]
+    int K;                       // combined (candidate, category) indices
     const int64_t* perm;         // [F] bin order
     int n_bins;
     int bin_width[16];
@@ -273,6 +281,7 @@ struct FallbackPlanArgs {
     const int32_t* cats;         // [n_cats] category indices to recompute
     int n_cats;
     int64_t* fb_perm;            // [F]
+    int64_t* fb_bins;            // [2 * 16]: start and count of each bin's families in fb_perm
     PruneTile* fb_tiles;         // [n_cats * (F / 32 + n_bins + 1)]
     int32_t* out_counts;         // [2]
     const int32_t* any_flag;     // optional: zero means no family is flagged

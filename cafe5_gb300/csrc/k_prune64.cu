@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(NT) k_prune64(Prune64Args a) {
             }
             red[warp][lane] = any ? best : NAN;
             __syncthreads();
-            if (warp == 0 && f >= 0) {
+            if (warp == 0 && f >= 0 && (!a.term_mask || a.term_mask[(size_t)f * a.K + k])) {
                 double b = -INFINITY;
                 bool got = false;
                 for (int w = 0; w < NT / 32; ++w) {
@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(NT) k_prune64(Prune64Args a) {
             red[warp][lane] = mx;
             redi[warp][lane] = nz;
             __syncthreads();
-            if (warp == 0 && f >= 0) {
+            if (warp == 0 && f >= 0 && (!a.term_mask || a.term_mask[(size_t)f * a.K + k])) {
                 double m = 0.0;
                 int z = 0;
                 for (int w = 0; w < NT / 32; ++w) {

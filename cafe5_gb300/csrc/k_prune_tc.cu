@@ -1139,6 +1139,7 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
         }
         if (flag && fam >= 0 && h == 0) {
             atomicOr(&a.flags[fam], 1);
+            if (a.term_flags) a.term_flags[(size_t)fam * a.K + k] = 1;   // this category term
             atomicOr(a.status + 3, 1);     // "some family is flagged"
         }
         __syncthreads();
@@ -1199,11 +1200,11 @@ __global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict
 }
 
 // One block: flagged families of each bin, compacted in permutation order
-// (a block-wide prefix sum per 256-family chunk), then tiles bin by bin.
+// (a block-wide prefix sum per 256-family chunk); each bin's range of
+// fb_perm goes to fb_bins for k_fallback_tiles.
 __global__ void __launch_bounds__(256) k_fallback_plan(FallbackPlanArgs a) {
     __shared__ int scan[256];
     __shared__ int64_t base_sh;
-    __shared__ int n_tiles_sh;
     if (a.any_flag && *a.any_flag == 0) {     // nothing flagged: no work
         if (threadIdx.x == 0) {
             a.out_counts[0] = 0;
@@ -1211,10 +1212,7 @@ __global__ void __launch_bounds__(256) k_fallback_plan(FallbackPlanArgs a) {
         }
         return;
     }
-    if (threadIdx.x == 0) {
-        base_sh = 0;
-        n_tiles_sh = 0;
-    }
+    if (threadIdx.x == 0) base_sh = 0;
     __syncthreads();
     for (int b = 0; b < a.n_bins; ++b) {
         const int64_t start = base_sh;
@@ -1241,25 +1239,42 @@ __global__ void __launch_bounds__(256) k_fallback_plan(FallbackPlanArgs a) {
             __syncthreads();
         }
         if (threadIdx.x == 0) {
-            const int64_t cnt = base_sh - start;
-            for (int q = 0; q < a.n_cats; ++q)
-                for (int64_t i = 0; i < cnt; i += 32) {
-                    const int k = a.cats[q];
-                    PruneTile t;
-                    t.first = (int)(start + i);
-                    t.count = (int)(cnt - i < 32 ? cnt - i : 32);
-                    t.k = k;
-                    t.S = a.bin_width[b] - 1;
-                    t.R = a.bin_width[b] - 1;
-                    t.root_lo = t.pad[0] = t.pad[1] = 0;
-                    a.fb_tiles[n_tiles_sh++] = t;
-                }
+            a.fb_bins[2 * b] = start;
+            a.fb_bins[2 * b + 1] = base_sh - start;
         }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
         a.out_counts[0] = (int32_t)base_sh;
-        a.out_counts[1] = n_tiles_sh;
+        a.out_counts[1] = 0;      // k_fallback_tiles counts the tiles
+    }
+}
+
+// A tile for every (32-family chunk of a bin's compacted families, listed
+// category) in which some family has that term flagged: one warp per chunk,
+// one block per category in turn. Tiles are appended in any order.
+__global__ void __launch_bounds__(256) k_fallback_tiles(FallbackPlanArgs a) {
+    if (a.any_flag && *a.any_flag == 0) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int q = blockIdx.x; q < a.n_cats; q += gridDim.x) {
+        const int k = a.cats[q];
+        for (int b = 0; b < a.n_bins; ++b) {
+            const int64_t start = a.fb_bins[2 * b], cnt = a.fb_bins[2 * b + 1];
+            for (int64_t c0 = (int64_t)warp * 32; c0 < cnt; c0 += 8 * 32) {
+                const int64_t i = c0 + lane;
+                const bool need = i < cnt && a.term_flags[(size_t)a.fb_perm[start + i] * a.K + k] != 0;
+                if (__any_sync(0xffffffffu, need) && lane == 0) {
+                    PruneTile t;
+                    t.first = (int)(start + c0);
+                    t.count = (int)(cnt - c0 < 32 ? cnt - c0 : 32);
+                    t.k = k;
+                    t.S = a.bin_width[b] - 1;
+                    t.R = a.bin_width[b] - 1;
+                    t.root_lo = t.pad[0] = t.pad[1] = 0;
+                    a.fb_tiles[atomicAdd(&a.out_counts[1], 1)] = t;
+                }
+            }
+        }
     }
 }
 
@@ -1287,10 +1302,28 @@ __global__ void __launch_bounds__(256) k_range_flags(RangeFlagArgs a) {
             w += x;
             we += x * (double)e[k];
         }
+        uint8_t* tf = a.term_flags + (size_t)f * a.K + (size_t)b * a.KC;
+        // a term the walk left to the FP64 pass carries no weight here, so the
+        // others' shares are unknown: every term of the candidate is recomputed
+        bool walk = false;
+        for (int k = 0; k < a.KC; ++k) walk |= tf[k] != 0;
+        if (walk) {
+            for (int k = 0; k < a.KC; ++k) tf[k] = 1;
+            continue;      // (the family is flagged already)
+        }
         if (!(we != 0.0)) continue;      // no range loss in any term (or a candidate that was not pruned)
         const double lnl = m + log(w);
         const double bound = we / w;
-        if (!(bound <= a.tau * fabs(lnl))) {
+        const double lim = a.tau * fabs(lnl);
+        if (!(bound <= lim)) {
+            // recompute the terms whose share of the bound is over lim / (2 KC):
+            // the others' shares add up to at most lim / 2
+            const double each = lim * w / (2.0 * a.KC);
+            for (int k = 0; k < a.KC; ++k) {
+                const bool fin = isfinite(c[k]);
+                const double share = fin ? exp(c[k] - m) * (double)e[k] : 0.0;
+                if (!(share <= each) || !(lim > 0.0)) tf[k] = 1;
+            }
             atomicOr(&a.flags[f], 2);
             atomicOr(a.any_flag, 1);
         }
@@ -1320,6 +1353,9 @@ cudaError_t tc_kernels_init() {
 
 cudaError_t launch_fallback_plan(const FallbackPlanArgs& a, cudaStream_t s) {
     k_fallback_plan<<<1, 256, 0, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || a.n_cats <= 0) return e;
+    k_fallback_tiles<<<a.n_cats < 1024 ? a.n_cats : 1024, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
