@@ -509,11 +509,15 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
         CK(cudaEventSynchronize(ws.ev_jobs), "jobs");
         ws.jobs_pending = false;
     }
-    // bump allocation from large slabs (no cudaMalloc per evaluation)
+    // bump allocation from large slabs (no cudaMalloc per evaluation); each
+    // new slab is twice the last, up to 4 GB, so a long search allocates
+    // rarely (an allocation costs ~0.3 ms of host time) while a small
+    // workload keeps a small footprint
     const size_t need = (total + 255) & ~(size_t)255;
     if (C->slabs.empty() || C->slabs.back().used + need > C->slabs.back().size) {
         Slab sl;
-        sl.size = std::max(need, (size_t)256 << 20);
+        const size_t grown = C->slabs.empty() ? ((size_t)256 << 20) : std::min(2 * C->slabs.back().size, (size_t)4 << 30);
+        sl.size = std::max(need, grown);
         // stream-ordered when a request is being enqueued: requests on other
         // streams reach these matrices only through the build's ready event
         CK(t_alloc_stream ? cudaMallocAsync(&sl.p, sl.size, t_alloc_stream) : cudaMalloc(&sl.p, sl.size),
