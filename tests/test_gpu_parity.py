@@ -431,6 +431,28 @@ def test_mixed_results_do_not_depend_on_batch_composition(ctx):
     assert np.array_equal(d.family_lnl, b.family_lnl[:300])
 
 
+def test_mixed_term_recompute_is_per_family_and_exact(ctx):
+    """Config-3 families (48 taxa, K = 8): the smallest categories' nearly
+    diagonal matrices push some families' FP32 range bound over budget, and
+    the FP64 pass recomputes only the flagged (family, category) terms,
+    sharing 32-family tiles with families whose terms it must not write.
+    Every family's result is the same bits in a batch of 2,000 and in
+    subsets that change which families share its tiles, and within 1e-6 of
+    the rescaled oracle."""
+    from cafe5_gb300.synth import workload
+    w = workload(3, n_families=2000, seed=0)
+    lam = [0.001]
+    a, b = _both(ctx, w.tree, w.families.counts, lam, model=1, mult=w.multipliers, probs=w.cat_probs)
+    assert b.n_fallback > 0, "no family was flagged: the case does not reach the per-term recompute"
+    rng = np.random.default_rng(5)
+    for take in (np.arange(0, 2000, 3), np.sort(rng.choice(2000, 400, replace=False))):
+        c, d = _both(ctx, w.tree, w.families.counts[take], lam, model=1, mult=w.multipliers, probs=w.cat_probs)
+        assert np.array_equal(d.family_lnl, b.family_lnl[take])
+        assert np.array_equal(d.category_lnl, b.category_lnl[take])
+    _check_vs_oracle(b, *_scaled_oracle_binned(w.tree, w.families.counts, lam, model=1, mult=w.multipliers,
+                                               probs=w.cat_probs))
+
+
 @pytest.mark.parametrize("wl,model", [(2, 0), (0, 1)], ids=["two_lambda_error_model", "gamma_k4"])
 def test_sparse_fp64_bins_walk_one_family_per_cluster(ctx, wl, model):
     """FP64 bins too sparse to fill the GPU with 32-family tiles are walked
