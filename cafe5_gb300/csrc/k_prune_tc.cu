@@ -841,9 +841,7 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                         uint8_t* base = smem + st * sbytes;
                         float* Ahi = reinterpret_cast<float*>(base);
                         float* Alo = Ahi + TM * KC;
-                        float* Bhi = Alo + TM * KC;
-                        float* Blo = Bhi + a.Ws * KC;   // (the matrix box lands hi, then lo)
-                        (void)Blo;
+                        float* Bhi = Alo + TM * KC;     // the matrix box lands hi, then lo (Bhi + Ws KC)
                         // the first NS chunks of a node find their stages free: the
                         // previous node's MMAs completed before its epilogue and its
                         // staging-tile stores were waited for at the node start
