@@ -462,10 +462,10 @@ __device__ __noinline__ int epi_maxexp(const NodeSrc<NC> ns, int W, int s_off, i
 
 // Columns c32 .. c32 + SC - 1 of this thread's row of the scaled product
 // into a staging tile in the 128-byte-swizzled layout (warp-collective:
-// TMEM loads).
+// TMEM loads; a thread with write = false loads but writes nothing).
 template <int NC>
 __device__ __forceinline__ void epi_fill_chunk(const NodeSrc<NC>& ns, int c32, const float (&scl)[NC], float* tile,
-                                               int tid) {
+                                               int tid, bool write = true) {
     uint8_t* row = reinterpret_cast<uint8_t*>(tile) + (size_t)(tid >> 3) * 1024 + (size_t)(tid & 7) * 128;
     for (int col0 = c32; col0 < c32 + SC; col0 += CW) {
         uint32_t r[NC][CW];
@@ -477,6 +477,7 @@ __device__ __forceinline__ void epi_fill_chunk(const NodeSrc<NC>& ns, int c32, c
         for (int c = 0; c < NC; ++c)
 #pragma unroll
             for (int j = 0; j < CW; ++j) p[j] *= __uint_as_float(r[c][j]) * scl[c];
+        if (!write) continue;
 #pragma unroll
         for (int q = 0; q < CW / 4; ++q) {
             const int j = ((col0 - c32) >> 2) + q;          // 16-byte piece of the 128-byte row
@@ -1080,13 +1081,17 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
             if (!is_root) {
                 float flush = kTiny;   // values flushed on the store, in the stored vector's units
                 if (fused) {
-                    // a warp with a family on the exact path writes its rows again
-                    // with the factors scaled before the product; otherwise a
-                    // family brought back to [0.5, 1) is scaled in place, where a
-                    // value below 2^-126 before the scaling was flushed
+                    // a family on the exact path writes its row again with the
+                    // factors scaled before the product (the TMEM loads are
+                    // warp-collective, the writes its own); a family brought back
+                    // to [0.5, 1) is scaled in place, where a value below 2^-126
+                    // before the scaling was flushed. Either way a family's row
+                    // depends on its own values only.
                     if (__any_sync(0xffffffffu, need)) {
-                        for (int c32 = 0; c32 < Wn; c32 += SC) epi_fill_chunk<2>(ns2, c32, scl, stg + (size_t)(c32 / SC) * TM * SC, tid);
-                    } else if (scl[0] != 1.0f) {
+                        for (int c32 = 0; c32 < Wn; c32 += SC)
+                            epi_fill_chunk<2>(ns2, c32, scl, stg + (size_t)(c32 / SC) * TM * SC, tid, need);
+                    }
+                    if (!need && scl[0] != 1.0f) {
                         rescale_row(stg, tid, Wn, scl[0]);
                         flush = kTiny * scl[0];
                     }
