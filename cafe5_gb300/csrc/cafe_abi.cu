@@ -461,10 +461,50 @@ void cache_reset(cafe_ctx* C) {
         if (sl.ev_alloc) cudaEventDestroy(sl.ev_alloc);
     }
     C->slabs.clear();
+    C->slab_cur = 0;
     for (cudaEvent_t e : C->batch_events) cudaEventDestroy(e);
     C->batch_events.clear();
     C->cache.clear();
     C->cache_bytes = 0;
+    C->reset_wait = false;
+}
+
+// Empties the cache but keeps its slabs for the next builds, without a
+// device synchronisation: every stream that may still read a cached matrix
+// (each workspace's two request streams; auxiliary streams join them before
+// a request ends) or write one (the build streams) records an event, and
+// every build until the next reset waits for all of them before it writes
+// (cache_build_impl). Caller holds C->mu, so no request is between looking
+// up its matrices and enqueueing the work that reads them.
+cudaError_t cache_recycle(cafe_ctx* C) {
+    std::vector<cudaStream_t> streams;
+    auto add = [&](const Workspace* w) {
+        if (!w) return;
+        for (cudaStream_t s : {w->stream_hi, w->stream_lo, w->build})
+            if (s) streams.push_back(s);
+    };
+    for (const auto& w : C->ws) add(w.get());
+    add(C->ws_alt.get());
+    while (C->reset_events.size() < streams.size()) {
+        cudaEvent_t e;
+        const cudaError_t err = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        if (err != cudaSuccess) return err;
+        C->reset_events.push_back(e);
+    }
+    for (size_t i = 0; i < streams.size(); ++i) {
+        const cudaError_t err = cudaEventRecord(C->reset_events[i], streams[i]);
+        if (err != cudaSuccess) return err;
+    }
+    C->n_reset_marks = (int)streams.size();
+    C->reset_wait = true;
+    for (auto& sl : C->slabs) sl.used = 0;
+    C->slab_cur = 0;
+    // (waits enqueued on these events keep what they captured)
+    for (cudaEvent_t e : C->batch_events) cudaEventDestroy(e);
+    C->batch_events.clear();
+    C->cache.clear();
+    C->cache_bytes = 0;
+    return cudaSuccess;
 }
 
 int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P);
@@ -514,7 +554,9 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
     // rarely (an allocation costs ~0.3 ms of host time) while a small
     // workload keeps a small footprint
     const size_t need = (total + 255) & ~(size_t)255;
-    if (C->slabs.empty() || C->slabs.back().used + need > C->slabs.back().size) {
+    while (C->slab_cur < C->slabs.size() && C->slabs[C->slab_cur].used + need > C->slabs[C->slab_cur].size)
+        C->slab_cur++;
+    if (C->slab_cur == C->slabs.size()) {
         Slab sl;
         const size_t grown = C->slabs.empty() ? ((size_t)256 << 20) : std::min(2 * C->slabs.back().size, (size_t)4 << 30);
         sl.size = std::max(need, grown);
@@ -527,9 +569,13 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
         CK(cudaEventRecord(sl.ev_alloc, bs), "event");
         C->slabs.push_back(sl);
     }
-    Slab& slab = C->slabs.back();
+    Slab& slab = C->slabs[C->slab_cur];
     // a slab another workspace allocated is written only after its allocation
     CK(cudaStreamWaitEvent(bs, slab.ev_alloc, 0), "event");
+    // recycled memory is written only after everything that used the cache
+    // before the last recycle
+    if (C->reset_wait)
+        for (int q = 0; q < C->n_reset_marks; ++q) CK(cudaStreamWaitEvent(bs, C->reset_events[q], 0), "event");
     void* chunk = static_cast<char*>(slab.p) + slab.used;
     slab.used += need;
     C->cache_bytes += total;
@@ -596,20 +642,14 @@ MatEntry* schedule(cafe_ctx* C, PendingJobs& P, const MatKey& k) {
     return e;
 }
 
-// Over the cap with nothing else in flight: start a fresh cache before a
+// Over the cap: start a fresh cache in the same device memory before a
 // request inserts its keys (the reference's cache lives for one evaluation;
 // keeping matrices across calls is only a speed-up). `bytes` bounds what the
-// request may add.
+// request may add. Recycling keeps the memory bounded and spares the
+// allocations (about 1 ms per GB of new device memory).
 void cache_make_room(cafe_ctx* C, size_t bytes) {
-    if (!C->cache_cap || C->cache_bytes + bytes <= C->cache_cap) return;
-    bool idle;
-    {
-        std::lock_guard<std::mutex> lk(C->qmu);
-        idle = C->in_flight == 0 && C->queue.empty();
-    }
-    if (!idle) return;
-    cudaDeviceSynchronize();
-    cache_reset(C);
+    if (!C->cache_cap || C->cache_bytes + bytes <= C->cache_cap || C->cache_bytes == 0) return;
+    if (cache_recycle(C) != cudaSuccess) cudaGetLastError();
 }
 
 struct ScoreInfo {
@@ -2713,7 +2753,9 @@ int cafe_ctx_create(const cafe_config* cfg, cafe_ctx** out) {
     C->n_ctas = prop.multiProcessorCount * 4;
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
-    C->cache_cap = (cfg && cfg->matrix_cache_bytes) ? cfg->matrix_cache_bytes : fr / 4;
+    // 4 GB of matrices by default (a 16-candidate step of 24 taxa and side 96
+    // adds 0.2 GB; a 64-candidate K = 8 round of 48 taxa, 3.5 GB)
+    C->cache_cap = (cfg && cfg->matrix_cache_bytes) ? cfg->matrix_cache_bytes : std::min(fr / 4, (size_t)4 << 30);
     {
         // stream-ordered buffer growth draws on the device's default pool;
         // keep what it frees instead of returning it at every synchronisation
@@ -2754,6 +2796,7 @@ int cafe_ctx_destroy(cafe_ctx* C) {
     cafe_serving_stop(C);
     cudaDeviceSynchronize();
     cache_reset(C);
+    for (cudaEvent_t e : C->reset_events) cudaEventDestroy(e);
     if (C->gate) cudaEventDestroy(C->gate);
     if (C->serve_epoch) cudaEventDestroy(C->serve_epoch);
     delete C;

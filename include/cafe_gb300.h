@@ -64,7 +64,9 @@ typedef struct cafe_ctx cafe_ctx;
 
 typedef struct {
     int device;                  /* CUDA device ordinal */
-    size_t matrix_cache_bytes;   /* cap on cached matrices; 0 = 25% of free HBM */
+    size_t matrix_cache_bytes;   /* cap on cached matrices; 0 = the smaller of 4 GB and 25% of free
+                                    HBM. Past the cap the cache starts over in the same device memory
+                                    (builds into it wait for every earlier user, no synchronisation) */
     int n_streams;               /* concurrent request streams for cafe_submit; 0 = 4 */
     int max_bins;                /* reserved, 0 */
 } cafe_config;
