@@ -533,16 +533,18 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
         total += (size_t)k.size * k.size * sizeof(double);
         max_size = std::max(max_size, k.size);
     }
-    // a build of up to 256 MB of matrices runs on the workspace's build
+    // a build of up to 1 GB of matrices runs on the workspace's build
     // stream, so it fills the gaps the previous request's pruning leaves
-    // (16-candidate config-1 steps: 3.43 -> 3.24 ms); a larger one runs in
-    // line, since streaming gigabytes of matrices beside the pruning evicts
-    // its working set from L2 (64-candidate K = 8 rounds: 116 -> 127 ms).
+    // (16-candidate config-1 steps: 3.43 -> 3.24 ms; 4-candidate config-2
+    // steps, 0.5 GB of side-512 matrices beside the wide bins' walks: 4.0 ->
+    // 3.5 ms); a larger one runs in line, since streaming gigabytes of
+    // matrices beside the pruning evicts its working set from L2
+    // (64-candidate K = 8 rounds: 116 -> 127 ms).
     // Synchronous calls build in line (nothing of theirs to hide behind), and
     // so do profiled calls, so each kernel is timed alone. Slab and
     // job-table growth follow the build's stream; every user of the
     // matrices waits on the ready event below.
-    const bool beside = ws.build && !ws.build_inline && !(C->prof.on && ws.sync) && total <= ((size_t)256 << 20);
+    const bool beside = ws.build && !ws.build_inline && !(C->prof.on && ws.sync) && total <= ((size_t)1 << 30);
     const cudaStream_t bs = beside ? ws.build : ws.stream;
     AllocScope scope(bs);
     if (ws.jobs_pending) {   // the previous build has read h_jobs and ws.jobs
