@@ -1131,6 +1131,11 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
         tb.lo = ws.tc_hi.as<float>() + fl;
         tb.tr = ws.tc_tr.as<float>();
         tb.Wm = Wm;
+        if (R->use_error_model) {
+            tb.err = C->d_err.as<double>();
+            tb.err_rows = C->err_rows;
+            tb.err_ndev = C->err_ndev;
+        }
         if (prof) C->prof.begin(3, ws.stream, &ev);
         const ConvertJob* cj = ws.conv.as<ConvertJob>();
         CK(op_launch(ws, 4, [&] { return launch_convert_tc(cj, n_mat, tb, ws.stream); }, cj, n_mat, tb, ws.stream),
@@ -1686,7 +1691,9 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
         // polytomies stay on the FP64 path; saturated keys (1 - 2a < 0) run
         // on the tensor cores (a family that is exactly zero through one ends
         // there)
-        const bool to_fp64 = T.max_children > 2;
+        // (and error models wider than the +-kMaxErrHalf deviations the
+        // transposed leaf rows fold in)
+        const bool to_fp64 = T.max_children > 2 || (R->use_error_model && C->err_ndev > 2 * kMaxErrHalf + 1);
         (void)any_saturated;
         if (!to_fp64) {
             CK(ws.catids.reserve(active.size() * sizeof(int32_t)), "categories");

@@ -137,9 +137,15 @@ struct ConvertJob {
 struct TcBuffers {
     float* hi;           // [n_mat][Wm][Wm] TF32 hi part, row-major M[s][c]
     float* lo;           // [n_mat][Wm][Wm] TF32 lo part
-    float* tr;           // [n_mat][Wm][Wm] FP32 transpose: tr[c][s] = M[s][c] (leaf factors)
+    float* tr;           // [n_mat][Wm][Wm] FP32 transpose: tr[c][s] = M[s][c] (leaf factors); with an
+                         // error model, the leaf factor of an observed count c: sum over deviations d of
+                         // w_d(c) M[s][c + d] (columns 0 .. Wm - 1, zero weights skipped), summed in FP32
+                         // in deviation order
     int Wm;
+    const double* err;   // [err_rows][err_ndev] error model, or null
+    int err_rows, err_ndev;
 };
+constexpr int kMaxErrHalf = 8;   // deviations up to +-8 fold into the transposed leaf rows
 
 cudaError_t launch_convert_tc(const ConvertJob* d_jobs, int n_jobs, TcBuffers b, cudaStream_t s);
 

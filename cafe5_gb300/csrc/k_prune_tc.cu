@@ -221,16 +221,18 @@ __device__ __forceinline__ bool leaf_weights(const PruneTcArgs& a, int64_t fam, 
     if (fam < 0) return true;
     bool any = false;
     if (a.err) {
+        // the transposed matrix's row n holds the error model's weighted sum
+        // over columns 0 .. Wm - 1 (k_convert_tc): the same as the bin's own
+        // columns 0 .. S when the deviations stay within S (always for
+        // per-family bins, whose S is at least the largest count + 20);
+        // otherwise, or with no column of positive weight, FP64 recomputes
+        const int h = (a.err_ndev - 1) / 2;
+        if (n < 0 || n + h > S) return false;
         const double* pr = a.err + (size_t)(n < a.err_rows ? n : a.err_rows - 1) * a.err_ndev;
-        const int off = n - (a.err_ndev - 1) / 2;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const int col = off + d;
-            if (d < a.err_ndev && col >= 0 && col <= S && pr[d] > 0) {
-                L.col[d] = col;
-                L.w[d] = (float)pr[d];
-                any = true;
-            }
+        for (int d = 0; d < a.err_ndev; ++d) any |= (n - h + d >= 0) && pr[d] > 0;
+        if (any) {
+            L.col[0] = n;
+            L.w[0] = 1.0f;
         }
     } else if (n >= 0 && n <= S) {
         L.col[0] = n;
@@ -1176,28 +1178,54 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
 
 // FP64 matrix -> TF32 hi/lo operands (row-major, pitch Wm) and the FP32
 // transpose tr[c][s] = M[s][c] (a leaf factor, column c of M, as one row).
-// A block converts a band of 32 rows of one matrix, 32 columns at a time
-// through a shared-memory tile, so the row-major and the transposed stores
-// both write whole 128-byte lines. Wm is a multiple of 32.
+// With an error model the transpose's row c is already the leaf factor of
+// an observed count c: sum_d w_d(c) M[s][c - h + d] over the model's 2h + 1
+// deviations, in deviation order, as FP32 products and sums (the walk then
+// reads one row per leaf, whatever the model's width). A block converts a
+// band of 32 rows of one matrix, 32 columns (plus h on either side) at a
+// time through a shared-memory tile, so the row-major and the transposed
+// stores both write whole 128-byte lines. Wm is a multiple of 32.
 __global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict__ jobs, TcBuffers b) {
-    __shared__ float tile[32][33];
+    constexpr int TW = 32 + 2 * kMaxErrHalf;
+    __shared__ float tile[32][TW + 1];
     const int Wm = b.Wm;
     const int bands = Wm / 32;
     const ConvertJob J = jobs[blockIdx.x / bands];
     const int s0 = (int)(blockIdx.x % bands) * 32;
     const size_t base = (size_t)J.mat * Wm * Wm;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int h = b.err ? (b.err_ndev - 1) / 2 : 0;
     for (int c0 = 0; c0 < Wm; c0 += 32) {
         for (int r = ty; r < 32; r += 8) {
             const int s = s0 + r, c = c0 + tx;
             const float x = (float)J.src[(size_t)s * J.ld + c];
-            const float h = tc::round_tf32(x);
-            b.hi[base + (size_t)s * Wm + c] = h;
-            b.lo[base + (size_t)s * Wm + c] = tc::round_tf32(x - h);
-            tile[r][tx] = x;
+            const float hi = tc::round_tf32(x);
+            b.hi[base + (size_t)s * Wm + c] = hi;
+            b.lo[base + (size_t)s * Wm + c] = tc::round_tf32(x - hi);
+            tile[r][h + tx] = x;
+            // the deviations' columns either side of the band (within 0 .. Wm - 1)
+            if (tx < 2 * h) {
+                const int cc = tx < h ? c0 - h + tx : c0 + 32 + (tx - h);
+                const int col = tx < h ? tx : 32 + tx;
+                tile[r][col] = (cc >= 0 && cc < Wm) ? (float)J.src[(size_t)s * J.ld + cc] : 0.0f;
+            }
         }
         __syncthreads();
-        for (int r = ty; r < 32; r += 8) b.tr[base + (size_t)(c0 + r) * Wm + s0 + tx] = tile[tx][r];
+        for (int r = ty; r < 32; r += 8) {
+            const int c = c0 + r;      // the count (row of tr); tx: the state s0 + tx
+            float v;
+            if (!b.err) {
+                v = tile[tx][r];
+            } else {
+                const double* pr = b.err + (size_t)(c < b.err_rows ? c : b.err_rows - 1) * b.err_ndev;
+                v = 0.0f;
+                for (int d = 0; d < b.err_ndev; ++d) {
+                    const int col = c - h + d;
+                    if (col >= 0 && col < Wm && pr[d] > 0) v = fmaf((float)pr[d], tile[tx][r + d], v);
+                }
+            }
+            b.tr[base + (size_t)c * Wm + s0 + tx] = v;
+        }
         __syncthreads();
     }
 }
