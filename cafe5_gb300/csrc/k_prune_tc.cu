@@ -1188,6 +1188,7 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
 __global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict__ jobs, TcBuffers b) {
     constexpr int TW = 32 + 2 * kMaxErrHalf;
     __shared__ float tile[32][TW + 1];
+    __shared__ float wsh[32][2 * kMaxErrHalf + 1];   // the band's rows' deviation weights (0: skipped)
     const int Wm = b.Wm;
     const int bands = Wm / 32;
     const ConvertJob J = jobs[blockIdx.x / bands];
@@ -1210,6 +1211,12 @@ __global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict
                 tile[r][col] = (cc >= 0 && cc < Wm) ? (float)J.src[(size_t)s * J.ld + cc] : 0.0f;
             }
         }
+        if (b.err)
+            for (int q = threadIdx.x; q < 32 * b.err_ndev; q += blockDim.x) {
+                const int r = q / b.err_ndev, d = q % b.err_ndev, c = c0 + r, col = c - h + d;
+                const double w = b.err[(size_t)(c < b.err_rows ? c : b.err_rows - 1) * b.err_ndev + d];
+                wsh[r][d] = (col >= 0 && col < Wm && w > 0) ? (float)w : 0.0f;
+            }
         __syncthreads();
         for (int r = ty; r < 32; r += 8) {
             const int c = c0 + r;      // the count (row of tr); tx: the state s0 + tx
@@ -1217,12 +1224,9 @@ __global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict
             if (!b.err) {
                 v = tile[tx][r];
             } else {
-                const double* pr = b.err + (size_t)(c < b.err_rows ? c : b.err_rows - 1) * b.err_ndev;
+                // a skipped deviation has weight 0 here: fmaf(0, x, v) = v
                 v = 0.0f;
-                for (int d = 0; d < b.err_ndev; ++d) {
-                    const int col = c - h + d;
-                    if (col >= 0 && col < Wm && pr[d] > 0) v = fmaf((float)pr[d], tile[tx][r + d], v);
-                }
+                for (int d = 0; d < b.err_ndev; ++d) v = fmaf(wsh[r][d], tile[tx][r + d], v);
             }
             b.tr[base + (size_t)c * Wm + s0 + tx] = v;
         }
