@@ -1275,6 +1275,9 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             C->prof.begin(1, ws.stream, &ev);
             C->prof.acc.prune_flops += tiles_flops(T, tc_tiles, R->use_error_model);
         }
+        // tile counters of the one-CTA-per-tile launches, zeroed before the fork
+        CK(ws.tile_ctr.reserve(std::max<size_t>(launches.size(), 1) * sizeof(int)), "tile counters");
+        CK(op_memset(ws, ws.tile_ctr.p, 0, std::max<size_t>(launches.size(), 1) * sizeof(int), ws.stream), "tile counters");
         // fork: bins run on the auxiliary streams after everything queued so far
         const bool fork = launches.size() > 1;
         if (fork) {
@@ -1294,6 +1297,7 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             b.Ws = L.W / L.nsplit;
             b.stages = L.stages;
             b.vrow_base = L.vrow_base;
+            b.tile_counter = L.nsplit == 1 ? ws.tile_ctr.as<int>() + li : nullptr;
             cudaStream_t st = fork ? ws.aux[q % Workspace::kAux] : ws.stream;
             if (b.Ws % 32 || b.Ws < 32 || b.Ws > 256) return fail(C, CAFE_ERR_INVALID, "tensor-core tile of %d rows", b.Ws);
             TcMaps lm;

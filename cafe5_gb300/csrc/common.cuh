@@ -187,6 +187,8 @@ struct PruneTcArgs {
     unsigned long long* phase_clocks;   // optional [kPhases]: SM clocks of thread 0 in child setup, GEMMs,
                                         // epilogue, root bookkeeping, end-of-node barrier; tile-nodes;
                                         // then the GEMM chain's parts (k_prune_tc.cu)
+    int* tile_counter;           // one CTA per tile (nsplit 1): zeroed tile counter the CTAs take
+                                 // tiles from; null: a fixed stride
     int debug_wait_limit;        // > 0: the wait for a node's GEMMs gives up after this many polls
                                  // minus one (tests of the time-out path); 0: the default bound
 };

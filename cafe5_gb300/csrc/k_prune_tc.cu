@@ -684,7 +684,19 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
         for (int q = 0; q < kPhases; ++q) ph[q] = 0;
     const bool timing = a.phase_clocks != nullptr && tid == 0;
 
-    for (int t = cid; t < a.n_tiles; t += n_cl) {
+    // one CTA per tile: CTAs take tiles from a counter, so a CTA that starts
+    // late (its SM was held by another bin's launch) takes fewer; a cluster's
+    // CTAs walk their tiles in lockstep and keep the fixed stride
+    __shared__ int t_sh;
+    auto next_tile = [&](int done) -> int {
+        if (NSPLIT > 1 || !a.tile_counter) return done < 0 ? cid : done + n_cl;
+        if (tid == 0) t_sh = atomicAdd(a.tile_counter, 1);
+        __syncthreads();
+        const int t = t_sh;
+        __syncthreads();     // (t_sh is rewritten at the next tile)
+        return t;
+    };
+    for (int t = next_tile(-1); t < a.n_tiles; t = next_tile(t)) {
         const PruneTile tile = a.tiles[t];
         const int cnt = tile.count, k = tile.k, S = tile.S, W = tile.S + 1;
         const int Wn = W / NSPLIT;              // output states (TMEM columns) per child in this CTA

@@ -164,7 +164,7 @@ struct Workspace {
     DevBuf scratch, tiles, mats, cat, fam_lnl, total, nfail, jobs, catp;
     PinnedBuf h_tiles, h_mats, h_jobs, h_out, h_catp;
     // tensor-core path
-    DevBuf term_flags, fb_bins, tc_hi, tc_tr, tc_mi, tc_vec, conv, flags, fb_perm, tiles64, tiles_fb, parts, fb_count, phase,
+    DevBuf term_flags, fb_bins, tile_ctr, tc_hi, tc_tr, tc_mi, tc_vec, conv, flags, fb_perm, tiles64, tiles_fb, parts, fb_count, phase,
         catids, cerr;
     PinnedBuf h_conv, h_mi, h_flags, h_tiles64, h_tiles_fb, h_tail, h_catids;
     // FP64 bins walked one family per cluster
