@@ -321,6 +321,45 @@ def test_mixed_error_model_two_lambdas(ctx):
                                                kind=1, err=case.err_rows))
 
 
+def _wide_error_model(ndev, max_count=1100):
+    """An error model with deviations -h .. +h (ndev = 2h + 1): weight 0.9
+    at 0 and the rest shared, halving per step away; deviations below zero
+    count are left out of the first rows, as the reference's files do."""
+    h = (ndev - 1) // 2
+    base = np.array([0.5 ** abs(d) for d in range(-h, h + 1)])
+    base[h] = 0.0
+    base *= 0.1 / base.sum()
+    base[h] = 0.9
+    rows = np.tile(base, (max_count + 1, 1))
+    for n in range(h):
+        rows[n, :h - n] = 0.0
+        rows[n] /= rows[n].sum()
+    return rows
+
+
+@pytest.mark.parametrize("ndev", [5, 19])
+def test_mixed_wide_error_models(ctx, ndev):
+    """Error models of 5 and 19 deviations on the two-lambda tree. Up to
+    +-8 deviations the conversion folds the model into each leaf's row of
+    the transposed matrix: the tensor-core path within 1e-6 of the rescaled
+    oracle; wider models take the FP64 path (every family counted as
+    recomputed in FP64)."""
+    case = [c for c in CASES if c.name == "syn_multilambda_error_32taxa"][0]
+    err = _wide_error_model(ndev)
+    a, b = _both(ctx, case.tree, case.counts, case.lambdas, lam_idx=case.lambda_of_node, kind=1, err=err)
+    tot, fam = _scaled_oracle_binned(case.tree, case.counts, case.lambdas, lam_idx=case.lambda_of_node, kind=1,
+                                     err=err)
+    fin = np.isfinite(fam)
+    assert fin.all()
+    assert np.allclose(a.family_lnl, fam, rtol=1e-10, atol=0)
+    if ndev <= 17:
+        _check_vs_oracle(b, tot, fam)
+        _check_mixed(a, b)
+    else:
+        assert b.n_fallback == len(case.counts)
+        _check_mixed(a, b)
+
+
 def test_mixed_polytomy_and_underflow_cases(ctx):
     for name in ["syn_polytomy", "syn_base_underflow", "syn_base_zero_family", "syn_gamma_24taxa_k4"]:
         case = [c for c in CASES if c.name == name][0]
