@@ -980,13 +980,10 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
             int E = ns2.Eacc;
             bool nflag = ns2.flag;
             float maxp, bf, bp, bq, be, fmx[2], fmn[2];
-            // an inner node whose slice of the vector (up to 128 states) fits
-            // the stage region as staging tiles: the statistics and the
-            // unscaled product in one pass over TMEM (a cluster exchanges the
-            // statistics before the rows are scaled in place)
-            const bool fused = !is_root && Wn <= 4 * SC &&
-                               (size_t)(Wn / SC) * TM * SC * sizeof(float) <= stages_region(a.Ws, NS);
-            float* stg = reinterpret_cast<float*>(smem);     // the stage region holds the staging tiles
+            // one CTA per tile and a vector that fits the staging tiles: the
+            // statistics and the unscaled product in one pass over TMEM
+            const bool fused = NSPLIT == 1 && !is_root && Wn <= 2 * SC;
+            float* stg = reinterpret_cast<float*>(smem);     // stage 0 holds the two staging tiles
             if (fused) {
                 epi_scan_fill<2>(ns2, Wn, stg, tid, maxp, fmx, fmn);
                 bf = bp = bq = be = 0.0f;
@@ -1116,8 +1113,7 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                     __syncthreads();
                     if (tid == 0) {
                         const int vrow = (int)(vrow_cta + (int64_t)vs * TM);
-                        for (int c32 = 0; c32 < Wn; c32 += SC)
-                            tc::tma_store_2d(&map_vst, s_off + c32, vrow, stg + (size_t)(c32 / SC) * TM * SC);
+                        for (int c32 = 0; c32 < Wn; c32 += SC) tc::tma_store_2d(&map_vst, c32, vrow, stg + (size_t)(c32 / SC) * TM * SC);
                         tc::bulk_commit();
                     }
                 } else {
