@@ -203,8 +203,11 @@ __device__ __forceinline__ float fac_err(const NodeSrc<NC>& ns, int c, float raw
     return ns.leaf[c] ? (raw < 0x1p-100f ? ns.ue[c] : 0.0f) : ns.ue[c];
 }
 
-// Leaf weights of this thread's family: up to three (column, weight) pairs
-// (one-hot column n, or the error model's columns n-1, n, n+1).
+// Leaf weights of this thread's family as (column, weight) pairs. Only
+// col[0] is set now (weight 1): with an error model k_convert_tc has folded
+// the model's deviations into that row of the transposed matrix, so the
+// multi-column paths below see col[1], col[2] = -1 (kept: removing them
+// changes the walk's register allocation, which then spills).
 struct LeafW {
     int col[3];
     float w[3];
