@@ -311,6 +311,52 @@ def test_families_update_rebuilds_derived_tables(ctx):
         assert np.array_equal(e.family_lnl, f.family_lnl)
 
 
+def test_matrix_cache_recycling_keeps_results():
+    """A context whose matrix cache is capped below one call's matrices
+    starts the cache over in the same device memory at every call, while the
+    device-pointer calls issued before it may still be reading theirs (no
+    synchronisation: its builds wait for those calls). Every call's results
+    equal the same request scored in a context with the default cache, bit
+    for bit, in both precisions, and the cache never holds more than one
+    call's matrices."""
+    import torch
+    from cafe5_gb300.engine import Context
+    from cafe5_gb300.inputs import RootPrior
+    from cafe5_gb300.synth import workload
+    w = workload(1, n_families=2000, seed=44)
+    small, ref = Context(matrix_cache_bytes=16 << 20), Context()
+    try:
+        prior = RootPrior.uniform(400).vector()
+        t1, s1 = _setup(small, w.tree, w.families.counts, prior=prior)
+        t2, s2 = _setup(ref, w.tree, w.families.counts, prior=prior)
+        F = w.families.n_families
+        B, steps = 4, 6
+        dev = torch.device("cuda", 0)
+        stream = torch.cuda.Stream(dev)
+        for precision in ("mixed_tf32x3", "fp64_binned"):
+            kw = dict(model=1, precision=precision)
+            cands = [[dict(lambdas=[0.002 * (1 + 0.01 * b) * (1 + 1e-5 * (s + 1))], multipliers=w.multipliers,
+                           cat_probs=w.cat_probs) for b in range(B)] for s in range(steps)]
+            fam = [torch.empty(B * F, dtype=torch.float64, device=dev) for _ in range(steps)]
+            tot = [torch.empty(B, dtype=torch.float64, device=dev) for _ in range(steps)]
+            with torch.cuda.stream(stream):
+                for s in range(steps):
+                    small.score_batch_device(t1, s1, cands[s], fam[s].data_ptr(), tot[s].data_ptr(),
+                                             stream.cuda_stream, **kw)
+            stream.synchronize()
+            assert 0 < small.cache_size() <= B * len(w.multipliers) * len(w.tree.parent)
+            for s in range(steps):
+                want = ref.score_batch(t2, s2, cands[s], **kw)
+                got = fam[s].view(B, F).cpu().numpy()
+                got_tot = tot[s].cpu().numpy()
+                for b in range(B):
+                    assert np.array_equal(got[b], want[b].family_lnl), (precision, s, b)
+                    assert got_tot[b] == want[b].total, (precision, s, b)
+    finally:
+        small.close()
+        ref.close()
+
+
 def test_back_to_back_device_calls_match_synchronous_calls(ctx):
     """Device-pointer calls issued back to back build each call's matrices on
     a build stream while the previous call still prunes, and alternate
