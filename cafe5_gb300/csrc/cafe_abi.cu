@@ -1052,8 +1052,11 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             if (e->stamp != stamp) {
                 e->stamp = stamp;
                 e->conv = (int)jobs.size();
-                jobs.push_back(ConvertJob{e->d, msize, e->conv});
+                jobs.push_back(ConvertJob{e->d, msize, e->conv, 0});
             }
+            // a leaf's branch is read as transposed rows, an internal child's
+            // as the GEMM's hi and lo operands
+            jobs[(size_t)e->conv].what |= T.leaf_col[v] >= 0 ? 2 : 1;
             mat_index[(size_t)k * T.n_nodes + v] = e->conv | (ws.sat_vec[(size_t)k * T.n_nodes + v] ? (1 << 30) : 0);
         }
     const int n_mat = (int)jobs.size();

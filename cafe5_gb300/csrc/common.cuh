@@ -132,6 +132,8 @@ struct ConvertJob {
     const double* src;   // FP64 row-major, leading dimension `ld`
     int ld;
     int mat;             // index into the request's converted arrays
+    int what;            // 1: the TF32 hi/lo operands (an internal child's branch), 2: the
+                         // FP32 transpose (a leaf's branch); both where a matrix serves both
 };
 
 struct TcBuffers {

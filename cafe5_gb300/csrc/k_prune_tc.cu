@@ -1211,13 +1211,19 @@ __global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict
     const size_t base = (size_t)J.mat * Wm * Wm;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int h = b.err ? (b.err_ndev - 1) / 2 : 0;
+    // only what the walk reads: hi/lo for internal children's branches, the
+    // transpose for leaves' (block-uniform)
+    const bool want_hl = (J.what & 1) != 0, want_tr = (J.what & 2) != 0;
     for (int c0 = 0; c0 < Wm; c0 += 32) {
         for (int r = ty; r < 32; r += 8) {
             const int s = s0 + r, c = c0 + tx;
             const float x = (float)J.src[(size_t)s * J.ld + c];
-            const float hi = tc::round_tf32(x);
-            b.hi[base + (size_t)s * Wm + c] = hi;
-            b.lo[base + (size_t)s * Wm + c] = tc::round_tf32(x - hi);
+            if (want_hl) {
+                const float hi = tc::round_tf32(x);
+                b.hi[base + (size_t)s * Wm + c] = hi;
+                b.lo[base + (size_t)s * Wm + c] = tc::round_tf32(x - hi);
+            }
+            if (!want_tr) continue;
             tile[r][h + tx] = x;
             // the deviations' columns either side of the band (within 0 .. Wm - 1)
             if (tx < 2 * h) {
@@ -1226,6 +1232,7 @@ __global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict
                 tile[r][col] = (cc >= 0 && cc < Wm) ? (float)J.src[(size_t)s * J.ld + cc] : 0.0f;
             }
         }
+        if (!want_tr) continue;
         if (b.err)
             for (int q = threadIdx.x; q < 32 * b.err_ndev; q += blockDim.x) {
                 const int r = q / b.err_ndev, d = q % b.err_ndev, c = c0 + r, col = c - h + d;
