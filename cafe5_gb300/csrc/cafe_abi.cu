@@ -456,26 +456,31 @@ struct PendingJobs {
 };
 
 void cache_reset(cafe_ctx* C) {
-    for (auto& sl : C->slabs) {
-        cudaFree(sl.p);
-        if (sl.ev_alloc) cudaEventDestroy(sl.ev_alloc);
+    for (auto& g : C->gens) {
+        for (auto& sl : g.slabs) {
+            cudaFree(sl.p);
+            if (sl.ev_alloc) cudaEventDestroy(sl.ev_alloc);
+        }
+        g.slabs.clear();
+        g.cur = 0;
+        g.n_marks = 0;
     }
-    C->slabs.clear();
-    C->slab_cur = 0;
+    C->gen = 0;
     for (cudaEvent_t e : C->batch_events) cudaEventDestroy(e);
     C->batch_events.clear();
     C->cache.clear();
     C->cache_bytes = 0;
-    C->reset_wait = false;
 }
 
-// Empties the cache but keeps its slabs for the next builds, without a
-// device synchronisation: every stream that may still read a cached matrix
-// (each workspace's two request streams; auxiliary streams join them before
-// a request ends) or write one (the build streams) records an event, and
-// every build until the next reset waits for all of them before it writes
-// (cache_build_impl). Caller holds C->mu, so no request is between looking
-// up its matrices and enqueueing the work that reads them.
+// Empties the cache and moves it to the other generation of slabs, without
+// a device synchronisation: every stream that may still read a matrix of
+// the generation being left (each workspace's two request streams;
+// auxiliary streams join them before a request ends) or write one (the
+// build streams) records that generation's marks, and builds into a
+// generation wait for its marks (cache_build_impl) -- recorded a whole
+// generation earlier, so normally long complete. Caller holds C->mu, so no
+// request is between looking up its matrices and enqueueing the work that
+// reads them.
 cudaError_t cache_recycle(cafe_ctx* C) {
     std::vector<cudaStream_t> streams;
     auto add = [&](const Workspace* w) {
@@ -485,20 +490,22 @@ cudaError_t cache_recycle(cafe_ctx* C) {
     };
     for (const auto& w : C->ws) add(w.get());
     add(C->ws_alt.get());
-    while (C->reset_events.size() < streams.size()) {
+    cafe_ctx::SlabGen& old = C->gens[C->gen];
+    while (old.marks.size() < streams.size()) {
         cudaEvent_t e;
         const cudaError_t err = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
         if (err != cudaSuccess) return err;
-        C->reset_events.push_back(e);
+        old.marks.push_back(e);
     }
     for (size_t i = 0; i < streams.size(); ++i) {
-        const cudaError_t err = cudaEventRecord(C->reset_events[i], streams[i]);
+        const cudaError_t err = cudaEventRecord(old.marks[i], streams[i]);
         if (err != cudaSuccess) return err;
     }
-    C->n_reset_marks = (int)streams.size();
-    C->reset_wait = true;
-    for (auto& sl : C->slabs) sl.used = 0;
-    C->slab_cur = 0;
+    old.n_marks = (int)streams.size();
+    C->gen ^= 1;
+    cafe_ctx::SlabGen& g = C->gens[C->gen];
+    for (auto& sl : g.slabs) sl.used = 0;
+    g.cur = 0;
     // (waits enqueued on these events keep what they captured)
     for (cudaEvent_t e : C->batch_events) cudaEventDestroy(e);
     C->batch_events.clear();
@@ -556,11 +563,11 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
     // rarely (an allocation costs ~0.3 ms of host time) while a small
     // workload keeps a small footprint
     const size_t need = (total + 255) & ~(size_t)255;
-    while (C->slab_cur < C->slabs.size() && C->slabs[C->slab_cur].used + need > C->slabs[C->slab_cur].size)
-        C->slab_cur++;
-    if (C->slab_cur == C->slabs.size()) {
+    cafe_ctx::SlabGen& G = C->gens[C->gen];
+    while (G.cur < G.slabs.size() && G.slabs[G.cur].used + need > G.slabs[G.cur].size) G.cur++;
+    if (G.cur == G.slabs.size()) {
         Slab sl;
-        const size_t grown = C->slabs.empty() ? ((size_t)256 << 20) : std::min(2 * C->slabs.back().size, (size_t)4 << 30);
+        const size_t grown = G.slabs.empty() ? ((size_t)256 << 20) : std::min(2 * G.slabs.back().size, (size_t)4 << 30);
         sl.size = std::max(need, grown);
         // stream-ordered when a request is being enqueued: requests on other
         // streams reach these matrices only through the build's ready event
@@ -569,15 +576,14 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
         sl.used = 0;
         CK(cudaEventCreateWithFlags(&sl.ev_alloc, cudaEventDisableTiming), "event");
         CK(cudaEventRecord(sl.ev_alloc, bs), "event");
-        C->slabs.push_back(sl);
+        G.slabs.push_back(sl);
     }
-    Slab& slab = C->slabs[C->slab_cur];
+    Slab& slab = G.slabs[G.cur];
     // a slab another workspace allocated is written only after its allocation
     CK(cudaStreamWaitEvent(bs, slab.ev_alloc, 0), "event");
-    // recycled memory is written only after everything that used the cache
-    // before the last recycle
-    if (C->reset_wait)
-        for (int q = 0; q < C->n_reset_marks; ++q) CK(cudaStreamWaitEvent(bs, C->reset_events[q], 0), "event");
+    // recycled memory is written only after everything that used it the
+    // last time the cache held this generation
+    for (int q = 0; q < G.n_marks; ++q) CK(cudaStreamWaitEvent(bs, G.marks[q], 0), "event");
     void* chunk = static_cast<char*>(slab.p) + slab.used;
     slab.used += need;
     C->cache_bytes += total;
@@ -2769,9 +2775,10 @@ int cafe_ctx_create(const cafe_config* cfg, cafe_ctx** out) {
     C->n_ctas = prop.multiProcessorCount * 4;
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
-    // 4 GB of matrices by default (a 16-candidate step of 24 taxa and side 96
-    // adds 0.2 GB; a 64-candidate K = 8 round of 48 taxa, 3.5 GB)
-    C->cache_cap = (cfg && cfg->matrix_cache_bytes) ? cfg->matrix_cache_bytes : std::min(fr / 4, (size_t)4 << 30);
+    // 4 GB of matrices per generation by default (a 16-candidate step of 24
+    // taxa and side 96 adds 0.2 GB; a 64-candidate K = 8 round of 48 taxa,
+    // 3.5 GB)
+    C->cache_cap = (cfg && cfg->matrix_cache_bytes) ? cfg->matrix_cache_bytes : std::min(fr / 8, (size_t)4 << 30);
     {
         // stream-ordered buffer growth draws on the device's default pool;
         // keep what it frees instead of returning it at every synchronisation
@@ -2812,7 +2819,8 @@ int cafe_ctx_destroy(cafe_ctx* C) {
     cafe_serving_stop(C);
     cudaDeviceSynchronize();
     cache_reset(C);
-    for (cudaEvent_t e : C->reset_events) cudaEventDestroy(e);
+    for (auto& g : C->gens)
+        for (cudaEvent_t e : g.marks) cudaEventDestroy(e);
     if (C->gate) cudaEventDestroy(C->gate);
     if (C->serve_epoch) cudaEventDestroy(C->serve_epoch);
     delete C;

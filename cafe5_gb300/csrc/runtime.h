@@ -227,15 +227,18 @@ struct cafe_ctx {
     cafe::DevBuf d_err;
     // matrix cache
     cafe::MatCache cache;
-    std::vector<cafe::Slab> slabs;
-    size_t slab_cur = 0;                        // the slab builds draw from (slabs before it are full)
+    // two generations of slabs, used in turn: the cache fills one; past the
+    // cap it starts over in the other (whose users were issued a whole
+    // generation earlier)
+    struct SlabGen {
+        std::vector<cafe::Slab> slabs;
+        size_t cur = 0;                         // the slab builds draw from (slabs before it are full)
+        std::vector<cudaEvent_t> marks;         // recorded on every stream when the cache left this generation
+        int n_marks = 0;                        // builds into this generation wait for them
+    } gens[2];
+    int gen = 0;
     std::vector<cudaEvent_t> batch_events;
-    size_t cache_bytes = 0, cache_cap = 0;
-    // recycling: at a reset every stream that may still read or write cached
-    // matrices records one of these; builds into the recycled slabs wait for them
-    std::vector<cudaEvent_t> reset_events;
-    int n_reset_marks = 0;
-    bool reset_wait = false;
+    size_t cache_bytes = 0, cache_cap = 0;      // bytes of the current generation, cap of one
     uint64_t request_stamp = 0;
     std::map<int, std::pair<int, int>> tuned;   // bin width -> (CTAs per SM, stages) chosen by cafe_autotune
     int debug_wait_limit = 0;    // cafe_debug_set: polls before the tensor-core wait for a node's GEMMs gives up

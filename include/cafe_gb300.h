@@ -64,9 +64,10 @@ typedef struct cafe_ctx cafe_ctx;
 
 typedef struct {
     int device;                  /* CUDA device ordinal */
-    size_t matrix_cache_bytes;   /* cap on cached matrices; 0 = the smaller of 4 GB and 25% of free
-                                    HBM. Past the cap the cache starts over in the same device memory
-                                    (builds into it wait for every earlier user, no synchronisation) */
+    size_t matrix_cache_bytes;   /* cap on the matrices of each of the cache's two generations of
+                                    device memory; 0 = the smaller of 4 GB and 1/8 of free HBM. Past the
+                                    cap the cache starts over in its other generation, whose builds wait
+                                    for that generation's earlier users (no synchronisation) */
     int n_streams;               /* concurrent request streams for cafe_submit; 0 = 4 */
     int max_bins;                /* reserved, 0 */
 } cafe_config;
