@@ -995,10 +995,8 @@ int tc_by_smem(const TreeHost& T, int W, int stages, size_t* smem, int nsplit = 
 
 TcShape tc_shape(cafe_ctx* C, const TreeHost& T, int W) {
     TcShape sh;
-    // two children's factors; at W = 32 also the vector a node hands to
-    // its parent in TMEM (TF32 hi and lo), which keeps 4 CTAs per SM
     sh.tmem_cols = 32;
-    while (sh.tmem_cols < (W == 32 ? 4 : 2) * W) sh.tmem_cols *= 2;
+    while (sh.tmem_cols < 2 * W) sh.tmem_cols *= 2;
     const int by_tmem = 512 / sh.tmem_cols;
     auto it = C->tuned.find(W);
     if (it != C->tuned.end()) {

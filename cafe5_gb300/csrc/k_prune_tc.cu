@@ -119,7 +119,6 @@ struct ChildInfo {
     int leaf_col;   // >= 0: leaf
     int mat;
     int tcol;       // TMEM column base of the child's factor, in units of W
-    int in_tmem;    // the child is the previous node and left its vector in TMEM (TF32 hi, lo)
 };
 
 // One internal node of the post-order walk, as the tile's table in shared
@@ -130,7 +129,6 @@ struct NodeInfo {
     int nch;
     int is_root;
     int sat;        // a child's matrix is saturated (rows s >= 1 all zero)
-    int pass;       // the next node is the parent: the vector goes to it through TMEM
     ChildInfo c[2];
 };
 
@@ -560,35 +558,6 @@ __device__ __forceinline__ void epi_scan_fill(const NodeSrc<NC>& ns, int W, floa
     }
 }
 
-// This thread's staged row (its final values) into TMEM as the parent's A
-// operand: hi = tf32(v) at columns hi .. hi + W - 1 of its lane, lo =
-// tf32(v - hi) at lo .., the split the parent's load would make
-// (warp-collective: TMEM stores).
-__device__ __forceinline__ void epi_pass_tmem(const float* stg, int tid, int W, uint32_t t_hi, uint32_t t_lo) {
-    for (int c32 = 0; c32 < W; c32 += SC) {
-        const uint8_t* row = reinterpret_cast<const uint8_t*>(stg + (size_t)(c32 / SC) * TM * SC) +
-                             (size_t)(tid >> 3) * 1024 + (size_t)(tid & 7) * 128;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            float hi[16], lo[16];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int piece = 4 * h + q;
-                const float4 v = *reinterpret_cast<const float4*>(row + ((piece ^ (tid & 7)) << 4));
-                const float x[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    hi[4 * q + e] = tc::round_tf32_bits(x[e]);
-                    lo[4 * q + e] = tc::round_tf32_bits(x[e] - hi[4 * q + e]);
-                }
-            }
-            tc::tmem_st16(t_hi + (uint32_t)(c32 + 16 * h), hi);
-            tc::tmem_st16(t_lo + (uint32_t)(c32 + 16 * h), lo);
-        }
-    }
-    tc::tmem_wait_st();
-}
-
 // This thread's staged row times a power of two s (exact unless a value
 // was already below the FP32 normal range before the scaling).
 __device__ __forceinline__ void rescale_row(float* stg, int tid, int W, float s) {
@@ -739,10 +708,6 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
         const int Rf = (fam >= 0 && a.fam_R) ? a.fam_R[fam] : tile.R;
         const int32_t* mi = a.mat_index + (size_t)k * P.n_nodes;
         const uint32_t idesc = tc::idesc_tf32(TM, Wn);
-        // one CTA per tile and TMEM for two more vectors: a node whose parent
-        // comes next hands its vector over in TMEM, split into TF32 hi
-        // (columns 2W ..) and lo (3W ..) -- the parent's A operand
-        const bool tpass = NSPLIT == 1 && a.tmem_cols >= 4 * W;
         bool flag = false;
         bool dead = false;   // an exact zero vector through a saturated branch: the family's term is 0
 
@@ -754,17 +719,13 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
             e.is_root = v == P.root;
             e.nch = P.cstart[ii + 1] - P.cstart[ii];
             e.sat = 0;
-            e.pass = 0;
-            if (tpass && ii + 1 < P.n_internal)
-                for (int q = P.cstart[ii + 1]; q < P.cstart[ii + 2]; ++q) e.pass |= P.child[q] == v;
             for (int c = 0; c < 2; ++c) {
-                ChildInfo ci{0, -1, 0, c, 0};
+                ChildInfo ci{0, -1, 0, c};
                 if (c < e.nch) {
                     const int ch = P.child[P.cstart[ii] + c];
                     ci.slot = P.slot[ch];
                     ci.leaf_col = P.leaf_col[ch];
                     ci.mat = mi[ch] & ~kSatBit;
-                    ci.in_tmem = tpass && ii > 0 && ch == P.internal[ii - 1];
                     e.sat |= (mi[ch] & kSatBit) != 0;
                 }
                 e.c[c] = ci;
@@ -910,14 +871,13 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                         if (timing) ph[6] += clock64() - te;
                         const long long ti = timing ? clock64() : 0;
                         if (tid == 0 && !abort_sh) {
+                            tc::mbar_expect_tx(&bar_full[st], (uint32_t)((TM + 2 * Wn) * KC * sizeof(float)));
                             // the FP32 node vector lands in the hi operand; the
-                            // consumer splits it into hi and lo in place (a vector
-                            // in TMEM needs no load: only the matrix comes)
+                            // consumer splits it into hi and lo in place
                             // one box each: the vector's TM rows, the matrices' Wn rows
                             // (TMA issue is slow enough per instruction to count)
-                            tc::mbar_expect_tx(&bar_full[st], (uint32_t)(((chi.in_tmem ? 0 : TM) + 2 * Wn) * KC * sizeof(float)));
                             const int vrow = (int)(vrow_cta + (int64_t)chi.slot * TM);
-                            if (!chi.in_tmem) tc::tma_load_2d(Ahi, &map_vec, kc * KC, vrow, &bar_full[st]);
+                            tc::tma_load_2d(Ahi, &map_vec, kc * KC, vrow, &bar_full[st]);
                             const int mrow = chi.mat * Wm + s_off;     // this CTA's output states
                             tc::tma_load_3d(Bhi, &map_mat, kc * KC, mrow, 0, &bar_full[st]);   // hi, then lo at Blo
                             last_full[st] = 1;
@@ -941,7 +901,6 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                         const uint32_t cg = g + (uint32_t)j;
                         const int st = (int)(cg % (uint32_t)NS);
                         float* Ahi = reinterpret_cast<float*>(smem + st * sbytes);
-                        const bool a_tmem = nd.c[j < n0 ? 0 : 1].in_tmem != 0;
                         const long long tf = timing ? clock64() : 0;
                         const bool ok = abort_sh || tc::mbar_wait(&bar_full[st], (cg / (uint32_t)NS) & 1);
                         const long long tf1 = timing ? clock64() : 0;
@@ -950,7 +909,7 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                         if (!ok) {
                             atomicExch(a.status, 1);
                             abort_sh = 1;
-                        } else if (!abort_sh && !a_tmem) {
+                        } else if (!abort_sh) {
                             split_row_tf32(Ahi, Ahi + TM * KC, tid);
                             tc::fence_proxy_async_shared();
                         }
@@ -979,26 +938,13 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                             tc::fence_after();
                             if (timing) ph[14] += clock64() - tm;
                             const uint32_t d = tmem + (uint32_t)(chi.tcol * Wn);
-                            if (chi.in_tmem) {
-                                // A from TMEM: hi at columns 2W + k, lo at 3W + k
-                                const int kc = c == 0 ? j : j - n0;
-                                const uint32_t a_hi = tmem + (uint32_t)(2 * W + kc * KC), a_lo = a_hi + (uint32_t)W;
 #pragma unroll
-                                for (int ks = 0; ks < KC / 8; ++ks) {
-                                    const uint64_t bh = desc_k(Bhi + ks * 8), bl = desc_k(Blo + ks * 8);
-                                    tc::mma_tf32_at(d, a_hi + 8 * ks, bh, idesc, (first && ks == 0) ? 0u : 1u);
-                                    tc::mma_tf32_at(d, a_hi + 8 * ks, bl, idesc, 1);
-                                    tc::mma_tf32_at(d, a_lo + 8 * ks, bh, idesc, 1);
-                                }
-                            } else {
-#pragma unroll
-                                for (int ks = 0; ks < KC / 8; ++ks) {
-                                    const uint64_t ah = desc_k(Ahi + ks * 8), al = desc_k(Alo + ks * 8);
-                                    const uint64_t bh = desc_k(Bhi + ks * 8), bl = desc_k(Blo + ks * 8);
-                                    tc::mma_tf32(d, ah, bh, idesc, (first && ks == 0) ? 0u : 1u);
-                                    tc::mma_tf32(d, ah, bl, idesc, 1);
-                                    tc::mma_tf32(d, al, bh, idesc, 1);
-                                }
+                            for (int ks = 0; ks < KC / 8; ++ks) {
+                                const uint64_t ah = desc_k(Ahi + ks * 8), al = desc_k(Alo + ks * 8);
+                                const uint64_t bh = desc_k(Bhi + ks * 8), bl = desc_k(Blo + ks * 8);
+                                tc::mma_tf32(d, ah, bh, idesc, (first && ks == 0) ? 0u : 1u);
+                                tc::mma_tf32(d, ah, bl, idesc, 1);
+                                tc::mma_tf32(d, al, bh, idesc, 1);
                             }
                             tc::mma_commit(&bar_empty[st]);
                             if (timing) ph[9] += clock64() - tm;
@@ -1166,17 +1112,12 @@ __global__ void __launch_bounds__(NTHREADS, NSPLIT == 1 ? CAFE_TC_MINB : 1)
                         rescale_row(stg, tid, Wn, scl[0]);
                         flush = kTiny * scl[0];
                     }
-                    if (tpass && nd.pass) {
-                        // the parent comes next: the vector stays in TMEM
-                        epi_pass_tmem(stg, tid, Wn, tmem + lane_base + (uint32_t)(2 * W), tmem + lane_base + (uint32_t)(3 * W));
-                    } else {
-                        tc::fence_proxy_async_shared();
-                        __syncthreads();
-                        if (tid == 0) {
-                            const int vrow = (int)(vrow_cta + (int64_t)vs * TM);
-                            for (int c32 = 0; c32 < Wn; c32 += SC) tc::tma_store_2d(&map_vst, c32, vrow, stg + (size_t)(c32 / SC) * TM * SC);
-                            tc::bulk_commit();
-                        }
+                    tc::fence_proxy_async_shared();
+                    __syncthreads();
+                    if (tid == 0) {
+                        const int vrow = (int)(vrow_cta + (int64_t)vs * TM);
+                        for (int c32 = 0; c32 < Wn; c32 += SC) tc::tma_store_2d(&map_vst, c32, vrow, stg + (size_t)(c32 / SC) * TM * SC);
+                        tc::bulk_commit();
                     }
                 } else {
                     epi_store<2>(ns2, Wn, scl, stg, tid, &map_vst, (int)(vrow_cta + (int64_t)vs * TM), s_off);

@@ -93,14 +93,6 @@ CAFE_DEV void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, 
             d_tmem),
         "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
 }
-// The same MMA with the A operand in TMEM (lane = row, one TF32 element
-// per column, K-major) at column address a_tmem.
-CAFE_DEV void mma_tf32_at(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t idesc, uint32_t accumulate) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(
-            d_tmem),
-        "r"(a_tmem), "l"(b), "r"(idesc), "r"(accumulate));
-}
 CAFE_DEV void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                  : "memory");
