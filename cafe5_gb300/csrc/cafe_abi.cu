@@ -558,9 +558,9 @@ int cache_build_impl(cafe_ctx* C, Workspace& ws, PendingJobs& P) {
         CK(cudaEventSynchronize(ws.ev_jobs), "jobs");
         ws.jobs_pending = false;
     }
-    // bump allocation from large slabs (no cudaMalloc per evaluation); each
-    // new slab is twice the last, up to 4 GB, so a long search allocates
-    // rarely (an allocation costs ~0.3 ms of host time) while a small
+    // bump allocation from large slabs of the current generation (no
+    // cudaMalloc per evaluation); each new slab is twice the last, up to
+    // 4 GB, so a generation fills up with few allocations while a small
     // workload keeps a small footprint
     const size_t need = (total + 255) & ~(size_t)255;
     cafe_ctx::SlabGen& G = C->gens[C->gen];
@@ -650,11 +650,12 @@ MatEntry* schedule(cafe_ctx* C, PendingJobs& P, const MatKey& k) {
     return e;
 }
 
-// Over the cap: start a fresh cache in the same device memory before a
-// request inserts its keys (the reference's cache lives for one evaluation;
-// keeping matrices across calls is only a speed-up). `bytes` bounds what the
-// request may add. Recycling keeps the memory bounded and spares the
-// allocations (about 1 ms per GB of new device memory).
+// Over the cap: start a fresh cache in the other generation of slabs before
+// a request inserts its keys (the reference's cache lives for one
+// evaluation; keeping matrices across calls is only a speed-up). `bytes`
+// bounds what the request may add. Recycling keeps the memory bounded and
+// spares the allocations (about 1 ms of host time per GB of new device
+// memory).
 void cache_make_room(cafe_ctx* C, size_t bytes) {
     if (!C->cache_cap || C->cache_bytes + bytes <= C->cache_cap || C->cache_bytes == 0) return;
     if (cache_recycle(C) != cudaSuccess) cudaGetLastError();
