@@ -1213,12 +1213,8 @@ int enqueue_mixed(cafe_ctx* C, Workspace& ws, const cafe_request* R, TreeHost& T
             L.stages = shape.stages;
             L.smem = shape.smem;
             L.per_sm = shape.per_sm;
-            // pad shared memory so no more CTAs of this launch than TMEM allows
-            // share an SM -- only where shared memory would not cap them anyway
-            // (unpadded, the leftover lets the next request's matrix builds run
-            // beside the pruning)
-            if ((int)((227 * 1024) / (L.smem + 1024)) > L.per_sm)
-                L.smem = std::max(L.smem, (size_t)((227 * 1024) / L.per_sm) - 2048);
+            // pad shared memory so no more CTAs of this launch than TMEM allows share an SM
+            L.smem = std::max(L.smem, (size_t)((227 * 1024) / L.per_sm) - 2048);
             L.smem = std::min(L.smem, (size_t)prune_tc_max_smem());
             L.n_ctas = (int)std::max<int64_t>(1, std::min<int64_t>(L.n_tiles, (int64_t)C->sm_count * L.per_sm));
             L.vrow_base = vrows;
