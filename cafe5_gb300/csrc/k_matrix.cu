@@ -92,16 +92,20 @@ struct RowChain {
 constexpr int kStageCols = 16;   // columns of a warp's staging tile
 constexpr int kStagePitch = 33;  // padded row pitch (doubles) of the staging tile
 
-// One CTA per matrix. Lane l of warp w owns the row pair p = 32 w + l: the
-// short row 1 + p and the long row W - 1 - p, one after the other. Each
-// step c writes two entries of row s's chain: the mirror P(c->s) =
-// (c/s) P(s->c) of row c < s, contiguous across the warp (neighbouring lanes
-// own neighbouring rows), and P(s->c) itself, which is strided across the
-// warp and so goes through a 16-column staging tile in shared memory and
-// leaves as contiguous row segments. Row 0 is delta(c, 0).
-__global__ void __launch_bounds__(128) k_matrix_build(const MatrixJob* __restrict__ jobs) {
+// `parts` CTAs of T threads per matrix, each with an equal share of its row
+// pairs (every pair costs about W steps), so a side-512 build spreads over
+// the SMs in small CTAs. Thread t of part q owns the row pairs
+// p = q T + t + j parts T: the short row 1 + p and the long row W - 1 - p,
+// one after the other. Each step c writes two entries of row s's chain:
+// the mirror P(c->s) = (c/s) P(s->c) of row c < s, contiguous across the
+// warp (neighbouring lanes own neighbouring rows), and P(s->c) itself,
+// which is strided across the warp and so goes through a 16-column staging
+// tile in shared memory and leaves as contiguous row segments. Row 0 is
+// delta(c, 0).
+__global__ void __launch_bounds__(128) k_matrix_build(const MatrixJob* __restrict__ jobs, int parts) {
     extern __shared__ double sh[];
-    const MatrixJob J = jobs[blockIdx.x];
+    const int part = blockIdx.x % parts;
+    const MatrixJob J = jobs[blockIdx.x / parts];
     const int W = J.size;
     double* inv = sh;                  // inv[k] = 1/k, k = 0..W
     double* p1 = sh + (W + 1);         // coefficient tables (Coeffs), k = 0..W
@@ -125,15 +129,17 @@ __global__ void __launch_bounds__(128) k_matrix_build(const MatrixJob* __restric
         bb[k] = coeff * ((double)(k - 1) * ik);
     }
     const Coeffs cf{p1, p2, bb};
-    for (int c = threadIdx.x; c < W; c += blockDim.x) M[c] = (c == 0) ? 1.0 : 0.0;
+    if (part == 0)
+        for (int c = threadIdx.x; c < W; c += blockDim.x) M[c] = (c == 0) ? 1.0 : 0.0;
     if (!live) {
-        for (size_t i = (size_t)W + threadIdx.x; i < (size_t)W * W; i += blockDim.x) M[i] = 0.0;
+        const size_t stride = (size_t)parts * blockDim.x;
+        for (size_t i = (size_t)W + (size_t)part * blockDim.x + threadIdx.x; i < (size_t)W * W; i += stride) M[i] = 0.0;
         return;
     }
     __syncthreads();
     const double la = log(alpha);
     const int npairs = W / 2;   // rows 1..W-1 in pairs (the middle row once when W is even)
-    for (int p0 = warp * 32; p0 < npairs; p0 += blockDim.x) {
+    for (int p0 = part * blockDim.x + warp * 32; p0 < npairs; p0 += parts * blockDim.x) {
         const int p = p0 + lane;
         for (int set = 0; set < 2; ++set) {
             const int s = set == 0 ? 1 + p : W - 1 - p;
@@ -173,16 +179,18 @@ __global__ void __launch_bounds__(128) k_matrix_build(const MatrixJob* __restric
 
 cudaError_t launch_matrix_build(const MatrixJob* d_jobs, int n_jobs, int max_size, cudaStream_t s) {
     if (n_jobs <= 0) return cudaSuccess;
-    // one thread per row pair, in whole warps (at most 128)
+    // one thread per row pair, in whole warps: at most 64 per CTA, and as
+    // many CTAs per matrix as its pairs need
     const int pairs = max_size / 2;
-    const int threads = std::min(128, std::max(32, (pairs + 31) / 32 * 32));
+    const int threads = std::min(64, std::max(32, (pairs + 31) / 32 * 32));
+    const int parts = std::max(1, (pairs + threads - 1) / threads);
     size_t smem = sizeof(double) * (4 * (size_t)(max_size + 1) + (size_t)(threads / 32) * kStageCols * kStagePitch) +
                   sizeof(int) * (size_t)threads;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_matrix_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    k_matrix_build<<<n_jobs, threads, smem, s>>>(d_jobs);
+    k_matrix_build<<<n_jobs * parts, threads, smem, s>>>(d_jobs, parts);
     return cudaGetLastError();
 }
 
