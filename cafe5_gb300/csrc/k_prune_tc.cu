@@ -1214,23 +1214,35 @@ __global__ void __launch_bounds__(256) k_convert_tc(const ConvertJob* __restrict
     // only what the walk reads: hi/lo for internal children's branches, the
     // transpose for leaves' (block-uniform)
     const bool want_hl = (J.what & 1) != 0, want_tr = (J.what & 2) != 0;
+    // the deviations' columns either side of a 32-column step (within
+    // 0 .. Wm - 1): lane tx < 2h loads column c0 + hoff into tile column hcol
+    const bool halo = want_tr && tx < 2 * h;
+    const int hoff = tx < h ? tx - h : 32 + (tx - h);
+    const int hcol = tx < h ? tx : 32 + tx;
     for (int c0 = 0; c0 < Wm; c0 += 32) {
-        for (int r = ty; r < 32; r += 8) {
-            const int s = s0 + r, c = c0 + tx;
-            const float x = (float)J.src[(size_t)s * J.ld + c];
+        // the thread's four rows (ty + 8 i) of this step, and their halo
+        // entries, are loaded before any store (the stores might alias the
+        // source as far as the compiler knows), so the loads overlap
+        const int c = c0 + tx, cc = c0 + hoff;
+        float x[4], xh[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) x[i] = (float)J.src[(size_t)(s0 + ty + 8 * i) * J.ld + c];
+        if (halo) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                xh[i] = (cc >= 0 && cc < Wm) ? (float)J.src[(size_t)(s0 + ty + 8 * i) * J.ld + cc] : 0.0f;
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int r = ty + 8 * i, s = s0 + r;
             if (want_hl) {
-                const float hi = tc::round_tf32(x);
+                const float hi = tc::round_tf32(x[i]);
                 b.hi[base + (size_t)s * Wm + c] = hi;
-                b.lo[base + (size_t)s * Wm + c] = tc::round_tf32(x - hi);
+                b.lo[base + (size_t)s * Wm + c] = tc::round_tf32(x[i] - hi);
             }
             if (!want_tr) continue;
-            tile[r][h + tx] = x;
-            // the deviations' columns either side of the band (within 0 .. Wm - 1)
-            if (tx < 2 * h) {
-                const int cc = tx < h ? c0 - h + tx : c0 + 32 + (tx - h);
-                const int col = tx < h ? tx : 32 + tx;
-                tile[r][col] = (cc >= 0 && cc < Wm) ? (float)J.src[(size_t)s * J.ld + cc] : 0.0f;
-            }
+            tile[r][h + tx] = x[i];
+            if (halo) tile[r][hcol] = xh[i];
         }
         if (!want_tr) continue;
         if (b.err)
