@@ -1652,7 +1652,6 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     PendingJobs P;
     std::vector<MatEntry*>& node_entry = ws.entry_vec;
     node_entry.assign((size_t)CT * T.n_nodes, nullptr);
-    bool any_saturated = false;   // a key with 1 - 2a outside (0, 1): zero rows
     ws.sat_vec.assign((size_t)CT * T.n_nodes, 0);
     // the request's keys first, with their table slots prefetched (a large
     // cache misses in the CPU caches on every probe), then one
@@ -1676,10 +1675,7 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
             node_entry[(size_t)c * T.n_nodes + v] = schedule(C, P, key);
             const double lq = (double)key.lq / 1000000000.0, tq = (double)key.tq / 1000.0;
             const double al = lq * tq / (1 + lq * tq), co = 1 - 2 * al;
-            if (!(co > 0 && co != 1)) {
-                any_saturated = true;
-                ws.sat_vec[(size_t)c * T.n_nodes + v] = 1;
-            }
+            if (!(co > 0 && co != 1)) ws.sat_vec[(size_t)c * T.n_nodes + v] = 1;   // zero rows below row 0
         }
     int rc = cache_build(C, ws, P);
     if (rc) return rc;
@@ -1702,13 +1698,11 @@ int enqueue_score(cafe_ctx* C, Workspace& ws, const cafe_request* Rs, int NB, do
     if (C->prof.on) C->prof.acc.host_keys_ms += host_ms_since(t_keys);
     CK(ws.cat.reserve((size_t)std::max<int64_t>(F, 1) * CT * sizeof(double)), "category buffer");
     if (R->precision == CAFE_PREC_MIXED_TF32X3) {
-        // polytomies stay on the FP64 path; saturated keys (1 - 2a < 0) run
-        // on the tensor cores (a family that is exactly zero through one ends
-        // there)
-        // (and error models wider than the +-kMaxErrHalf deviations the
-        // transposed leaf rows fold in)
+        // polytomies stay on the FP64 path, and so do error models wider than
+        // the +-kMaxErrHalf deviations the transposed leaf rows fold in;
+        // saturated keys (1 - 2a < 0) run on the tensor cores (a family that
+        // is exactly zero through one ends there)
         const bool to_fp64 = T.max_children > 2 || (R->use_error_model && C->err_ndev > 2 * kMaxErrHalf + 1);
-        (void)any_saturated;
         if (!to_fp64) {
             CK(ws.catids.reserve(active.size() * sizeof(int32_t)), "categories");
             CK(ws.h_catids.reserve(active.size() * sizeof(int32_t)), "categories");

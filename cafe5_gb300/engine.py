@@ -23,7 +23,7 @@ from typing import List, Optional, Sequence
 import numpy as np
 
 from . import _lib
-from .families import FamilySet, global_bounds
+from .families import FamilySet
 from .inputs import ErrorModel, RootPrior, discrete_gamma
 from .tree import Tree, lambda_index_of_nodes
 

@@ -14,7 +14,7 @@ reports +inf (a family failed, a lambda was rejected) makes the total +inf.
 from __future__ import annotations
 
 import math
-from typing import List, Optional, Sequence, Tuple
+from typing import List, Sequence, Tuple
 
 import numpy as np
 

@@ -18,7 +18,7 @@ No public dataset is named for this path, so every workload is generated:
 from __future__ import annotations
 
 from dataclasses import dataclass, field
-from typing import Dict, List, Optional
+from typing import List, Optional
 
 import numpy as np
 

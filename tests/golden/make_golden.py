@@ -37,9 +37,9 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from cafe5_gb300.families import FamilySet, global_bounds, write_families  # noqa: E402
-from cafe5_gb300.inputs import ErrorModel, RootPrior, discrete_gamma  # noqa: E402
-from cafe5_gb300.synth import simulate_families, workload, yule_tree  # noqa: E402
-from cafe5_gb300.tree import lambda_index_of_nodes, parse_newick  # noqa: E402
+from cafe5_gb300.inputs import RootPrior, discrete_gamma  # noqa: E402
+from cafe5_gb300.synth import simulate_families, workload  # noqa: E402
+from cafe5_gb300.tree import parse_newick  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "cafe_ref_harness")
 

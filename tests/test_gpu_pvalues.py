@@ -86,7 +86,7 @@ def test_pvalue_seed_changes_simulation(ctx):
 
 
 def test_model_mirror_pvalues(ctx):
-    from cafe5_gb300.engine import BaseModel, MultipleLambda, SingleLambda
+    from cafe5_gb300.engine import BaseModel, SingleLambda
     from cafe5_gb300.families import FamilySet
     case = CASES[0]
     fams = FamilySet([f"f{i}" for i in range(len(case.counts))], case.counts)
